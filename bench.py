@@ -1,0 +1,300 @@
+"""Benchmark of the GB300 D2Q9 BGK step (one JSON line on stdout).
+
+Workload: lid-driven cavity 4096 x 4096, Re = 10000, U = 0.1, nu = 0.04096 (the reference's GPU
+benchmark input UTIL/bgk.gpu.input), FP32 storage and arithmetic, fused ping-pong scheme.
+A bench "step" is one lattice time step over the whole 4096^2 domain; the metric is GLUPS
+(lx * ly * steps / time / 1e9, interior nodes, as SRC/finalize.F90:60-61 counts Mlups).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With N > 1 (torchrun) every rank advances its own cavity (independent domains, no exchange):
+weak scaling, value = sum over ranks.  `--impl reference` times the CPU restatement of the
+reference step (the oracle) on this machine's host cores for the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+LX = LY = 4096
+SVISC, U0 = 0.04096, 0.1
+BYTES_PER_CELL = {"f32": 72, "f64": 144, "f16": 36, "bf16": 36}
+WORKLOAD = "lid-driven cavity 4096x4096, Re=10000, U=0.1 (UTIL/bgk.gpu.input), FP32, fused ping-pong"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel_key):
+    """DRAM bytes per launch recorded from an ncu capture (profiles/dram_traffic.txt)."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == kernel_key:
+                return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 7:
+                continue
+            try:
+                sm.append(float(p[0]))
+                mx.append(float(p[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_reference(steps_budget_s=15.0, max_steps=None):
+    """Time the oracle's threaded fused step on the host cores (bounded sample of the workload)."""
+    from oracle import oracle as orc
+    orc.build()
+    threads = os.cpu_count() or 1
+    o = orc.Oracle(LX, LY, prec=orc.SINGLE, tcase=orc.LDC, svisc=SVISC, u0=U0)
+    o.step(1, threads=threads)  # warm-up (page in)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.step(1, threads=threads)
+        n += 1
+        el = time.perf_counter() - t0
+        if el > steps_budget_s or (max_steps and n >= max_steps):
+            break
+    glups = LX * LY * n / el / 1e9
+    o.close()
+    return {"value": glups, "unit": "GLUPS", "cores": threads, "kind": "port",
+            "sample": f"{n} fused steps of the 4096^2 FP32 cavity on {threads} threads ({el:.1f} s), "
+                      "oracle/bgk_oracle.c (C restatement of SRC/col_MC.F90 + SRC/bcond.driven.F90)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    cb = cpu_reference(steps_budget_s=max(5.0, 2.0 * args.steps / 2000 * 5), max_steps=max(args.steps, 3))
+    line = {"metric": "GLUPS", "value": cb["value"], "unit": "GLUPS", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": LX * LY / (cb["value"] * 1e9) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "lx": LX, "ly": LY}, "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_profile(args):
+    """Small case for ncu captures: warm-up steps, then `--steps` steps, nothing printed but a tag."""
+    import bgk2d_gpu_gb300 as bgk
+    scheme, storage = args.profile.split("_")
+    compute = "f64" if storage == "f64" else "f32"
+    with bgk.Solver(args.size, args.size, tcase="LDC", svisc=SVISC * args.size / LX, u0=U0, storage=storage,
+                    compute=compute, scheme=scheme) as s:
+        s.step(args.warmup)
+        s.step(args.steps)
+        s.sync()
+    print(f"profile run {args.profile} {args.size}^2 warmup={args.warmup} steps={args.steps}")
+    return 0
+
+
+def measure_variant(bgk, storage, scheme, steps, warmup, dev):
+    compute = "f64" if storage == "f64" else "f32"
+    with bgk.Solver(LX, LY, tcase="LDC", svisc=SVISC, u0=U0, storage=storage, compute=compute, scheme=scheme,
+                    device=dev) as s:
+        s.step(warmup)
+        s.sync()
+        ms = s.step_timed(steps)
+    glups = LX * LY * steps / (ms * 1e-3) / 1e9
+    return glups, ms / steps
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", default=None,
+                    help="run only <scheme>_<storage> (e.g. pingpong_f32) on a --size^2 cavity, for ncu")
+    ap.add_argument("--size", type=int, default=2048)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.profile:
+        return run_profile(args)
+
+    rank, world, local = dist_env()
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    import bgk2d_gpu_gb300 as bgk
+    bgk.load()
+    peak, peak_kind = peaks()
+
+    # ---- device-timed value: K steps from HBM-resident state --------------------------------
+    s = bgk.Solver(LX, LY, tcase="LDC", svisc=SVISC, u0=U0, storage="f32", scheme="pingpong", device=local)
+    s.step(args.warmup)
+    s.sync()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    n0 = s.launches()
+    with ClockSampler(local) as clk:
+        ms = s.step_timed(args.steps)
+    torch.cuda.synchronize()
+    launches = s.launches() - n0
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    glups = world * LX * LY * args.steps / (ms * 1e-3) / 1e9
+    ms_step = ms / args.steps
+    achieved = BYTES_PER_CELL["f32"] * LX * LY / (ms_step * 1e-3) / 1e9
+    diag = s.diagno()
+
+    # ---- end-to-end through the C ABI with host buffers --------------------------------------
+    npl = (LX + 2) * (LY + 2)
+    host = torch.zeros((9, LY + 2, LX + 2), dtype=torch.float32, pin_memory=True)
+    out = torch.empty_like(host).pin_memory()
+    import ctypes
+    L = bgk.load()
+    ptr_in = (ctypes.c_void_p * 9)(*[host[q].data_ptr() for q in range(9)])
+    ptr_out = (ctypes.c_void_p * 9)(*[out[q].data_ptr() for q in range(9)])
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    rc = L.bgk_upload(s._h, ptr_in, LX + 2)
+    rc |= L.bgk_step(s._h, args.steps)
+    rc |= L.bgk_download(s._h, ptr_out, LX + 2)
+    e2e_s = time.perf_counter() - t0
+    if rc:
+        raise RuntimeError("e2e path failed")
+    if dist:
+        t = torch.tensor([e2e_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * LX * LY * args.steps / e2e_s / 1e9, "unit": "GLUPS",
+           "h2d_bytes_per_step": 9 * npl * 4 / args.steps, "d2h_bytes_per_step": 9 * npl * 4 / args.steps,
+           "timed": "bgk_upload (pinned host, 9 planes) + bgk_step(K) + bgk_download (9 planes)"}
+    s.close()
+
+    variants = {}
+    if not args.no_variants and rank == 0:
+        vsteps = max(20, args.steps // 10)
+        for name, st, sch in (("pingpong_f32", "f32", "pingpong"), ("aa_f32", "f32", "aa"),
+                              ("pingpong_f16", "f16", "pingpong"), ("aa_f16", "f16", "aa"),
+                              ("pingpong_bf16", "bf16", "pingpong"), ("pingpong_f64", "f64", "pingpong"),
+                              ("aa_f64", "f64", "aa")):
+            n = vsteps if st != "f64" else max(10, vsteps // 4)
+            g, msv = measure_variant(bgk, st, sch, n, 5, local)
+            bw = BYTES_PER_CELL[st] * LX * LY / (msv * 1e-3) / 1e9
+            variants[name] = {"GLUPS": round(g, 3), "ms_per_step": round(msv, 4), "algorithmic_GBps": round(bw, 1),
+                              "hbm_frac": round(bw / peak, 4), "steps": n}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu and world == 1:
+        cpu = cpu_reference(steps_budget_s=12.0)
+
+    if rank == 0:
+        kt = traffic_from_profiles("pp_kernel_f32_ldc4096")
+        line = {
+            "metric": "GLUPS", "value": round(glups, 3), "unit": "GLUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_step, 5), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (rest-state start, no dataset)",
+            "config": {"workload": WORKLOAD, "lx": LX, "ly": LY, "scheme": "pingpong", "storage": "f32",
+                       "l2": "inputs larger than L2: 1.21 GB of populations per step",
+                       "parallelism": f"{world} independent cavities" if world > 1 else "single domain"},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": kt, "peak_kind": peak_kind,
+                         "kernel": "bgk::pp_kernel<float,float,128,1,false>", "bytes_per_cell": 72},
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "diagno": [float(x) for x in diag],
+            "variants": variants,
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

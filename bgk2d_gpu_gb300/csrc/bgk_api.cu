@@ -1,0 +1,633 @@
+// bgk_api.cu -- C ABI of libbgk2d_gb300.so: handle lifecycle, transfers, stepping, reductions.
+//
+// The reference keeps its populations in `module storage` and runs boundaries, propagation
+// and collision as separate directive loops (SRC/bgk2d.F90:100-102).  Here a handle owns the
+// populations in HBM; one fused kernel per time step applies the boundary rules, streams and
+// collides; steps are replayed from CUDA graphs; reductions run in FP64 on the device.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bgk2d_gb300.h"
+#include "bgk_common.cuh"
+#include "bgk_setup.h"
+#include "bgk_table.h"
+
+using namespace bgk;
+
+namespace bgk {
+
+__global__ void finalize4_kernel(const double *partial, int nb, double *out)
+{
+    __shared__ double sh[256][4];
+    double s[4] = {0, 0, 0, 0};
+    for (int b = threadIdx.x; b < nb; b += blockDim.x)
+        for (int i = 0; i < 4; ++i) s[i] += partial[4 * b + i];
+    for (int i = 0; i < 4; ++i) sh[threadIdx.x][i] = s[i];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w)
+            for (int i = 0; i < 4; ++i) sh[threadIdx.x][i] += sh[threadIdx.x + w][i];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int i = 0; i < 4; ++i) out[i] = sh[0][i];
+}
+
+cudaError_t launch_finalize4(const double *partial, int nb, double *out, cudaStream_t st)
+{
+    finalize4_kernel<<<1, 256, 0, st>>>(partial, nb, out);
+    return cudaGetLastError();
+}
+
+}  // namespace bgk
+
+struct bgk_handle {
+    bgk_case_desc desc;
+    int dev = 0;
+    KernelTable T{};
+    Lattice L{};
+    CaseSetup cs;
+    void *d_planes = nullptr;
+    size_t planes_bytes = 0;
+    uint32_t *d_mask = nullptr;
+    double *d_inflow = nullptr;
+    double *d_partial = nullptr;
+    double *d_out = nullptr;
+    int nb_red = 0;
+    double *d_uprev = nullptr, *d_vprev = nullptr;
+    int64_t res_itime = -1;
+    void *d_stage = nullptr;
+    size_t stage_bytes = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int graph_steps = 32;
+    int cur = 0;     // ping-pong: buffer holding the current state
+    int phase = 0;   // AA: 0 = post-collision (swapped slots), 1 = streamed
+    int64_t itime = 0;
+    int64_t launches = 0;
+    int cfg = 2;
+    int host_bytes = 4;
+    int sticky = BGK_OK;
+    std::string err;
+};
+
+namespace {
+
+int fail(bgk_handle *h, int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (h) {
+        if (h->err.empty()) h->err = buf;
+        if (code == BGK_E_CUDA) h->sticky = code;
+    }
+    return code;
+}
+
+#define CK(h, call)                                                                          \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) return fail(h, BGK_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+#define CHECK_HANDLE(h)                                     \
+    do {                                                    \
+        if (!(h)) return BGK_E_INVALID;                     \
+        if ((h)->sticky != BGK_OK) return (h)->sticky;      \
+        if (cudaSetDevice((h)->dev) != cudaSuccess) return fail(h, BGK_E_CUDA, "cudaSetDevice"); \
+    } while (0)
+
+bool get_table(int storage, int compute, KernelTable &t)
+{
+    if (storage == BGK_STORE_F32 && compute == BGK_COMPUTE_F32) t = table_f32_f32();
+    else if (storage == BGK_STORE_F32 && compute == BGK_COMPUTE_F64) t = table_f32_f64();
+    else if (storage == BGK_STORE_F64 && compute == BGK_COMPUTE_F64) t = table_f64_f64();
+    else if (storage == BGK_STORE_F16 && compute == BGK_COMPUTE_F32) t = table_f16_f32();
+    else if (storage == BGK_STORE_BF16 && compute == BGK_COMPUTE_F32) t = table_bf16_f32();
+    else return false;
+    return true;
+}
+
+int default_cfg(int nvec)
+{
+    if (nvec >= 128) return 2;  // 128 x 1
+    if (nvec >= 64) return 1;   // 64 x 2
+    return 0;                   // 32 x 4
+}
+
+int ensure_stage(bgk_handle *h)
+{
+    const size_t need = (size_t)(h->desc.lx + 2) * (size_t)(h->desc.ly + 2) * (size_t)h->host_bytes;
+    if (h->stage_bytes >= need) return BGK_OK;
+    if (h->d_stage) cudaFree(h->d_stage);
+    h->d_stage = nullptr;
+    h->stage_bytes = 0;
+    if (cudaMalloc(&h->d_stage, need) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(h, BGK_E_NOMEM, "staging buffer of %zu bytes", need);
+    }
+    h->stage_bytes = need;
+    return BGK_OK;
+}
+
+// host population arrays (reference layout) -> device state
+int upload_impl(bgk_handle *h, const void *const pops[9], int64_t ld)
+{
+    const int l = h->desc.lx, m = h->desc.ly;
+    if (ld < l + 2) return fail(h, BGK_E_INVALID, "leading dimension %lld < lx+2", (long long)ld);
+    int rc = ensure_stage(h);
+    if (rc) return rc;
+    const size_t hb = (size_t)h->host_bytes;
+    for (int q = 0; q < 9; ++q) {
+        if (!pops[q]) return fail(h, BGK_E_INVALID, "population %d is NULL", q);
+        CK(h, cudaMemcpy2DAsync(h->d_stage, (l + 2) * hb, pops[q], (size_t)ld * hb, (l + 2) * hb, m + 2,
+                                cudaMemcpyHostToDevice, h->st));
+        CK(h, h->T.scatter(h->L, h->cur, q, h->d_stage, h->st));
+        h->launches++;
+    }
+    if (h->L.scheme == BGK_SCHEME_AA) {
+        h->phase = 0;
+        if (h->cs.faces[XHI] == FK_OUTFLOW_EQ || h->cs.faces[XHI] == FK_OUTFLOW_ZG) {
+            CK(h, h->T.fill_outflow(h->L, h->st));
+            h->launches++;
+        }
+    }
+    CK(h, cudaStreamSynchronize(h->st));
+    return BGK_OK;
+}
+
+int launch_step(bgk_handle *h)
+{
+    if (h->L.scheme == BGK_SCHEME_PINGPONG) {
+        CK(h, h->T.step(STEP_PP, h->L, h->cur, h->cs.has_obs, h->cfg, h->st));
+        h->cur ^= 1;
+    } else {
+        CK(h, h->T.step(h->phase == 0 ? STEP_AA_P : STEP_AA_L, h->L, 0, h->cs.has_obs, h->cfg, h->st));
+        h->phase ^= 1;
+    }
+    h->launches++;
+    h->itime++;
+    return BGK_OK;
+}
+
+// graph of graph_steps steps starting from the state slot `start` (PP buffer / AA phase 0)
+int build_graph(bgk_handle *h, int start)
+{
+    cudaGraph_t g = nullptr;
+    const int cur0 = h->cur, ph0 = h->phase;
+    const int64_t it0 = h->itime, ln0 = h->launches;
+    if (h->L.scheme == BGK_SCHEME_PINGPONG) h->cur = start;
+    else h->phase = 0;
+    CK(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    int rc = BGK_OK;
+    for (int s = 0; s < h->graph_steps && rc == BGK_OK; ++s) rc = launch_step(h);
+    cudaError_t e = cudaStreamEndCapture(h->st, &g);
+    h->cur = cur0;
+    h->phase = ph0;
+    h->itime = it0;
+    h->launches = ln0;
+    if (rc != BGK_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail(h, BGK_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&h->graph[start], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(h, BGK_E_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    return BGK_OK;
+}
+
+int steps_impl(bgk_handle *h, int32_t n)
+{
+    if (n < 0) return fail(h, BGK_E_INVALID, "negative step count");
+    int rc;
+    // AA graphs start at phase 0; the odd step that brings phase 1 back to 0 runs directly
+    if (h->L.scheme == BGK_SCHEME_AA && h->phase == 1 && n > 0) {
+        if ((rc = launch_step(h))) return rc;
+        --n;
+    }
+    while (n >= h->graph_steps) {
+        const int slot = h->L.scheme == BGK_SCHEME_PINGPONG ? h->cur : 0;
+        if (!h->graph[slot] && (rc = build_graph(h, slot))) return rc;
+        CK(h, cudaGraphLaunch(h->graph[slot], h->st));
+        h->launches += h->graph_steps;
+        h->itime += h->graph_steps;
+        n -= h->graph_steps;
+    }
+    while (n-- > 0)
+        if ((rc = launch_step(h))) return rc;
+    return BGK_OK;
+}
+
+int reduce4(bgk_handle *h, double out[4])
+{
+    CK(h, launch_finalize4(h->d_partial, h->nb_red, h->d_out, h->st));
+    h->launches++;
+    CK(h, cudaMemcpyAsync(out, h->d_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    return BGK_OK;
+}
+
+void release(bgk_handle *h)
+{
+    for (int i = 0; i < 2; ++i)
+        if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
+    if (h->d_planes) cudaFree(h->d_planes);
+    if (h->d_mask) cudaFree(h->d_mask);
+    if (h->d_inflow) cudaFree(h->d_inflow);
+    if (h->d_partial) cudaFree(h->d_partial);
+    if (h->d_out) cudaFree(h->d_out);
+    if (h->d_uprev) cudaFree(h->d_uprev);
+    if (h->d_vprev) cudaFree(h->d_vprev);
+    if (h->d_stage) cudaFree(h->d_stage);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->st) cudaStreamDestroy(h->st);
+}
+
+template <typename K>
+std::string setup_for(const bgk_case_desc &d, CaseSetup &cs) { return setup_case<K>(d, cs); }
+
+}  // namespace
+
+extern "C" {
+
+const char *bgk_version(void) { return "bgk2d_gb300 1.0 (sm_103a)"; }
+
+int bgk_default_desc(bgk_case_desc *d)
+{
+    if (!d) return BGK_E_INVALID;
+    std::memset(d, 0, sizeof(*d));
+    d->lx = 256; d->ly = 256;
+    d->storage = BGK_STORE_F32;
+    d->compute = BGK_COMPUTE_F32;
+    d->scheme = BGK_SCHEME_PINGPONG;
+    d->tcase = BGK_CASE_LDC;
+    d->svisc = 0.1;
+    d->u0 = 0.1;
+    d->radius = 16;
+    d->obs_icoord = -1;
+    d->obs_jcoord = -1;
+    d->tgv_u0 = 0.02;
+    return BGK_OK;
+}
+
+int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
+{
+    if (!desc || !out) return BGK_E_INVALID;
+    *out = nullptr;
+    const bgk_case_desc &d = *desc;
+    if (d.lx < 2 || d.ly < 2 || d.ipad < 0 || d.jpad < 0) return BGK_E_INVALID;
+    if (d.scheme != BGK_SCHEME_PINGPONG && d.scheme != BGK_SCHEME_AA) return BGK_E_INVALID;
+    KernelTable T;
+    if (!get_table(d.storage, d.compute, T)) return BGK_E_INVALID;
+
+    bgk_handle *h = new bgk_handle();
+    h->desc = d;
+    h->desc.obs_mask = nullptr;
+    h->dev = d.device;
+    h->T = T;
+    h->host_bytes = d.storage == BGK_STORE_F64 ? 8 : 4;
+    std::string msg = d.compute == BGK_COMPUTE_F64 ? setup_for<double>(d, h->cs) : setup_for<float>(d, h->cs);
+    if (!msg.empty()) {
+        delete h;
+        return BGK_E_INVALID;
+    }
+    if (cudaSetDevice(h->dev) != cudaSuccess) {
+        delete h;
+        return BGK_E_CUDA;
+    }
+
+    // geometry: interior cell x=1 starts a 16-byte vector; rows padded to 128 bytes
+    const int l = d.lx, m = d.ly, vec = T.vec, eb = T.elem_bytes;
+    const int nvec = (l + vec - 1) / vec;
+    const int row_align = 128 / eb;
+    int64_t pitch = (vec - 1) + 2 + (int64_t)(nvec + 1) * vec;
+    pitch = (pitch + row_align - 1) / row_align * row_align;
+    int64_t plane = pitch * (m + 2);
+    plane = (plane + 256 / eb - 1) / (256 / eb) * (256 / eb);
+    const int nplanes = d.scheme == BGK_SCHEME_PINGPONG ? 17 : 9;
+    h->planes_bytes = (size_t)plane * nplanes * eb;
+
+    // admission against free HBM (populations + staging plane + mask + reduction scratch)
+    const size_t stage = (size_t)(l + 2) * (m + 2) * h->host_bytes;
+    const size_t mask_words = (size_t)((l + 2 + 31) / 32) * (m + 2);
+    const size_t need = h->planes_bytes + stage + mask_words * 4 + (64u << 20);
+    size_t free_b = 0, total_b = 0;
+    const char *inj = std::getenv("BGK_FAULT_INJECT_NOMEM");
+    if (inj && inj[0] == '1') { delete h; return BGK_E_NOMEM; }
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { delete h; return BGK_E_CUDA; }
+    if (need > free_b) { delete h; return BGK_E_NOMEM; }
+
+    if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) {
+        release(h); delete h; return BGK_E_CUDA;
+    }
+    if (cudaMalloc(&h->d_planes, h->planes_bytes) != cudaSuccess) {
+        cudaGetLastError(); release(h); delete h; return BGK_E_NOMEM;
+    }
+    cudaMemsetAsync(h->d_planes, 0, h->planes_bytes, h->st);
+
+    Lattice &L = h->L;
+    L.planes = h->d_planes;
+    L.plane_elems = plane;
+    L.pitch = (int32_t)pitch;
+    L.lx = l; L.ly = m;
+    L.nvec = nvec;
+    L.scheme = d.scheme;
+    for (int f = 0; f < 4; ++f) {
+        L.faces[f] = h->cs.faces[f];
+        for (int q = 0; q < 9; ++q) L.wt[f][q] = h->cs.wt[f][q];
+    }
+    L.omega = h->cs.omega;
+    L.fgrad = h->cs.fgrad;
+    L.forced = h->cs.forced;
+
+    // inflow table
+    if (cudaMalloc(&h->d_inflow, h->cs.inflow.size() * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError(); release(h); delete h; return BGK_E_NOMEM;
+    }
+    cudaMemcpy(h->d_inflow, h->cs.inflow.data(), h->cs.inflow.size() * sizeof(double), cudaMemcpyHostToDevice);
+    L.inflow = h->d_inflow;
+
+    // obstacle bits, rows 0..m+1, bit x for x = 0..l+1
+    L.mask_pitch = (l + 2 + 31) / 32;
+    std::vector<uint32_t> bits((size_t)L.mask_pitch * (m + 2), 0u);
+    for (int j = 1; j <= m; ++j)
+        for (int i = 1; i <= l; ++i)
+            if (h->cs.obs[(size_t)(i - 1) + (size_t)(j - 1) * l] == 1)
+                bits[(size_t)j * L.mask_pitch + (i >> 5)] |= 1u << (i & 31);
+    if (cudaMalloc(&h->d_mask, bits.size() * 4) != cudaSuccess) {
+        cudaGetLastError(); release(h); delete h; return BGK_E_NOMEM;
+    }
+    cudaMemcpy(h->d_mask, bits.data(), bits.size() * 4, cudaMemcpyHostToDevice);
+    L.mask = h->d_mask;
+    if (h->cs.has_obs) {
+        L.ob_x0 = h->cs.bbox[0] - 1; L.ob_x1 = h->cs.bbox[1] + 1;
+        L.ob_y0 = h->cs.bbox[2] - 1; L.ob_y1 = h->cs.bbox[3] + 1;
+    } else {
+        L.ob_x0 = L.ob_y0 = 1 << 30; L.ob_x1 = L.ob_y1 = -1;
+    }
+
+    // reduction scratch
+    h->nb_red = 4 * 152;
+    if (cudaMalloc(&h->d_partial, (size_t)h->nb_red * 4 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&h->d_out, 4 * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError(); release(h); delete h; return BGK_E_NOMEM;
+    }
+    h->cfg = default_cfg(nvec);
+
+    // initial state (SRC/initialize.F90:85-125: init(init_v))
+    int rc = BGK_OK;
+    if (d.init_v == BGK_INIT_TGV_REF || d.init_v == BGK_INIT_TGV) {
+        const size_t n = (size_t)(l + 2) * (m + 2);
+        void *ptrs[9];
+        if (h->host_bytes == 8) {
+            std::vector<double> a;
+            if (d.init_v == BGK_INIT_TGV) init_tgv<double>(l, m, d.tgv_u0, a);
+            else init_reference<double, double>(l, m, true, a);
+            for (int q = 0; q < 9; ++q) ptrs[q] = a.data() + q * n;
+            rc = upload_impl(h, ptrs, l + 2);
+        } else {
+            std::vector<float> a;
+            if (d.init_v == BGK_INIT_TGV) init_tgv<float>(l, m, d.tgv_u0, a);
+            else if (d.compute == BGK_COMPUTE_F64) init_reference<double, float>(l, m, true, a);
+            else init_reference<float, float>(l, m, true, a);
+            for (int q = 0; q < 9; ++q) ptrs[q] = a.data() + q * n;
+            rc = upload_impl(h, ptrs, l + 2);
+        }
+    } else if (d.init_v != BGK_INIT_REST) {
+        rc = BGK_E_INVALID;
+    }
+    if (rc == BGK_OK && cudaStreamSynchronize(h->st) != cudaSuccess) rc = BGK_E_CUDA;
+    if (rc != BGK_OK) { release(h); delete h; return rc; }
+    *out = h;
+    return BGK_OK;
+}
+
+int bgk_destroy(bgk_handle *h)
+{
+    if (!h) return BGK_E_INVALID;
+    cudaSetDevice(h->dev);
+    if (h->st) cudaStreamSynchronize(h->st);
+    release(h);
+    delete h;
+    return BGK_OK;
+}
+
+int bgk_upload(bgk_handle *h, void *const pops[9], int64_t ld)
+{
+    CHECK_HANDLE(h);
+    if (!pops) return BGK_E_INVALID;
+    return upload_impl(h, pops, ld);
+}
+
+int bgk_download(bgk_handle *h, void *const pops[9], int64_t ld)
+{
+    CHECK_HANDLE(h);
+    const int l = h->desc.lx, m = h->desc.ly;
+    if (!pops || ld < l + 2) return fail(h, BGK_E_INVALID, "bad download arguments");
+    int rc = ensure_stage(h);
+    if (rc) return rc;
+    const size_t hb = (size_t)h->host_bytes;
+    for (int q = 0; q < 9; ++q) {
+        if (!pops[q]) return fail(h, BGK_E_INVALID, "population %d is NULL", q);
+        CK(h, h->T.gather(h->L, h->cur, h->phase, q, h->d_stage, h->cs.has_obs, h->st));
+        h->launches++;
+        CK(h, cudaMemcpy2DAsync(pops[q], (size_t)ld * hb, h->d_stage, (l + 2) * hb, (l + 2) * hb, m + 2,
+                                cudaMemcpyDeviceToHost, h->st));
+    }
+    CK(h, cudaStreamSynchronize(h->st));
+    return BGK_OK;
+}
+
+int bgk_boundaries(bgk_handle *h)
+{
+    CHECK_HANDLE(h);
+    return BGK_OK;  // folded into the fused step launched by bgk_collision
+}
+
+int bgk_propagation(bgk_handle *h)
+{
+    CHECK_HANDLE(h);
+    return BGK_OK;  // the pull streaming is part of the fused step
+}
+
+int bgk_collision(bgk_handle *h, int32_t itime)
+{
+    CHECK_HANDLE(h);
+    (void)itime;
+    return launch_step(h);
+}
+
+int bgk_step(bgk_handle *h, int32_t nsteps)
+{
+    CHECK_HANDLE(h);
+    return steps_impl(h, nsteps);
+}
+
+int bgk_step_timed(bgk_handle *h, int32_t nsteps, float *ms)
+{
+    CHECK_HANDLE(h);
+    if (!ms) return BGK_E_INVALID;
+    CK(h, cudaEventRecord(h->ev0, h->st));
+    int rc = steps_impl(h, nsteps);
+    if (rc) return rc;
+    CK(h, cudaEventRecord(h->ev1, h->st));
+    CK(h, cudaEventSynchronize(h->ev1));
+    CK(h, cudaEventElapsedTime(ms, h->ev0, h->ev1));
+    return BGK_OK;
+}
+
+int bgk_sync(bgk_handle *h)
+{
+    CHECK_HANDLE(h);
+    CK(h, cudaStreamSynchronize(h->st));
+    return BGK_OK;
+}
+
+int bgk_diagno(bgk_handle *h, int32_t fluid_only, double out[4])
+{
+    CHECK_HANDLE(h);
+    if (!out) return BGK_E_INVALID;
+    CK(h, h->T.diagno(h->L, h->cur, h->phase, fluid_only, h->cs.has_obs, h->d_partial, h->nb_red, h->st));
+    h->launches++;
+    double s[4];
+    int rc = reduce4(h, s);
+    if (rc) return rc;
+    const double l = h->desc.lx, m = h->desc.ly;
+    for (int i = 0; i < 4; ++i) out[i] = (s[i] / l) / m;  // SRC/diagno.F90:317-320
+    for (int i = 0; i < 4; ++i)
+        if (!std::isfinite(s[i])) return fail(h, BGK_E_NUMERIC, "diagno: non-finite sum");
+    return BGK_OK;
+}
+
+int bgk_residual(bgk_handle *h, double *out)
+{
+    CHECK_HANDLE(h);
+    if (!out) return BGK_E_INVALID;
+    const size_t n = (size_t)h->desc.lx * h->desc.ly;
+    bool first = false;
+    if (!h->d_uprev) {
+        if (cudaMalloc(&h->d_uprev, n * sizeof(double)) != cudaSuccess ||
+            cudaMalloc(&h->d_vprev, n * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(h, BGK_E_NOMEM, "residual snapshot");
+        }
+        CK(h, cudaMemsetAsync(h->d_uprev, 0, n * sizeof(double), h->st));
+        CK(h, cudaMemsetAsync(h->d_vprev, 0, n * sizeof(double), h->st));
+        first = true;
+    }
+    CK(h, h->T.residual(h->L, h->cur, h->phase, h->cs.has_obs, h->d_uprev, h->d_vprev, h->d_partial, h->nb_red, h->st));
+    h->launches++;
+    double s[4];
+    int rc = reduce4(h, s);
+    if (rc) return rc;
+    const int64_t dt = h->itime - h->res_itime;
+    h->res_itime = h->itime;
+    if (s[2] != 0.0 || !std::isfinite(s[0]) || !std::isfinite(s[1])) {
+        *out = NAN;
+        return fail(h, BGK_E_NUMERIC, "residual: non-finite velocity");
+    }
+    if (first || dt <= 0) *out = 1.0;
+    else *out = (s[1] > 0 ? std::sqrt(s[0] / s[1]) : (s[0] > 0 ? 1.0 : 0.0)) / (double)dt;
+    return BGK_OK;
+}
+
+int bgk_draglift(bgk_handle *h, double out[2])
+{
+    CHECK_HANDLE(h);
+    if (!out) return BGK_E_INVALID;
+    if (!h->cs.has_obs) return fail(h, BGK_E_UNSUPPORTED, "draglift needs an obstacle");
+    const int l = h->desc.lx, m = h->desc.ly, r = h->cs.radius, delta = 3;
+    int i0 = h->cs.icoord - r - delta, i1 = h->cs.icoord + r + delta;
+    int j0 = h->cs.jcoord - r - delta, j1 = h->cs.jcoord + r + delta;
+    i0 = std::max(i0, 1); j0 = std::max(j0, 1); i1 = std::min(i1, l); j1 = std::min(j1, m);
+    CK(h, h->T.draglift(h->L, h->cur, h->phase, i0, i1, j0, j1, h->d_partial, h->nb_red, h->st));
+    h->launches++;
+    double s[4];
+    int rc = reduce4(h, s);
+    if (rc) return rc;
+    double norm;
+    if (h->desc.compute == BGK_COMPUTE_F64) {
+        const double u = h->cs.u_inflow;
+        norm = 1.0 / ((u * u) * (double)r);
+    } else {
+        const float u = (float)h->cs.u_inflow;
+        norm = (double)(1.0f / ((u * u) * (float)r));
+    }
+    out[0] = s[0] * norm;
+    out[1] = s[1] * norm;
+    return BGK_OK;
+}
+
+int bgk_fields(bgk_handle *h, double *rho, double *u, double *v)
+{
+    CHECK_HANDLE(h);
+    if (!rho || !u || !v) return BGK_E_INVALID;
+    const size_t n = (size_t)h->desc.lx * h->desc.ly;
+    double *d = nullptr;
+    if (cudaMalloc(&d, 3 * n * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(h, BGK_E_NOMEM, "fields buffer");
+    }
+    cudaError_t e = h->T.fields(h->L, h->cur, h->phase, h->cs.has_obs, d, d + n, d + 2 * n, h->st);
+    h->launches++;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rho, d, n * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(u, d + n, n * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(v, d + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(h, BGK_E_CUDA, "fields: %s", cudaGetErrorString(e));
+    return BGK_OK;
+}
+
+int bgk_get_obs(bgk_handle *h, int32_t *mask, int32_t bbox[5])
+{
+    if (!h || !bbox) return BGK_E_INVALID;
+    if (mask) std::memcpy(mask, h->cs.obs.data(), h->cs.obs.size() * sizeof(int32_t));
+    for (int i = 0; i < 5; ++i) bbox[i] = h->cs.bbox[i];
+    return BGK_OK;
+}
+
+int bgk_get_scalars(bgk_handle *h, double out[4], int64_t *itime)
+{
+    if (!h || !out) return BGK_E_INVALID;
+    out[0] = h->cs.omega; out[1] = h->cs.fgrad; out[2] = h->cs.u00; out[3] = h->cs.u0;
+    if (itime) *itime = h->itime;
+    return BGK_OK;
+}
+
+int bgk_footprint(bgk_handle *h, int64_t *device_bytes, int32_t *bytes_per_cell)
+{
+    if (!h) return BGK_E_INVALID;
+    if (device_bytes) *device_bytes = (int64_t)(h->planes_bytes + h->stage_bytes);
+    if (bytes_per_cell) *bytes_per_cell = 18 * h->T.elem_bytes;
+    return BGK_OK;
+}
+
+int bgk_launch_count(bgk_handle *h, int64_t *launches)
+{
+    if (!h || !launches) return BGK_E_INVALID;
+    *launches = h->launches;
+    return BGK_OK;
+}
+
+int bgk_last_error(bgk_handle *h, char *buf, size_t len)
+{
+    if (!h || !buf || len == 0) return BGK_E_INVALID;
+    std::snprintf(buf, len, "%s", h->err.c_str());
+    return BGK_OK;
+}
+
+}  // extern "C"

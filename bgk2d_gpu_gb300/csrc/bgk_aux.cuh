@@ -1,0 +1,220 @@
+// bgk_aux.cuh -- state access, host-layout conversion and FP64 reductions (templated bodies).
+#pragma once
+
+#include "bgk_kernels.cuh"
+
+namespace bgk {
+
+// Post-collision value of direction q at interior cell (x, y), i.e. the reference's a_q(x, y)
+// after `collision` (SRC/col_MC.F90:311-341 swap included), for every scheme and phase.
+template <typename S, typename K, bool HAS_OBS>
+__device__ __forceinline__ K post_value(const Lattice &L, int cur, int phase, int q, int x, int y)
+{
+    const S *base = reinterpret_cast<const S *>(L.planes);
+    const int64_t pe = L.plane_elems;
+    if (L.scheme == 0) {
+        const int p = (q == D19) ? 8 : (cur ? 9 + q : q);
+        return ldq<S, K>(base + p * pe, cell_index<S>(L, x, y), q);
+    }
+    if (phase == 0 || q == D19) return ldq<S, K>(base + opp_of(q) * pe, cell_index<S>(L, x, y), q);
+    // phase 1: the value was pushed to x + c_q (or kept where the push rule put it)
+    int tx = x + cx_of(q), ty = y + cy_of(q);
+    if (ty < 1 || ty > L.ly) {
+        if (L.faces[ty < 1 ? YLO : YHI] != FK_PERIODIC) return ldq<S, K>(base + q * pe, cell_index<S>(L, tx, ty), q);
+        ty = ty < 1 ? L.ly : 1;
+    }
+    if (tx < 1 || tx > L.lx) {
+        if (L.faces[tx < 1 ? XLO : XHI] != FK_PERIODIC) return ldq<S, K>(base + q * pe, cell_index<S>(L, tx, ty), q);
+        tx = tx < 1 ? L.lx : 1;
+    }
+    if (HAS_OBS) {
+        if (obs_bit(L, tx, ty)) return ldq<S, K>(base + opp_of(q) * pe, cell_index<S>(L, x, y), q);
+    }
+    return ldq<S, K>(base + q * pe, cell_index<S>(L, tx, ty), q);
+}
+
+// host-kind staging plane (lx+2) x (ly+2), i fastest, -> device storage
+template <typename S, typename H>
+__global__ void scatter_plane_kernel(Lattice L, int cur, int q, const H *__restrict__ stage)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x > L.lx + 1) return;
+    S *base = reinterpret_cast<S *>(L.planes);
+    const int64_t pe = L.plane_elems;
+    int p;
+    if (L.scheme == 0) p = (q == D19) ? 8 : (cur ? 9 + q : q);
+    else p = opp_of(q);
+    const H v = stage[(int64_t)y * (L.lx + 2) + x];
+    base[p * pe + cell_index<S>(L, x, y)] = Store<S>::template putq<double>((double)v, q);
+}
+
+// device storage -> host-kind staging plane; ghost entries are written as zero
+template <typename S, typename K, typename H, bool HAS_OBS>
+__global__ void gather_plane_kernel(Lattice L, int cur, int phase, int q, H *__restrict__ stage)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x > L.lx + 1) return;
+    H v = (H)0;
+    if (x >= 1 && x <= L.lx && y >= 1 && y <= L.ly) v = (H)post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
+    stage[(int64_t)y * (L.lx + 2) + x] = v;
+}
+
+// AA phase-0 outflow ghosts at x = lx+1, from cell (lx, y)'s stored post-collision values
+template <typename S, typename K>
+__global__ void aa_fill_outflow_kernel(Lattice L)
+{
+    const int y = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (y > L.ly) return;
+    S *base = reinterpret_cast<S *>(L.planes);
+    const int64_t pe = L.plane_elems;
+    const int64_t i = cell_index<S>(L, L.lx, y);
+    K g[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) g[q] = ldq<S, K>(base + opp_of(q) * pe, i, q);
+    aa_outflow_ghost<S, K>(L, base, y, g);
+}
+
+// moments with the reference's per-cell arithmetic (SRC/diagno.F90:285-307)
+template <typename K>
+__device__ __forceinline__ void moments(const K (&a)[9], K &rho, K &xj, K &yj)
+{
+    const K cte1 = (K)1, uno = (K)1;
+    rho = ((((a[0] + a[1]) + a[4]) + a[5]) + (((a[2] + a[3]) + a[6]) + a[7]) + a[8]) + cte1;
+    K rhoinv = uno / rho;
+    xj = (((a[1] - a[5]) + (a[0] - a[4])) + (a[2] - a[6])) * rhoinv;
+    yj = (((a[1] - a[0]) + (a[5] - a[4])) + (a[3] - a[7])) * rhoinv;
+}
+
+template <int NT>
+__device__ __forceinline__ void block_sum4(double (&v)[4], double *out)
+{
+    __shared__ double sh[NT / 32][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_down_sync(0xffffffffu, v[i], o);
+    }
+    const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+    if (ln == 0) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) sh[w][i] = v[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s[4] = {0, 0, 0, 0};
+        for (int k = 0; k < NT / 32; ++k)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) s[i] += sh[k][i];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) out[i] = s[i];
+    }
+}
+
+constexpr int RED_NT = 256;
+
+// diagno: partial sums of rho, u, v, |u|^2 (FP64) per block
+template <typename S, typename K, bool HAS_OBS>
+__global__ void __launch_bounds__(RED_NT) diagno_kernel(Lattice L, int cur, int phase, int fluid_only, double *partial)
+{
+    double acc[4] = {0, 0, 0, 0};
+    const int64_t n = (int64_t)L.lx * L.ly;
+    for (int64_t c = (int64_t)blockIdx.x * RED_NT + threadIdx.x; c < n; c += (int64_t)gridDim.x * RED_NT) {
+        const int x = (int)(c % L.lx) + 1, y = (int)(c / L.lx) + 1;
+        if (HAS_OBS && fluid_only) {
+            if (obs_bit(L, x, y)) continue;
+        }
+        K a[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) a[q] = post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
+        K rho, xj, yj;
+        moments<K>(a, rho, xj, yj);
+        acc[0] += (double)xj;
+        acc[1] += (double)yj;
+        acc[2] += (double)rho;
+        acc[3] += (double)(xj * xj + yj * yj);
+    }
+    block_sum4<RED_NT>(acc, partial + 4 * blockIdx.x);
+}
+
+// residual: sum |u - u_prev|^2 and |u|^2 (FP64); the snapshot is refreshed
+template <typename S, typename K, bool HAS_OBS>
+__global__ void __launch_bounds__(RED_NT) residual_kernel(Lattice L, int cur, int phase, double *uprev, double *vprev,
+                                                          double *partial)
+{
+    double acc[4] = {0, 0, 0, 0};
+    const int64_t n = (int64_t)L.lx * L.ly;
+    for (int64_t c = (int64_t)blockIdx.x * RED_NT + threadIdx.x; c < n; c += (int64_t)gridDim.x * RED_NT) {
+        const int x = (int)(c % L.lx) + 1, y = (int)(c / L.lx) + 1;
+        if (HAS_OBS) {
+            if (obs_bit(L, x, y)) continue;
+        }
+        K a[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) a[q] = post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
+        K rho, xj, yj;
+        moments<K>(a, rho, xj, yj);
+        const double u = (double)xj, v = (double)yj;
+        const double du = u - uprev[c], dv = v - vprev[c];
+        acc[0] += du * du + dv * dv;
+        acc[1] += u * u + v * v;
+        acc[2] += (isfinite(u) && isfinite(v)) ? 0.0 : 1.0;
+        uprev[c] = u;
+        vprev[c] = v;
+    }
+    block_sum4<RED_NT>(acc, partial + 4 * blockIdx.x);
+}
+
+// momentum-exchange force on the obstacle (SRC/draglift.F90:405-441) over a box of cells
+template <typename S, typename K, bool HAS_OBS>
+__global__ void __launch_bounds__(RED_NT) draglift_kernel(Lattice L, int cur, int phase, int i0, int i1, int j0, int j1,
+                                                          double *partial)
+{
+    double acc[4] = {0, 0, 0, 0};
+    const int nx = i1 - i0 + 1, ny = j1 - j0 + 1;
+    const int64_t n = (int64_t)nx * ny;
+    for (int64_t c = (int64_t)blockIdx.x * RED_NT + threadIdx.x; c < n; c += (int64_t)gridDim.x * RED_NT) {
+        const int x = i0 + (int)(c % nx), y = j0 + (int)(c / nx);
+        if (!HAS_OBS) continue;
+        if (obs_bit(L, x, y)) continue;
+        K fx[8], fy[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int ox = x + cx_of(q), oy = y + cy_of(q);
+            const bool ob = ox >= 1 && ox <= L.lx && oy >= 1 && oy <= L.ly && obs_bit(L, ox, oy);
+            const K a = post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
+            const K o = ob ? (K)1 : (K)0;
+            fx[q] = (((K)2 * (K)cx_of(q)) * a) * o;
+            fy[q] = (((K)2 * (K)cy_of(q)) * a) * o;
+        }
+        K sx = ((((((fx[0] + fx[1]) + fx[2]) + fx[3]) + fx[4]) + fx[5]) + fx[6]) + fx[7];
+        K sy = ((((((fy[0] + fy[1]) + fy[2]) + fy[3]) + fy[4]) + fy[5]) + fy[6]) + fy[7];
+        acc[0] += (double)sx;
+        acc[1] += (double)sy;
+    }
+    block_sum4<RED_NT>(acc, partial + 4 * blockIdx.x);
+}
+
+// rho, u, v fields of the interior (double), i fastest
+template <typename S, typename K, bool HAS_OBS>
+__global__ void fields_kernel(Lattice L, int cur, int phase, double *rho, double *u, double *v)
+{
+    const int64_t n = (int64_t)L.lx * L.ly;
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        const int x = (int)(c % L.lx) + 1, y = (int)(c / L.lx) + 1;
+        K a[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) a[q] = post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
+        K r, xj, yj;
+        moments<K>(a, r, xj, yj);
+        rho[c] = (double)r;
+        u[c] = (double)xj;
+        v[c] = (double)yj;
+    }
+}
+
+// fixed-order sum of nb partial 4-vectors (deterministic)
+__global__ void finalize4_kernel(const double *partial, int nb, double *out);
+
+}  // namespace bgk

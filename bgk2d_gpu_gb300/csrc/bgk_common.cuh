@@ -1,0 +1,125 @@
+// bgk_common.cuh -- shared device definitions for the GB300 D2Q9 BGK step.
+//
+// Direction order and vectors follow the reference (SRC/bgk2d.F90:29-39):
+//   q : 01      03     05     08     10       12      14      17      19
+//   c : (1,-1) (1,1)  (1,0)  (0,1)  (-1,-1)  (-1,1)  (-1,0)  (0,-1)  (0,0)
+// Populations are stored as deviations f_q - w_q (the reference's "shifted" form,
+// SRC/col_MC.F90:70-75).
+//
+// HBM layout of one domain ("lattice"): SoA planes.  Plane p holds rows y = 0..ly+1 (ghost
+// rows included), each row `pitch` elements long; cell (x, y), x = 0..lx+1, sits at element
+//   p * plane_elems + y * pitch + xoff + x,   xoff = VEC - 1,
+// so that interior cell x = 1 starts a 16-byte vector (VEC = 16 / sizeof(storage)).
+// Ping-pong keeps planes 0..7 (moving, buffer A), 8 (rest, updated in place like a19 in
+// SRC/col_MC.F90:293) and 9..16 (moving, buffer B).  AA keeps planes 0..8 only.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace bgk {
+
+constexpr int Q = 9;
+constexpr int D01 = 0, D03 = 1, D05 = 2, D08 = 3, D10 = 4, D12 = 5, D14 = 6, D17 = 7, D19 = 8;
+
+__host__ __device__ constexpr int cx_of(int q) {
+    return q == D01 ? 1 : q == D03 ? 1 : q == D05 ? 1 : q == D08 ? 0 : q == D10 ? -1 : q == D12 ? -1 : q == D14 ? -1 : 0;
+}
+__host__ __device__ constexpr int cy_of(int q) {
+    return q == D01 ? -1 : q == D03 ? 1 : q == D05 ? 0 : q == D08 ? 1 : q == D10 ? -1 : q == D12 ? 1 : q == D14 ? 0 : q == D17 ? -1 : 0;
+}
+// opposite direction: 01<->12, 03<->10, 05<->14, 08<->17, 19<->19
+__host__ __device__ constexpr int opp_of(int q) {
+    return q == D01 ? D12 : q == D03 ? D10 : q == D05 ? D14 : q == D08 ? D17 : q == D10 ? D03 : q == D12 ? D01 : q == D14 ? D05 : q == D17 ? D08 : D19;
+}
+
+enum Face { XLO = 0, XHI = 1, YLO = 2, YHI = 3 };
+enum FaceKind { FK_WALL = 0, FK_PERIODIC = 1, FK_INFLOW = 2, FK_OUTFLOW_EQ = 3, FK_OUTFLOW_ZG = 4 };
+
+// 16-bit storage keeps (f_q - w_q) * s_q with a power-of-two s_q close to 1/w_q, so the
+// scaling is exact and only the 16-bit rounding loses information.
+__host__ __device__ constexpr float scale_of(int q) {
+    return q == D19 ? 2.0f : ((q == D05 || q == D08 || q == D14 || q == D17) ? 8.0f : 32.0f);
+}
+
+// Storage traits: conversion between the stored element and the compute kind K.
+template <typename S> struct Store;
+template <> struct Store<float> {
+    static constexpr int VEC = 4;
+    template <typename K, int q> __device__ __forceinline__ static K get(float v) { return (K)v; }
+    template <typename K, int q> __device__ __forceinline__ static float put(K v) { return (float)v; }
+    template <typename K> __device__ __forceinline__ static K getq(float v, int) { return (K)v; }
+    template <typename K> __device__ __forceinline__ static float putq(K v, int) { return (float)v; }
+};
+template <> struct Store<double> {
+    static constexpr int VEC = 2;
+    template <typename K, int q> __device__ __forceinline__ static K get(double v) { return (K)v; }
+    template <typename K, int q> __device__ __forceinline__ static double put(K v) { return (double)v; }
+    template <typename K> __device__ __forceinline__ static K getq(double v, int) { return (K)v; }
+    template <typename K> __device__ __forceinline__ static double putq(K v, int) { return (double)v; }
+};
+template <> struct Store<__half> {
+    static constexpr int VEC = 8;
+    template <typename K, int q> __device__ __forceinline__ static K get(__half v) {
+        return (K)(__half2float(v) * (1.0f / scale_of(q)));
+    }
+    template <typename K, int q> __device__ __forceinline__ static __half put(K v) {
+        return __float2half_rn((float)v * scale_of(q));
+    }
+    template <typename K> __device__ __forceinline__ static K getq(__half v, int q) {
+        return (K)(__half2float(v) * (1.0f / scale_of(q)));
+    }
+    template <typename K> __device__ __forceinline__ static __half putq(K v, int q) {
+        return __float2half_rn((float)v * scale_of(q));
+    }
+};
+template <> struct Store<__nv_bfloat16> {
+    static constexpr int VEC = 8;
+    template <typename K, int q> __device__ __forceinline__ static K get(__nv_bfloat16 v) {
+        return (K)(__bfloat162float(v) * (1.0f / scale_of(q)));
+    }
+    template <typename K, int q> __device__ __forceinline__ static __nv_bfloat16 put(K v) {
+        return __float2bfloat16_rn((float)v * scale_of(q));
+    }
+    template <typename K> __device__ __forceinline__ static K getq(__nv_bfloat16 v, int q) {
+        return (K)(__bfloat162float(v) * (1.0f / scale_of(q)));
+    }
+    template <typename K> __device__ __forceinline__ static __nv_bfloat16 putq(K v, int q) {
+        return __float2bfloat16_rn((float)v * scale_of(q));
+    }
+};
+
+// One domain as the kernels see it.  Scalars of the compute kind are kept in double and
+// cast in the kernel (exact for both kinds, since they were computed in that kind).
+struct Lattice {
+    void *planes;            // base of all planes (storage elements)
+    int64_t plane_elems;     // elements per plane (rows * pitch, padded)
+    int32_t pitch;           // elements per row
+    int32_t lx, ly;          // interior size
+    int32_t nvec;            // ceil(lx / VEC)
+    int32_t scheme;          // 0 ping-pong, 1 AA
+    int32_t faces[4];        // FaceKind per face
+    double wt[4][9];         // wall term added to the bounced population, per face and direction
+    double omega, fgrad;     // relaxation rate and body-force gradient (compute kind)
+    int32_t forced;          // 1 when the x body force fgrad*rho is applied (CHANNEL)
+    const double *inflow;    // [3][ly+2] equilibrium deviations of 01,03,05 at the x_lo inflow
+    const uint32_t *mask;    // obstacle bits, row y (0..ly+1) at mask + y*mask_pitch, bit x
+    int32_t mask_pitch;      // 32-bit words per mask row
+    int32_t ob_x0, ob_x1, ob_y0, ob_y1;  // cells whose pull may touch an obstacle
+};
+
+template <typename S> __host__ __device__ constexpr int vec_of() { return 16 / (int)sizeof(S); }
+
+template <typename S>
+__device__ __forceinline__ int64_t cell_index(const Lattice &L, int x, int y) {
+    return (int64_t)y * L.pitch + (vec_of<S>() - 1) + x;
+}
+
+__device__ __forceinline__ bool obs_bit(const Lattice &L, int x, int y) {
+    uint32_t w = __ldg(L.mask + (int64_t)y * L.mask_pitch + (x >> 5));
+    return (w >> (x & 31)) & 1u;
+}
+
+}  // namespace bgk

@@ -1,0 +1,117 @@
+// bgk_instantiate.cuh -- builds the KernelTable of one (storage S, compute K) pair.
+// Each bgk_inst_*.cu translation unit includes this once, so the pairs compile in parallel.
+#pragma once
+
+#include "bgk_aux.cuh"
+#include "bgk_table.h"
+
+namespace bgk {
+namespace inst {
+
+template <typename S> using Host = typename std::conditional<std::is_same<S, double>::value, double, float>::type;
+
+template <typename S, typename K, int TXV, int TY, bool OBS>
+cudaError_t step_cfg(int kind, const Lattice &L, int parity, cudaStream_t st)
+{
+    const dim3 block(TXV, TY);
+    const dim3 grid((unsigned)((L.nvec + TXV - 1) / TXV), (unsigned)((L.ly + TY - 1) / TY));
+    if (kind == STEP_PP) pp_kernel<S, K, TXV, TY, OBS><<<grid, block, 0, st>>>(L, parity);
+    else if (kind == STEP_AA_P) aa_p_kernel<S, K, TXV, TY, OBS><<<grid, block, 0, st>>>(L);
+    else aa_l_kernel<S, K, TXV, TY, OBS><<<grid, block, 0, st>>>(L);
+    return cudaGetLastError();
+}
+
+template <typename S, typename K, bool OBS>
+cudaError_t step_obs(int kind, const Lattice &L, int parity, int cfg, cudaStream_t st)
+{
+    switch (cfg) {
+    case 0: return step_cfg<S, K, 32, 4, OBS>(kind, L, parity, st);
+    case 1: return step_cfg<S, K, 64, 2, OBS>(kind, L, parity, st);
+    case 3: return step_cfg<S, K, 128, 2, OBS>(kind, L, parity, st);
+    default: return step_cfg<S, K, 128, 1, OBS>(kind, L, parity, st);
+    }
+}
+
+template <typename S, typename K>
+cudaError_t step(int kind, const Lattice &L, int parity, bool obs, int cfg, cudaStream_t st)
+{
+    return obs ? step_obs<S, K, true>(kind, L, parity, cfg, st) : step_obs<S, K, false>(kind, L, parity, cfg, st);
+}
+
+template <typename S>
+cudaError_t scatter(const Lattice &L, int cur, int q, const void *stage, cudaStream_t st)
+{
+    const dim3 block(256), grid((unsigned)((L.lx + 2 + 255) / 256), (unsigned)(L.ly + 2));
+    scatter_plane_kernel<S, Host<S>><<<grid, block, 0, st>>>(L, cur, q, reinterpret_cast<const Host<S> *>(stage));
+    return cudaGetLastError();
+}
+
+template <typename S, typename K>
+cudaError_t gather(const Lattice &L, int cur, int phase, int q, void *stage, bool obs, cudaStream_t st)
+{
+    const dim3 block(256), grid((unsigned)((L.lx + 2 + 255) / 256), (unsigned)(L.ly + 2));
+    if (obs) gather_plane_kernel<S, K, Host<S>, true><<<grid, block, 0, st>>>(L, cur, phase, q, reinterpret_cast<Host<S> *>(stage));
+    else gather_plane_kernel<S, K, Host<S>, false><<<grid, block, 0, st>>>(L, cur, phase, q, reinterpret_cast<Host<S> *>(stage));
+    return cudaGetLastError();
+}
+
+template <typename S, typename K>
+cudaError_t fill_outflow(const Lattice &L, cudaStream_t st)
+{
+    aa_fill_outflow_kernel<S, K><<<(L.ly + 127) / 128, 128, 0, st>>>(L);
+    return cudaGetLastError();
+}
+
+template <typename S, typename K>
+cudaError_t diagno(const Lattice &L, int cur, int phase, int fluid_only, bool obs, double *partial, int nb, cudaStream_t st)
+{
+    if (obs) diagno_kernel<S, K, true><<<nb, RED_NT, 0, st>>>(L, cur, phase, fluid_only, partial);
+    else diagno_kernel<S, K, false><<<nb, RED_NT, 0, st>>>(L, cur, phase, fluid_only, partial);
+    return cudaGetLastError();
+}
+
+template <typename S, typename K>
+cudaError_t residual(const Lattice &L, int cur, int phase, bool obs, double *uprev, double *vprev, double *partial, int nb,
+                     cudaStream_t st)
+{
+    if (obs) residual_kernel<S, K, true><<<nb, RED_NT, 0, st>>>(L, cur, phase, uprev, vprev, partial);
+    else residual_kernel<S, K, false><<<nb, RED_NT, 0, st>>>(L, cur, phase, uprev, vprev, partial);
+    return cudaGetLastError();
+}
+
+template <typename S, typename K>
+cudaError_t draglift(const Lattice &L, int cur, int phase, int i0, int i1, int j0, int j1, double *partial, int nb,
+                     cudaStream_t st)
+{
+    draglift_kernel<S, K, true><<<nb, RED_NT, 0, st>>>(L, cur, phase, i0, i1, j0, j1, partial);
+    return cudaGetLastError();
+}
+
+template <typename S, typename K>
+cudaError_t fields(const Lattice &L, int cur, int phase, bool obs, double *rho, double *u, double *v, cudaStream_t st)
+{
+    const int nb = 4 * 152;
+    if (obs) fields_kernel<S, K, true><<<nb, 256, 0, st>>>(L, cur, phase, rho, u, v);
+    else fields_kernel<S, K, false><<<nb, 256, 0, st>>>(L, cur, phase, rho, u, v);
+    return cudaGetLastError();
+}
+
+template <typename S, typename K>
+KernelTable make_table()
+{
+    KernelTable t;
+    t.vec = vec_of<S>();
+    t.elem_bytes = (int)sizeof(S);
+    t.step = &step<S, K>;
+    t.scatter = &scatter<S>;
+    t.gather = &gather<S, K>;
+    t.fill_outflow = &fill_outflow<S, K>;
+    t.diagno = &diagno<S, K>;
+    t.residual = &residual<S, K>;
+    t.draglift = &draglift<S, K>;
+    t.fields = &fields<S, K>;
+    return t;
+}
+
+}  // namespace inst
+}  // namespace bgk

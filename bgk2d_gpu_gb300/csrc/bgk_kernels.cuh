@@ -1,0 +1,624 @@
+// bgk_kernels.cuh -- fused stream + collide kernels for one lattice (templated bodies).
+//
+// Ping-pong (PP): the pull form of SRC/col_MC.F90:97-293.  Cell (x,y) reads population q from
+// (x - c_q) in the source buffer, relaxes, and writes the destination buffer at (x,y); the
+// rest population is updated in place (col_MC.F90:293).  The ghost-frame fills of
+// SRC/bcond.*.F90 are folded into the pull: a source outside the interior is replaced by the
+// value the reference's boundary routine would have written there, and an obstacle source by
+// the value SRC/bcond.obs.F90:59-71 would have written (the pulling cell's own opposite
+// population).
+//
+// AA: one buffer.  Phase 0 holds post-collision values in swapped slots (plane opp(q) at x holds
+// f*_q(x)); the "P" step pulls from the neighbours' swapped slots, relaxes and pushes to
+// (x + c_q) in plane q (phase 1: streamed, pre-collision values); the "L" step is purely local
+// and returns to phase 0.  Every cell reads and writes the same nine slots, so the update is
+// in place.  Boundary rules are applied in the P step when pulling and when pushing.
+//
+// All arithmetic is one IEEE operation per reference operation: this file is compiled with
+// -fmad=false for the FP32/FP64 kinds so that results are bit-identical to the reference's
+// serial arithmetic; the 16-bit storage kernels are compiled with contraction enabled.
+#pragma once
+
+#include "bgk_common.cuh"
+
+namespace bgk {
+
+// ---------------------------------------------------------------------------------------------
+// collision: SRC/col_MC.F90:128-176 (equilibrium) and :285-293 (relaxation + body force)
+// ---------------------------------------------------------------------------------------------
+template <typename K>
+__device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced)
+{
+    const K uno = (K)1, cte1 = (K)1, cte0 = uno - cte1;
+    const K tre = (K)3, qf = (K)1.5, rf = (K)3;
+    const K p0 = (K)(4.0 / 9.0), p1 = (K)(1.0 / 9.0), p2 = (K)(1.0 / 36.0);
+    K x01 = x[0], x03 = x[1], x05 = x[2], x08 = x[3], x10 = x[4];
+    K x12 = x[5], x14 = x[6], x17 = x[7], x19 = x[8];
+    K rho = ((((x01 + x03) + x10) + x12) + (((x05 + x08) + x14) + x17) + x19) + cte1;
+    K rhoinv = uno / rho;
+    K vx = (((x03 - x12) + (x01 - x10)) + (x05 - x14)) * rhoinv;
+    K vy = (((x03 - x01) + (x12 - x10)) + (x08 - x17)) * rhoinv;
+    K vx2 = vx * vx;
+    K vy2 = vy * vy;
+    K vsq = vx2 + vy2;
+    K vxpy = vx + vy;
+    K vxmy = vx - vy;
+    K qxpy = cte0 + qf * ((tre * vxpy) * vxpy - vsq);
+    K qxmy = cte0 + qf * ((tre * vxmy) * vxmy - vsq);
+    K qx = cte0 + qf * (tre * vx2 - vsq);
+    K qy = cte0 + qf * (tre * vy2 - vsq);
+    K q0 = cte0 + qf * (-vsq);
+    vx = rf * vx;
+    vy = rf * vy;
+    vxpy = rf * vxpy;
+    vxmy = rf * vxmy;
+    K rp0 = rho * p0;
+    K rp1 = rho * p1;
+    K rp2 = rho * p2;
+    K e01 = rp2 * (vxmy + qxmy) + cte1 * (rp2 - p2);
+    K e03 = rp2 * (vxpy + qxpy) + cte1 * (rp2 - p2);
+    K e05 = rp1 * (vx + qx) + cte1 * (rp1 - p1);
+    K e08 = rp1 * (vy + qy) + cte1 * (rp1 - p1);
+    K e10 = rp2 * (-vxpy + qxpy) + cte1 * (rp2 - p2);
+    K e12 = rp2 * (-vxmy + qxmy) + cte1 * (rp2 - p2);
+    K e14 = rp1 * (-vx + qx) + cte1 * (rp1 - p1);
+    K e17 = rp1 * (-vy + qy) + cte1 * (rp1 - p1);
+    K e19 = rp0 * (q0) + cte1 * (rp0 - p0);
+    K fx = (K)0, fy = (K)0;
+    if (forced) fx = fgrad * rho;
+    x[0] = (x01 - omega * (x01 - e01)) + (fx - fy);
+    x[1] = (x03 - omega * (x03 - e03)) + (fx + fy);
+    x[2] = (x05 - omega * (x05 - e05)) + (fx);
+    x[3] = (x08 - omega * (x08 - e08)) + (fy);
+    x[4] = (x10 - omega * (x10 - e10)) + ((-fx) - fy);
+    x[5] = (x12 - omega * (x12 - e12)) + ((-fx) + fy);
+    x[6] = (x14 - omega * (x14 - e14)) + (-fx);
+    x[7] = (x17 - omega * (x17 - e17)) + (-fy);
+    x[8] = x19 - omega * (x19 - e19);
+}
+
+// equilibrium deviation of the outflow ghost (rho = 1, local u): bcond.inflow.F90:211-230
+template <typename K>
+__device__ __forceinline__ K outflow_eq(int q, K a01, K a03, K a05, K a08, K a10, K a12, K a14, K a17)
+{
+    const K rhoinv = (K)1, crho = (K)1, cte1 = (K)0, rf = (K)3, qf = (K)1.5;
+    const K p1 = (K)(1.0 / 9.0), p2 = (K)(1.0 / 36.0);
+    K xj = (((a03 - a12) + (a01 - a10)) + (a05 - a14)) * rhoinv;
+    K yj = (((a03 - a01) + (a12 - a10)) + (a08 - a17)) * rhoinv;
+    K cvsq = xj * xj + yj * yj;
+    if (q == D10) {
+        K c = rf * (-xj - yj) + qf * (((K)3 * (xj + yj)) * (xj + yj) - cvsq);
+        return (crho * p2) * (cte1 + c);
+    } else if (q == D12) {
+        K c = rf * (-xj + yj) + qf * (((K)3 * (xj - yj)) * (xj - yj) - cvsq);
+        return (crho * p2) * (cte1 + c);
+    } else {
+        K c = rf * (-xj) + qf * (((K)3 * (xj)) * (xj) - cvsq);
+        return (crho * p1) * (cte1 + c);
+    }
+}
+
+// value rounded through the storage kind of plane q (a ghost value lives in storage)
+template <typename S, typename K>
+__device__ __forceinline__ K rnd(int q, K v) { return Store<S>::template getq<K>(Store<S>::template putq<K>(v, q), q); }
+
+template <typename S, typename K>
+__device__ __forceinline__ K ldq(const S *plane, int64_t i, int q) { return Store<S>::template getq<K>(plane[i], q); }
+
+// 16-byte vector access
+template <typename S> union V16 {
+    uint4 u;
+    S s[16 / sizeof(S)];
+};
+
+template <typename S>
+__device__ __forceinline__ void ldv(const S *p, S (&o)[16 / sizeof(S)])
+{
+    V16<S> t;
+    t.u = __ldg(reinterpret_cast<const uint4 *>(p));
+#pragma unroll
+    for (int c = 0; c < 16 / (int)sizeof(S); ++c) o[c] = t.s[c];
+}
+template <typename S>
+__device__ __forceinline__ void stv(S *p, const S (&v)[16 / sizeof(S)])
+{
+    V16<S> t;
+#pragma unroll
+    for (int c = 0; c < 16 / (int)sizeof(S); ++c) t.s[c] = v[c];
+    *reinterpret_cast<uint4 *>(p) = t.u;
+}
+
+template <typename K>
+__device__ __forceinline__ K shfl_up(K v, int w) { return __shfl_up_sync(0xffffffffu, v, 1, w); }
+template <typename K>
+__device__ __forceinline__ K shfl_down(K v, int w) { return __shfl_down_sync(0xffffffffu, v, 1, w); }
+
+// Load VEC consecutive values of direction q pulled from (x - c_q): aligned 16-byte load of
+// row y - cy at the thread's own columns; the +-1 column shift comes from the neighbouring
+// lane, or from one scalar load at a segment edge.
+template <typename S, typename K, int q, int W>
+__device__ __forceinline__ void pull_vec(const Lattice &L, const S *plane, int xv, int y, bool loads,
+                                         int seg_lane, K (&out)[vec_of<S>()])
+{
+    constexpr int VEC = vec_of<S>();
+    constexpr int sx = -cx_of(q), sy = -cy_of(q);
+    const int64_t idx = cell_index<S>(L, xv, y + sy);
+    S v[VEC];
+    if (loads) ldv<S>(plane + idx, v);
+    else {
+#pragma unroll
+        for (int c = 0; c < VEC; ++c) v[c] = S(0.0f);
+    }
+    K kv[VEC];
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) kv[c] = Store<S>::template get<K, q>(v[c]);
+    if (sx == 0) {
+#pragma unroll
+        for (int c = 0; c < VEC; ++c) out[c] = kv[c];
+    } else if (sx == -1) {
+        K left = shfl_up(kv[VEC - 1], W);
+        if ((seg_lane % W) == 0 && loads) left = Store<S>::template get<K, q>(plane[idx - 1]);
+        out[0] = left;
+#pragma unroll
+        for (int c = 1; c < VEC; ++c) out[c] = kv[c - 1];
+    } else {
+        K right = shfl_down(kv[0], W);
+        if ((seg_lane % W) == W - 1 && loads) right = Store<S>::template get<K, q>(plane[idx + VEC]);
+#pragma unroll
+        for (int c = 0; c < VEC - 1; ++c) out[c] = kv[c + 1];
+        out[VEC - 1] = right;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Boundary rules for one pulled value.  (sx, sy) is the source of direction q for cell (x, y).
+// The y-face rule is applied first and wins at corners, as the reference's y-loop runs after
+// its x-loop (e.g. SRC/bcond.driven.F90:100-108 then :136-143).
+//   plane_of(q, cx, cy): element holding the value of direction q "at" (cx, cy) in the
+//   current state; own(q): the pulling cell's own post-collision value of direction q.
+// ---------------------------------------------------------------------------------------------
+template <typename S, typename K, bool HAS_OBS, typename PlaneAt, typename Own, typename Ghost>
+__device__ __forceinline__ K pull_rule(const Lattice &L, int q, int x, int y, PlaneAt plane_at, Own own,
+                                       Ghost ghost_xhi)
+{
+    int sx = x - cx_of(q), sy = y - cy_of(q);
+    const int l = L.lx, m = L.ly;
+    const int oq = opp_of(q);
+    if (sy < 1 || sy > m) {
+        const int f = sy < 1 ? YLO : YHI;
+        if (L.faces[f] == FK_PERIODIC) {
+            sy = (sy < 1) ? m : 1;
+        } else {
+            K v = own(oq);
+            const K wt = (K)L.wt[f][q];
+            return wt != (K)0 ? rnd<S, K>(q, v + wt) : v;
+        }
+    }
+    if (sx < 1 || sx > l) {
+        const int f = sx < 1 ? XLO : XHI;
+        const int kind = L.faces[f];
+        if (kind == FK_PERIODIC) {
+            sx = (sx < 1) ? l : 1;
+        } else if (kind == FK_WALL) {
+            K v = own(oq);
+            const K wt = (K)L.wt[f][q];
+            return wt != (K)0 ? rnd<S, K>(q, v + wt) : v;
+        } else if (kind == FK_INFLOW) {
+            // directions 01, 03, 05 enter through x_lo
+            const int t = (q == D01) ? 0 : (q == D03) ? 1 : 2;
+            return rnd<S, K>(q, (K)L.inflow[(int64_t)t * (m + 2) + sy]);
+        } else {
+            return ghost_xhi(q, sy);
+        }
+    }
+    if (HAS_OBS) {
+        if (obs_bit(L, sx, sy)) return own(oq);
+    }
+    return plane_at(q, sx, sy);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Ping-pong kernel
+// ---------------------------------------------------------------------------------------------
+template <typename S, typename K, bool HAS_OBS>
+__device__ void pp_cell_slow(const Lattice &L, const S *src, S *dst, S *rest, int x, int y)
+{
+    const int64_t pe = L.plane_elems;
+    const int64_t me = cell_index<S>(L, x, y);
+    auto plane_at = [&](int q, int sx, int sy) -> K { return ldq<S, K>(src + q * pe, cell_index<S>(L, sx, sy), q); };
+    auto own = [&](int q) -> K { return ldq<S, K>(src + q * pe, me, q); };
+    auto ghost_xhi = [&](int q, int sy) -> K {
+        const int l = L.lx;
+        if (L.faces[XHI] == FK_OUTFLOW_ZG) return plane_at(q, l, sy);
+        const int64_t i = cell_index<S>(L, l, sy);
+        K a[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = ldq<S, K>(src + k * pe, i, k);
+        return rnd<S, K>(q, outflow_eq<K>(q, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7]));
+    };
+    K v[9];
+#pragma unroll 1
+    for (int q = 0; q < 8; ++q) v[q] = pull_rule<S, K, HAS_OBS>(L, q, x, y, plane_at, own, ghost_xhi);
+    v[8] = ldq<S, K>(rest, me, D19);
+    collide<K>(v, (K)L.omega, (K)L.fgrad, L.forced != 0);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) dst[q * pe + me] = Store<S>::template putq<K>(v[q], q);
+    rest[me] = Store<S>::template putq<K>(v[8], D19);
+}
+
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS>
+__global__ void __launch_bounds__(TXV *TY) pp_kernel(const Lattice L, const int parity)
+{
+    constexpr int VEC = vec_of<S>();
+    constexpr int W = TXV < 32 ? TXV : 32;
+    const int tx = threadIdx.x;
+    const int k = blockIdx.x * TXV + tx;
+    const int y = blockIdx.y * TY + threadIdx.y + 1;
+    const bool in_rows = y <= L.ly;
+    const bool loads = in_rows && k <= L.nvec;
+    const bool active = in_rows && k < L.nvec;
+    const int xv = 1 + k * VEC;
+    const int64_t pe = L.plane_elems;
+    S *base = reinterpret_cast<S *>(L.planes);
+    const S *src = base + (parity ? 9 : 0) * pe;
+    S *dst = base + (parity ? 0 : 9) * pe;
+    S *rest = base + 8 * pe;
+
+    K x[9][VEC];
+    pull_vec<S, K, D01, W>(L, src + D01 * pe, xv, y, loads, tx, x[D01]);
+    pull_vec<S, K, D03, W>(L, src + D03 * pe, xv, y, loads, tx, x[D03]);
+    pull_vec<S, K, D05, W>(L, src + D05 * pe, xv, y, loads, tx, x[D05]);
+    pull_vec<S, K, D08, W>(L, src + D08 * pe, xv, y, loads, tx, x[D08]);
+    pull_vec<S, K, D10, W>(L, src + D10 * pe, xv, y, loads, tx, x[D10]);
+    pull_vec<S, K, D12, W>(L, src + D12 * pe, xv, y, loads, tx, x[D12]);
+    pull_vec<S, K, D14, W>(L, src + D14 * pe, xv, y, loads, tx, x[D14]);
+    pull_vec<S, K, D17, W>(L, src + D17 * pe, xv, y, loads, tx, x[D17]);
+    pull_vec<S, K, D19, W>(L, rest, xv, y, loads, tx, x[D19]);
+    if (!active) return;
+
+    bool slow = (y == 1) || (y == L.ly) || (k == 0) || (k == L.nvec - 1);
+    if (HAS_OBS) slow = slow || (y >= L.ob_y0 && y <= L.ob_y1 && xv + VEC - 1 >= L.ob_x0 && xv <= L.ob_x1);
+    if (slow) {
+        const int xe = min(xv + VEC - 1, L.lx);
+#pragma unroll 1
+        for (int xc = xv; xc <= xe; ++xc) pp_cell_slow<S, K, HAS_OBS>(L, src, dst, rest, xc, y);
+        return;
+    }
+    const K omega = (K)L.omega, fgrad = (K)L.fgrad;
+    const bool forced = L.forced != 0;
+    S o[9][VEC];
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) {
+        K v[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) v[q] = x[q][c];
+        collide<K>(v, omega, fgrad, forced);
+        o[0][c] = Store<S>::template put<K, D01>(v[0]);
+        o[1][c] = Store<S>::template put<K, D03>(v[1]);
+        o[2][c] = Store<S>::template put<K, D05>(v[2]);
+        o[3][c] = Store<S>::template put<K, D08>(v[3]);
+        o[4][c] = Store<S>::template put<K, D10>(v[4]);
+        o[5][c] = Store<S>::template put<K, D12>(v[5]);
+        o[6][c] = Store<S>::template put<K, D14>(v[6]);
+        o[7][c] = Store<S>::template put<K, D17>(v[7]);
+        o[8][c] = Store<S>::template put<K, D19>(v[8]);
+    }
+    const int64_t me = cell_index<S>(L, xv, y);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) stv<S>(dst + q * pe + me, o[q]);
+    stv<S>(rest + me, o[8]);
+}
+
+// ---------------------------------------------------------------------------------------------
+// AA kernels
+// ---------------------------------------------------------------------------------------------
+
+// Where the value of direction q pushed by (x, y) is needed next, and what it must be.
+// Returns false when the push leaves the domain through a face that absorbs it.
+template <typename S, typename K, bool HAS_OBS>
+__device__ __forceinline__ void aa_push_rule(const Lattice &L, S *base, int q, int x, int y, K g)
+{
+    const int64_t pe = L.plane_elems;
+    const int l = L.lx, m = L.ly;
+    int tx = x + cx_of(q), ty = y + cy_of(q);
+    const int oq = opp_of(q);
+    const S gs = Store<S>::template putq<K>(g, q);
+    if (ty < 1 || ty > m) {
+        const int f = ty < 1 ? YLO : YHI;
+        if (L.faces[f] == FK_PERIODIC) {
+            ty = (ty < 1) ? m : 1;
+        } else {
+            base[q * pe + cell_index<S>(L, tx, ty)] = gs;  // raw value kept in the ghost frame
+            const K wt = (K)L.wt[f][oq];
+            const S b = wt != (K)0 ? Store<S>::template putq<K>(g + wt, oq) : Store<S>::template putq<K>(g, oq);
+            base[oq * pe + cell_index<S>(L, x, y)] = b;
+            return;
+        }
+    }
+    if (tx < 1 || tx > l) {
+        const int f = tx < 1 ? XLO : XHI;
+        const int kind = L.faces[f];
+        if (kind == FK_PERIODIC) {
+            tx = (tx < 1) ? l : 1;
+        } else {
+            base[q * pe + cell_index<S>(L, tx, ty)] = gs;
+            if (kind == FK_WALL) {
+                const K wt = (K)L.wt[f][oq];
+                const S b = wt != (K)0 ? Store<S>::template putq<K>(g + wt, oq) : Store<S>::template putq<K>(g, oq);
+                base[oq * pe + cell_index<S>(L, x, y)] = b;
+            }
+            return;
+        }
+    }
+    if (HAS_OBS) {
+        if (obs_bit(L, tx, ty)) {
+            base[oq * pe + cell_index<S>(L, x, y)] = Store<S>::template putq<K>(g, oq);
+            return;
+        }
+    }
+    base[q * pe + cell_index<S>(L, tx, ty)] = gs;
+}
+
+// values entering (x, y) next step from an x_lo inflow or x_hi outflow ghost (the cells that
+// own those slots write them); g holds the post-collision values of (x, y), already rounded
+// through storage.
+template <typename S, typename K>
+__device__ __forceinline__ void aa_incoming(const Lattice &L, S *base, int x, int y, const K (&g)[9])
+{
+    const int64_t pe = L.plane_elems;
+    const int l = L.lx, m = L.ly;
+    if (x == 1 && L.faces[XLO] == FK_INFLOW) {
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            const int q = t == 0 ? D01 : t == 1 ? D03 : D05;
+            int sy = y - cy_of(q);
+            if (sy < 1 || sy > m) {
+                if (L.faces[sy < 1 ? YLO : YHI] != FK_PERIODIC) continue;  // bounced instead
+                sy = sy < 1 ? m : 1;
+            }
+            base[q * pe + cell_index<S>(L, x, y)] =
+                Store<S>::template putq<K>((K)L.inflow[(int64_t)t * (m + 2) + sy], q);
+        }
+    }
+    if (x == l && (L.faces[XHI] == FK_OUTFLOW_EQ || L.faces[XHI] == FK_OUTFLOW_ZG)) {
+        // cell (l, y) supplies direction q of cell (l, y + cy_q) for q = 10, 12, 14
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            const int q = t == 0 ? D10 : t == 1 ? D12 : D14;
+            int ty = y + cy_of(q);
+            if (ty < 1 || ty > m) {
+                if (L.faces[ty < 1 ? YLO : YHI] != FK_PERIODIC) continue;
+                ty = ty < 1 ? m : 1;
+            }
+            K v = (L.faces[XHI] == FK_OUTFLOW_ZG)
+                      ? g[q]
+                      : outflow_eq<K>(q, g[0], g[1], g[2], g[3], g[4], g[5], g[6], g[7]);
+            base[q * pe + cell_index<S>(L, l, ty)] = Store<S>::template putq<K>(v, q);
+        }
+    }
+}
+
+// Phase-0 ghost column x = lx+1 for outflow faces: value of direction q (10,12,14) at
+// (lx+1, y), stored in plane opp(q), computed from cell (lx, y)'s post-collision values.
+template <typename S, typename K>
+__device__ __forceinline__ void aa_outflow_ghost(const Lattice &L, S *base, int y, const K (&g)[9])
+{
+    const int64_t pe = L.plane_elems;
+    const int l = L.lx;
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+        const int q = t == 0 ? D10 : t == 1 ? D12 : D14;
+        K v = (L.faces[XHI] == FK_OUTFLOW_ZG) ? g[q]
+                                              : outflow_eq<K>(q, g[0], g[1], g[2], g[3], g[4], g[5], g[6], g[7]);
+        base[opp_of(q) * pe + cell_index<S>(L, l + 1, y)] = Store<S>::template putq<K>(v, q);
+    }
+}
+
+template <typename S, typename K, bool HAS_OBS>
+__device__ void aa_p_cell_slow(const Lattice &L, S *base, int x, int y)
+{
+    const int64_t pe = L.plane_elems;
+    const int64_t me = cell_index<S>(L, x, y);
+    if (HAS_OBS) {
+        if (obs_bit(L, x, y)) return;  // obstacle interiors are not advanced by the AA scheme
+    }
+    // phase 0: f*_q(c) is in plane opp(q) at c
+    auto plane_at = [&](int q, int sx, int sy) -> K {
+        const int oq = opp_of(q);
+        return ldq<S, K>(base + oq * pe, cell_index<S>(L, sx, sy), q);
+    };
+    auto own = [&](int q) -> K { return ldq<S, K>(base + opp_of(q) * pe, me, q); };
+    auto ghost_xhi = [&](int q, int sy) -> K { return plane_at(q, L.lx + 1, sy); };
+    K v[9];
+#pragma unroll 1
+    for (int q = 0; q < 8; ++q) v[q] = pull_rule<S, K, HAS_OBS>(L, q, x, y, plane_at, own, ghost_xhi);
+    v[8] = ldq<S, K>(base + D19 * pe, me, D19);
+    collide<K>(v, (K)L.omega, (K)L.fgrad, L.forced != 0);
+#pragma unroll 1
+    for (int q = 0; q < 8; ++q) aa_push_rule<S, K, HAS_OBS>(L, base, q, x, y, v[q]);
+    base[D19 * pe + me] = Store<S>::template putq<K>(v[8], D19);
+    K g[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) g[q] = rnd<S, K>(q, v[q]);
+    aa_incoming<S, K>(L, base, x, y, g);
+}
+
+// push VEC values of direction q to (x + c_q) in plane q; lanes at an edge (segment end or a
+// neighbour on the slow path) store the elements that cross into the neighbour's vector.
+template <typename S, typename K, int q, int W>
+__device__ __forceinline__ void push_vec(const Lattice &L, S *plane, int xv, int y, bool left_edge,
+                                         bool right_edge, const K (&g)[vec_of<S>()], bool store)
+{
+    constexpr int VEC = vec_of<S>();
+    constexpr int cx = cx_of(q), cy = cy_of(q);
+    const int64_t idx = cell_index<S>(L, xv, y + cy);
+    S s[VEC];
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) s[c] = Store<S>::template put<K, q>(g[c]);
+    if (cx == 0) {
+        if (store) stv<S>(plane + idx, s);
+    } else if (cx == 1) {
+        K fl = shfl_up(g[VEC - 1], W);
+        if (!store) return;
+        if (!left_edge) {
+            S v[VEC];
+            v[0] = Store<S>::template put<K, q>(fl);
+#pragma unroll
+            for (int c = 1; c < VEC; ++c) v[c] = s[c - 1];
+            stv<S>(plane + idx, v);
+        } else {
+#pragma unroll
+            for (int c = 0; c < VEC - 1; ++c) plane[idx + 1 + c] = s[c];
+        }
+        if (right_edge) plane[idx + VEC] = s[VEC - 1];
+    } else {
+        K fr = shfl_down(g[0], W);
+        if (!store) return;
+        if (!right_edge) {
+            S v[VEC];
+#pragma unroll
+            for (int c = 0; c < VEC - 1; ++c) v[c] = s[c + 1];
+            v[VEC - 1] = Store<S>::template put<K, q>(fr);
+            stv<S>(plane + idx, v);
+        } else {
+#pragma unroll
+            for (int c = 1; c < VEC; ++c) plane[idx - 1 + c] = s[c];
+        }
+        if (left_edge) plane[idx - 1] = s[0];
+    }
+}
+
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS>
+__global__ void __launch_bounds__(TXV *TY) aa_p_kernel(const Lattice L)
+{
+    constexpr int VEC = vec_of<S>();
+    constexpr int W = TXV < 32 ? TXV : 32;
+    const int tx = threadIdx.x;
+    const int k = blockIdx.x * TXV + tx;
+    const int y = blockIdx.y * TY + threadIdx.y + 1;
+    const bool in_rows = y <= L.ly;
+    const bool loads = in_rows && k <= L.nvec;
+    const bool active = in_rows && k < L.nvec;
+    const int xv = 1 + k * VEC;
+    const int64_t pe = L.plane_elems;
+    S *base = reinterpret_cast<S *>(L.planes);
+
+    // pull f*_q from plane opp(q) at x - c_q
+    K x[9][VEC];
+    pull_vec<S, K, D01, W>(L, base + D12 * pe, xv, y, loads, tx, x[D01]);
+    pull_vec<S, K, D03, W>(L, base + D10 * pe, xv, y, loads, tx, x[D03]);
+    pull_vec<S, K, D05, W>(L, base + D14 * pe, xv, y, loads, tx, x[D05]);
+    pull_vec<S, K, D08, W>(L, base + D17 * pe, xv, y, loads, tx, x[D08]);
+    pull_vec<S, K, D10, W>(L, base + D03 * pe, xv, y, loads, tx, x[D10]);
+    pull_vec<S, K, D12, W>(L, base + D01 * pe, xv, y, loads, tx, x[D12]);
+    pull_vec<S, K, D14, W>(L, base + D05 * pe, xv, y, loads, tx, x[D14]);
+    pull_vec<S, K, D17, W>(L, base + D08 * pe, xv, y, loads, tx, x[D17]);
+    pull_vec<S, K, D19, W>(L, base + D19 * pe, xv, y, loads, tx, x[D19]);
+
+    bool slow = (y == 1) || (y == L.ly) || (k == 0) || (k >= L.nvec - 1);
+    if (HAS_OBS) slow = slow || (y >= L.ob_y0 && y <= L.ob_y1 && xv + VEC - 1 >= L.ob_x0 && xv <= L.ob_x1);
+    slow = slow || !active;
+    // neighbours on the slow path do not take part in the vector stores
+    const bool left_slow = __shfl_up_sync(0xffffffffu, slow ? 1 : 0, 1, W) != 0;
+    const bool right_slow = __shfl_down_sync(0xffffffffu, slow ? 1 : 0, 1, W) != 0;
+    const bool left_edge = (tx % W) == 0 || left_slow;
+    const bool right_edge = (tx % W) == W - 1 || right_slow;
+
+    const K omega = (K)L.omega, fgrad = (K)L.fgrad;
+    const bool forced = L.forced != 0;
+    K g[9][VEC];
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) {
+        K v[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) v[q] = x[q][c];
+        collide<K>(v, omega, fgrad, forced);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) g[q][c] = v[q];
+    }
+    const bool store = !slow;
+    push_vec<S, K, D01, W>(L, base + D01 * pe, xv, y, left_edge, right_edge, g[D01], store);
+    push_vec<S, K, D03, W>(L, base + D03 * pe, xv, y, left_edge, right_edge, g[D03], store);
+    push_vec<S, K, D05, W>(L, base + D05 * pe, xv, y, left_edge, right_edge, g[D05], store);
+    push_vec<S, K, D08, W>(L, base + D08 * pe, xv, y, left_edge, right_edge, g[D08], store);
+    push_vec<S, K, D10, W>(L, base + D10 * pe, xv, y, left_edge, right_edge, g[D10], store);
+    push_vec<S, K, D12, W>(L, base + D12 * pe, xv, y, left_edge, right_edge, g[D12], store);
+    push_vec<S, K, D14, W>(L, base + D14 * pe, xv, y, left_edge, right_edge, g[D14], store);
+    push_vec<S, K, D17, W>(L, base + D17 * pe, xv, y, left_edge, right_edge, g[D17], store);
+    push_vec<S, K, D19, W>(L, base + D19 * pe, xv, y, left_edge, right_edge, g[D19], store);
+    if (!active || !slow) return;
+    const int xe = min(xv + VEC - 1, L.lx);
+#pragma unroll 1
+    for (int xc = xv; xc <= xe; ++xc) aa_p_cell_slow<S, K, HAS_OBS>(L, base, xc, y);
+}
+
+// L step: local collision, phase 1 -> 0
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS>
+__global__ void __launch_bounds__(TXV *TY) aa_l_kernel(const Lattice L)
+{
+    constexpr int VEC = vec_of<S>();
+    const int k = blockIdx.x * TXV + threadIdx.x;
+    const int y = blockIdx.y * TY + threadIdx.y + 1;
+    if (y > L.ly || k >= L.nvec) return;
+    const int xv = 1 + k * VEC;
+    const int64_t pe = L.plane_elems;
+    S *base = reinterpret_cast<S *>(L.planes);
+    const int64_t me = cell_index<S>(L, xv, y);
+    const bool outflow = L.faces[XHI] == FK_OUTFLOW_EQ || L.faces[XHI] == FK_OUTFLOW_ZG;
+    bool slow = (k == L.nvec - 1) && ((L.lx % VEC) != 0 || outflow);
+    if (HAS_OBS) slow = slow || (y >= L.ob_y0 && y <= L.ob_y1 && xv + VEC - 1 >= L.ob_x0 && xv <= L.ob_x1);
+    const K omega = (K)L.omega, fgrad = (K)L.fgrad;
+    const bool forced = L.forced != 0;
+    if (slow) {
+        const int xe = min(xv + VEC - 1, L.lx);
+#pragma unroll 1
+        for (int xc = xv; xc <= xe; ++xc) {
+            const int64_t i = cell_index<S>(L, xc, y);
+            if (HAS_OBS) {
+                if (obs_bit(L, xc, y)) continue;
+            }
+            K v[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) v[q] = ldq<S, K>(base + q * pe, i, q);
+            collide<K>(v, omega, fgrad, forced);
+            K g[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                const S s = Store<S>::template putq<K>(v[q], q);
+                base[opp_of(q) * pe + i] = s;
+                g[q] = Store<S>::template getq<K>(s, q);
+            }
+            if (xc == L.lx && outflow) aa_outflow_ghost<S, K>(L, base, y, g);
+        }
+        return;
+    }
+    K x[9][VEC];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        S v[VEC];
+        ldv<S>(base + q * pe + me, v);
+#pragma unroll
+        for (int c = 0; c < VEC; ++c) x[q][c] = Store<S>::template getq<K>(v[c], q);
+    }
+    S o[9][VEC];
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) {
+        K v[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) v[q] = x[q][c];
+        collide<K>(v, omega, fgrad, forced);
+        o[D12][c] = Store<S>::template put<K, D01>(v[0]);
+        o[D10][c] = Store<S>::template put<K, D03>(v[1]);
+        o[D14][c] = Store<S>::template put<K, D05>(v[2]);
+        o[D17][c] = Store<S>::template put<K, D08>(v[3]);
+        o[D03][c] = Store<S>::template put<K, D10>(v[4]);
+        o[D01][c] = Store<S>::template put<K, D12>(v[5]);
+        o[D05][c] = Store<S>::template put<K, D14>(v[6]);
+        o[D08][c] = Store<S>::template put<K, D17>(v[7]);
+        o[D19][c] = Store<S>::template put<K, D19>(v[8]);
+    }
+#pragma unroll
+    for (int q = 0; q < 9; ++q) stv<S>(base + q * pe + me, o[q]);
+}
+
+}  // namespace bgk

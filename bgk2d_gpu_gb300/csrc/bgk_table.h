@@ -1,0 +1,44 @@
+// bgk_table.h -- host-side table of the kernels instantiated for one (storage, compute) pair.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace bgk {
+
+struct Lattice;
+
+// step kinds
+enum StepKind { STEP_PP = 0, STEP_AA_P = 1, STEP_AA_L = 2 };
+
+// thread-block shapes (threads along a row segment x rows); cells per block = TXV*VEC x TY
+struct TileCfg { int txv, ty; };
+constexpr int NUM_CFG = 4;
+constexpr TileCfg TILE_CFGS[NUM_CFG] = {{32, 4}, {64, 2}, {128, 1}, {128, 2}};
+
+struct KernelTable {
+    int vec;  // cells per 16-byte vector
+    int elem_bytes;
+    cudaError_t (*step)(int kind, const Lattice &L, int parity, bool obs, int cfg, cudaStream_t st);
+    cudaError_t (*scatter)(const Lattice &L, int cur, int q, const void *stage, cudaStream_t st);
+    cudaError_t (*gather)(const Lattice &L, int cur, int phase, int q, void *stage, bool obs, cudaStream_t st);
+    cudaError_t (*fill_outflow)(const Lattice &L, cudaStream_t st);
+    cudaError_t (*diagno)(const Lattice &L, int cur, int phase, int fluid_only, bool obs, double *partial, int nb,
+                          cudaStream_t st);
+    cudaError_t (*residual)(const Lattice &L, int cur, int phase, bool obs, double *uprev, double *vprev,
+                            double *partial, int nb, cudaStream_t st);
+    cudaError_t (*draglift)(const Lattice &L, int cur, int phase, int i0, int i1, int j0, int j1, double *partial,
+                            int nb, cudaStream_t st);
+    cudaError_t (*fields)(const Lattice &L, int cur, int phase, bool obs, double *rho, double *u, double *v,
+                          cudaStream_t st);
+};
+
+KernelTable table_f32_f32();
+KernelTable table_f32_f64();
+KernelTable table_f64_f64();
+KernelTable table_f16_f32();
+KernelTable table_bf16_f32();
+
+cudaError_t launch_finalize4(const double *partial, int nb, double *out, cudaStream_t st);
+
+}  // namespace bgk

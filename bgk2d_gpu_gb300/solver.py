@@ -1,0 +1,237 @@
+"""Host-side mirror of the reference's step interface over the C ABI.
+
+The reference driver (SRC/bgk2d.F90:92-113) calls `boundaries`, `propagation` and
+`collision(itime)` once per step and reads the populations through `diagno`, `probe`,
+`prof_i`/`prof_j`, `draglift`, `vtk_*` and `save_raw`.  `Solver` offers the same calls on a
+device-resident case; readers that stay host-side in the reference (probe, prof_i, prof_j,
+varm) work on downloaded populations with the reference's single-step arithmetic.
+"""
+from __future__ import annotations
+
+import ctypes
+import re
+
+import numpy as np
+
+from . import _lib
+from ._lib import BgkError, CaseDesc
+
+# direction order of the reference (SRC/bgk2d.F90:29-39): 01,03,05,08,10,12,14,17,19
+CX = np.array([1, 1, 1, 0, -1, -1, -1, 0, 0])
+CY = np.array([-1, 1, 0, 1, -1, 1, 0, -1, 0])
+WEIGHTS = np.array([1 / 36, 1 / 36, 1 / 9, 1 / 9, 1 / 36, 1 / 36, 1 / 9, 1 / 9, 4 / 9])
+
+
+def read_namelist(path: str) -> dict:
+    """Parse the `&parameters` namelist of bgk.input (SRC/input.F90:44-65) into a dict,
+    with the reference defaults (SRC/input.F90:51-61) for absent keys."""
+    text = open(path).read()
+    m = re.search(r"&parameters(.*?)/", text, flags=re.S | re.I)
+    if not m:
+        raise ValueError(f"{path}: no &parameters namelist")
+    vals = dict(flag1=0, flag2=0, flag3=0, init_v=0, cteS=0.1, ipad=0, jpad=0, radius=16)
+    for key, val in re.findall(r"(\w+)\s*=\s*([^,\s/]+)", m.group(1)):
+        v = val.strip().rstrip(",").replace("d", "e").replace("D", "e")
+        try:
+            num = int(v)
+        except ValueError:
+            num = float(v)
+        vals[key.strip()] = num
+    return vals
+
+
+class Solver:
+    """One device-resident BGK2D case (ping-pong or AA scheme)."""
+
+    def __init__(self, lx, ly, tcase="LDC", svisc=0.1, u0=0.1, storage="f32", compute=None,
+                 scheme="pingpong", radius=16, obstacle=None, obs_center=(-1, -1), obs_mask=None,
+                 init="rest", omega=None, u_inflow=None, inflow_profile=0, faces=None,
+                 wall_u=None, tgv_u0=0.02, ipad=0, jpad=0, device=0):
+        L = _lib.load()
+        d = CaseDesc()
+        L.bgk_default_desc(ctypes.byref(d))
+        d.lx, d.ly, d.ipad, d.jpad = int(lx), int(ly), int(ipad), int(jpad)
+        if compute is None:
+            compute = "f64" if storage == "f64" else "f32"
+        d.storage = _lib.STORE[storage]
+        d.compute = _lib.COMPUTE[compute]
+        d.scheme = _lib.SCHEME[scheme]
+        d.tcase = _lib.CASE[tcase]
+        d.svisc = float(svisc)
+        d.u0 = float(u0)
+        d.omega = float(omega) if omega else 0.0
+        d.u_inflow = float(u_inflow) if u_inflow else 0.0
+        d.inflow_profile = int(inflow_profile)
+        d.radius = int(radius)
+        d.obs_icoord, d.obs_jcoord = int(obs_center[0]), int(obs_center[1])
+        self._mask_keep = None
+        if obs_mask is not None:
+            mk = np.ascontiguousarray(obs_mask, dtype=np.int32)
+            assert mk.shape == (ly, lx)
+            self._mask_keep = mk
+            d.obstacle = _lib.OBS["mask"]
+            d.obs_mask = mk.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        else:
+            d.obstacle = _lib.OBS[obstacle]
+        d.init_v = _lib.INIT[init]
+        d.tgv_u0 = float(tgv_u0)
+        d.device = int(device)
+        if faces is not None:
+            for i, f in enumerate(faces):
+                d.faces[i] = _lib.FACE[f]
+        if wall_u is not None:
+            for i, (ux, uy) in enumerate(wall_u):
+                d.wall_u[i][0], d.wall_u[i][1] = float(ux), float(uy)
+        self.desc = d
+        self.lx, self.ly = int(lx), int(ly)
+        self.storage, self.compute, self.scheme, self.tcase = storage, compute, scheme, tcase
+        self.hdtype = np.float64 if storage == "f64" else np.float32
+        self._L = L
+        h = ctypes.c_void_p()
+        rc = L.bgk_create(ctypes.byref(d), ctypes.byref(h))
+        if rc != 0:
+            raise BgkError(rc, f"bgk_create({lx}x{ly}, {tcase}, {storage}/{compute}, {scheme})")
+        self._h = h
+
+    @classmethod
+    def from_namelist(cls, path, tcase="LDC", **kw):
+        p = read_namelist(path)
+        return cls(p["lx"], p["ly"], tcase=tcase, svisc=p["svisc"], u0=p["u0"],
+                   radius=p.get("radius", 16), ipad=p.get("ipad", 0), jpad=p.get("jpad", 0), **kw)
+
+    # -- lifecycle ----------------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.bgk_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc, what):
+        if rc != 0:
+            buf = ctypes.create_string_buffer(512)
+            self._L.bgk_last_error(self._h, buf, 512)
+            raise BgkError(rc, f"{what}: {buf.value.decode()}")
+
+    # -- the reference's step sequence (SRC/bgk2d.F90:100-102) ---------------------------------
+    def boundaries(self):
+        self._check(self._L.bgk_boundaries(self._h), "boundaries")
+
+    def propagation(self):
+        self._check(self._L.bgk_propagation(self._h), "propagation")
+
+    def collision(self, itime=0):
+        self._check(self._L.bgk_collision(self._h, int(itime)), "collision")
+
+    def step(self, n=1):
+        self._check(self._L.bgk_step(self._h, int(n)), "step")
+
+    def step_timed(self, n):
+        ms = ctypes.c_float()
+        self._check(self._L.bgk_step_timed(self._h, int(n), ctypes.byref(ms)), "step_timed")
+        return ms.value
+
+    def sync(self):
+        self._check(self._L.bgk_sync(self._h), "sync")
+
+    # -- populations ------------------------------------------------------------------------
+    def _ptrs(self, arr):
+        return (ctypes.c_void_p * 9)(*[arr[q].ctypes.data for q in range(9)])
+
+    def download(self):
+        """(9, ly+2, lx+2) host-kind array a01..a19, index [q, j, i]; ghost entries are zero."""
+        out = np.zeros((9, self.ly + 2, self.lx + 2), dtype=self.hdtype)
+        self._check(self._L.bgk_download(self._h, self._ptrs(out), self.lx + 2), "download")
+        return out
+
+    def upload(self, arr):
+        a = np.ascontiguousarray(arr, dtype=self.hdtype)
+        assert a.shape == (9, self.ly + 2, self.lx + 2)
+        self._check(self._L.bgk_upload(self._h, self._ptrs(a), self.lx + 2), "upload")
+
+    # -- reductions (FP64 on the device) ------------------------------------------------------
+    def diagno(self, fluid_only=False):
+        """(<u>, <v>, <rho>, <|u|^2>) as written to diagno.dat (SRC/diagno.F90:327)."""
+        out = np.zeros(4)
+        self._check(self._L.bgk_diagno(self._h, int(bool(fluid_only)),
+                                       out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))), "diagno")
+        return out
+
+    def draglift(self):
+        out = np.zeros(2)
+        self._check(self._L.bgk_draglift(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+                    "draglift")
+        return out
+
+    def residual(self):
+        out = ctypes.c_double()
+        self._check(self._L.bgk_residual(self._h, ctypes.byref(out)), "residual")
+        return out.value
+
+    def fields(self):
+        n = self.lx * self.ly
+        r, u, v = np.empty(n), np.empty(n), np.empty(n)
+        P = ctypes.POINTER(ctypes.c_double)
+        self._check(self._L.bgk_fields(self._h, r.ctypes.data_as(P), u.ctypes.data_as(P), v.ctypes.data_as(P)),
+                    "fields")
+        sh = (self.ly, self.lx)
+        return r.reshape(sh), u.reshape(sh), v.reshape(sh)
+
+    def obs(self):
+        mask = np.zeros(self.lx * self.ly, dtype=np.int32)
+        bb = np.zeros(5, dtype=np.int32)
+        P = ctypes.POINTER(ctypes.c_int32)
+        self._check(self._L.bgk_get_obs(self._h, mask.ctypes.data_as(P), bb.ctypes.data_as(P)), "get_obs")
+        return mask.reshape(self.ly, self.lx), bb
+
+    def scalars(self):
+        out = np.zeros(4)
+        it = ctypes.c_int64()
+        self._check(self._L.bgk_get_scalars(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                            ctypes.byref(it)), "get_scalars")
+        return dict(omega=out[0], fgrad=out[1], u00=out[2], u0=out[3], itime=it.value)
+
+    def footprint(self):
+        b = ctypes.c_int64()
+        c = ctypes.c_int32()
+        self._check(self._L.bgk_footprint(self._h, ctypes.byref(b), ctypes.byref(c)), "footprint")
+        return b.value, c.value
+
+    def launches(self):
+        n = ctypes.c_int64()
+        self._check(self._L.bgk_launch_count(self._h, ctypes.byref(n)), "launch_count")
+        return n.value
+
+    # -- host-side readers of downloaded populations (reference arithmetic, storage kind) ----
+    def prof_j(self, icoord, pops=None):
+        """u, v, rho along column icoord, j = 1..ly (SRC/prof_j.F90:47-67)."""
+        a = self.download() if pops is None else pops
+        k = a.dtype.type
+        c = a[:, 1:self.ly + 1, icoord]
+        den = c[0] + c[1]
+        for q in range(2, 8):
+            den = den + c[q]
+        den = (den + c[8]) + k(1)
+        u = ((c[0] - c[4]) + (c[1] - c[5]) + (c[2] - c[6])) / den
+        v = ((c[1] - c[0]) + (c[3] - c[7]) + (c[5] - c[4])) / den
+        return u, v, den
+
+    def probe(self, i0, j0, pops=None):
+        """u, v, rho at one node (SRC/probe.F90:57-66)."""
+        a = self.download() if pops is None else pops
+        x = a[:, j0, i0]
+        k = a.dtype.type
+        rho = x[0] + x[1] + x[2] + x[3] + x[4] + x[5] + x[6] + x[7] + x[8] + k(1)
+        xj = x[0] + x[1] + x[2] - x[4] - x[5] - x[6]
+        yj = x[1] + x[3] + x[5] - x[0] - x[4] - x[7]
+        return xj / rho, yj / rho, rho

@@ -1,0 +1,168 @@
+/*
+ * bgk2d_gb300.h -- C ABI of libbgk2d_gb300.so, the GB300 (sm_103a) D2Q9 BGK time step.
+ *
+ * Drop-in boundary for the hot path of BGK2D.  The reference driver runs, once per step,
+ *     call boundaries          (SRC/boundaries.F90:23-64  -> SRC/bcond.*.F90)
+ *     call propagation         (SRC/propagation.F90:24-53 -> SRC/movef.F90)
+ *     call collision(itime)    (SRC/collision.F90:24-55   -> SRC/col_MC.F90 / SRC/col.F90)
+ * on populations held in `module storage` (SRC/storage.F90:86-112).  This library keeps the
+ * populations resident in HBM behind an opaque handle; the three calls above map to
+ * bgk_boundaries / bgk_propagation / bgk_collision (or one bgk_step), and the host-side
+ * readers (diagno, draglift, probe/prof, vtk, save_raw) get their data from bgk_diagno,
+ * bgk_draglift and bgk_download.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: BGK_OK (0) or a BGK_E_* code.  After an error
+ *    the handle keeps the first message; read it with bgk_last_error.  CUDA errors are
+ *    sticky for the handle.
+ *  - Host population arrays use the reference layout (SRC/alloca.F90:220-238): nine
+ *    column-major arrays (0:lx+1+ipad, 0:ly+1+jpad), i fastest, leading dimension
+ *    ld = lx+2+ipad, direction order 01,03,05,08,10,12,14,17,19 (SRC/bgk2d.F90:29-39),
+ *    holding the deviations f_i - w_i (the reference's default "shifted" storage).
+ *    The host element type is double for BGK_STORE_F64 and float otherwise.
+ *  - One handle is used by one host thread at a time.
+ */
+#ifndef BGK2D_GB300_H
+#define BGK2D_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BGK_ABI_VERSION 1
+
+/* status codes */
+#define BGK_OK 0
+#define BGK_E_INVALID 1      /* bad argument or unsupported combination */
+#define BGK_E_NOMEM 2        /* device allocation or admission failed */
+#define BGK_E_CUDA 3         /* a CUDA call failed (sticky) */
+#define BGK_E_UNSUPPORTED 4  /* feature not available for this case/scheme */
+#define BGK_E_NUMERIC 5      /* NaN or Inf seen by a reduction */
+#define BGK_E_CANCELLED 6    /* work cancelled by the host */
+#define BGK_E_TIMEOUT 7      /* a bounded wait ran out */
+#define BGK_E_NOTFOUND 8     /* unknown id */
+
+/* storage kind of the populations in HBM (SRC/precision.F90:13-47, `mystorage`) */
+#define BGK_STORE_F32 0   /* SINGLE / MIXED2 */
+#define BGK_STORE_F64 1   /* DOUBLE */
+#define BGK_STORE_F16 2   /* 16-bit: (f_i - w_i) * s_i as IEEE half, s_i a power of two */
+#define BGK_STORE_BF16 3  /* 16-bit: (f_i - w_i) * s_i as bfloat16 */
+
+/* arithmetic kind of the collision (`mykind`) */
+#define BGK_COMPUTE_F32 0
+#define BGK_COMPUTE_F64 1
+
+/* scheme */
+#define BGK_SCHEME_PINGPONG 0  /* fused pull stream+collide, two buffers (SRC/col_MC.F90) */
+#define BGK_SCHEME_AA 1        /* fused, one buffer, alternating even/odd access pattern */
+
+/* test case presets: the reference's compile-time case flags (SRC/Makefile:155-187) */
+#define BGK_CASE_LDC 0     /* bcond_driven: walls + moving lid at y = ly+1 */
+#define BGK_CASE_TGV 1     /* bcond_periodic */
+#define BGK_CASE_POF 2     /* bcond_channel + body force fgrad */
+#define BGK_CASE_VKS 3     /* bcond_inflow (+ obstacle, drag/lift) */
+#define BGK_CASE_COU 4     /* bcond_couette */
+#define BGK_CASE_CUSTOM 9  /* faces[] and wall_u[] given explicitly */
+
+/* face kinds for BGK_CASE_CUSTOM; faces are x_lo (i=0), x_hi (i=lx+1), y_lo, y_hi */
+#define BGK_FACE_WALL 0         /* half-way bounce-back, optional wall velocity */
+#define BGK_FACE_PERIODIC 1
+#define BGK_FACE_INFLOW 2       /* x faces: equilibrium at rho=1, prescribed u (bcond.inflow.F90:233-244) */
+#define BGK_FACE_OUTFLOW_EQ 3   /* x_hi: equilibrium at rho=1 and the local u (bcond.inflow.F90:211-230) */
+#define BGK_FACE_OUTFLOW_ZG 4   /* x_hi: zero-gradient copy of column lx */
+
+/* obstacle shapes (SRC/build.obs.F90) */
+#define BGK_OBS_NONE 0
+#define BGK_OBS_CIRCLE 1
+#define BGK_OBS_SQUARE 2
+#define BGK_OBS_HALF_CIRCLE 3
+#define BGK_OBS_MASK 4      /* caller passes obs(1:lx,1:ly) */
+
+/* initial states */
+#define BGK_INIT_REST 0     /* init.F90 rest flow: all deviations zero */
+#define BGK_INIT_TGV_REF 1  /* init.F90 periodic vortex, amplitude 0.1, rho = 1 */
+#define BGK_INIT_TGV 2      /* vortex of amplitude tgv_u0 with rho = 1 - 3 u0^2/4 (cos 2kx + cos 2ky) */
+
+typedef struct bgk_case_desc {
+    int32_t lx, ly;           /* interior nodes (namelist lx, ly; SRC/input.F90:67-68) */
+    int32_t ipad, jpad;       /* host array padding (namelist ipad, jpad) */
+    int32_t storage;          /* BGK_STORE_* */
+    int32_t compute;          /* BGK_COMPUTE_* */
+    int32_t scheme;           /* BGK_SCHEME_* */
+    int32_t tcase;            /* BGK_CASE_* */
+    int32_t faces[4];         /* BGK_FACE_* for x_lo, x_hi, y_lo, y_hi (BGK_CASE_CUSTOM only) */
+    double wall_u[4][2];      /* wall velocity (ux, uy) per face (BGK_CASE_CUSTOM only) */
+    double svisc;             /* namelist svisc; omega = 2/(6 svisc + 1) (SRC/hencol.F90:30) */
+    double u0;                /* namelist u0: lid speed (LDC/COU) or forcing velocity (POF) */
+    double omega;             /* > 0 overrides the omega computed from svisc */
+    double u_inflow;          /* peak inflow speed; <= 0 selects the reference's 0.1 */
+    int32_t inflow_profile;   /* 0 uniform, 1 parabolic between half-way walls */
+    int32_t obstacle;         /* BGK_OBS_* */
+    int32_t radius;           /* namelist radius (SRC/input.F90:61) */
+    int32_t obs_icoord;       /* obstacle centre; < 0 selects 2*lx/5 (SRC/build.obs.F90:174) */
+    int32_t obs_jcoord;       /* < 0 selects ly/2 */
+    const int32_t *obs_mask;  /* BGK_OBS_MASK: obs(1:lx,1:ly), column-major */
+    int32_t init_v;           /* BGK_INIT_* applied by bgk_create */
+    double tgv_u0;            /* amplitude for BGK_INIT_TGV */
+    int32_t device;           /* CUDA device ordinal */
+    int32_t reserved[7];
+} bgk_case_desc;
+
+typedef struct bgk_handle bgk_handle;
+
+/* Fill a descriptor with the reference defaults (LDC, FP32, ping-pong, radius 16). */
+int bgk_default_desc(bgk_case_desc *desc);
+
+/* Allocate the device state for one case and set it up like alloca + initialize
+ * (SRC/alloca.F90, SRC/initialize.F90:70-128: build_bcond, build_obs, init, hencol).
+ * Returns BGK_E_NOMEM when the populations do not fit in free HBM. */
+int bgk_create(const bgk_case_desc *desc, bgk_handle **out);
+int bgk_destroy(bgk_handle *h);
+
+/* Copy populations host -> device / device -> host (reference layout, see top).
+ * pops[q] points at direction q's array; ld is its leading dimension in elements. */
+int bgk_upload(bgk_handle *h, void *const pops[9], int64_t ld);
+int bgk_download(bgk_handle *h, void *const pops[9], int64_t ld);
+
+/* The reference's per-step call sequence.  bgk_boundaries and bgk_propagation record the
+ * call order; the boundary rules and the streaming run inside the fused kernel launched by
+ * bgk_collision (SRC/collision.F90:37-41 with FUSED).  Asynchronous. */
+int bgk_boundaries(bgk_handle *h);
+int bgk_propagation(bgk_handle *h);
+int bgk_collision(bgk_handle *h, int32_t itime);
+
+/* nsteps full time steps (boundaries + propagation + collision), replayed from CUDA graphs.
+ * Asynchronous on the handle's stream. */
+int bgk_step(bgk_handle *h, int32_t nsteps);
+/* Same, bracketed by CUDA events on the handle's stream; *ms = device time (synchronises). */
+int bgk_step_timed(bgk_handle *h, int32_t nsteps, float *ms);
+int bgk_sync(bgk_handle *h);
+
+/* Reductions over the interior in FP64 (synchronise).
+ * diagno (SRC/diagno.F90:282-320): out = <u>, <v>, <rho>, <|u|^2>; fluid_only skips obstacle cells. */
+int bgk_diagno(bgk_handle *h, int32_t fluid_only, double out[4]);
+/* momentum-exchange drag/lift (SRC/draglift.F90:383-444): out = Fx*norm, Fy*norm */
+int bgk_draglift(bgk_handle *h, double out[2]);
+/* steady-state residual: ||u - u_prev||_2 / ||u||_2 since the previous call (first call: 1) */
+int bgk_residual(bgk_handle *h, double *out);
+/* macroscopic fields rho, u, v of the interior to host arrays of lx*ly doubles, i fastest */
+int bgk_fields(bgk_handle *h, double *rho, double *u, double *v);
+/* obstacle mask obs(1:lx,1:ly) and imin,imax,jmin,jmax,nobs (SRC/build.obs.F90) */
+int bgk_get_obs(bgk_handle *h, int32_t *mask, int32_t bbox[5]);
+/* omega, fgrad, u00, u0 after build_bcond + hencol, and the step counter */
+int bgk_get_scalars(bgk_handle *h, double out[4], int64_t *itime);
+
+/* bytes of HBM the handle holds, and the algorithmic bytes moved per lattice update */
+int bgk_footprint(bgk_handle *h, int64_t *device_bytes, int32_t *bytes_per_cell);
+/* number of kernels this library launched on the handle so far */
+int bgk_launch_count(bgk_handle *h, int64_t *launches);
+int bgk_last_error(bgk_handle *h, char *buf, size_t len);
+const char *bgk_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

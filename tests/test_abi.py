@@ -1,0 +1,74 @@
+"""C ABI surface (no GPU needed): the library loads and exports every entry point that
+include/bgk2d_gb300.h declares; the Python mirror's descriptor matches the C layout."""
+import ctypes
+import os
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_header_symbols(bgk):
+    from bgk2d_gpu_gb300 import _lib
+    path = _lib.lib_path()
+    L = ctypes.CDLL(path)
+    names = _lib.exported_symbols()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(L, n), n
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+
+
+def test_version_and_default_desc(bgk):
+    from bgk2d_gpu_gb300 import _lib
+    L = _lib.load()
+    assert b"sm_103a" in L.bgk_version()
+    d = _lib.CaseDesc()
+    assert L.bgk_default_desc(ctypes.byref(d)) == 0
+    assert (d.lx, d.ly, d.radius, d.obs_icoord) == (256, 256, 16, -1)
+
+
+def test_desc_layout_matches_c():
+    """sizeof/offsets of bgk_case_desc compiled by the C compiler vs the ctypes mirror."""
+    from bgk2d_gpu_gb300 import _lib
+    src = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "bgk2d_gb300.h"
+int main(void){printf("%zu %zu %zu %zu %zu\n", sizeof(bgk_case_desc), offsetof(bgk_case_desc, svisc),
+ offsetof(bgk_case_desc, obs_mask), offsetof(bgk_case_desc, tgv_u0), offsetof(bgk_case_desc, device));return 0;}
+'''
+    exe = os.path.join(ROOT, "bgk2d_gpu_gb300", "_build", "desc_layout")
+    os.makedirs(os.path.dirname(exe), exist_ok=True)
+    r = subprocess.run(["gcc", "-x", "c", "-", "-I", os.path.join(ROOT, "include"), "-o", exe], input=src,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    vals = [int(x) for x in subprocess.run([exe], capture_output=True, text=True).stdout.split()]
+    C = _lib.CaseDesc
+    assert vals == [ctypes.sizeof(C), C.svisc.offset, C.obs_mask.offset, C.tgv_u0.offset, C.device.offset]
+
+
+def test_no_device_means_loud_error(bgk):
+    """Without a usable GPU, creating a case fails with a CUDA status; there is no CPU path."""
+    import bgk2d_gpu_gb300 as m
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    with pytest.raises(m.BgkError):
+        m.Solver(32, 32)
+
+
+def test_namelist_reader(tmp_path):
+    from bgk2d_gpu_gb300 import read_namelist
+    p = tmp_path / "bgk.input"
+    p.write_text("&parameters\nlx = 4096\nly = 4096\nsvisc=0.04096\nu0=0.1\nitfin=2000\n"
+                 "ivtim=500000\nisignal=5000\nitsave=1000000\nicheck=100000\nirestart=0\ninit_v=0\nipad=0        /\n")
+    v = read_namelist(str(p))
+    assert v["lx"] == 4096 and v["svisc"] == 0.04096 and v["radius"] == 16 and v["itfin"] == 2000

@@ -1,0 +1,184 @@
+"""GPU parity: the CUDA step through the C ABI against the CPU oracle on the same inputs.
+
+FP32 (SINGLE), FP64 (DOUBLE) and FP32-storage/FP64-compute (MIXED2) kernels perform one IEEE
+operation per reference operation, so after any number of steps the interior populations must
+be bit-identical to the oracle (which restates SRC/col_MC.F90 and SRC/bcond.*.F90).  Obstacle
+interiors follow the snapshot order of SRC/bcond.obs.F90 in the ping-pong scheme and are not
+advanced by the AA scheme (they never influence fluid cells), so AA comparisons mask them.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PRECS = {  # name: (oracle precision, storage, compute)
+    "single": (0, "f32", "f32"),
+    "double": (1, "f64", "f64"),
+    "mixed2": (2, "f32", "f64"),
+}
+
+# (case, lx, ly, svisc, u0, extra oracle kwargs, extra solver kwargs)
+CASES = {
+    "ldc": ("LDC", 70, 37, 0.05, 0.1, {}, {}),
+    "tgv": ("TGV", 64, 48, 0.05, 0.0, {}, {"init": "tgv_ref"}),
+    "pof": ("POF", 96, 34, 0.1, 0.1, {}, {}),
+    "cou": ("COU", 80, 40, 0.1, 0.1, {}, {}),
+    "vks": ("VKS", 160, 62, 0.05, 0.1, {"obstacle": 1, "radius": 6}, {"radius": 6}),
+}
+ORACLE_CASE = {"LDC": 0, "TGV": 1, "POF": 2, "VKS": 3, "COU": 4}
+
+
+def make_pair(oracle_mod, bgk, case, prec, scheme):
+    tc, lx, ly, svisc, u0, okw, skw = CASES[case]
+    oprec, st, cp = PRECS[prec]
+    o = oracle_mod.Oracle(lx, ly, prec=oprec, tcase=ORACLE_CASE[tc], svisc=svisc, u0=u0,
+                          obs_order=oracle_mod.OBS_SNAPSHOT, **okw)
+    s = bgk.Solver(lx, ly, tcase=tc, svisc=svisc, u0=u0, storage=st, compute=cp, scheme=scheme, **skw)
+    return o, s
+
+
+def interior(a, lx, ly):
+    return a[:, 1:ly + 1, 1:lx + 1]
+
+
+def assert_same(o, s, scheme):
+    lx, ly = s.lx, s.ly
+    g = interior(s.download(), lx, ly)
+    r = interior(o.raw(), lx, ly)
+    if scheme == "aa":
+        mask, bb = o.obs()
+        keep = np.broadcast_to(mask == 0, g.shape)
+        g, r = g[keep], r[keep]
+    bad = np.argwhere(g != r) if g.ndim == 3 else np.flatnonzero(g != r)
+    assert bad.size == 0, f"{len(bad)} populations differ; first {bad[:5]}; max|d|={np.abs(g - r).max()}"
+
+
+@pytest.mark.parametrize("scheme", ["pingpong", "aa"])
+@pytest.mark.parametrize("prec", ["single", "double", "mixed2"])
+@pytest.mark.parametrize("case", list(CASES))
+def test_step_bit_exact(oracle_mod, bgk, case, prec, scheme):
+    o, s = make_pair(oracle_mod, bgk, case, prec, scheme)
+    with s:
+        assert_same(o, s, scheme)          # initial state (init.F90) identical
+        done = 0
+        for n in (1, 2, 7, 40, 75):        # odd/even counts, direct launches and graph replays
+            s.step(n)
+            o.step(n)
+            done += n
+            assert_same(o, s, scheme)
+        assert s.scalars()["itime"] == done
+
+
+@pytest.mark.parametrize("prec", ["single", "double", "mixed2"])
+def test_reference_call_sequence(oracle_mod, bgk, prec):
+    """boundaries / propagation / collision(itime), one call each per step, as SRC/bgk2d.F90:100-102."""
+    o, s = make_pair(oracle_mod, bgk, "ldc", prec, "pingpong")
+    with s:
+        for it in range(1, 6):
+            s.boundaries()
+            s.propagation()
+            s.collision(it)
+        o.step(5)
+        assert_same(o, s, "pingpong")
+
+
+@pytest.mark.parametrize("case", ["ldc", "tgv", "vks"])
+@pytest.mark.parametrize("prec", ["single", "double"])
+def test_diagno_and_fields(oracle_mod, bgk, case, prec):
+    o, s = make_pair(oracle_mod, bgk, case, prec, "pingpong")
+    with s:
+        s.step(33)
+        o.step(33)
+        d = s.diagno()
+        ref = o.diagno(1)   # same per-cell arithmetic, FP64 accumulation
+        np.testing.assert_allclose(d, ref, rtol=1e-12, atol=1e-15)
+        ref0 = o.diagno(0)  # the reference's own mykind accumulation
+        np.testing.assert_allclose(d, ref0, rtol=1e-4 if prec == "single" else 1e-12, atol=1e-7 if prec == "single" else 1e-15)
+        r, u, v = s.fields()
+        rr, ru, rv = o.fields()
+        assert np.array_equal(r, rr) and np.array_equal(u, ru) and np.array_equal(v, rv)
+
+
+@pytest.mark.parametrize("prec", ["single", "double"])
+@pytest.mark.parametrize("scheme", ["pingpong", "aa"])
+def test_draglift(oracle_mod, bgk, prec, scheme):
+    o, s = make_pair(oracle_mod, bgk, "vks", prec, scheme)
+    with s:
+        for n in (20, 13):
+            s.step(n)
+            o.step(n)
+            np.testing.assert_allclose(s.draglift(), o.draglift(1), rtol=1e-12, atol=1e-14)
+        d = s.diagno(fluid_only=True)
+        np.testing.assert_allclose(d, o.diagno(2), rtol=1e-12, atol=1e-15)
+
+
+def test_obstacle_mask_bit_exact(oracle_mod, bgk):
+    """build_obs (SRC/build.obs.F90): circle, square, half circle, custom centre."""
+    for shape, name in ((1, "circle"), (2, "square"), (3, "half_circle")):
+        for (lx, ly, r, c) in ((200, 80, 9, (-1, -1)), (256, 64, 16, (64, 33)), (97, 51, 5, (-1, -1))):
+            ref, rbb = oracle_mod.build_obs(lx, ly, shape, r, c[0], c[1])
+            with bgk.Solver(lx, ly, tcase="CUSTOM", faces=("inflow", "outflow_zg", "wall", "wall"),
+                            obstacle=name, radius=r, obs_center=c, u0=0.0, svisc=0.05) as s:
+                mask, bb = s.obs()
+            assert np.array_equal(mask, ref), (name, lx, ly)
+            assert np.array_equal(bb, rbb)
+
+
+def test_scalars_match_hencol(oracle_mod, bgk):
+    for prec in ("single", "double"):
+        for case in ("ldc", "pof", "cou"):
+            o, s = make_pair(oracle_mod, bgk, case, prec, "pingpong")
+            with s:
+                a, b = s.scalars(), o.scalars()
+                for k in ("omega", "fgrad", "u00", "u0"):
+                    assert a[k] == b[k], (case, prec, k, a[k], b[k])
+
+
+def test_upload_download_roundtrip(oracle_mod, bgk):
+    for scheme in ("pingpong", "aa"):
+        o, s = make_pair(oracle_mod, bgk, "tgv", "single", scheme)
+        with s:
+            o.step(9)
+            s.upload(o.raw())
+            assert_same(o, s, scheme)
+            s.step(5)
+            o.step(5)
+            assert_same(o, s, scheme)
+
+
+def test_ldc_256_re100_20000_steps(oracle_mod, bgk):
+    """The small plain case: LDC 256^2, Re=100, FP32, 20000 steps, bit-identical to the oracle."""
+    o = oracle_mod.Oracle(256, 256, prec=0, tcase=0, svisc=0.256, u0=0.1)
+    with bgk.Solver(256, 256, tcase="LDC", svisc=0.256, u0=0.1) as s:
+        s.step(20000)
+        o.step(20000, threads=16)
+        assert_same(o, s, "pingpong")
+        u, v, d = s.prof_j(128)
+        ou, ov, od = o.prof_j(128)
+        assert np.array_equal(u, ou.astype(np.float32)) and np.array_equal(d, od.astype(np.float32))
+
+
+@pytest.mark.parametrize("prec", ["single", "double"])
+def test_4096_first_steps_bit_exact(oracle_mod, bgk, prec):
+    """Full-size lid-driven cavity (4096^2, Re=10000): first steps against the threaded oracle,
+    then ping-pong and AA must stay bit-identical to each other."""
+    oprec, st, cp = PRECS[prec]
+    o = oracle_mod.Oracle(4096, 4096, prec=oprec, tcase=0, svisc=0.04096, u0=0.1)
+    a = bgk.Solver(4096, 4096, tcase="LDC", svisc=0.04096, u0=0.1, storage=st, compute=cp)
+    b = bgk.Solver(4096, 4096, tcase="LDC", svisc=0.04096, u0=0.1, storage=st, compute=cp, scheme="aa")
+    try:
+        o.step(3, threads=16)
+        a.step(3)
+        b.step(3)
+        assert_same(o, a, "pingpong")
+        assert_same(o, b, "aa")
+        a.step(97)
+        b.step(97)
+        ga, gb = interior(a.download(), 4096, 4096), interior(b.download(), 4096, 4096)
+        assert np.array_equal(ga, gb)
+        # mass: bounce-back and the lid's +-u00/6 pair conserve it
+        d = a.diagno()
+        assert abs(d[2] - 1.0) < (2e-6 if prec == "single" else 1e-13)
+    finally:
+        a.close()
+        b.close()

@@ -1,0 +1,142 @@
+"""CPU oracle pinning (no GPU).
+
+The reference's own acceptance checks for this path are analytic or read by eye
+(TEST/*/plot*.gnu): Taylor-Green energy decay against E0 exp(-2 nu (kx^2+ky^2) t), the
+Poiseuille parabola and its mean energy 8 u0^2/15, and the lid-driven cavity against Ghia's
+table.  These tests run the same checks on the oracle, plus internal identities of the
+restatement (FUSED == ORIGINAL, obstacle loop order only touches obstacle interiors).
+"""
+import os
+
+import numpy as np
+import pytest
+
+GHIA = "/root/reference/TEST/DrivenCavity/ghia.y.dat"
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_hencol_scalars(oracle_mod):
+    o = oracle_mod.Oracle(256, 256, prec=oracle_mod.SINGLE, tcase=oracle_mod.LDC, svisc=0.256, u0=0.1)
+    s = o.scalars()
+    sv = np.float32(0.256)
+    assert s["omega"] == float(np.float32(2) / (np.float32(6) * sv + np.float32(1)))
+    assert s["u00"] == float(np.float32(0.1)) and s["u0"] == 0.0 and s["fgrad"] == 0.0
+    p = oracle_mod.Oracle(64, 32, prec=oracle_mod.DOUBLE, tcase=oracle_mod.POF, svisc=0.1, u0=0.1).scalars()
+    assert p["u00"] == 0.0 and p["fgrad"] == 4 * 0.1 * 0.1 / (3 * 32.0 * 32.0)
+
+
+@pytest.mark.parametrize("tcase", ["LDC", "TGV", "POF", "COU", "VKS", "BFS"])
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_fused_equals_original(oracle_mod, tcase, prec):
+    """col_MC (FUSED) and movef+col (ORIGINAL) perform the same operations on the same values."""
+    O = oracle_mod
+    kw = dict(tcase=getattr(O, tcase), prec=prec, svisc=0.05, u0=0.1)
+    if tcase == "VKS":
+        kw.update(obstacle=O.OBS_CIRCLE, radius=5)
+    l, m = (120, 50) if tcase in ("VKS", "BFS") else (48, 40)
+    if tcase == "TGV":
+        kw["u0"] = 0.0
+    a = O.Oracle(l, m, fused=True, **kw)
+    b = O.Oracle(l, m, fused=False, **kw)
+    a.step(37)
+    b.step(37)
+    ia, ib = a.raw()[:, 1:m + 1, 1:l + 1], b.raw()[:, 1:m + 1, 1:l + 1]
+    if tcase == "BFS":  # the step routine writes into solid cells in between; compare the fluid part
+        sx, sy = l // 20, m // 2
+        keep = np.ones((m, l), bool)
+        keep[:sy - 1, :sx - 1] = False
+        ia, ib = ia[:, keep], ib[:, keep]
+    assert np.array_equal(ia, ib)
+
+
+def test_obstacle_loop_order_only_affects_obstacle_cells(oracle_mod):
+    O = oracle_mod
+    a = O.Oracle(160, 62, tcase=O.VKS, svisc=0.05, u0=0.1, obstacle=O.OBS_CIRCLE, radius=6, obs_order=O.OBS_SERIAL)
+    b = O.Oracle(160, 62, tcase=O.VKS, svisc=0.05, u0=0.1, obstacle=O.OBS_CIRCLE, radius=6, obs_order=O.OBS_SNAPSHOT)
+    a.step(60)
+    b.step(60)
+    mask, bb = a.obs()
+    fluid = mask == 0
+    ra, rb = a.raw()[:, 1:63, 1:161], b.raw()[:, 1:63, 1:161]
+    assert np.array_equal(ra[:, fluid], rb[:, fluid])
+    assert np.array_equal(a.draglift(0), b.draglift(0))
+    assert bb[4] == 113 and (bb[0], bb[1], bb[2], bb[3]) == (58, 70, 25, 37)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_mass_conserved_ldc(oracle_mod, prec):
+    O = oracle_mod
+    o = O.Oracle(64, 64, prec=prec, tcase=O.LDC, svisc=0.064, u0=0.1)
+    o.step(500)
+    d = o.diagno(1)
+    assert abs(d[2] - 1.0) < (2e-6 if prec == 0 else 1e-13)
+
+
+def test_tgv_energy_decay_rate(oracle_mod):
+    """TEST/TaylorGreenVortex/plot*.gnu: <|u|^2> decays as exp(-2 nu (kx^2 + ky^2) t)."""
+    O = oracle_mod
+    n, svisc = 128, 0.05
+    o = O.Oracle(n, n, prec=O.DOUBLE, tcase=O.TGV, svisc=svisc, u0=0.0)
+    e0 = o.diagno(1)[3]
+    t = 2000
+    o.step(t)
+    e1 = o.diagno(1)[3]
+    rate = -np.log(e1 / e0) / t
+    k2 = 2 * (2 * np.pi / n) ** 2
+    assert abs(rate / (2 * svisc * k2) - 1) < 1e-3
+    assert abs(e0 / 0.005 - 1) < 2e-3  # amplitude 0.1: <u^2+v^2> = 0.005 (plot.gnu)
+
+
+def test_poiseuille_profile_and_energy(oracle_mod):
+    """TEST/PoiseuilleFlow/plot.small.gnu: u(y) = 4 u0 (y/H)(1 - y/H), <|u|^2> = 8 u0^2 / 15."""
+    O = oracle_mod
+    l, m, u0, svisc = 16, 32, 0.1, 0.1
+    o = O.Oracle(l, m, prec=O.DOUBLE, tcase=O.POF, svisc=svisc, u0=u0)
+    o.step(30000, threads=4)
+    u, v, d = o.prof_j(l // 2)
+    y = (np.arange(1, m + 1) - 0.5) / m
+    prof = 4 * u0 * y * (1 - y)
+    assert np.max(np.abs(u - prof)) < 2e-3 * u0
+    e = o.diagno(1)[3]
+    assert abs(e / (8 * u0 ** 2 / 15) - 1) < 5e-3
+
+
+@pytest.mark.skipif(not os.path.exists(GHIA), reason="reference tree not mounted")
+def test_ldc_re100_against_ghia(oracle_mod):
+    """TEST/DrivenCavity/plot.R00100.gnu: u(y)/U at x = l/2 against ghia.y.dat (read in place)."""
+    O = oracle_mod
+    g = np.loadtxt(GHIA)
+    o = O.Oracle(128, 128, prec=O.DOUBLE, tcase=O.LDC, svisc=0.128, u0=0.1)
+    o.step(50000, threads=8)
+    u, v, d = o.prof_j(64)
+    y = (np.arange(1, 129) - 0.5) / 128
+    ui = np.interp(g[1:-1, 0], y, u / 0.1)
+    assert np.max(np.abs(ui - g[1:-1, 1])) < 5e-3
+
+
+def test_reference_profile_fixture(oracle_mod):
+    """TEST/DrivenCavity/prof_j.0000.dat (committed as tests/golden/ldc256_prof_j_ref.txt).
+
+    Its t=0 block is the rest state the oracle starts from.  Its later blocks cannot come from
+    the published SRC/: the density at the lid row reaches 1.17-1.18 (a 17% compression that
+    the half-way bounce-back with the +-u00/6 lid pair of SRC/bcond.driven.F90:141-143 does not
+    produce at Re=100, Ma=0.06), and the centre-line u stays near zero.  The oracle is therefore
+    pinned to the analytic and Ghia checks above, not to these blocks."""
+    O = oracle_mod
+    blocks = {}
+    cur = None
+    for line in open(os.path.join(GOLDEN, "ldc256_prof_j_ref.txt")):
+        if line.startswith("# t="):
+            cur = int(line.split("=")[1])
+            blocks[cur] = []
+        elif line.strip() and cur is not None:
+            blocks[cur].append([float(x) for x in line.split()])
+    g0 = np.array(blocks[0])
+    o = O.Oracle(256, 256, prec=O.SINGLE, tcase=O.LDC, svisc=0.256, u0=0.1)
+    u, v, d = o.prof_j(128)
+    np.testing.assert_allclose(np.c_[u, v, d], g0[:, 1:], atol=1e-6)
+    g20 = np.array(blocks[20000])
+    o.step(20000, threads=8)
+    u, v, d = o.prof_j(128)
+    assert g20[-1, 3] > 1.15 and abs(d[-1] - 1.0) < 0.02
+    assert np.abs(g20[:, 1]).max() < 0.01 and u.max() > 0.05
