@@ -90,6 +90,20 @@ def load(build_if_missing: bool = True):
         "bgk_launch_count": (I32, [H, P(I64)]),
         "bgk_last_error": (I32, [H, ctypes.c_char_p, ctypes.c_size_t]),
         "bgk_version": (ctypes.c_char_p, []),
+        "bgk_set_tile": (I32, [H, I32]),
+        "bgk_tune": (I32, [H, I32, P(I32), P(I32)]),
+        "bgk_batch_create": (I32, [I32, I32, I32, P(VP)]),
+        "bgk_batch_destroy": (I32, [VP]),
+        "bgk_batch_add": (I32, [VP, H]),
+        "bgk_batch_remove": (I32, [VP, H]),
+        "bgk_batch_size": (I32, [VP, P(I32), P(I64)]),
+        "bgk_batch_step": (I32, [VP, I32]),
+        "bgk_batch_step_timed": (I32, [VP, I32, P(ctypes.c_float)]),
+        "bgk_batch_sync": (I32, [VP]),
+        "bgk_batch_set_config": (I32, [VP, I32, I32, I32]),
+        "bgk_batch_get_config": (I32, [VP, P(I32)]),
+        "bgk_batch_tune": (I32, [VP, I32, P(I32)]),
+        "bgk_batch_launch_count": (I32, [VP, P(I64)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

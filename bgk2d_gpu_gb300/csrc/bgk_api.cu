@@ -47,36 +47,7 @@ cudaError_t launch_finalize4(const double *partial, int nb, double *out, cudaStr
 
 }  // namespace bgk
 
-struct bgk_handle {
-    bgk_case_desc desc;
-    int dev = 0;
-    KernelTable T{};
-    Lattice L{};
-    CaseSetup cs;
-    void *d_planes = nullptr;
-    size_t planes_bytes = 0;
-    uint32_t *d_mask = nullptr;
-    double *d_inflow = nullptr;
-    double *d_partial = nullptr;
-    double *d_out = nullptr;
-    int nb_red = 0;
-    double *d_uprev = nullptr, *d_vprev = nullptr;
-    int64_t res_itime = -1;
-    void *d_stage = nullptr;
-    size_t stage_bytes = 0;
-    cudaStream_t st = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    int graph_steps = 32;
-    int cur = 0;     // ping-pong: buffer holding the current state
-    int phase = 0;   // AA: 0 = post-collision (swapped slots), 1 = streamed
-    int64_t itime = 0;
-    int64_t launches = 0;
-    int cfg = 2;
-    int host_bytes = 4;
-    int sticky = BGK_OK;
-    std::string err;
-};
+#include "bgk_handle.h"
 
 namespace {
 
@@ -105,7 +76,11 @@ int fail(bgk_handle *h, int code, const char *fmt, ...)
         if (!(h)) return BGK_E_INVALID;                     \
         if ((h)->sticky != BGK_OK) return (h)->sticky;      \
         if (cudaSetDevice((h)->dev) != cudaSuccess) return fail(h, BGK_E_CUDA, "cudaSetDevice"); \
+        if ((h)->wait_ev) CK(h, cudaStreamWaitEvent((h)->st, (h)->wait_ev, 0)); \
     } while (0)
+
+#define NOT_IN_BATCH(h) \
+    do { if ((h)->batch) return fail(h, BGK_E_INVALID, "handle is attached to a batch; step the batch"); } while (0)
 
 bool get_table(int storage, int compute, KernelTable &t)
 {
@@ -418,6 +393,7 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
 int bgk_destroy(bgk_handle *h)
 {
     if (!h) return BGK_E_INVALID;
+    if (h->batch) bgk_batch_remove((bgk_batch *)h->batch, h);
     cudaSetDevice(h->dev);
     if (h->st) cudaStreamSynchronize(h->st);
     release(h);
@@ -466,6 +442,7 @@ int bgk_propagation(bgk_handle *h)
 int bgk_collision(bgk_handle *h, int32_t itime)
 {
     CHECK_HANDLE(h);
+    NOT_IN_BATCH(h);
     (void)itime;
     return launch_step(h);
 }
@@ -473,12 +450,14 @@ int bgk_collision(bgk_handle *h, int32_t itime)
 int bgk_step(bgk_handle *h, int32_t nsteps)
 {
     CHECK_HANDLE(h);
+    NOT_IN_BATCH(h);
     return steps_impl(h, nsteps);
 }
 
 int bgk_step_timed(bgk_handle *h, int32_t nsteps, float *ms)
 {
     CHECK_HANDLE(h);
+    NOT_IN_BATCH(h);
     if (!ms) return BGK_E_INVALID;
     CK(h, cudaEventRecord(h->ev0, h->st));
     int rc = steps_impl(h, nsteps);
@@ -613,6 +592,47 @@ int bgk_footprint(bgk_handle *h, int64_t *device_bytes, int32_t *bytes_per_cell)
     if (!h) return BGK_E_INVALID;
     if (device_bytes) *device_bytes = (int64_t)(h->planes_bytes + h->stage_bytes);
     if (bytes_per_cell) *bytes_per_cell = 18 * h->T.elem_bytes;
+    return BGK_OK;
+}
+
+int bgk_set_tile(bgk_handle *h, int32_t tile_cfg)
+{
+    CHECK_HANDLE(h);
+    if (tile_cfg < 0 || tile_cfg >= NUM_CFG) return fail(h, BGK_E_INVALID, "tile configuration %d", tile_cfg);
+    if (tile_cfg != h->cfg) {
+        for (int i = 0; i < 2; ++i)
+            if (h->graph[i]) { cudaGraphExecDestroy(h->graph[i]); h->graph[i] = nullptr; }
+        h->cfg = tile_cfg;
+    }
+    return BGK_OK;
+}
+
+int bgk_tune(bgk_handle *h, int32_t trial_steps, int32_t *tile_cfg, int32_t *steps_run)
+{
+    CHECK_HANDLE(h);
+    NOT_IN_BATCH(h);
+    if (trial_steps < 2) return fail(h, BGK_E_INVALID, "trial_steps < 2");
+    const int n = trial_steps & ~1;
+    float best = 1e30f;
+    int best_cfg = h->cfg, rc;
+    int64_t run = 0;
+    for (int c = 0; c < NUM_CFG; ++c) {
+        if ((rc = bgk_set_tile(h, c))) return rc;
+        for (int s = 0; s < 2; ++s)
+            if ((rc = launch_step(h))) return rc;
+        float ms = 0;
+        CK(h, cudaEventRecord(h->ev0, h->st));
+        for (int s = 0; s < n; ++s)
+            if ((rc = launch_step(h))) return rc;
+        CK(h, cudaEventRecord(h->ev1, h->st));
+        CK(h, cudaEventSynchronize(h->ev1));
+        CK(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+        run += n + 2;
+        if (ms < best) { best = ms; best_cfg = c; }
+    }
+    if ((rc = bgk_set_tile(h, best_cfg))) return rc;
+    if (tile_cfg) *tile_cfg = best_cfg;
+    if (steps_run) *steps_run = (int32_t)run;
     return BGK_OK;
 }
 

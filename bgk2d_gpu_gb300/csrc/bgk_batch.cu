@@ -1,0 +1,370 @@
+// bgk_batch.cu -- many independent lattices advanced by one persistent launch per time step.
+//
+// The reference advances one domain per run (SRC/bgk2d.F90:92-113).  A batch keeps any number
+// of ping-pong handles of the same (storage, compute) kind resident; one persistent kernel per
+// time step walks a work list of row-segment tiles over all of them (batch_pp_kernel), and the
+// step loop is replayed from CUDA graphs.  Tile shape, persistent grid size and steps per
+// graph are chosen by bgk_batch_tune from timed trial steps.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "bgk_handle.h"
+
+using namespace bgk;
+
+struct bgk_batch {
+    int storage = 0, compute = 0, dev = 0;
+    KernelTable T{};
+    std::vector<bgk_handle *> members;
+    Lattice *d_lats = nullptr;
+    int *d_cur = nullptr;
+    int4 *d_tiles = nullptr;
+    int ntiles = 0;
+    size_t cap_lats = 0, cap_tiles = 0;
+    bool dirty = true;              // work list / device arrays need a rebuild
+    cudaStream_t st = nullptr;
+    cudaEvent_t done = nullptr, ev0 = nullptr, ev1 = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_built_for = -1;       // generation the graph was captured for
+    int generation = 0;
+    int cfg = 2;                    // tile shape index (TILE_CFGS)
+    int blocks_per_sm = 8;
+    int graph_steps = 32;           // even
+    int sms = 152;
+    int64_t launches = 0;
+    int64_t steps = 0;
+};
+
+namespace {
+
+int bfail(bgk_handle *h, int code) { (void)h; return code; }
+
+int rebuild(bgk_batch *b)
+{
+    if (!b->dirty) return BGK_OK;
+    const TileCfg tc = TILE_CFGS[b->cfg];
+    std::vector<Lattice> lats;
+    std::vector<int> cur;
+    std::vector<int4> tiles;
+    for (size_t i = 0; i < b->members.size(); ++i) {
+        bgk_handle *h = b->members[i];
+        lats.push_back(h->L);
+        cur.push_back(h->cur);
+        const int gx = (h->L.nvec + tc.txv - 1) / tc.txv, gy = (h->L.ly + tc.ty - 1) / tc.ty;
+        for (int by = 0; by < gy; ++by)
+            for (int bx = 0; bx < gx; ++bx) tiles.push_back(make_int4((int)i, bx, by, 0));
+    }
+    if (lats.size() > b->cap_lats) {
+        if (b->d_lats) cudaFree(b->d_lats);
+        if (b->d_cur) cudaFree(b->d_cur);
+        b->cap_lats = std::max<size_t>(lats.size(), 2 * b->cap_lats);
+        if (cudaMalloc(&b->d_lats, b->cap_lats * sizeof(Lattice)) != cudaSuccess ||
+            cudaMalloc(&b->d_cur, b->cap_lats * sizeof(int)) != cudaSuccess) {
+            cudaGetLastError();
+            b->cap_lats = 0;
+            return BGK_E_NOMEM;
+        }
+    }
+    if (tiles.size() > b->cap_tiles) {
+        if (b->d_tiles) cudaFree(b->d_tiles);
+        b->cap_tiles = std::max<size_t>(tiles.size(), 2 * b->cap_tiles);
+        if (cudaMalloc(&b->d_tiles, b->cap_tiles * sizeof(int4)) != cudaSuccess) {
+            cudaGetLastError();
+            b->cap_tiles = 0;
+            return BGK_E_NOMEM;
+        }
+    }
+    if (!lats.empty()) {
+        if (cudaMemcpyAsync(b->d_lats, lats.data(), lats.size() * sizeof(Lattice), cudaMemcpyHostToDevice, b->st) ||
+            cudaMemcpyAsync(b->d_cur, cur.data(), cur.size() * sizeof(int), cudaMemcpyHostToDevice, b->st) ||
+            cudaMemcpyAsync(b->d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, b->st))
+            return BGK_E_CUDA;
+    }
+    if (cudaStreamSynchronize(b->st) != cudaSuccess) return BGK_E_CUDA;
+    b->ntiles = (int)tiles.size();
+    b->dirty = false;
+    b->generation++;
+    return BGK_OK;
+}
+
+int sync_cur(bgk_batch *b)
+{
+    std::vector<int> cur;
+    for (auto *h : b->members) cur.push_back(h->cur);
+    if (cur.empty()) return BGK_OK;
+    if (cudaMemcpyAsync(b->d_cur, cur.data(), cur.size() * sizeof(int), cudaMemcpyHostToDevice, b->st) != cudaSuccess)
+        return BGK_E_CUDA;
+    return cudaStreamSynchronize(b->st) == cudaSuccess ? BGK_OK : BGK_E_CUDA;
+}
+
+int grid_of(const bgk_batch *b) { return std::max(1, std::min(b->ntiles, b->blocks_per_sm * b->sms)); }
+
+int launch_one(bgk_batch *b, int parity)
+{
+    if (b->ntiles == 0) return BGK_OK;
+    if (b->T.batch_step(b->d_lats, b->d_cur, b->d_tiles, b->ntiles, parity, b->cfg, grid_of(b), b->st) != cudaSuccess)
+        return BGK_E_CUDA;
+    b->launches++;
+    return BGK_OK;
+}
+
+int capture(bgk_batch *b)
+{
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return BGK_E_CUDA;
+    const int64_t l0 = b->launches;
+    int rc = BGK_OK;
+    for (int s = 0; s < b->graph_steps && rc == BGK_OK; ++s) rc = launch_one(b, s & 1);
+    b->launches = l0;
+    cudaError_t e = cudaStreamEndCapture(b->st, &g);
+    if (rc != BGK_OK || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return rc != BGK_OK ? rc : BGK_E_CUDA;
+    }
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return BGK_E_CUDA;
+    b->graph_built_for = b->generation;
+    return BGK_OK;
+}
+
+void advance_members(bgk_batch *b, int n)
+{
+    for (auto *h : b->members) {
+        h->itime += n;
+        h->launches += n;
+        if (n & 1) h->cur ^= 1;
+    }
+    b->steps += n;
+}
+
+int step_impl(bgk_batch *b, int n, bool use_graph)
+{
+    int rc = rebuild(b);
+    if (rc) return rc;
+    if (b->members.empty() || n <= 0) return BGK_OK;
+    if (use_graph) {
+        while (n >= b->graph_steps) {
+            if (b->graph_built_for != b->generation && (rc = capture(b))) return rc;
+            if (cudaGraphLaunch(b->graph, b->st) != cudaSuccess) return BGK_E_CUDA;
+            b->launches += b->graph_steps;
+            advance_members(b, b->graph_steps);  // graph_steps is even: buffers unchanged
+            n -= b->graph_steps;
+        }
+    }
+    for (int s = 0; s < n; ++s)
+        if ((rc = launch_one(b, s & 1))) return rc;
+    advance_members(b, n);
+    if (n & 1) {
+        // members flipped buffers: refresh the device copy before the next launch
+        if (cudaStreamSynchronize(b->st) != cudaSuccess) return BGK_E_CUDA;
+        if ((rc = sync_cur(b))) return rc;
+    }
+    if (cudaEventRecord(b->done, b->st) != cudaSuccess) return BGK_E_CUDA;
+    return BGK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bgk_batch_create(int32_t storage, int32_t compute, int32_t device, bgk_batch **out)
+{
+    if (!out) return BGK_E_INVALID;
+    *out = nullptr;
+    bgk_batch *b = new bgk_batch();
+    b->storage = storage;
+    b->compute = compute;
+    b->dev = device;
+    bgk_case_desc d;
+    bgk_default_desc(&d);
+    d.lx = d.ly = 8;
+    d.storage = storage;
+    d.compute = compute;
+    d.device = device;
+    // the kernel table comes from a probe handle of the same kind
+    bgk_handle *probe = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) { delete b; return BGK_E_CUDA; }
+    int rc = bgk_create(&d, &probe);
+    if (rc) { delete b; return rc; }
+    b->T = probe->T;
+    bgk_destroy(probe);
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
+        delete b;
+        return BGK_E_CUDA;
+    }
+    *out = b;
+    return BGK_OK;
+}
+
+int bgk_batch_destroy(bgk_batch *b)
+{
+    if (!b) return BGK_E_INVALID;
+    cudaSetDevice(b->dev);
+    cudaStreamSynchronize(b->st);
+    for (auto *h : b->members) { h->batch = nullptr; h->wait_ev = nullptr; }
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->d_lats) cudaFree(b->d_lats);
+    if (b->d_cur) cudaFree(b->d_cur);
+    if (b->d_tiles) cudaFree(b->d_tiles);
+    if (b->done) cudaEventDestroy(b->done);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+    return BGK_OK;
+}
+
+int bgk_batch_add(bgk_batch *b, bgk_handle *h)
+{
+    if (!b || !h) return BGK_E_INVALID;
+    if (h->batch) return BGK_E_INVALID;
+    if (h->desc.storage != b->storage || h->desc.compute != b->compute || h->dev != b->dev ||
+        h->L.scheme != BGK_SCHEME_PINGPONG)
+        return BGK_E_INVALID;
+    if (h->sticky) return h->sticky;
+    cudaSetDevice(b->dev);
+    if (cudaStreamSynchronize(h->st) != cudaSuccess || cudaStreamSynchronize(b->st) != cudaSuccess) return BGK_E_CUDA;
+    b->members.push_back(h);
+    h->batch = b;
+    h->wait_ev = b->done;
+    b->dirty = true;
+    return BGK_OK;
+}
+
+int bgk_batch_remove(bgk_batch *b, bgk_handle *h)
+{
+    if (!b || !h) return BGK_E_INVALID;
+    auto it = std::find(b->members.begin(), b->members.end(), h);
+    if (it == b->members.end()) return BGK_E_NOTFOUND;
+    cudaSetDevice(b->dev);
+    if (cudaStreamSynchronize(b->st) != cudaSuccess) return BGK_E_CUDA;
+    b->members.erase(it);
+    h->batch = nullptr;
+    h->wait_ev = nullptr;
+    b->dirty = true;
+    return BGK_OK;
+}
+
+int bgk_batch_size(bgk_batch *b, int32_t *members, int64_t *cells)
+{
+    if (!b) return BGK_E_INVALID;
+    int64_t c = 0;
+    for (auto *h : b->members) c += (int64_t)h->desc.lx * h->desc.ly;
+    if (members) *members = (int32_t)b->members.size();
+    if (cells) *cells = c;
+    return BGK_OK;
+}
+
+int bgk_batch_step(bgk_batch *b, int32_t nsteps)
+{
+    if (!b || nsteps < 0) return BGK_E_INVALID;
+    if (cudaSetDevice(b->dev) != cudaSuccess) return BGK_E_CUDA;
+    return step_impl(b, nsteps, true);
+}
+
+int bgk_batch_step_timed(bgk_batch *b, int32_t nsteps, float *ms)
+{
+    if (!b || !ms || nsteps < 0) return BGK_E_INVALID;
+    if (cudaSetDevice(b->dev) != cudaSuccess) return BGK_E_CUDA;
+    int rc = rebuild(b);
+    if (rc) return rc;
+    if (cudaEventRecord(b->ev0, b->st) != cudaSuccess) return BGK_E_CUDA;
+    if ((rc = step_impl(b, nsteps, true))) return rc;
+    if (cudaEventRecord(b->ev1, b->st) != cudaSuccess || cudaEventSynchronize(b->ev1) != cudaSuccess ||
+        cudaEventElapsedTime(ms, b->ev0, b->ev1) != cudaSuccess)
+        return BGK_E_CUDA;
+    return BGK_OK;
+}
+
+int bgk_batch_sync(bgk_batch *b)
+{
+    if (!b) return BGK_E_INVALID;
+    cudaSetDevice(b->dev);
+    return cudaStreamSynchronize(b->st) == cudaSuccess ? BGK_OK : BGK_E_CUDA;
+}
+
+int bgk_batch_set_config(bgk_batch *b, int32_t tile_cfg, int32_t blocks_per_sm, int32_t graph_steps)
+{
+    if (!b || tile_cfg < 0 || tile_cfg >= NUM_CFG || blocks_per_sm < 1 || graph_steps < 2 || (graph_steps & 1))
+        return BGK_E_INVALID;
+    if (tile_cfg != b->cfg) b->dirty = true;
+    if (tile_cfg != b->cfg || blocks_per_sm != b->blocks_per_sm || graph_steps != b->graph_steps) b->graph_built_for = -1;
+    b->cfg = tile_cfg;
+    b->blocks_per_sm = blocks_per_sm;
+    b->graph_steps = graph_steps;
+    return BGK_OK;
+}
+
+int bgk_batch_get_config(bgk_batch *b, int32_t out[3])
+{
+    if (!b || !out) return BGK_E_INVALID;
+    out[0] = b->cfg; out[1] = b->blocks_per_sm; out[2] = b->graph_steps;
+    return BGK_OK;
+}
+
+// Autotuner: times `trial_steps` real steps (they advance the members) for every tile shape
+// and persistent grid size, then the steps-per-graph candidates, and keeps the fastest.
+int bgk_batch_tune(bgk_batch *b, int32_t trial_steps, int32_t *steps_run)
+{
+    if (!b || trial_steps < 2) return BGK_E_INVALID;
+    if (cudaSetDevice(b->dev) != cudaSuccess) return BGK_E_CUDA;
+    int64_t run = 0;
+    const int bps_opts[4] = {2, 4, 8, 16};
+    float best = 1e30f;
+    int best_cfg = b->cfg, best_bps = b->blocks_per_sm;
+    const int n = trial_steps & ~1;
+    for (int c = 0; c < NUM_CFG; ++c) {
+        for (int bi = 0; bi < 4; ++bi) {
+            int rc = bgk_batch_set_config(b, c, bps_opts[bi], b->graph_steps);
+            if (rc) return rc;
+            if ((rc = rebuild(b))) return rc;
+            if ((rc = step_impl(b, 2, false))) return rc;  // warm-up at this shape
+            run += 2;
+            if (cudaEventRecord(b->ev0, b->st) != cudaSuccess) return BGK_E_CUDA;
+            if ((rc = step_impl(b, n, false))) return rc;
+            run += n;
+            float ms = 0;
+            if (cudaEventRecord(b->ev1, b->st) != cudaSuccess || cudaEventSynchronize(b->ev1) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, b->ev0, b->ev1) != cudaSuccess)
+                return BGK_E_CUDA;
+            if (ms < best) { best = ms; best_cfg = c; best_bps = bps_opts[bi]; }
+        }
+    }
+    const int g_opts[3] = {8, 32, 128};
+    float gbest = 1e30f;
+    int best_g = b->graph_steps;
+    for (int gi = 0; gi < 3; ++gi) {
+        int rc = bgk_batch_set_config(b, best_cfg, best_bps, g_opts[gi]);
+        if (rc) return rc;
+        const int m = std::max(g_opts[gi], n) / g_opts[gi] * g_opts[gi];
+        if ((rc = step_impl(b, g_opts[gi], true))) return rc;  // capture + warm-up
+        run += g_opts[gi];
+        float ms = 0;
+        if ((rc = bgk_batch_step_timed(b, m, &ms))) return rc;
+        run += m;
+        const float per = ms / m;
+        if (per < gbest) { gbest = per; best_g = g_opts[gi]; }
+    }
+    int rc = bgk_batch_set_config(b, best_cfg, best_bps, best_g);
+    if (rc) return rc;
+    if (steps_run) *steps_run = (int32_t)run;
+    return BGK_OK;
+}
+
+int bgk_batch_launch_count(bgk_batch *b, int64_t *launches)
+{
+    if (!b || !launches) return BGK_E_INVALID;
+    *launches = b->launches;
+    return BGK_OK;
+}
+
+}  // extern "C"

@@ -46,8 +46,14 @@ __host__ __device__ constexpr float scale_of(int q) {
 
 // Storage traits: conversion between the stored element and the compute kind K.
 template <typename S> struct Store;
+template <typename S> struct Is16 { static constexpr bool value = false; };
+template <> struct Is16<__half> { static constexpr bool value = true; };
+template <> struct Is16<__nv_bfloat16> { static constexpr bool value = true; };
+
 template <> struct Store<float> {
     static constexpr int VEC = 4;
+    __device__ __forceinline__ static float raw_get(float v) { return v; }
+    __device__ __forceinline__ static float raw_put(float v) { return v; }
     template <typename K, int q> __device__ __forceinline__ static K get(float v) { return (K)v; }
     template <typename K, int q> __device__ __forceinline__ static float put(K v) { return (float)v; }
     template <typename K> __device__ __forceinline__ static K getq(float v, int) { return (K)v; }
@@ -55,6 +61,8 @@ template <> struct Store<float> {
 };
 template <> struct Store<double> {
     static constexpr int VEC = 2;
+    __device__ __forceinline__ static double raw_get(double v) { return v; }
+    __device__ __forceinline__ static double raw_put(double v) { return v; }
     template <typename K, int q> __device__ __forceinline__ static K get(double v) { return (K)v; }
     template <typename K, int q> __device__ __forceinline__ static double put(K v) { return (double)v; }
     template <typename K> __device__ __forceinline__ static K getq(double v, int) { return (K)v; }
@@ -62,6 +70,12 @@ template <> struct Store<double> {
 };
 template <> struct Store<__half> {
     static constexpr int VEC = 8;
+    __device__ __forceinline__ static float raw_get(__half v) { return __half2float(v); }
+    __device__ __forceinline__ static __half raw_put(float v) { return __float2half_rn(v); }
+    __device__ __forceinline__ static uint32_t pack2(float a, float b) {
+        __half2 h = __floats2half2_rn(a, b);
+        return *reinterpret_cast<uint32_t *>(&h);
+    }
     template <typename K, int q> __device__ __forceinline__ static K get(__half v) {
         return (K)(__half2float(v) * (1.0f / scale_of(q)));
     }
@@ -77,6 +91,12 @@ template <> struct Store<__half> {
 };
 template <> struct Store<__nv_bfloat16> {
     static constexpr int VEC = 8;
+    __device__ __forceinline__ static float raw_get(__nv_bfloat16 v) { return __bfloat162float(v); }
+    __device__ __forceinline__ static __nv_bfloat16 raw_put(float v) { return __float2bfloat16_rn(v); }
+    __device__ __forceinline__ static uint32_t pack2(float a, float b) {
+        __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        return *reinterpret_cast<uint32_t *>(&h);
+    }
     template <typename K, int q> __device__ __forceinline__ static K get(__nv_bfloat16 v) {
         return (K)(__bfloat162float(v) * (1.0f / scale_of(q)));
     }

@@ -97,6 +97,19 @@ cudaError_t fields(const Lattice &L, int cur, int phase, bool obs, double *rho, 
 }
 
 template <typename S, typename K>
+cudaError_t batch_step(const Lattice *lats, const int *cur, const int4 *tiles, int ntiles, int parity, int cfg, int grid,
+                       cudaStream_t st)
+{
+    switch (cfg) {
+    case 0: batch_pp_kernel<S, K, 32, 4><<<grid, dim3(32, 4), 0, st>>>(lats, cur, tiles, ntiles, parity); break;
+    case 1: batch_pp_kernel<S, K, 64, 2><<<grid, dim3(64, 2), 0, st>>>(lats, cur, tiles, ntiles, parity); break;
+    case 3: batch_pp_kernel<S, K, 128, 2><<<grid, dim3(128, 2), 0, st>>>(lats, cur, tiles, ntiles, parity); break;
+    default: batch_pp_kernel<S, K, 128, 1><<<grid, dim3(128, 1), 0, st>>>(lats, cur, tiles, ntiles, parity); break;
+    }
+    return cudaGetLastError();
+}
+
+template <typename S, typename K>
 KernelTable make_table()
 {
     KernelTable t;
@@ -110,6 +123,7 @@ KernelTable make_table()
     t.residual = &residual<S, K>;
     t.draglift = &draglift<S, K>;
     t.fields = &fields<S, K>;
+    t.batch_step = &batch_step<S, K>;
     return t;
 }
 

@@ -77,6 +77,59 @@ __device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced
     x[8] = x19 - omega * (x19 - e19);
 }
 
+// Collision of the 16-bit storage kernels, on scaled deviations D_q = s_q (f_q - w_q) in FP32.
+// Same BGK relaxation as collide<K> rewritten for throughput: with j = rho u and
+// A = (rho - 1) - 1.5 j.u, the equilibrium deviation is w_q (A + 3 c.j + 4.5 (c.j)(c.u)); the
+// scales satisfy s_q w_q = 8/9 for every q, so D_q' = (1 - omega) D_q + (8/9) omega (...).
+__device__ __forceinline__ void collide_scaled(float (&D)[9], float omega, float fgrad, bool forced)
+{
+    const float i32 = 1.0f / 32.0f, i8 = 1.0f / 8.0f;
+    const float sd = (D[D01] + D[D03]) + (D[D10] + D[D12]);
+    const float sa = (D[D05] + D[D08]) + (D[D14] + D[D17]);
+    const float rho1 = fmaf(sd, i32, fmaf(sa, i8, D[D19] * 0.5f));
+    const float rho = 1.0f + rho1;
+    const float dpp = D[D03] - D[D10];  // c = (1, 1)
+    const float dpm = D[D01] - D[D12];  // c = (1,-1)
+    const float jx = fmaf(dpp + dpm, i32, (D[D05] - D[D14]) * i8);
+    const float jy = fmaf(dpp - dpm, i32, (D[D08] - D[D17]) * i8);
+    const float rinv = __fdividef(1.0f, rho);
+    const float ux = jx * rinv, uy = jy * rinv;
+    const float A = fmaf(-1.5f, fmaf(jx, ux, jy * uy), rho1);
+    const float omc = 1.0f - omega, k = omega * (8.0f / 9.0f);
+    auto pair = [&](int qp, int qm, float cj, float cu) {
+        const float t = fmaf(4.5f * cj, cu, A);
+        const float s3 = 3.0f * cj;
+        D[qp] = fmaf(omc, D[qp], k * (t + s3));
+        D[qm] = fmaf(omc, D[qm], k * (t - s3));
+    };
+    pair(D05, D14, jx, ux);
+    pair(D08, D17, jy, uy);
+    pair(D03, D10, jx + jy, ux + uy);
+    pair(D01, D12, jx - jy, ux - uy);
+    D[D19] = fmaf(omc, D[D19], k * A);
+    if (forced) {
+        const float F = fgrad * rho;  // +F on 01,03,05 and -F on 10,12,14 (SRC/col_MC.F90:285-291)
+        D[D01] += 32.0f * F; D[D03] += 32.0f * F; D[D05] += 8.0f * F;
+        D[D10] -= 32.0f * F; D[D12] -= 32.0f * F; D[D14] -= 8.0f * F;
+    }
+}
+
+// collision on unscaled deviations in compute kind K, for any storage kind
+template <typename S, typename K>
+__device__ __forceinline__ void collide_stored(K (&v)[9], K omega, K fgrad, bool forced)
+{
+    if constexpr (Is16<S>::value) {
+        float D[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) D[q] = (float)v[q] * scale_of(q);  // exact: powers of two
+        collide_scaled(D, (float)omega, (float)fgrad, forced);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) v[q] = (K)(D[q] * (1.0f / scale_of(q)));
+    } else {
+        collide<K>(v, omega, fgrad, forced);
+    }
+}
+
 // equilibrium deviation of the outflow ghost (rho = 1, local u): bcond.inflow.F90:211-230
 template <typename K>
 __device__ __forceinline__ K outflow_eq(int q, K a01, K a03, K a05, K a08, K a10, K a12, K a14, K a17)
@@ -136,10 +189,14 @@ __device__ __forceinline__ K shfl_down(K v, int w) { return __shfl_down_sync(0xf
 // Load VEC consecutive values of direction q pulled from (x - c_q): aligned 16-byte load of
 // row y - cy at the thread's own columns; the +-1 column shift comes from the neighbouring
 // lane, or from one scalar load at a segment edge.
-template <typename S, typename K, int q, int W>
+template <typename S, typename K, int q, int W, bool RAW = false>
 __device__ __forceinline__ void pull_vec(const Lattice &L, const S *plane, int xv, int y, bool loads,
                                          int seg_lane, K (&out)[vec_of<S>()])
 {
+    auto cvt = [](S v) -> K {
+        if constexpr (RAW) return (K)Store<S>::raw_get(v);
+        else return Store<S>::template get<K, q>(v);
+    };
     constexpr int VEC = vec_of<S>();
     constexpr int sx = -cx_of(q), sy = -cy_of(q);
     const int64_t idx = cell_index<S>(L, xv, y + sy);
@@ -151,19 +208,19 @@ __device__ __forceinline__ void pull_vec(const Lattice &L, const S *plane, int x
     }
     K kv[VEC];
 #pragma unroll
-    for (int c = 0; c < VEC; ++c) kv[c] = Store<S>::template get<K, q>(v[c]);
+    for (int c = 0; c < VEC; ++c) kv[c] = cvt(v[c]);
     if (sx == 0) {
 #pragma unroll
         for (int c = 0; c < VEC; ++c) out[c] = kv[c];
     } else if (sx == -1) {
         K left = shfl_up(kv[VEC - 1], W);
-        if ((seg_lane % W) == 0 && loads) left = Store<S>::template get<K, q>(plane[idx - 1]);
+        if ((seg_lane % W) == 0 && loads) left = cvt(plane[idx - 1]);
         out[0] = left;
 #pragma unroll
         for (int c = 1; c < VEC; ++c) out[c] = kv[c - 1];
     } else {
         K right = shfl_down(kv[0], W);
-        if ((seg_lane % W) == W - 1 && loads) right = Store<S>::template get<K, q>(plane[idx + VEC]);
+        if ((seg_lane % W) == W - 1 && loads) right = cvt(plane[idx + VEC]);
 #pragma unroll
         for (int c = 0; c < VEC - 1; ++c) out[c] = kv[c + 1];
         out[VEC - 1] = right;
@@ -217,6 +274,42 @@ __device__ __forceinline__ K pull_rule(const Lattice &L, int q, int x, int y, Pl
     return plane_at(q, sx, sy);
 }
 
+// relax VEC cells in place: x[q][c] holds direction q of cell c (scaled 16-bit units when RAW)
+template <typename S, typename K, bool RAW>
+__device__ __forceinline__ void relax_vec(K (&x)[9][vec_of<S>()], K omega, K fgrad, bool forced)
+{
+#pragma unroll
+    for (int c = 0; c < vec_of<S>(); ++c) {
+        K v[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) v[q] = x[q][c];
+        if constexpr (RAW) collide_scaled(v, (float)omega, (float)fgrad, forced);
+        else collide<K>(v, omega, fgrad, forced);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) x[q][c] = v[q];
+    }
+}
+
+// store VEC values of direction q as one 16-byte vector
+template <typename S, typename K, int q, bool RAW>
+__device__ __forceinline__ void store_vec(S *p, const K (&v)[vec_of<S>()])
+{
+    constexpr int VEC = vec_of<S>();
+    if constexpr (RAW) {
+        uint4 u;
+        u.x = Store<S>::pack2((float)v[0], (float)v[1]);
+        u.y = Store<S>::pack2((float)v[2], (float)v[3]);
+        u.z = Store<S>::pack2((float)v[4], (float)v[5]);
+        u.w = Store<S>::pack2((float)v[6], (float)v[7]);
+        *reinterpret_cast<uint4 *>(p) = u;
+    } else {
+        S o[VEC];
+#pragma unroll
+        for (int c = 0; c < VEC; ++c) o[c] = Store<S>::template put<K, q>(v[c]);
+        stv<S>(p, o);
+    }
+}
+
 // ---------------------------------------------------------------------------------------------
 // Ping-pong kernel
 // ---------------------------------------------------------------------------------------------
@@ -240,20 +333,21 @@ __device__ void pp_cell_slow(const Lattice &L, const S *src, S *dst, S *rest, in
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) v[q] = pull_rule<S, K, HAS_OBS>(L, q, x, y, plane_at, own, ghost_xhi);
     v[8] = ldq<S, K>(rest, me, D19);
-    collide<K>(v, (K)L.omega, (K)L.fgrad, L.forced != 0);
+    collide_stored<S, K>(v, (K)L.omega, (K)L.fgrad, L.forced != 0);
 #pragma unroll
     for (int q = 0; q < 8; ++q) dst[q * pe + me] = Store<S>::template putq<K>(v[q], q);
     rest[me] = Store<S>::template putq<K>(v[8], D19);
 }
 
+// one tile of TXV*VEC x TY cells at tile coordinates (bx, by) of lattice L
 template <typename S, typename K, int TXV, int TY, bool HAS_OBS>
-__global__ void __launch_bounds__(TXV *TY) pp_kernel(const Lattice L, const int parity)
+__device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const int by, const int parity)
 {
     constexpr int VEC = vec_of<S>();
     constexpr int W = TXV < 32 ? TXV : 32;
     const int tx = threadIdx.x;
-    const int k = blockIdx.x * TXV + tx;
-    const int y = blockIdx.y * TY + threadIdx.y + 1;
+    const int k = bx * TXV + tx;
+    const int y = by * TY + threadIdx.y + 1;
     const bool in_rows = y <= L.ly;
     const bool loads = in_rows && k <= L.nvec;
     const bool active = in_rows && k < L.nvec;
@@ -264,16 +358,17 @@ __global__ void __launch_bounds__(TXV *TY) pp_kernel(const Lattice L, const int 
     S *dst = base + (parity ? 0 : 9) * pe;
     S *rest = base + 8 * pe;
 
+    constexpr bool RAW = Is16<S>::value;
     K x[9][VEC];
-    pull_vec<S, K, D01, W>(L, src + D01 * pe, xv, y, loads, tx, x[D01]);
-    pull_vec<S, K, D03, W>(L, src + D03 * pe, xv, y, loads, tx, x[D03]);
-    pull_vec<S, K, D05, W>(L, src + D05 * pe, xv, y, loads, tx, x[D05]);
-    pull_vec<S, K, D08, W>(L, src + D08 * pe, xv, y, loads, tx, x[D08]);
-    pull_vec<S, K, D10, W>(L, src + D10 * pe, xv, y, loads, tx, x[D10]);
-    pull_vec<S, K, D12, W>(L, src + D12 * pe, xv, y, loads, tx, x[D12]);
-    pull_vec<S, K, D14, W>(L, src + D14 * pe, xv, y, loads, tx, x[D14]);
-    pull_vec<S, K, D17, W>(L, src + D17 * pe, xv, y, loads, tx, x[D17]);
-    pull_vec<S, K, D19, W>(L, rest, xv, y, loads, tx, x[D19]);
+    pull_vec<S, K, D01, W, RAW>(L, src + D01 * pe, xv, y, loads, tx, x[D01]);
+    pull_vec<S, K, D03, W, RAW>(L, src + D03 * pe, xv, y, loads, tx, x[D03]);
+    pull_vec<S, K, D05, W, RAW>(L, src + D05 * pe, xv, y, loads, tx, x[D05]);
+    pull_vec<S, K, D08, W, RAW>(L, src + D08 * pe, xv, y, loads, tx, x[D08]);
+    pull_vec<S, K, D10, W, RAW>(L, src + D10 * pe, xv, y, loads, tx, x[D10]);
+    pull_vec<S, K, D12, W, RAW>(L, src + D12 * pe, xv, y, loads, tx, x[D12]);
+    pull_vec<S, K, D14, W, RAW>(L, src + D14 * pe, xv, y, loads, tx, x[D14]);
+    pull_vec<S, K, D17, W, RAW>(L, src + D17 * pe, xv, y, loads, tx, x[D17]);
+    pull_vec<S, K, D19, W, RAW>(L, rest, xv, y, loads, tx, x[D19]);
     if (!active) return;
 
     bool slow = (y == 1) || (y == L.ly) || (k == 0) || (k == L.nvec - 1);
@@ -284,29 +379,45 @@ __global__ void __launch_bounds__(TXV *TY) pp_kernel(const Lattice L, const int 
         for (int xc = xv; xc <= xe; ++xc) pp_cell_slow<S, K, HAS_OBS>(L, src, dst, rest, xc, y);
         return;
     }
-    const K omega = (K)L.omega, fgrad = (K)L.fgrad;
-    const bool forced = L.forced != 0;
-    S o[9][VEC];
-#pragma unroll
-    for (int c = 0; c < VEC; ++c) {
-        K v[9];
-#pragma unroll
-        for (int q = 0; q < 9; ++q) v[q] = x[q][c];
-        collide<K>(v, omega, fgrad, forced);
-        o[0][c] = Store<S>::template put<K, D01>(v[0]);
-        o[1][c] = Store<S>::template put<K, D03>(v[1]);
-        o[2][c] = Store<S>::template put<K, D05>(v[2]);
-        o[3][c] = Store<S>::template put<K, D08>(v[3]);
-        o[4][c] = Store<S>::template put<K, D10>(v[4]);
-        o[5][c] = Store<S>::template put<K, D12>(v[5]);
-        o[6][c] = Store<S>::template put<K, D14>(v[6]);
-        o[7][c] = Store<S>::template put<K, D17>(v[7]);
-        o[8][c] = Store<S>::template put<K, D19>(v[8]);
-    }
+    relax_vec<S, K, RAW>(x, (K)L.omega, (K)L.fgrad, L.forced != 0);
     const int64_t me = cell_index<S>(L, xv, y);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) stv<S>(dst + q * pe + me, o[q]);
-    stv<S>(rest + me, o[8]);
+    store_vec<S, K, D01, RAW>(dst + D01 * pe + me, x[D01]);
+    store_vec<S, K, D03, RAW>(dst + D03 * pe + me, x[D03]);
+    store_vec<S, K, D05, RAW>(dst + D05 * pe + me, x[D05]);
+    store_vec<S, K, D08, RAW>(dst + D08 * pe + me, x[D08]);
+    store_vec<S, K, D10, RAW>(dst + D10 * pe + me, x[D10]);
+    store_vec<S, K, D12, RAW>(dst + D12 * pe + me, x[D12]);
+    store_vec<S, K, D14, RAW>(dst + D14 * pe + me, x[D14]);
+    store_vec<S, K, D17, RAW>(dst + D17 * pe + me, x[D17]);
+    store_vec<S, K, D19, RAW>(rest + me, x[D19]);
+}
+
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS>
+__global__ void __launch_bounds__(TXV *TY) pp_kernel(const Lattice L, const int parity)
+{
+    pp_tile<S, K, TXV, TY, HAS_OBS>(L, blockIdx.x, blockIdx.y, parity);
+}
+
+// Persistent ping-pong step over many lattices: block b takes tiles b, b + gridDim.x, ...
+// of the work list (lattice index, tile x, tile y).  Lattice i uses buffer cur[i] ^ parity.
+template <typename S, typename K, int TXV, int TY>
+__global__ void __launch_bounds__(TXV *TY) batch_pp_kernel(const Lattice *__restrict__ lats,
+                                                           const int *__restrict__ cur,
+                                                           const int4 *__restrict__ tiles, const int ntiles,
+                                                           const int parity)
+{
+    __shared__ Lattice sL;
+    constexpr int NW = (int)(sizeof(Lattice) / sizeof(int));
+    const int tid = threadIdx.y * TXV + threadIdx.x;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int4 tile = __ldg(tiles + t);
+        __syncthreads();
+        const int *srcw = reinterpret_cast<const int *>(lats + tile.x);
+        int *dstw = reinterpret_cast<int *>(&sL);
+        for (int i = tid; i < NW; i += TXV * TY) dstw[i] = __ldg(srcw + i);
+        __syncthreads();
+        pp_tile<S, K, TXV, TY, true>(sL, tile.y, tile.z, __ldg(cur + tile.x) ^ parity);
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -323,6 +434,8 @@ __device__ __forceinline__ void aa_push_rule(const Lattice &L, S *base, int q, i
     int tx = x + cx_of(q), ty = y + cy_of(q);
     const int oq = opp_of(q);
     const S gs = Store<S>::template putq<K>(g, q);
+    // the reference adds the wall term to the stored value (SRC/bcond.driven.F90:141-143)
+    const K gr = Store<S>::template getq<K>(gs, q);
     if (ty < 1 || ty > m) {
         const int f = ty < 1 ? YLO : YHI;
         if (L.faces[f] == FK_PERIODIC) {
@@ -330,7 +443,7 @@ __device__ __forceinline__ void aa_push_rule(const Lattice &L, S *base, int q, i
         } else {
             base[q * pe + cell_index<S>(L, tx, ty)] = gs;  // raw value kept in the ghost frame
             const K wt = (K)L.wt[f][oq];
-            const S b = wt != (K)0 ? Store<S>::template putq<K>(g + wt, oq) : Store<S>::template putq<K>(g, oq);
+            const S b = wt != (K)0 ? Store<S>::template putq<K>(gr + wt, oq) : Store<S>::template putq<K>(gr, oq);
             base[oq * pe + cell_index<S>(L, x, y)] = b;
             return;
         }
@@ -344,7 +457,7 @@ __device__ __forceinline__ void aa_push_rule(const Lattice &L, S *base, int q, i
             base[q * pe + cell_index<S>(L, tx, ty)] = gs;
             if (kind == FK_WALL) {
                 const K wt = (K)L.wt[f][oq];
-                const S b = wt != (K)0 ? Store<S>::template putq<K>(g + wt, oq) : Store<S>::template putq<K>(g, oq);
+                const S b = wt != (K)0 ? Store<S>::template putq<K>(gr + wt, oq) : Store<S>::template putq<K>(gr, oq);
                 base[oq * pe + cell_index<S>(L, x, y)] = b;
             }
             return;
@@ -352,7 +465,7 @@ __device__ __forceinline__ void aa_push_rule(const Lattice &L, S *base, int q, i
     }
     if (HAS_OBS) {
         if (obs_bit(L, tx, ty)) {
-            base[oq * pe + cell_index<S>(L, x, y)] = Store<S>::template putq<K>(g, oq);
+            base[oq * pe + cell_index<S>(L, x, y)] = Store<S>::template putq<K>(gr, oq);
             return;
         }
     }
@@ -433,7 +546,7 @@ __device__ void aa_p_cell_slow(const Lattice &L, S *base, int x, int y)
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) v[q] = pull_rule<S, K, HAS_OBS>(L, q, x, y, plane_at, own, ghost_xhi);
     v[8] = ldq<S, K>(base + D19 * pe, me, D19);
-    collide<K>(v, (K)L.omega, (K)L.fgrad, L.forced != 0);
+    collide_stored<S, K>(v, (K)L.omega, (K)L.fgrad, L.forced != 0);
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) aa_push_rule<S, K, HAS_OBS>(L, base, q, x, y, v[q]);
     base[D19 * pe + me] = Store<S>::template putq<K>(v[8], D19);
@@ -445,16 +558,20 @@ __device__ void aa_p_cell_slow(const Lattice &L, S *base, int x, int y)
 
 // push VEC values of direction q to (x + c_q) in plane q; lanes at an edge (segment end or a
 // neighbour on the slow path) store the elements that cross into the neighbour's vector.
-template <typename S, typename K, int q, int W>
+template <typename S, typename K, int q, int W, bool RAW = false>
 __device__ __forceinline__ void push_vec(const Lattice &L, S *plane, int xv, int y, bool left_edge,
                                          bool right_edge, const K (&g)[vec_of<S>()], bool store)
 {
     constexpr int VEC = vec_of<S>();
     constexpr int cx = cx_of(q), cy = cy_of(q);
     const int64_t idx = cell_index<S>(L, xv, y + cy);
+    auto cvt = [](K v) -> S {
+        if constexpr (RAW) return Store<S>::raw_put((float)v);
+        else return Store<S>::template put<K, q>(v);
+    };
     S s[VEC];
 #pragma unroll
-    for (int c = 0; c < VEC; ++c) s[c] = Store<S>::template put<K, q>(g[c]);
+    for (int c = 0; c < VEC; ++c) s[c] = cvt(g[c]);
     if (cx == 0) {
         if (store) stv<S>(plane + idx, s);
     } else if (cx == 1) {
@@ -462,7 +579,7 @@ __device__ __forceinline__ void push_vec(const Lattice &L, S *plane, int xv, int
         if (!store) return;
         if (!left_edge) {
             S v[VEC];
-            v[0] = Store<S>::template put<K, q>(fl);
+            v[0] = cvt(fl);
 #pragma unroll
             for (int c = 1; c < VEC; ++c) v[c] = s[c - 1];
             stv<S>(plane + idx, v);
@@ -478,7 +595,7 @@ __device__ __forceinline__ void push_vec(const Lattice &L, S *plane, int xv, int
             S v[VEC];
 #pragma unroll
             for (int c = 0; c < VEC - 1; ++c) v[c] = s[c + 1];
-            v[VEC - 1] = Store<S>::template put<K, q>(fr);
+            v[VEC - 1] = cvt(fr);
             stv<S>(plane + idx, v);
         } else {
 #pragma unroll
@@ -504,16 +621,17 @@ __global__ void __launch_bounds__(TXV *TY) aa_p_kernel(const Lattice L)
     S *base = reinterpret_cast<S *>(L.planes);
 
     // pull f*_q from plane opp(q) at x - c_q
+    constexpr bool RAW = Is16<S>::value;
     K x[9][VEC];
-    pull_vec<S, K, D01, W>(L, base + D12 * pe, xv, y, loads, tx, x[D01]);
-    pull_vec<S, K, D03, W>(L, base + D10 * pe, xv, y, loads, tx, x[D03]);
-    pull_vec<S, K, D05, W>(L, base + D14 * pe, xv, y, loads, tx, x[D05]);
-    pull_vec<S, K, D08, W>(L, base + D17 * pe, xv, y, loads, tx, x[D08]);
-    pull_vec<S, K, D10, W>(L, base + D03 * pe, xv, y, loads, tx, x[D10]);
-    pull_vec<S, K, D12, W>(L, base + D01 * pe, xv, y, loads, tx, x[D12]);
-    pull_vec<S, K, D14, W>(L, base + D05 * pe, xv, y, loads, tx, x[D14]);
-    pull_vec<S, K, D17, W>(L, base + D08 * pe, xv, y, loads, tx, x[D17]);
-    pull_vec<S, K, D19, W>(L, base + D19 * pe, xv, y, loads, tx, x[D19]);
+    pull_vec<S, K, D01, W, RAW>(L, base + D12 * pe, xv, y, loads, tx, x[D01]);
+    pull_vec<S, K, D03, W, RAW>(L, base + D10 * pe, xv, y, loads, tx, x[D03]);
+    pull_vec<S, K, D05, W, RAW>(L, base + D14 * pe, xv, y, loads, tx, x[D05]);
+    pull_vec<S, K, D08, W, RAW>(L, base + D17 * pe, xv, y, loads, tx, x[D08]);
+    pull_vec<S, K, D10, W, RAW>(L, base + D03 * pe, xv, y, loads, tx, x[D10]);
+    pull_vec<S, K, D12, W, RAW>(L, base + D01 * pe, xv, y, loads, tx, x[D12]);
+    pull_vec<S, K, D14, W, RAW>(L, base + D05 * pe, xv, y, loads, tx, x[D14]);
+    pull_vec<S, K, D17, W, RAW>(L, base + D08 * pe, xv, y, loads, tx, x[D17]);
+    pull_vec<S, K, D19, W, RAW>(L, base + D19 * pe, xv, y, loads, tx, x[D19]);
 
     bool slow = (y == 1) || (y == L.ly) || (k == 0) || (k >= L.nvec - 1);
     if (HAS_OBS) slow = slow || (y >= L.ob_y0 && y <= L.ob_y1 && xv + VEC - 1 >= L.ob_x0 && xv <= L.ob_x1);
@@ -524,28 +642,18 @@ __global__ void __launch_bounds__(TXV *TY) aa_p_kernel(const Lattice L)
     const bool left_edge = (tx % W) == 0 || left_slow;
     const bool right_edge = (tx % W) == W - 1 || right_slow;
 
-    const K omega = (K)L.omega, fgrad = (K)L.fgrad;
-    const bool forced = L.forced != 0;
-    K g[9][VEC];
-#pragma unroll
-    for (int c = 0; c < VEC; ++c) {
-        K v[9];
-#pragma unroll
-        for (int q = 0; q < 9; ++q) v[q] = x[q][c];
-        collide<K>(v, omega, fgrad, forced);
-#pragma unroll
-        for (int q = 0; q < 9; ++q) g[q][c] = v[q];
-    }
+    relax_vec<S, K, RAW>(x, (K)L.omega, (K)L.fgrad, L.forced != 0);
+    K (&g)[9][VEC] = x;
     const bool store = !slow;
-    push_vec<S, K, D01, W>(L, base + D01 * pe, xv, y, left_edge, right_edge, g[D01], store);
-    push_vec<S, K, D03, W>(L, base + D03 * pe, xv, y, left_edge, right_edge, g[D03], store);
-    push_vec<S, K, D05, W>(L, base + D05 * pe, xv, y, left_edge, right_edge, g[D05], store);
-    push_vec<S, K, D08, W>(L, base + D08 * pe, xv, y, left_edge, right_edge, g[D08], store);
-    push_vec<S, K, D10, W>(L, base + D10 * pe, xv, y, left_edge, right_edge, g[D10], store);
-    push_vec<S, K, D12, W>(L, base + D12 * pe, xv, y, left_edge, right_edge, g[D12], store);
-    push_vec<S, K, D14, W>(L, base + D14 * pe, xv, y, left_edge, right_edge, g[D14], store);
-    push_vec<S, K, D17, W>(L, base + D17 * pe, xv, y, left_edge, right_edge, g[D17], store);
-    push_vec<S, K, D19, W>(L, base + D19 * pe, xv, y, left_edge, right_edge, g[D19], store);
+    push_vec<S, K, D01, W, RAW>(L, base + D01 * pe, xv, y, left_edge, right_edge, g[D01], store);
+    push_vec<S, K, D03, W, RAW>(L, base + D03 * pe, xv, y, left_edge, right_edge, g[D03], store);
+    push_vec<S, K, D05, W, RAW>(L, base + D05 * pe, xv, y, left_edge, right_edge, g[D05], store);
+    push_vec<S, K, D08, W, RAW>(L, base + D08 * pe, xv, y, left_edge, right_edge, g[D08], store);
+    push_vec<S, K, D10, W, RAW>(L, base + D10 * pe, xv, y, left_edge, right_edge, g[D10], store);
+    push_vec<S, K, D12, W, RAW>(L, base + D12 * pe, xv, y, left_edge, right_edge, g[D12], store);
+    push_vec<S, K, D14, W, RAW>(L, base + D14 * pe, xv, y, left_edge, right_edge, g[D14], store);
+    push_vec<S, K, D17, W, RAW>(L, base + D17 * pe, xv, y, left_edge, right_edge, g[D17], store);
+    push_vec<S, K, D19, W, RAW>(L, base + D19 * pe, xv, y, left_edge, right_edge, g[D19], store);
     if (!active || !slow) return;
     const int xe = min(xv + VEC - 1, L.lx);
 #pragma unroll 1
@@ -580,7 +688,7 @@ __global__ void __launch_bounds__(TXV *TY) aa_l_kernel(const Lattice L)
             K v[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) v[q] = ldq<S, K>(base + q * pe, i, q);
-            collide<K>(v, omega, fgrad, forced);
+            collide_stored<S, K>(v, omega, fgrad, forced);
             K g[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) {
@@ -592,33 +700,28 @@ __global__ void __launch_bounds__(TXV *TY) aa_l_kernel(const Lattice L)
         }
         return;
     }
+    constexpr bool RAW = Is16<S>::value;
     K x[9][VEC];
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         S v[VEC];
         ldv<S>(base + q * pe + me, v);
 #pragma unroll
-        for (int c = 0; c < VEC; ++c) x[q][c] = Store<S>::template getq<K>(v[c], q);
+        for (int c = 0; c < VEC; ++c) {
+            if constexpr (RAW) x[q][c] = (K)Store<S>::raw_get(v[c]);
+            else x[q][c] = Store<S>::template getq<K>(v[c], q);
+        }
     }
-    S o[9][VEC];
-#pragma unroll
-    for (int c = 0; c < VEC; ++c) {
-        K v[9];
-#pragma unroll
-        for (int q = 0; q < 9; ++q) v[q] = x[q][c];
-        collide<K>(v, omega, fgrad, forced);
-        o[D12][c] = Store<S>::template put<K, D01>(v[0]);
-        o[D10][c] = Store<S>::template put<K, D03>(v[1]);
-        o[D14][c] = Store<S>::template put<K, D05>(v[2]);
-        o[D17][c] = Store<S>::template put<K, D08>(v[3]);
-        o[D03][c] = Store<S>::template put<K, D10>(v[4]);
-        o[D01][c] = Store<S>::template put<K, D12>(v[5]);
-        o[D05][c] = Store<S>::template put<K, D14>(v[6]);
-        o[D08][c] = Store<S>::template put<K, D17>(v[7]);
-        o[D19][c] = Store<S>::template put<K, D19>(v[8]);
-    }
-#pragma unroll
-    for (int q = 0; q < 9; ++q) stv<S>(base + q * pe + me, o[q]);
+    relax_vec<S, K, RAW>(x, omega, fgrad, forced);
+    store_vec<S, K, D01, RAW>(base + D12 * pe + me, x[D01]);
+    store_vec<S, K, D03, RAW>(base + D10 * pe + me, x[D03]);
+    store_vec<S, K, D05, RAW>(base + D14 * pe + me, x[D05]);
+    store_vec<S, K, D08, RAW>(base + D17 * pe + me, x[D08]);
+    store_vec<S, K, D10, RAW>(base + D03 * pe + me, x[D10]);
+    store_vec<S, K, D12, RAW>(base + D01 * pe + me, x[D12]);
+    store_vec<S, K, D14, RAW>(base + D05 * pe + me, x[D14]);
+    store_vec<S, K, D17, RAW>(base + D08 * pe + me, x[D17]);
+    store_vec<S, K, D19, RAW>(base + D19 * pe + me, x[D19]);
 }
 
 }  // namespace bgk

@@ -207,6 +207,15 @@ class Solver:
         self._check(self._L.bgk_footprint(self._h, ctypes.byref(b), ctypes.byref(c)), "footprint")
         return b.value, c.value
 
+    def set_tile(self, cfg):
+        self._check(self._L.bgk_set_tile(self._h, int(cfg)), "set_tile")
+
+    def tune(self, trial_steps=20):
+        """Time real steps per tile shape (the state advances); returns (tile_cfg, steps_run)."""
+        c, n = ctypes.c_int32(), ctypes.c_int32()
+        self._check(self._L.bgk_tune(self._h, int(trial_steps), ctypes.byref(c), ctypes.byref(n)), "tune")
+        return c.value, n.value
+
     def launches(self):
         n = ctypes.c_int64()
         self._check(self._L.bgk_launch_count(self._h, ctypes.byref(n)), "launch_count")
@@ -235,3 +244,83 @@ class Solver:
         xj = x[0] + x[1] + x[2] - x[4] - x[5] - x[6]
         yj = x[1] + x[3] + x[5] - x[0] - x[4] - x[7]
         return xj / rho, yj / rho, rho
+
+
+class Batch:
+    """Independent ping-pong cases of one (storage, compute) kind advanced together: one
+    persistent work-list launch per time step, replayed from CUDA graphs."""
+
+    def __init__(self, storage="f32", compute=None, device=0):
+        self._L = _lib.load()
+        if compute is None:
+            compute = "f64" if storage == "f64" else "f32"
+        b = ctypes.c_void_p()
+        rc = self._L.bgk_batch_create(_lib.STORE[storage], _lib.COMPUTE[compute], int(device), ctypes.byref(b))
+        if rc != 0:
+            raise BgkError(rc, "bgk_batch_create")
+        self._b = b
+        self.members = []
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise BgkError(rc, what)
+
+    def add(self, solver):
+        self._check(self._L.bgk_batch_add(self._b, solver._h), "batch_add")
+        self.members.append(solver)
+
+    def remove(self, solver):
+        self._check(self._L.bgk_batch_remove(self._b, solver._h), "batch_remove")
+        self.members.remove(solver)
+
+    def size(self):
+        n, c = ctypes.c_int32(), ctypes.c_int64()
+        self._check(self._L.bgk_batch_size(self._b, ctypes.byref(n), ctypes.byref(c)), "batch_size")
+        return n.value, c.value
+
+    def step(self, n=1):
+        self._check(self._L.bgk_batch_step(self._b, int(n)), "batch_step")
+
+    def step_timed(self, n):
+        ms = ctypes.c_float()
+        self._check(self._L.bgk_batch_step_timed(self._b, int(n), ctypes.byref(ms)), "batch_step_timed")
+        return ms.value
+
+    def sync(self):
+        self._check(self._L.bgk_batch_sync(self._b), "batch_sync")
+
+    def set_config(self, tile_cfg, blocks_per_sm, graph_steps):
+        self._check(self._L.bgk_batch_set_config(self._b, int(tile_cfg), int(blocks_per_sm), int(graph_steps)),
+                    "batch_set_config")
+
+    def config(self):
+        out = (ctypes.c_int32 * 3)()
+        self._check(self._L.bgk_batch_get_config(self._b, out), "batch_get_config")
+        return tuple(out)
+
+    def tune(self, trial_steps=10):
+        n = ctypes.c_int32()
+        self._check(self._L.bgk_batch_tune(self._b, int(trial_steps), ctypes.byref(n)), "batch_tune")
+        return n.value
+
+    def launches(self):
+        n = ctypes.c_int64()
+        self._check(self._L.bgk_batch_launch_count(self._b, ctypes.byref(n)), "batch_launch_count")
+        return n.value
+
+    def close(self):
+        if getattr(self, "_b", None):
+            self._L.bgk_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

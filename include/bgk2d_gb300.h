@@ -155,12 +155,41 @@ int bgk_get_obs(bgk_handle *h, int32_t *mask, int32_t bbox[5]);
 /* omega, fgrad, u00, u0 after build_bcond + hencol, and the step counter */
 int bgk_get_scalars(bgk_handle *h, double out[4], int64_t *itime);
 
+/* thread-block tile shape of the step kernels: 0 = 32x4 threads, 1 = 64x2, 2 = 128x1, 3 = 128x2
+ * (each thread updates one 16-byte vector of cells; no reference counterpart) */
+int bgk_set_tile(bgk_handle *h, int32_t tile_cfg);
+/* time `trial_steps` real steps per tile shape (the state advances) and keep the fastest */
+int bgk_tune(bgk_handle *h, int32_t trial_steps, int32_t *tile_cfg, int32_t *steps_run);
+
 /* bytes of HBM the handle holds, and the algorithmic bytes moved per lattice update */
 int bgk_footprint(bgk_handle *h, int64_t *device_bytes, int32_t *bytes_per_cell);
 /* number of kernels this library launched on the handle so far */
 int bgk_launch_count(bgk_handle *h, int64_t *launches);
 int bgk_last_error(bgk_handle *h, char *buf, size_t len);
 const char *bgk_version(void);
+
+/* ---------------------------------------------------------------------------------------------
+ * Batches: many independent ping-pong cases of one (storage, compute) kind advanced together,
+ * one persistent work-list launch per time step, replayed from CUDA graphs.  No reference
+ * counterpart (the reference runs one domain per process, SRC/bgk2d.F90:92-113).  While a
+ * handle is attached, bgk_step/bgk_collision on it return BGK_E_INVALID; every other handle
+ * call works and waits for the batch's last step.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct bgk_batch bgk_batch;
+int bgk_batch_create(int32_t storage, int32_t compute, int32_t device, bgk_batch **out);
+int bgk_batch_destroy(bgk_batch *b);
+int bgk_batch_add(bgk_batch *b, bgk_handle *h);
+int bgk_batch_remove(bgk_batch *b, bgk_handle *h);
+int bgk_batch_size(bgk_batch *b, int32_t *members, int64_t *cells);
+int bgk_batch_step(bgk_batch *b, int32_t nsteps);
+int bgk_batch_step_timed(bgk_batch *b, int32_t nsteps, float *ms);
+int bgk_batch_sync(bgk_batch *b);
+/* tile shape (as bgk_set_tile), persistent blocks per SM, steps per CUDA graph (even) */
+int bgk_batch_set_config(bgk_batch *b, int32_t tile_cfg, int32_t blocks_per_sm, int32_t graph_steps);
+int bgk_batch_get_config(bgk_batch *b, int32_t out[3]);
+/* autotuner: times real steps over tile shapes, grid sizes and graph lengths; keeps the best */
+int bgk_batch_tune(bgk_batch *b, int32_t trial_steps, int32_t *steps_run);
+int bgk_batch_launch_count(bgk_batch *b, int64_t *launches);
 
 #ifdef __cplusplus
 }

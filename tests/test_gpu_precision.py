@@ -1,0 +1,67 @@
+"""Precision form: 16-bit storage of scaled deviations (FP16, BF16) with FP32 collision,
+against an FP64 run of the same Taylor-Green case, and the FP64/FP32 decay against the
+analytic rate.  Velocity-field L2 errors are relative: ||u - u64||_2 / ||u64||_2."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N, U0, TAU = 256, 0.02, 0.6
+NU = (TAU - 0.5) / 3.0
+OMEGA = 1.0 / TAU
+
+
+def tgv(bgk, storage, scheme="pingpong"):
+    return bgk.Solver(N, N, tcase="TGV", storage=storage, omega=OMEGA, svisc=NU, u0=0.0, init="tgv",
+                      tgv_u0=U0, scheme=scheme)
+
+
+def l2(u, v, u0, v0):
+    return np.sqrt(np.sum((u - u0) ** 2 + (v - v0) ** 2) / np.sum(u0 ** 2 + v0 ** 2))
+
+
+@pytest.mark.parametrize("scheme", ["pingpong", "aa"])
+def test_16bit_storage_error_vs_fp64(bgk, scheme):
+    steps = 2000
+    ref = tgv(bgk, "f64")
+    ref.step(steps)
+    _, u0, v0 = ref.fields()
+    errs = {}
+    for st in ("f32", "f16", "bf16"):
+        s = tgv(bgk, st, scheme)
+        s.step(steps)
+        _, u, v = s.fields()
+        errs[st] = l2(u, v, u0, v0)
+        s.close()
+    ref.close()
+    print("velocity L2 error vs FP64:", errs)
+    assert errs["f32"] < 1e-5
+    assert errs["f16"] < 1e-3
+    assert errs["bf16"] < 2e-2
+
+
+@pytest.mark.parametrize("storage", ["f64", "f32"])
+def test_tgv_decay_rate_analytic(bgk, storage):
+    """Velocity amplitude decays as exp(-nu (kx^2 + ky^2) t); <|u|^2> at twice that rate."""
+    s = tgv(bgk, storage)
+    e0 = s.diagno()[3]
+    t = 4000
+    s.step(t)
+    e1 = s.diagno()[3]
+    rate = -np.log(e1 / e0) / (2 * t)
+    k2 = 2 * (2 * np.pi / N) ** 2
+    assert abs(rate / (NU * k2) - 1) < 1e-3
+    s.close()
+
+
+def test_residual_decreases_to_steady_state(bgk):
+    s = bgk.Solver(64, 64, tcase="LDC", svisc=0.064, u0=0.1)
+    assert s.residual() == 1.0
+    s.step(200)
+    r1 = s.residual()
+    s.step(20000)
+    s.residual()
+    s.step(200)
+    r2 = s.residual()
+    assert 0 < r2 < r1 * 1e-2 and r2 < 1e-5
+    s.close()
