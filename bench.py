@@ -175,6 +175,132 @@ def measure_variant(bgk, storage, scheme, steps, warmup, dev):
     return glups, ms / steps
 
 
+# ---------------------------------------------------------------------------------------------
+# Other forms of the path, reported beside the headline (each bounded in time)
+# ---------------------------------------------------------------------------------------------
+def bench_precision(bgk, dev, n=2048, steps=10000):
+    """Taylor-Green 2048^2, U0 = 0.02, tau = 0.6: 16-bit storage against an FP64 run."""
+    import numpy as np
+    tau, u0 = 0.6, 0.02
+    nu = (tau - 0.5) / 3.0
+
+    def run(st):
+        with bgk.Solver(n, n, tcase="TGV", storage=st, omega=1.0 / tau, svisc=nu, u0=0.0, init="tgv", tgv_u0=u0,
+                        device=dev) as s:
+            e0 = s.diagno()[3]
+            ms = s.step_timed(steps)
+            e1 = s.diagno()[3]
+            _, u, v = s.fields()
+        return u, v, ms, e0, e1
+
+    u64, v64, ms64, e0, e1 = run("f64")
+    k2 = 2 * (2 * np.pi / n) ** 2
+    rate = -np.log(e1 / e0) / (2 * steps)
+    out = {"workload": f"Taylor-Green {n}x{n}, U0={u0}, tau={tau}, {steps} steps",
+           "fp64_decay_rate_rel_err": float(abs(rate / (nu * k2) - 1)),
+           "fp64_GLUPS": round(n * n * steps / (ms64 * 1e-3) / 1e9, 3)}
+    den = float(np.sqrt(np.sum(u64 ** 2 + v64 ** 2)))
+    for st in ("f32", "f16", "bf16"):
+        u, v, ms, _, _ = run(st)
+        err = float(np.sqrt(np.sum((u - u64) ** 2 + (v - v64) ** 2)) / den)
+        out[st] = {"velocity_L2_vs_fp64": err, "GLUPS": round(n * n * steps / (ms * 1e-3) / 1e9, 3)}
+    return out
+
+
+def cfg3_cases(seed=0, count=96):
+    """96 lid-driven cavities: edge in {128, 192, ..., 1536}, Re log-uniform [100, 5000],
+    lid speed uniform [0.05, 0.1], tau = 3 U N / Re + 1/2."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    edges = np.arange(128, 1537, 64)
+    out = []
+    for _ in range(count):
+        n = int(rng.choice(edges))
+        re = float(np.exp(rng.uniform(np.log(100), np.log(5000))))
+        u = float(rng.uniform(0.05, 0.1))
+        out.append((n, re, u))
+    return out
+
+
+def bench_batched(bgk, dev, steps=5000, seq_steps=1000):
+    cases = cfg3_cases()
+    cells = sum(n * n for n, _, _ in cases)
+    solvers = [bgk.Solver(n, n, tcase="LDC", svisc=u * n / re, u0=u, device=dev) for n, re, u in cases]
+    with bgk.Batch("f32", device=dev) as b:
+        for s in solvers:
+            b.add(s)
+        tuned = b.tune(6)
+        b.sync()
+        l0 = b.launches()
+        ms = b.step_timed(steps - tuned)
+        launches = b.launches() - l0
+        cfg = b.config()
+    for s in solvers:
+        s.close()
+    batched = cells * (steps - tuned) / (ms * 1e-3) / 1e9
+    # the same cases one at a time with the plain single-domain kernel
+    t_seq = 0.0
+    for n, re, u in cases:
+        with bgk.Solver(n, n, tcase="LDC", svisc=u * n / re, u0=u, device=dev) as s:
+            s.step(4)
+            s.sync()
+            t_seq += s.step_timed(seq_steps) * 1e-3
+    seq = cells * seq_steps / t_seq / 1e9
+    return {"workload": f"96 lid-driven cavities (seed 0), {cells} cells, FP32, {steps} steps each",
+            "batched_GLUPS": round(batched, 3), "one_at_a_time_GLUPS": round(seq, 3),
+            "speedup": round(batched / seq, 3), "tuned_config": {"tile": cfg[0], "blocks_per_sm": cfg[1],
+                                                                  "graph_steps": cfg[2]},
+            "autotune_steps": tuned, "launches": launches,
+            "hbm_frac": round(72 * batched / peaks()[0], 4)}
+
+
+def cfg4_stream(rate, count, seed=1):
+    """Poisson arrivals of three case types (cavity, cylinder channel, Taylor-Green)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    reqs = []
+    for _ in range(count):
+        t += rng.exponential(1.0 / rate)
+        kind = rng.choice(["ldc", "cylinder", "tgv"])
+        storage = "f32" if rng.uniform() < 0.5 else "f16"
+        if kind == "ldc":
+            n = int(rng.choice(np.arange(128, 2049, 64)))
+            re = float(np.exp(rng.uniform(np.log(100), np.log(min(10000, 5 * n)))))
+            tol = 1e-7 if rng.uniform() < 0.5 else 0.0
+            r = dict(kind="ldc", n=n, re=re, u=0.1, storage=storage, max_steps=2000, tol=tol, check_every=500)
+        elif kind == "cylinder":
+            d = int(rng.choice([32, 48, 64, 96]))
+            r = dict(kind="cylinder", n=d, re=float(rng.uniform(60, 200)), u=0.05, storage=storage, max_steps=2000)
+        else:
+            n = int(rng.choice(np.arange(512, 2049, 128)))
+            r = dict(kind="tgv", n=n, re=float(rng.uniform(100, 1000)), u=0.02, storage=storage, max_steps=2000)
+        reqs.append((t, r))
+    return reqs
+
+
+def bench_serving(bgk, dev, rates=(10.0, 30.0, 100.0), count=40):
+    out = []
+    for rate in rates:
+        stream = cfg4_stream(rate, count)
+        with bgk.Server(max_slots=64, chunk_steps=200, device=dev) as srv:
+            t0 = time.perf_counter()
+            for t, r in stream:
+                dt = t - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                srv.submit(**r)
+            srv.drain(600)
+            res = srv.poll()
+            st = srv.stats()
+        out.append({"rate_per_s": rate, "requests": count, "completed": st["completed"], "failed": st["failed"],
+                    "GLUPS": round(st["glups"], 3), "p50_s": round(st["p50_s"], 4), "p99_s": round(st["p99_s"], 4),
+                    "mean_queue_s": round(st["mean_queue_s"], 4), "peak_resident": st["peak_resident"],
+                    "launches": st["launches"],
+                    "steps": int(sum(r["steps"] for r in res))})
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -183,6 +309,7 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the precision, batched and serving forms")
     ap.add_argument("--profile", default=None,
                     help="run only <scheme>_<storage> (e.g. pingpong_f32) on a --size^2 cavity, for ncu")
     ap.add_argument("--size", type=int, default=2048)
@@ -265,6 +392,12 @@ def main():
             variants[name] = {"GLUPS": round(g, 3), "ms_per_step": round(msv, 4), "algorithmic_GBps": round(bw, 1),
                               "hbm_frac": round(bw / peak, 4), "steps": n}
 
+    forms = {}
+    if rank == 0 and not args.no_forms:
+        forms["precision_tgv2048"] = bench_precision(bgk, local)
+        forms["batched_96_cavities"] = bench_batched(bgk, local)
+        forms["serving_poisson"] = bench_serving(bgk, local)
+
     cpu = None
     if rank == 0 and not args.no_cpu and world == 1:
         cpu = cpu_reference(steps_budget_s=12.0)
@@ -286,6 +419,7 @@ def main():
             "clocks": clk.summary(),
             "diagno": [float(x) for x in diag],
             "variants": variants,
+            "forms": forms,
         }
         if cpu:
             line["cpu_baseline"] = cpu

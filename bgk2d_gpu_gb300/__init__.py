@@ -4,6 +4,6 @@
 the diagnostic readers) over libbgk2d_gb300.so; there is no CPU execution path.
 """
 from ._lib import BgkError, load, lib_path  # noqa: F401
-from .solver import Batch, Solver, read_namelist, CX, CY, WEIGHTS  # noqa: F401
+from .solver import Batch, Server, Solver, read_namelist, CX, CY, WEIGHTS  # noqa: F401
 
-__all__ = ["Batch", "Solver", "BgkError", "load", "lib_path", "read_namelist", "CX", "CY", "WEIGHTS"]
+__all__ = ["Batch", "Server", "Solver", "BgkError", "load", "lib_path", "read_namelist", "CX", "CY", "WEIGHTS"]

@@ -42,6 +42,29 @@ class CaseDesc(ctypes.Structure):
     ]
 
 
+REQ = {"ldc": 0, "cylinder": 1, "tgv": 2}
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("kind", I32), ("n", I32), ("re", F64), ("u", F64), ("storage", I32), ("max_steps", I32),
+                ("tol", F64), ("check_every", I32), ("keep_fields", I32)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("id", I64), ("status", I32), ("steps", I32), ("lx", I32), ("ly", I32), ("residual", F64),
+                ("diagno", F64 * 4), ("draglift", F64 * 2), ("t_submit", F64), ("t_admit", F64), ("t_done", F64)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", I32), ("max_slots", I32), ("hbm_budget", I64), ("chunk_steps", I32), ("tile_cfg", I32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", I64), ("admitted", I64), ("completed", I64), ("failed", I64),
+                ("cell_updates", I64), ("busy_s", F64), ("wall_s", F64), ("glups", F64), ("p50_s", F64),
+                ("p99_s", F64), ("mean_queue_s", F64), ("peak_resident", I32), ("launches", I64)]
+
+
 class BgkError(RuntimeError):
     def __init__(self, code, msg=""):
         self.code = code
@@ -104,6 +127,13 @@ def load(build_if_missing: bool = True):
         "bgk_batch_get_config": (I32, [VP, P(I32)]),
         "bgk_batch_tune": (I32, [VP, I32, P(I32)]),
         "bgk_batch_launch_count": (I32, [VP, P(I64)]),
+        "bgk_server_create": (I32, [P(ServerConfig), P(VP)]),
+        "bgk_server_destroy": (I32, [VP]),
+        "bgk_server_submit": (I32, [VP, P(Request), P(I64)]),
+        "bgk_server_poll": (I32, [VP, P(Result), I32, P(I32)]),
+        "bgk_server_drain": (I32, [VP, F64]),
+        "bgk_server_fields": (I32, [VP, I64, P(F64), P(F64), P(F64)]),
+        "bgk_server_get_stats": (I32, [VP, P(ServerStats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

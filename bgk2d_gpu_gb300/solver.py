@@ -324,3 +324,79 @@ class Batch:
 
     def __exit__(self, *a):
         self.close()
+
+
+class Server:
+    """Continuous-batching request loop (C++ scheduler thread inside the library)."""
+
+    def __init__(self, max_slots=64, chunk_steps=200, hbm_budget=0, tile_cfg=-1, device=0):
+        self._L = _lib.load()
+        cfg = _lib.ServerConfig(int(device), int(max_slots), int(hbm_budget), int(chunk_steps), int(tile_cfg))
+        h = ctypes.c_void_p()
+        rc = self._L.bgk_server_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != 0:
+            raise BgkError(rc, "bgk_server_create")
+        self._s = h
+        self.sizes = {}
+
+    def submit(self, kind, n, re, u, storage="f32", max_steps=1000, tol=0.0, check_every=500, keep_fields=False):
+        r = _lib.Request(_lib.REQ[kind], int(n), float(re), float(u), _lib.STORE[storage], int(max_steps),
+                         float(tol), int(check_every), int(bool(keep_fields)))
+        i = ctypes.c_int64()
+        rc = self._L.bgk_server_submit(self._s, ctypes.byref(r), ctypes.byref(i))
+        if rc != 0:
+            raise BgkError(rc, "bgk_server_submit")
+        return i.value
+
+    def poll(self, max_results=1024):
+        buf = (_lib.Result * max_results)()
+        n = ctypes.c_int32()
+        rc = self._L.bgk_server_poll(self._s, buf, int(max_results), ctypes.byref(n))
+        if rc != 0:
+            raise BgkError(rc, "bgk_server_poll")
+        out = []
+        for k in range(n.value):
+            r = buf[k]
+            out.append(dict(id=r.id, status=r.status, steps=r.steps, lx=r.lx, ly=r.ly, residual=r.residual,
+                            diagno=list(r.diagno), draglift=list(r.draglift), t_submit=r.t_submit,
+                            t_admit=r.t_admit, t_done=r.t_done))
+        return out
+
+    def drain(self, timeout_s=600.0):
+        rc = self._L.bgk_server_drain(self._s, float(timeout_s))
+        if rc != 0:
+            raise BgkError(rc, "bgk_server_drain")
+
+    def fields(self, rid, lx, ly):
+        n = lx * ly
+        r, u, v = np.empty(n), np.empty(n), np.empty(n)
+        P = ctypes.POINTER(ctypes.c_double)
+        rc = self._L.bgk_server_fields(self._s, int(rid), r.ctypes.data_as(P), u.ctypes.data_as(P),
+                                       v.ctypes.data_as(P))
+        if rc != 0:
+            raise BgkError(rc, "bgk_server_fields")
+        return r.reshape(ly, lx), u.reshape(ly, lx), v.reshape(ly, lx)
+
+    def stats(self):
+        st = _lib.ServerStats()
+        rc = self._L.bgk_server_get_stats(self._s, ctypes.byref(st))
+        if rc != 0:
+            raise BgkError(rc, "bgk_server_get_stats")
+        return {k: getattr(st, k) for k, _ in _lib.ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "_s", None):
+            self._L.bgk_server_destroy(self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -191,6 +191,74 @@ int bgk_batch_get_config(bgk_batch *b, int32_t out[3]);
 int bgk_batch_tune(bgk_batch *b, int32_t trial_steps, int32_t *steps_run);
 int bgk_batch_launch_count(bgk_batch *b, int64_t *launches);
 
+/* ---------------------------------------------------------------------------------------------
+ * Serving loop: solves submitted as they arrive are admitted against free HBM and a slot
+ * limit, keep their populations resident between step chunks, are advanced together in the
+ * batched kernel (one batch per storage kind, batches on separate streams), and return their
+ * diagnostics and fields on completion.  A request stops at max_steps, or earlier when its
+ * residual (checked every check_every of its own steps) drops below tol.  No reference
+ * counterpart.  All calls are thread-safe.
+ * ------------------------------------------------------------------------------------------- */
+#define BGK_REQ_LDC 0       /* lid-driven cavity n x n, lid speed u, nu = u n / re */
+#define BGK_REQ_CYLINDER 1  /* channel 16D x 4D, cylinder D = n at (4D, 2D+1), parabolic inflow of
+                               peak u, zero-gradient outflow, walls; nu = u D / re; drag/lift */
+#define BGK_REQ_TGV 2       /* periodic Taylor-Green n x n, amplitude u, nu = u n / re */
+
+typedef struct bgk_request {
+    int32_t kind;        /* BGK_REQ_* */
+    int32_t n;           /* cavity / vortex edge, or cylinder diameter */
+    double re;           /* Reynolds number */
+    double u;            /* lid speed, inflow peak or vortex amplitude */
+    int32_t storage;     /* BGK_STORE_F32 / F16 / BF16 */
+    int32_t max_steps;   /* step budget */
+    double tol;          /* residual tolerance; <= 0 runs max_steps */
+    int32_t check_every; /* steps between residual checks (> 0) */
+    int32_t keep_fields; /* 1: keep rho, u, v for bgk_server_fields */
+} bgk_request;
+
+typedef struct bgk_result {
+    int64_t id;
+    int32_t status;       /* BGK_OK, BGK_E_NUMERIC, BGK_E_NOMEM (never admissible), ... */
+    int32_t steps;
+    int32_t lx, ly;
+    double residual;      /* last residual (0 when never checked) */
+    double diagno[4];     /* <u>, <v>, <rho>, <|u|^2> at completion */
+    double draglift[2];   /* cylinder only */
+    double t_submit, t_admit, t_done;  /* seconds since server start */
+} bgk_result;
+
+typedef struct bgk_server_config {
+    int32_t device;
+    int32_t max_slots;       /* concurrently resident requests */
+    int64_t hbm_budget;      /* bytes the server may hold; <= 0: free HBM minus 4 GiB */
+    int32_t chunk_steps;     /* steps per scheduling round (upper bound) */
+    int32_t tile_cfg;        /* batch tile shape (bgk_set_tile numbering); < 0 selects 32x4 */
+} bgk_server_config;
+
+typedef struct bgk_server_stats {
+    int64_t submitted, admitted, completed, failed;
+    int64_t cell_updates;     /* lattice updates of all requests */
+    double busy_s;            /* wall time spent in step rounds */
+    double wall_s;            /* first admission to last completion */
+    double glups;             /* cell_updates / wall_s / 1e9 */
+    double p50_s, p99_s;      /* latency (t_done - t_submit) percentiles */
+    double mean_queue_s;      /* mean t_admit - t_submit */
+    int32_t peak_resident;
+    int64_t launches;         /* kernels launched by the server */
+} bgk_server_stats;
+
+typedef struct bgk_server bgk_server;
+int bgk_server_create(const bgk_server_config *cfg, bgk_server **out);
+int bgk_server_destroy(bgk_server *s);
+int bgk_server_submit(bgk_server *s, const bgk_request *req, int64_t *id);
+/* move up to max finished results into out (oldest first); *n = how many */
+int bgk_server_poll(bgk_server *s, bgk_result *out, int32_t max, int32_t *n);
+/* block until every submitted request finished or timeout_s elapsed (BGK_E_TIMEOUT) */
+int bgk_server_drain(bgk_server *s, double timeout_s);
+/* fields of a finished request that asked for them (lx*ly doubles each, i fastest) */
+int bgk_server_fields(bgk_server *s, int64_t id, double *rho, double *u, double *v);
+int bgk_server_get_stats(bgk_server *s, bgk_server_stats *out);
+
 #ifdef __cplusplus
 }
 #endif
