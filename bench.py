@@ -164,15 +164,16 @@ def run_profile(args):
     return 0
 
 
-def measure_variant(bgk, storage, scheme, steps, warmup, dev):
+def measure_variant(bgk, storage, scheme, steps, warmup, dev, tune=True):
     compute = "f64" if storage == "f64" else "f32"
     with bgk.Solver(LX, LY, tcase="LDC", svisc=SVISC, u0=U0, storage=storage, compute=compute, scheme=scheme,
                     device=dev) as s:
+        cfg = s.tune(4 if storage == "f64" else 10)[0] if tune else None
         s.step(warmup)
         s.sync()
         ms = s.step_timed(steps)
     glups = LX * LY * steps / (ms * 1e-3) / 1e9
-    return glups, ms / steps
+    return glups, ms / steps, cfg
 
 
 # ---------------------------------------------------------------------------------------------
@@ -334,6 +335,7 @@ def main():
 
     # ---- device-timed value: K steps from HBM-resident state --------------------------------
     s = bgk.Solver(LX, LY, tcase="LDC", svisc=SVISC, u0=U0, storage="f32", scheme="pingpong", device=local)
+    tile_cfg, _ = s.tune(10)
     s.step(args.warmup)
     s.sync()
     if dist:
@@ -387,10 +389,10 @@ def main():
                               ("pingpong_bf16", "bf16", "pingpong"), ("pingpong_f64", "f64", "pingpong"),
                               ("aa_f64", "f64", "aa")):
             n = vsteps if st != "f64" else max(10, vsteps // 4)
-            g, msv = measure_variant(bgk, st, sch, n, 5, local)
+            g, msv, cfg = measure_variant(bgk, st, sch, n, 5, local)
             bw = BYTES_PER_CELL[st] * LX * LY / (msv * 1e-3) / 1e9
             variants[name] = {"GLUPS": round(g, 3), "ms_per_step": round(msv, 4), "algorithmic_GBps": round(bw, 1),
-                              "hbm_frac": round(bw / peak, 4), "steps": n}
+                              "hbm_frac": round(bw / peak, 4), "steps": n, "tile_cfg": cfg}
 
     forms = {}
     if rank == 0 and not args.no_forms:
@@ -413,7 +415,8 @@ def main():
                        "parallelism": f"{world} independent cavities" if world > 1 else "single domain"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": kt, "peak_kind": peak_kind,
-                         "kernel": "bgk::pp_kernel<float,float,128,1,false>", "bytes_per_cell": 72},
+                         "kernel": "bgk::pp_kernel<float,float,...> (tile config %d)" % tile_cfg,
+                         "bytes_per_cell": 72},
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clk.summary(),

@@ -291,7 +291,7 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
     pitch = (pitch + row_align - 1) / row_align * row_align;
     int64_t plane = pitch * (m + 2);
     plane = (plane + 256 / eb - 1) / (256 / eb) * (256 / eb);
-    const int nplanes = d.scheme == BGK_SCHEME_PINGPONG ? 17 : 9;
+    const int nplanes = d.scheme == BGK_SCHEME_PINGPONG ? 18 : 9;
     h->planes_bytes = (size_t)plane * nplanes * eb;
 
     // admission against free HBM (populations + staging plane + mask + reduction scratch)

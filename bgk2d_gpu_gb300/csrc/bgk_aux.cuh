@@ -12,10 +12,7 @@ __device__ __forceinline__ K post_value(const Lattice &L, int cur, int phase, in
 {
     const S *base = reinterpret_cast<const S *>(L.planes);
     const int64_t pe = L.plane_elems;
-    if (L.scheme == 0) {
-        const int p = (q == D19) ? 8 : (cur ? 9 + q : q);
-        return ldq<S, K>(base + p * pe, cell_index<S>(L, x, y), q);
-    }
+    if (L.scheme == 0) return ldq<S, K>(base + ((cur ? 9 : 0) + q) * pe, cell_index<S>(L, x, y), q);
     if (phase == 0 || q == D19) return ldq<S, K>(base + opp_of(q) * pe, cell_index<S>(L, x, y), q);
     // phase 1: the value was pushed to x + c_q (or kept where the push rule put it)
     int tx = x + cx_of(q), ty = y + cy_of(q);
@@ -43,7 +40,7 @@ __global__ void scatter_plane_kernel(Lattice L, int cur, int q, const H *__restr
     S *base = reinterpret_cast<S *>(L.planes);
     const int64_t pe = L.plane_elems;
     int p;
-    if (L.scheme == 0) p = (q == D19) ? 8 : (cur ? 9 + q : q);
+    if (L.scheme == 0) p = (cur ? 9 : 0) + q;
     else p = opp_of(q);
     const H v = stage[(int64_t)y * (L.lx + 2) + x];
     base[p * pe + cell_index<S>(L, x, y)] = Store<S>::template putq<double>((double)v, q);

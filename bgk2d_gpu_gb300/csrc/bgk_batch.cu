@@ -53,7 +53,9 @@ int rebuild(bgk_batch *b)
         bgk_handle *h = b->members[i];
         lats.push_back(h->L);
         cur.push_back(h->cur);
-        const int gx = (h->L.nvec + tc.txv - 1) / tc.txv, gy = (h->L.ly + tc.ty - 1) / tc.ty;
+        const int n = b->T.vec / tc.cdiv;
+        const int nv = (h->L.lx + n - 1) / n;
+        const int gx = (nv + tc.txv - 1) / tc.txv, gy = (h->L.ly + tc.ty - 1) / tc.ty;
         for (int by = 0; by < gy; ++by)
             for (int bx = 0; bx < gx; ++bx) tiles.push_back(make_int4((int)i, bx, by, 0));
     }

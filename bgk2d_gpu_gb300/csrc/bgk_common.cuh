@@ -10,8 +10,8 @@
 // rows included), each row `pitch` elements long; cell (x, y), x = 0..lx+1, sits at element
 //   p * plane_elems + y * pitch + xoff + x,   xoff = VEC - 1,
 // so that interior cell x = 1 starts a 16-byte vector (VEC = 16 / sizeof(storage)).
-// Ping-pong keeps planes 0..7 (moving, buffer A), 8 (rest, updated in place like a19 in
-// SRC/col_MC.F90:293) and 9..16 (moving, buffer B).  AA keeps planes 0..8 only.
+// Ping-pong keeps buffer A in planes 0..8 and buffer B in planes 9..17 (the rest population is
+// double-buffered too, so a step never writes its source); AA keeps planes 0..8 only.
 #pragma once
 
 #include <cuda_runtime.h>

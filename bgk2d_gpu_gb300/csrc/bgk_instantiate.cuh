@@ -10,14 +10,20 @@ namespace inst {
 
 template <typename S> using Host = typename std::conditional<std::is_same<S, double>::value, double, float>::type;
 
-template <typename S, typename K, int TXV, int TY, bool OBS>
+template <typename S, typename K, int TXV, int TY, bool OBS, int CDIV>
 cudaError_t step_cfg(int kind, const Lattice &L, int parity, cudaStream_t st)
 {
     const dim3 block(TXV, TY);
-    const dim3 grid((unsigned)((L.nvec + TXV - 1) / TXV), (unsigned)((L.ly + TY - 1) / TY));
-    if (kind == STEP_PP) pp_kernel<S, K, TXV, TY, OBS><<<grid, block, 0, st>>>(L, parity);
-    else if (kind == STEP_AA_P) aa_p_kernel<S, K, TXV, TY, OBS><<<grid, block, 0, st>>>(L);
-    else aa_l_kernel<S, K, TXV, TY, OBS><<<grid, block, 0, st>>>(L);
+    if (kind == STEP_PP) {
+        constexpr int N = vec_of<S>() / CDIV;
+        const int nv = (L.lx + N - 1) / N;
+        const dim3 grid((unsigned)((nv + TXV - 1) / TXV), (unsigned)((L.ly + TY - 1) / TY));
+        pp_kernel<S, K, TXV, TY, OBS, N><<<grid, block, 0, st>>>(L, parity);
+    } else {
+        const dim3 grid((unsigned)((L.nvec + TXV - 1) / TXV), (unsigned)((L.ly + TY - 1) / TY));
+        if (kind == STEP_AA_P) aa_p_kernel<S, K, TXV, TY, OBS><<<grid, block, 0, st>>>(L);
+        else aa_l_kernel<S, K, TXV, TY, OBS><<<grid, block, 0, st>>>(L);
+    }
     return cudaGetLastError();
 }
 
@@ -25,10 +31,16 @@ template <typename S, typename K, bool OBS>
 cudaError_t step_obs(int kind, const Lattice &L, int parity, int cfg, cudaStream_t st)
 {
     switch (cfg) {
-    case 0: return step_cfg<S, K, 32, 4, OBS>(kind, L, parity, st);
-    case 1: return step_cfg<S, K, 64, 2, OBS>(kind, L, parity, st);
-    case 3: return step_cfg<S, K, 128, 2, OBS>(kind, L, parity, st);
-    default: return step_cfg<S, K, 128, 1, OBS>(kind, L, parity, st);
+    case 0: return step_cfg<S, K, 32, 4, OBS, 1>(kind, L, parity, st);
+    case 1: return step_cfg<S, K, 64, 2, OBS, 1>(kind, L, parity, st);
+    case 3: return step_cfg<S, K, 128, 2, OBS, 1>(kind, L, parity, st);
+    case 4:
+        if (kind == STEP_PP) return step_cfg<S, K, 32, 4, OBS, 2>(kind, L, parity, st);
+        return step_cfg<S, K, 32, 4, OBS, 1>(kind, L, parity, st);
+    case 5:
+        if (kind == STEP_PP) return step_cfg<S, K, 128, 1, OBS, 2>(kind, L, parity, st);
+        return step_cfg<S, K, 128, 1, OBS, 1>(kind, L, parity, st);
+    default: return step_cfg<S, K, 128, 1, OBS, 1>(kind, L, parity, st);
     }
 }
 
@@ -100,11 +112,14 @@ template <typename S, typename K>
 cudaError_t batch_step(const Lattice *lats, const int *cur, const int4 *tiles, int ntiles, int parity, int cfg, int grid,
                        cudaStream_t st)
 {
+    constexpr int V = vec_of<S>();
     switch (cfg) {
-    case 0: batch_pp_kernel<S, K, 32, 4><<<grid, dim3(32, 4), 0, st>>>(lats, cur, tiles, ntiles, parity); break;
-    case 1: batch_pp_kernel<S, K, 64, 2><<<grid, dim3(64, 2), 0, st>>>(lats, cur, tiles, ntiles, parity); break;
-    case 3: batch_pp_kernel<S, K, 128, 2><<<grid, dim3(128, 2), 0, st>>>(lats, cur, tiles, ntiles, parity); break;
-    default: batch_pp_kernel<S, K, 128, 1><<<grid, dim3(128, 1), 0, st>>>(lats, cur, tiles, ntiles, parity); break;
+    case 0: batch_pp_kernel<S, K, 32, 4, V><<<grid, dim3(32, 4), 0, st>>>(lats, cur, tiles, ntiles, parity); break;
+    case 1: batch_pp_kernel<S, K, 64, 2, V><<<grid, dim3(64, 2), 0, st>>>(lats, cur, tiles, ntiles, parity); break;
+    case 3: batch_pp_kernel<S, K, 128, 2, V><<<grid, dim3(128, 2), 0, st>>>(lats, cur, tiles, ntiles, parity); break;
+    case 4: batch_pp_kernel<S, K, 32, 4, V / 2><<<grid, dim3(32, 4), 0, st>>>(lats, cur, tiles, ntiles, parity); break;
+    case 5: batch_pp_kernel<S, K, 128, 1, V / 2><<<grid, dim3(128, 1), 0, st>>>(lats, cur, tiles, ntiles, parity); break;
+    default: batch_pp_kernel<S, K, 128, 1, V><<<grid, dim3(128, 1), 0, st>>>(lats, cur, tiles, ntiles, parity); break;
     }
     return cudaGetLastError();
 }

@@ -1,8 +1,8 @@
 // bgk_kernels.cuh -- fused stream + collide kernels for one lattice (templated bodies).
 //
 // Ping-pong (PP): the pull form of SRC/col_MC.F90:97-293.  Cell (x,y) reads population q from
-// (x - c_q) in the source buffer, relaxes, and writes the destination buffer at (x,y); the
-// rest population is updated in place (col_MC.F90:293).  The ghost-frame fills of
+// (x - c_q) in the source buffer, relaxes, and writes the destination buffer at (x,y) (the rest
+// population too, where col_MC.F90:293 updates a19 in place).  The ghost-frame fills of
 // SRC/bcond.*.F90 are folded into the pull: a source outside the interior is replaced by the
 // value the reference's boundary routine would have written there, and an obstacle source by
 // the value SRC/bcond.obs.F90:59-71 would have written (the pulling cell's own opposite
@@ -181,6 +181,33 @@ __device__ __forceinline__ void stv(S *p, const S (&v)[16 / sizeof(S)])
     *reinterpret_cast<uint4 *>(p) = t.u;
 }
 
+// N consecutive elements, N * sizeof(S) = 8 or 16 bytes
+template <typename S, int N> struct VecT;
+template <typename S> struct VecT<S, 16 / sizeof(S)> {
+    using U = uint4;
+};
+template <typename S> struct VecT<S, 8 / sizeof(S)> {
+    using U = uint2;
+};
+template <typename S, int N>
+__device__ __forceinline__ void ldn(const S *p, S (&o)[N])
+{
+    using U = typename VecT<S, N>::U;
+    union { U u; S s[N]; } t;
+    t.u = __ldg(reinterpret_cast<const U *>(p));
+#pragma unroll
+    for (int c = 0; c < N; ++c) o[c] = t.s[c];
+}
+template <typename S, int N>
+__device__ __forceinline__ void stn(S *p, const S (&v)[N])
+{
+    using U = typename VecT<S, N>::U;
+    union { U u; S s[N]; } t;
+#pragma unroll
+    for (int c = 0; c < N; ++c) t.s[c] = v[c];
+    *reinterpret_cast<U *>(p) = t.u;
+}
+
 template <typename K>
 __device__ __forceinline__ K shfl_up(K v, int w) { return __shfl_up_sync(0xffffffffu, v, 1, w); }
 template <typename K>
@@ -189,41 +216,40 @@ __device__ __forceinline__ K shfl_down(K v, int w) { return __shfl_down_sync(0xf
 // Load VEC consecutive values of direction q pulled from (x - c_q): aligned 16-byte load of
 // row y - cy at the thread's own columns; the +-1 column shift comes from the neighbouring
 // lane, or from one scalar load at a segment edge.
-template <typename S, typename K, int q, int W, bool RAW = false>
+template <typename S, typename K, int q, int W, bool RAW = false, int N = vec_of<S>()>
 __device__ __forceinline__ void pull_vec(const Lattice &L, const S *plane, int xv, int y, bool loads,
-                                         int seg_lane, K (&out)[vec_of<S>()])
+                                         int seg_lane, K (&out)[N])
 {
     auto cvt = [](S v) -> K {
         if constexpr (RAW) return (K)Store<S>::raw_get(v);
         else return Store<S>::template get<K, q>(v);
     };
-    constexpr int VEC = vec_of<S>();
     constexpr int sx = -cx_of(q), sy = -cy_of(q);
     const int64_t idx = cell_index<S>(L, xv, y + sy);
-    S v[VEC];
-    if (loads) ldv<S>(plane + idx, v);
+    S v[N];
+    if (loads) ldn<S, N>(plane + idx, v);
     else {
 #pragma unroll
-        for (int c = 0; c < VEC; ++c) v[c] = S(0.0f);
+        for (int c = 0; c < N; ++c) v[c] = S(0.0f);
     }
-    K kv[VEC];
+    K kv[N];
 #pragma unroll
-    for (int c = 0; c < VEC; ++c) kv[c] = cvt(v[c]);
+    for (int c = 0; c < N; ++c) kv[c] = cvt(v[c]);
     if (sx == 0) {
 #pragma unroll
-        for (int c = 0; c < VEC; ++c) out[c] = kv[c];
+        for (int c = 0; c < N; ++c) out[c] = kv[c];
     } else if (sx == -1) {
-        K left = shfl_up(kv[VEC - 1], W);
+        K left = shfl_up(kv[N - 1], W);
         if ((seg_lane % W) == 0 && loads) left = cvt(plane[idx - 1]);
         out[0] = left;
 #pragma unroll
-        for (int c = 1; c < VEC; ++c) out[c] = kv[c - 1];
+        for (int c = 1; c < N; ++c) out[c] = kv[c - 1];
     } else {
         K right = shfl_down(kv[0], W);
-        if ((seg_lane % W) == W - 1 && loads) right = cvt(plane[idx + VEC]);
+        if ((seg_lane % W) == W - 1 && loads) right = cvt(plane[idx + N]);
 #pragma unroll
-        for (int c = 0; c < VEC - 1; ++c) out[c] = kv[c + 1];
-        out[VEC - 1] = right;
+        for (int c = 0; c < N - 1; ++c) out[c] = kv[c + 1];
+        out[N - 1] = right;
     }
 }
 
@@ -274,12 +300,12 @@ __device__ __forceinline__ K pull_rule(const Lattice &L, int q, int x, int y, Pl
     return plane_at(q, sx, sy);
 }
 
-// relax VEC cells in place: x[q][c] holds direction q of cell c (scaled 16-bit units when RAW)
-template <typename S, typename K, bool RAW>
-__device__ __forceinline__ void relax_vec(K (&x)[9][vec_of<S>()], K omega, K fgrad, bool forced)
+// relax N cells in place: x[q][c] holds direction q of cell c (scaled 16-bit units when RAW)
+template <typename S, typename K, bool RAW, int N = vec_of<S>()>
+__device__ __forceinline__ void relax_vec(K (&x)[9][N], K omega, K fgrad, bool forced)
 {
 #pragma unroll
-    for (int c = 0; c < vec_of<S>(); ++c) {
+    for (int c = 0; c < N; ++c) {
         K v[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) v[q] = x[q][c];
@@ -290,31 +316,52 @@ __device__ __forceinline__ void relax_vec(K (&x)[9][vec_of<S>()], K omega, K fgr
     }
 }
 
-// store VEC values of direction q as one 16-byte vector
-template <typename S, typename K, int q, bool RAW>
-__device__ __forceinline__ void store_vec(S *p, const K (&v)[vec_of<S>()])
+// store N values of direction q as one 8- or 16-byte vector
+template <typename S, typename K, int q, bool RAW, int N = vec_of<S>()>
+__device__ __forceinline__ void store_vec(S *p, const K (&v)[N])
 {
-    constexpr int VEC = vec_of<S>();
-    if constexpr (RAW) {
+    if constexpr (RAW && N == 8) {
         uint4 u;
         u.x = Store<S>::pack2((float)v[0], (float)v[1]);
         u.y = Store<S>::pack2((float)v[2], (float)v[3]);
         u.z = Store<S>::pack2((float)v[4], (float)v[5]);
         u.w = Store<S>::pack2((float)v[6], (float)v[7]);
         *reinterpret_cast<uint4 *>(p) = u;
+    } else if constexpr (RAW && N == 4) {
+        uint2 u;
+        u.x = Store<S>::pack2((float)v[0], (float)v[1]);
+        u.y = Store<S>::pack2((float)v[2], (float)v[3]);
+        *reinterpret_cast<uint2 *>(p) = u;
     } else {
-        S o[VEC];
+        S o[N];
 #pragma unroll
-        for (int c = 0; c < VEC; ++c) o[c] = Store<S>::template put<K, q>(v[c]);
-        stv<S>(p, o);
+        for (int c = 0; c < N; ++c) o[c] = Store<S>::template put<K, q>(v[c]);
+        stn<S, N>(p, o);
     }
 }
 
 // ---------------------------------------------------------------------------------------------
 // Ping-pong kernel
 // ---------------------------------------------------------------------------------------------
+// Cell whose pull crosses the domain boundary or touches an obstacle: the boundary rules decide
+// at least one of its nine inputs.
+template <bool HAS_OBS>
+__device__ __forceinline__ bool needs_rule(const Lattice &L, int x, int y)
+{
+    if (x == 1 || x == L.lx || y == 1 || y == L.ly) return true;
+    if (HAS_OBS) {
+        if (y >= L.ob_y0 && y <= L.ob_y1 && x >= L.ob_x0 && x <= L.ob_x1) {
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx)
+                    if ((dx | dy) != 0 && obs_bit(L, x + dx, y + dy)) return true;
+        }
+    }
+    return false;
+}
+
+// one cell with the boundary rules: reads the source buffer only, writes the destination
 template <typename S, typename K, bool HAS_OBS>
-__device__ void pp_cell_slow(const Lattice &L, const S *src, S *dst, S *rest, int x, int y)
+__device__ void pp_cell_slow(const Lattice &L, const S *src, S *dst, int x, int y)
 {
     const int64_t pe = L.plane_elems;
     const int64_t me = cell_index<S>(L, x, y);
@@ -332,75 +379,77 @@ __device__ void pp_cell_slow(const Lattice &L, const S *src, S *dst, S *rest, in
     K v[9];
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) v[q] = pull_rule<S, K, HAS_OBS>(L, q, x, y, plane_at, own, ghost_xhi);
-    v[8] = ldq<S, K>(rest, me, D19);
+    v[8] = ldq<S, K>(src + D19 * pe, me, D19);
     collide_stored<S, K>(v, (K)L.omega, (K)L.fgrad, L.forced != 0);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) dst[q * pe + me] = Store<S>::template putq<K>(v[q], q);
-    rest[me] = Store<S>::template putq<K>(v[8], D19);
+    for (int q = 0; q < 9; ++q) dst[q * pe + me] = Store<S>::template putq<K>(v[q], q);
 }
 
-// one tile of TXV*VEC x TY cells at tile coordinates (bx, by) of lattice L
-template <typename S, typename K, int TXV, int TY, bool HAS_OBS>
+// one tile of TXV*VEC x TY cells at tile coordinates (bx, by) of lattice L.  Every lane takes the
+// vector path; cells whose inputs come from the boundary rules are then recomputed one by one
+// and overwritten (the source buffer is read-only during the step, so the recompute sees the
+// same inputs).
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N = vec_of<S>()>
 __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const int by, const int parity)
 {
-    constexpr int VEC = vec_of<S>();
     constexpr int W = TXV < 32 ? TXV : 32;
+    const int nv = (L.lx + N - 1) / N;
     const int tx = threadIdx.x;
     const int k = bx * TXV + tx;
     const int y = by * TY + threadIdx.y + 1;
     const bool in_rows = y <= L.ly;
-    const bool loads = in_rows && k <= L.nvec;
-    const bool active = in_rows && k < L.nvec;
-    const int xv = 1 + k * VEC;
+    const bool loads = in_rows && k <= nv;
+    const bool active = in_rows && k < nv;
+    const int xv = 1 + k * N;
     const int64_t pe = L.plane_elems;
     S *base = reinterpret_cast<S *>(L.planes);
     const S *src = base + (parity ? 9 : 0) * pe;
     S *dst = base + (parity ? 0 : 9) * pe;
-    S *rest = base + 8 * pe;
 
     constexpr bool RAW = Is16<S>::value;
-    K x[9][VEC];
-    pull_vec<S, K, D01, W, RAW>(L, src + D01 * pe, xv, y, loads, tx, x[D01]);
-    pull_vec<S, K, D03, W, RAW>(L, src + D03 * pe, xv, y, loads, tx, x[D03]);
-    pull_vec<S, K, D05, W, RAW>(L, src + D05 * pe, xv, y, loads, tx, x[D05]);
-    pull_vec<S, K, D08, W, RAW>(L, src + D08 * pe, xv, y, loads, tx, x[D08]);
-    pull_vec<S, K, D10, W, RAW>(L, src + D10 * pe, xv, y, loads, tx, x[D10]);
-    pull_vec<S, K, D12, W, RAW>(L, src + D12 * pe, xv, y, loads, tx, x[D12]);
-    pull_vec<S, K, D14, W, RAW>(L, src + D14 * pe, xv, y, loads, tx, x[D14]);
-    pull_vec<S, K, D17, W, RAW>(L, src + D17 * pe, xv, y, loads, tx, x[D17]);
-    pull_vec<S, K, D19, W, RAW>(L, rest, xv, y, loads, tx, x[D19]);
+    K x[9][N];
+    pull_vec<S, K, D01, W, RAW, N>(L, src + D01 * pe, xv, y, loads, tx, x[D01]);
+    pull_vec<S, K, D03, W, RAW, N>(L, src + D03 * pe, xv, y, loads, tx, x[D03]);
+    pull_vec<S, K, D05, W, RAW, N>(L, src + D05 * pe, xv, y, loads, tx, x[D05]);
+    pull_vec<S, K, D08, W, RAW, N>(L, src + D08 * pe, xv, y, loads, tx, x[D08]);
+    pull_vec<S, K, D10, W, RAW, N>(L, src + D10 * pe, xv, y, loads, tx, x[D10]);
+    pull_vec<S, K, D12, W, RAW, N>(L, src + D12 * pe, xv, y, loads, tx, x[D12]);
+    pull_vec<S, K, D14, W, RAW, N>(L, src + D14 * pe, xv, y, loads, tx, x[D14]);
+    pull_vec<S, K, D17, W, RAW, N>(L, src + D17 * pe, xv, y, loads, tx, x[D17]);
+    pull_vec<S, K, D19, W, RAW, N>(L, src + D19 * pe, xv, y, loads, tx, x[D19]);
     if (!active) return;
 
-    bool slow = (y == 1) || (y == L.ly) || (k == 0) || (k == L.nvec - 1);
-    if (HAS_OBS) slow = slow || (y >= L.ob_y0 && y <= L.ob_y1 && xv + VEC - 1 >= L.ob_x0 && xv <= L.ob_x1);
-    if (slow) {
-        const int xe = min(xv + VEC - 1, L.lx);
-#pragma unroll 1
-        for (int xc = xv; xc <= xe; ++xc) pp_cell_slow<S, K, HAS_OBS>(L, src, dst, rest, xc, y);
-        return;
-    }
-    relax_vec<S, K, RAW>(x, (K)L.omega, (K)L.fgrad, L.forced != 0);
+    relax_vec<S, K, RAW, N>(x, (K)L.omega, (K)L.fgrad, L.forced != 0);
     const int64_t me = cell_index<S>(L, xv, y);
-    store_vec<S, K, D01, RAW>(dst + D01 * pe + me, x[D01]);
-    store_vec<S, K, D03, RAW>(dst + D03 * pe + me, x[D03]);
-    store_vec<S, K, D05, RAW>(dst + D05 * pe + me, x[D05]);
-    store_vec<S, K, D08, RAW>(dst + D08 * pe + me, x[D08]);
-    store_vec<S, K, D10, RAW>(dst + D10 * pe + me, x[D10]);
-    store_vec<S, K, D12, RAW>(dst + D12 * pe + me, x[D12]);
-    store_vec<S, K, D14, RAW>(dst + D14 * pe + me, x[D14]);
-    store_vec<S, K, D17, RAW>(dst + D17 * pe + me, x[D17]);
-    store_vec<S, K, D19, RAW>(rest + me, x[D19]);
+    store_vec<S, K, D01, RAW, N>(dst + D01 * pe + me, x[D01]);
+    store_vec<S, K, D03, RAW, N>(dst + D03 * pe + me, x[D03]);
+    store_vec<S, K, D05, RAW, N>(dst + D05 * pe + me, x[D05]);
+    store_vec<S, K, D08, RAW, N>(dst + D08 * pe + me, x[D08]);
+    store_vec<S, K, D10, RAW, N>(dst + D10 * pe + me, x[D10]);
+    store_vec<S, K, D12, RAW, N>(dst + D12 * pe + me, x[D12]);
+    store_vec<S, K, D14, RAW, N>(dst + D14 * pe + me, x[D14]);
+    store_vec<S, K, D17, RAW, N>(dst + D17 * pe + me, x[D17]);
+    store_vec<S, K, D19, RAW, N>(dst + D19 * pe + me, x[D19]);
+
+    bool rules = (y == 1) || (y == L.ly) || (k == 0) || (k == nv - 1);
+    if (HAS_OBS) rules = rules || (y >= L.ob_y0 && y <= L.ob_y1 && xv + N - 1 >= L.ob_x0 && xv <= L.ob_x1);
+    if (rules) {
+        const int xe = min(xv + N - 1, L.lx);
+#pragma unroll 1
+        for (int xc = xv; xc <= xe; ++xc)
+            if (needs_rule<HAS_OBS>(L, xc, y)) pp_cell_slow<S, K, HAS_OBS>(L, src, dst, xc, y);
+    }
 }
 
-template <typename S, typename K, int TXV, int TY, bool HAS_OBS>
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N>
 __global__ void __launch_bounds__(TXV *TY) pp_kernel(const Lattice L, const int parity)
 {
-    pp_tile<S, K, TXV, TY, HAS_OBS>(L, blockIdx.x, blockIdx.y, parity);
+    pp_tile<S, K, TXV, TY, HAS_OBS, N>(L, blockIdx.x, blockIdx.y, parity);
 }
 
 // Persistent ping-pong step over many lattices: block b takes tiles b, b + gridDim.x, ...
 // of the work list (lattice index, tile x, tile y).  Lattice i uses buffer cur[i] ^ parity.
-template <typename S, typename K, int TXV, int TY>
+template <typename S, typename K, int TXV, int TY, int N>
 __global__ void __launch_bounds__(TXV *TY) batch_pp_kernel(const Lattice *__restrict__ lats,
                                                            const int *__restrict__ cur,
                                                            const int4 *__restrict__ tiles, const int ntiles,
@@ -416,7 +465,7 @@ __global__ void __launch_bounds__(TXV *TY) batch_pp_kernel(const Lattice *__rest
         int *dstw = reinterpret_cast<int *>(&sL);
         for (int i = tid; i < NW; i += TXV * TY) dstw[i] = __ldg(srcw + i);
         __syncthreads();
-        pp_tile<S, K, TXV, TY, true>(sL, tile.y, tile.z, __ldg(cur + tile.x) ^ parity);
+        pp_tile<S, K, TXV, TY, true, N>(sL, tile.y, tile.z, __ldg(cur + tile.x) ^ parity);
     }
 }
 

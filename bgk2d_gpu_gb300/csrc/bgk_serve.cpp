@@ -54,7 +54,7 @@ int64_t estimate_bytes(const bgk_request &r)
     geometry(r, lx, ly);
     const int64_t eb = store_bytes(r.storage);
     const int64_t pitch = ((lx + 32) * eb + 127) / 128 * 128;
-    const int64_t planes = 17 * pitch * (ly + 2);
+    const int64_t planes = 18 * pitch * (ly + 2);
     const int64_t stage = (int64_t)(lx + 2) * (ly + 2) * 4;
     const int64_t snap = (int64_t)lx * ly * 16;
     return planes + stage + snap + (int64_t)(ly + 2) * ((lx + 33) / 32) * 4 + (1 << 20);

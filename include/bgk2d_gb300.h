@@ -155,8 +155,10 @@ int bgk_get_obs(bgk_handle *h, int32_t *mask, int32_t bbox[5]);
 /* omega, fgrad, u00, u0 after build_bcond + hencol, and the step counter */
 int bgk_get_scalars(bgk_handle *h, double out[4], int64_t *itime);
 
-/* thread-block tile shape of the step kernels: 0 = 32x4 threads, 1 = 64x2, 2 = 128x1, 3 = 128x2
- * (each thread updates one 16-byte vector of cells; no reference counterpart) */
+/* thread-block tile shape of the step kernels (no reference counterpart):
+ *   0 = 32x4 threads, 1 = 64x2, 2 = 128x1, 3 = 128x2, each thread updating one 16-byte vector
+ *   of cells per plane; 4 = 32x4 and 5 = 128x1 with half a vector (8 bytes) per thread in the
+ *   ping-pong kernels.  Results do not depend on the choice. */
 int bgk_set_tile(bgk_handle *h, int32_t tile_cfg);
 /* time `trial_steps` real steps per tile shape (the state advances) and keep the fastest */
 int bgk_tune(bgk_handle *h, int32_t trial_steps, int32_t *tile_cfg, int32_t *steps_run);
