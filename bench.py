@@ -157,10 +157,12 @@ def run_profile(args):
     compute = "f64" if storage == "f64" else "f32"
     with bgk.Solver(args.size, args.size, tcase="LDC", svisc=SVISC * args.size / LX, u0=U0, storage=storage,
                     compute=compute, scheme=scheme) as s:
+        if args.tile >= 0:
+            s.set_tile(args.tile)
         s.step(args.warmup)
         s.step(args.steps)
         s.sync()
-    print(f"profile run {args.profile} {args.size}^2 warmup={args.warmup} steps={args.steps}")
+    print(f"profile run {args.profile} {args.size}^2 tile={args.tile} warmup={args.warmup} steps={args.steps}")
     return 0
 
 
@@ -314,6 +316,7 @@ def main():
     ap.add_argument("--profile", default=None,
                     help="run only <scheme>_<storage> (e.g. pingpong_f32) on a --size^2 cavity, for ncu")
     ap.add_argument("--size", type=int, default=2048)
+    ap.add_argument("--tile", type=int, default=-1, help="tile configuration for --profile")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
