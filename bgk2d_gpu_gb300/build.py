@@ -29,6 +29,8 @@ SOURCES = {
     "bgk_inst_bf16_f32.cu": ["-fmad=true"],
 }
 HOST_SOURCES = ["bgk_serve.cpp"]
+DRIVER = "bgk2d_main.cpp"          # host driver executable linked against the library
+EXE_PATH = os.path.join(OUT_DIR, "bgk2d_gb300")
 
 
 def nvcc() -> str:
@@ -93,6 +95,14 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB_PATH)
+    drv = os.path.join(CSRC, DRIVER)
+    if os.path.exists(drv) and (force or _stale(EXE_PATH, [drv, LIB_PATH])):
+        cxx = shutil.which("g++") or "g++"
+        cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(HERE, "..", "include"), drv,
+               "-L", OUT_DIR, "-lbgk2d_gb300", "-Wl,-rpath,$ORIGIN", "-o", EXE_PATH]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
     if verbose:
         for k, v in logs.items():
             sys.stdout.write(f"== {k}\n{v}\n")

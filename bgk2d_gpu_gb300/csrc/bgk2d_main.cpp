@@ -1,0 +1,301 @@
+// bgk2d_main.cpp -- host driver over the C ABI, in place of the reference's Fortran driver.
+//
+// Reads the reference's `bgk.input` namelist (SRC/input.F90:44-65), sets the case up like
+// SRC/initialize.F90, runs the time loop of SRC/bgk2d.F90:92-113 (boundaries, propagation and
+// collision are one fused step on the device) and writes the reference's text outputs at its
+// diagnostic cadence (SRC/diagnostic.F90): diagno.dat, probe.dat, prof_i.dat, prof_j.dat,
+// drag.lift.dat, save.XXXXXXXX.bin checkpoints (Fortran unformatted sequential records, as
+// SRC/save_raw.F90) and bgk.perf.  VTK output is not produced.
+//
+//   bgk2d_gb300 [--input bgk.input] [--case LDC|TGV|POF|VKS|COU] [--prec single|double|mixed2|f16|bf16]
+//               [--scheme pingpong|aa] [--dir OUTDIR]
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/bgk2d_gb300.h"
+
+namespace {
+
+std::string fortran_e(double v, int w = 14, int d = 6)
+{
+    // Fortran Ew.d: 0.ddddddE+xx, right-justified in w columns
+    char buf[64];
+    if (v == 0.0 || !std::isfinite(v)) {
+        if (!std::isfinite(v)) std::snprintf(buf, sizeof(buf), "%*s", w, std::isnan(v) ? "NaN" : (v > 0 ? "Infinity" : "-Infinity"));
+        else std::snprintf(buf, sizeof(buf), "%*s", w, "0.000000E+00");
+        return buf;
+    }
+    int e = (int)std::floor(std::log10(std::fabs(v))) + 1;
+    double m = v / std::pow(10.0, e);
+    char mant[32];
+    std::snprintf(mant, sizeof(mant), "%.*f", d, std::fabs(m));
+    if (mant[0] == '1') {  // rounding carried to 1.000000
+        e += 1;
+        m = v / std::pow(10.0, e);
+        std::snprintf(mant, sizeof(mant), "%.*f", d, std::fabs(m));
+    }
+    char s[64];
+    std::snprintf(s, sizeof(s), "%s%sE%c%02d", v < 0 ? "-" : "", mant, e < 0 ? '-' : '+', std::abs(e));
+    std::snprintf(buf, sizeof(buf), "%*s", w, s);
+    return buf;
+}
+
+std::map<std::string, std::string> read_namelist(const std::string &path)
+{
+    std::ifstream f(path);
+    std::stringstream ss;
+    ss << f.rdbuf();
+    std::string t = ss.str();
+    std::map<std::string, std::string> kv;
+    size_t a = t.find("&parameters");
+    if (a == std::string::npos) return kv;
+    size_t b = t.find('/', a);
+    std::string body = t.substr(a + 11, b - a - 11);
+    for (char &c : body)
+        if (c == ',' || c == '\n' || c == '\r' || c == '\t') c = ' ';
+    std::stringstream bs(body);
+    std::string tok, key;
+    std::vector<std::string> toks;
+    while (bs >> tok) toks.push_back(tok);
+    for (size_t i = 0; i < toks.size(); ++i) {
+        std::string s = toks[i];
+        size_t eq = s.find('=');
+        if (eq == std::string::npos) continue;
+        std::string k = s.substr(0, eq), v = s.substr(eq + 1);
+        if (k.empty() && i > 0) k = toks[i - 1];
+        if (v.empty() && i + 1 < toks.size()) v = toks[++i];
+        for (char &c : v)
+            if (c == 'd' || c == 'D') c = 'e';
+        kv[k] = v;
+    }
+    return kv;
+}
+
+struct Pops {
+    int lx, ly, hb;
+    std::vector<char> mem;
+    void *p[9];
+    size_t n;
+    Pops(int l, int m, int host_bytes) : lx(l), ly(m), hb(host_bytes)
+    {
+        n = (size_t)(l + 2) * (m + 2);
+        mem.resize(9 * n * hb);
+        for (int q = 0; q < 9; ++q) p[q] = mem.data() + q * n * hb;
+    }
+    double at(int q, int i, int j) const
+    {
+        const size_t k = (size_t)i + (size_t)j * (lx + 2);
+        return hb == 8 ? ((const double *)p[q])[k] : (double)((const float *)p[q])[k];
+    }
+};
+
+// host readers with the reference's per-cell arithmetic in the storage kind
+template <typename T>
+void prof_j(const Pops &a, int icoord, FILE *f, int itime)
+{
+    std::fprintf(f, "# t=%7d\n", itime);
+    for (int j = 1; j <= a.ly; ++j) {
+        T x[9];
+        for (int q = 0; q < 9; ++q) x[q] = (T)a.at(q, icoord, j);
+        T den = ((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8]) + (T)1;
+        T u = (((x[0] - x[4]) + (x[1] - x[5])) + (x[2] - x[6])) / den;
+        T v = (((x[1] - x[0]) + (x[3] - x[7])) + (x[5] - x[4])) / den;
+        std::fprintf(f, "%s %s %s %s \n", fortran_e(j - 0.5).c_str(), fortran_e(u).c_str(), fortran_e(v).c_str(),
+                     fortran_e(den).c_str());
+    }
+    std::fprintf(f, "\n\n");
+}
+
+template <typename T>
+void prof_i(const Pops &a, int jcoord, FILE *f, int itime)
+{
+    std::fprintf(f, "# t=%7d\n", itime);
+    for (int i = 1; i <= a.lx; ++i) {
+        T x[9];
+        for (int q = 0; q < 9; ++q) x[q] = (T)a.at(q, i, jcoord);
+        T den = ((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8]) + (T)1;
+        T u = (((((x[0] + x[1]) + x[2]) - x[4]) - x[5]) - x[6]) / den;
+        T v = (((((x[1] + x[3]) + x[5]) - x[0]) - x[4]) - x[7]) / den;
+        std::fprintf(f, "%s %s %s %s \n", fortran_e(i - 0.5).c_str(), fortran_e(u).c_str(), fortran_e(v).c_str(),
+                     fortran_e(den).c_str());
+    }
+    std::fprintf(f, "\n\n");
+}
+
+template <typename T>
+void probe(const Pops &a, int i0, int j0, FILE *f, int itime)
+{
+    T x[9];
+    for (int q = 0; q < 9; ++q) x[q] = (T)a.at(q, i0, j0);
+    T rho = (((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8])) + (T)1;
+    T xj = ((((x[0] + x[1]) + x[2]) - x[4]) - x[5]) - x[6];
+    T yj = ((((x[1] + x[3]) + x[5]) - x[0]) - x[4]) - x[7];
+    std::fprintf(f, "%8d%s %s %s \n", itime, fortran_e(xj / rho).c_str(), fortran_e(yj / rho).c_str(),
+                 fortran_e(rho).c_str());
+}
+
+// Fortran unformatted sequential record: int32 length, payload, int32 length
+void write_record(FILE *f, const void *data, uint32_t bytes)
+{
+    std::fwrite(&bytes, 4, 1, f);
+    std::fwrite(data, 1, bytes, f);
+    std::fwrite(&bytes, 4, 1, f);
+}
+
+bool read_record(FILE *f, void *data, uint32_t bytes)
+{
+    uint32_t a = 0, b = 0;
+    if (std::fread(&a, 4, 1, f) != 1 || a != bytes) return false;
+    if (std::fread(data, 1, bytes, f) != bytes) return false;
+    return std::fread(&b, 4, 1, f) == 1 && b == bytes;
+}
+
+int die(const char *what, int rc)
+{
+    std::fprintf(stderr, "bgk2d_gb300: %s failed (status %d)\n", what, rc);
+    return 1;
+}
+
+}  // namespace
+
+int main(int argc, char **argv)
+{
+    std::string input = "bgk.input", tcase = "LDC", prec = "single", scheme = "pingpong", dir = ".";
+    for (int i = 1; i + 1 < argc; i += 2) {
+        std::string k = argv[i], v = argv[i + 1];
+        if (k == "--input") input = v;
+        else if (k == "--case") tcase = v;
+        else if (k == "--prec") prec = v;
+        else if (k == "--scheme") scheme = v;
+        else if (k == "--dir") dir = v;
+    }
+    auto kv = read_namelist(input);
+    if (kv.empty()) { std::fprintf(stderr, "bgk2d_gb300: no &parameters namelist in %s\n", input.c_str()); return 1; }
+    auto geti = [&](const char *k, int d) { return kv.count(k) ? std::atoi(kv[k].c_str()) : d; };
+    auto getd = [&](const char *k, double d) { return kv.count(k) ? std::atof(kv[k].c_str()) : d; };
+    const int lx = geti("lx", 0), ly = geti("ly", 0), itfin = geti("itfin", 0);
+    const int ivtim = geti("ivtim", 1 << 30), isignal = geti("isignal", 1 << 30), itsave = geti("itsave", 1 << 30);
+    const int icheck = geti("icheck", 1 << 30), irestart = geti("irestart", 0), init_v = geti("init_v", 0);
+    (void)ivtim;
+
+    bgk_case_desc d;
+    bgk_default_desc(&d);
+    d.lx = lx;
+    d.ly = ly;
+    d.ipad = geti("ipad", 0);
+    d.jpad = geti("jpad", 0);
+    d.svisc = getd("svisc", 0.1);
+    d.u0 = getd("u0", 0.1);
+    d.radius = geti("radius", 16);
+    d.scheme = scheme == "aa" ? BGK_SCHEME_AA : BGK_SCHEME_PINGPONG;
+    if (prec == "double") { d.storage = BGK_STORE_F64; d.compute = BGK_COMPUTE_F64; }
+    else if (prec == "mixed2") { d.storage = BGK_STORE_F32; d.compute = BGK_COMPUTE_F64; }
+    else if (prec == "f16") d.storage = BGK_STORE_F16;
+    else if (prec == "bf16") d.storage = BGK_STORE_BF16;
+    const std::map<std::string, int> cases = {{"LDC", BGK_CASE_LDC}, {"TGV", BGK_CASE_TGV}, {"POF", BGK_CASE_POF},
+                                              {"VKS", BGK_CASE_VKS}, {"COU", BGK_CASE_COU}};
+    if (!cases.count(tcase)) { std::fprintf(stderr, "bgk2d_gb300: unknown case %s\n", tcase.c_str()); return 1; }
+    d.tcase = cases.at(tcase);
+    if (d.tcase == BGK_CASE_TGV) d.init_v = BGK_INIT_TGV_REF;
+    (void)init_v;
+
+    const auto t0 = std::chrono::steady_clock::now();
+    bgk_handle *h = nullptr;
+    int rc = bgk_create(&d, &h);
+    if (rc) return die("bgk_create", rc);
+    const int hb = d.storage == BGK_STORE_F64 ? 8 : 4;
+    const int64_t ld = lx + 2 + d.ipad;
+    Pops pops(lx, ly, hb);
+    int itstart = 0;
+    if (irestart == 1) {  // SRC/restore_raw.F90
+        FILE *f = std::fopen((dir + "/restore.bin").c_str(), "rb");
+        int32_t it = 0;
+        bool ok = f && read_record(f, &it, 4);
+        for (int q = 0; ok && q < 9; ++q) ok = read_record(f, pops.p[q], (uint32_t)(pops.n * hb));
+        if (f) std::fclose(f);
+        if (!ok) { std::fprintf(stderr, "bgk2d_gb300: cannot read restore.bin\n"); return 1; }
+        itstart = it;
+        if ((rc = bgk_upload(h, pops.p, lx + 2))) return die("bgk_upload", rc);
+    }
+    (void)ld;
+    FILE *fdiag = std::fopen((dir + "/diagno.dat").c_str(), "w");
+    FILE *fprobe = std::fopen((dir + "/probe.dat").c_str(), "w");
+    FILE *fpi = std::fopen((dir + "/prof_i.dat").c_str(), "w");
+    FILE *fpj = std::fopen((dir + "/prof_j.dat").c_str(), "w");
+    FILE *fdrag = d.tcase == BGK_CASE_VKS ? std::fopen((dir + "/drag.lift.dat").c_str(), "w") : nullptr;
+    const bool dbl = d.storage == BGK_STORE_F64;
+    auto diagnostic = [&](int itime) -> int {
+        double dg[4];
+        int r = bgk_diagno(h, 0, dg);
+        if (r && r != BGK_E_NUMERIC) return r;
+        std::fprintf(fdiag, "%8d%s %s %s %s \n", itime, fortran_e(dg[0]).c_str(), fortran_e(dg[1]).c_str(),
+                     fortran_e(dg[2]).c_str(), fortran_e(dg[3]).c_str());
+        std::fflush(fdiag);
+        if ((r = bgk_download(h, pops.p, lx + 2))) return r;
+        if (dbl) { probe<double>(pops, lx / 2, ly / 2, fprobe, itime); prof_i<double>(pops, ly / 2, fpi, itime); prof_j<double>(pops, lx / 2, fpj, itime); }
+        else { probe<float>(pops, lx / 2, ly / 2, fprobe, itime); prof_i<float>(pops, ly / 2, fpi, itime); prof_j<float>(pops, lx / 2, fpj, itime); }
+        if (fdrag) {
+            double fl[2];
+            if ((r = bgk_draglift(h, fl))) return r;
+            std::fprintf(fdrag, " %12d %24.16E %24.16E\n", itime, fl[0], fl[1]);
+        }
+        return BGK_OK;
+    };
+    if (irestart != 1) {  // SRC/initialize.F90:118-124 writes the initial profiles
+        if ((rc = bgk_download(h, pops.p, lx + 2))) return die("bgk_download", rc);
+        if (dbl) { prof_i<double>(pops, ly / 2, fpi, 0); prof_j<double>(pops, lx / 2, fpj, 0); }
+        else { prof_i<float>(pops, ly / 2, fpi, 0); prof_j<float>(pops, lx / 2, fpj, 0); }
+    }
+    const auto t1 = std::chrono::steady_clock::now();
+    double t_last = 0;
+    int itime = itstart;
+    while (itime < itfin) {
+        // advance to the next diagnostic, save or signal step
+        int next = itfin;
+        for (int every : {icheck, itsave, isignal})
+            if (every > 0) next = std::min(next, (itime / every + 1) * every);
+        if ((rc = bgk_step(h, next - itime))) return die("bgk_step", rc);
+        itime = next;
+        if (itime % icheck == 0 && (rc = diagnostic(itime))) return die("diagnostic", rc);
+        if (itime % itsave == 0) {  // SRC/save_raw.F90
+            if ((rc = bgk_download(h, pops.p, lx + 2))) return die("bgk_download", rc);
+            char name[64];
+            std::snprintf(name, sizeof(name), "/save.%08d.bin", itime);
+            FILE *f = std::fopen((dir + name).c_str(), "wb");
+            int32_t it = itime;
+            write_record(f, &it, 4);
+            for (int q = 0; q < 9; ++q) write_record(f, pops.p[q], (uint32_t)(pops.n * hb));
+            std::fclose(f);
+        }
+        if (itime % isignal == 0) {  // SRC/profile.F90: mean time per step
+            bgk_sync(h);
+            const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
+            std::printf(" Iteration %8d  time/step %12.5e s\n", itime, (t - t_last) / isignal);
+            t_last = t;
+        }
+    }
+    bgk_sync(h);
+    const auto t2 = std::chrono::steady_clock::now();
+    const double loop = std::chrono::duration<double>(t2 - t1).count();
+    diagnostic(itime);  // SRC/bgk2d.F90:122-125
+    const double mlups = (double)lx * ly * (itfin - itstart) / loop / 1e6;
+    FILE *fp = std::fopen((dir + "/bgk.perf").c_str(), "w");
+    std::fprintf(fp, "# Run info\n %d %d\n# Time for section\n init %.6f\n loop %.6f\n", lx, ly,
+                 std::chrono::duration<double>(t1 - t0).count(), loop);
+    std::fprintf(fp, "# Derived (global) metrics\n Mlups %.3f\n", mlups);
+    std::fclose(fp);
+    std::printf(" Mlups %.3f\n", mlups);
+    for (FILE *f : {fdiag, fprobe, fpi, fpj})
+        if (f) std::fclose(f);
+    if (fdrag) std::fclose(fdrag);
+    bgk_destroy(h);
+    return 0;
+}

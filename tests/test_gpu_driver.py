@@ -1,0 +1,78 @@
+"""Host driver over the C ABI: bgk.input in, the reference's text outputs and checkpoints out."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NAMELIST = """&parameters
+lx = {lx}
+ly = {ly}
+svisc={svisc}
+u0=0.1
+itfin={itfin}
+ivtim=1000000
+isignal={isignal}
+itsave={itsave}
+icheck={icheck}
+irestart={irestart}
+init_v=0
+ipad=0        /
+"""
+
+
+def run_driver(bgk, tmp, case="LDC", prec="single", **kw):
+    from bgk2d_gpu_gb300 import build
+    exe = build.EXE_PATH
+    assert os.path.exists(exe)
+    p = dict(lx=64, ly=48, svisc=0.0384, itfin=300, isignal=100, itsave=150, icheck=100, irestart=0)
+    p.update(kw)
+    (tmp / "bgk.input").write_text(NAMELIST.format(**p))
+    r = subprocess.run([exe, "--input", str(tmp / "bgk.input"), "--case", case, "--prec", prec, "--dir", str(tmp)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    return p
+
+
+def test_driver_outputs_match_solver(bgk, tmp_path):
+    p = run_driver(bgk, tmp_path)
+    rows = [ln.split() for ln in (tmp_path / "diagno.dat").read_text().splitlines()]
+    assert [int(r[0]) for r in rows] == [100, 200, 300, 300]
+    with bgk.Solver(p["lx"], p["ly"], tcase="LDC", svisc=p["svisc"], u0=0.1) as s:
+        s.step(300)
+        d = s.diagno()
+        u, v, den = s.prof_j(p["lx"] // 2)
+    np.testing.assert_allclose([float(x) for x in rows[-1][1:]], d, rtol=1e-5, atol=1e-12)
+    text = (tmp_path / "prof_j.dat").read_text()
+    assert text.count("# t=") == 5  # t=0, 100, 200, 300 and the final call
+    last = text.split("# t=")[-1].strip().splitlines()[1:]
+    vals = np.array([[float(x) for x in ln.split()] for ln in last])
+    np.testing.assert_allclose(vals[:, 1], u, rtol=1e-5, atol=1e-11)
+    assert (tmp_path / "save.00000150.bin").exists() and (tmp_path / "bgk.perf").exists()
+
+
+def test_checkpoint_restart_continues_exactly(bgk, tmp_path):
+    a = tmp_path / "a"
+    b = tmp_path / "b"
+    a.mkdir()
+    b.mkdir()
+    run_driver(bgk, a)
+    shutil.copy(a / "save.00000150.bin", b / "restore.bin")
+    run_driver(bgk, b, irestart=1)
+    ra = (a / "diagno.dat").read_text().splitlines()
+    rb = (b / "diagno.dat").read_text().splitlines()
+    assert ra[-1] == rb[-1] and ra[-2] == rb[-2]
+    # Fortran unformatted sequential records: 4-byte markers around the step and 9 planes
+    raw = (a / "save.00000150.bin").read_bytes()
+    n = 66 * 50 * 4
+    assert len(raw) == (4 + 4 + 4) + 9 * (4 + n + 4)
+    assert int.from_bytes(raw[4:8], "little") == 150
+
+
+def test_driver_vks_writes_drag_lift(bgk, tmp_path):
+    run_driver(bgk, tmp_path, case="VKS", lx=160, ly=62, svisc=0.05, itfin=200, itsave=1000000)
+    rows = [ln.split() for ln in (tmp_path / "drag.lift.dat").read_text().splitlines()]
+    assert len(rows) == 3 and all(np.isfinite(float(x)) for r in rows for x in r[1:])
