@@ -182,7 +182,10 @@ def measure_variant(bgk, storage, scheme, steps, warmup, dev, tune=True):
 # Other forms of the path, reported beside the headline (each bounded in time)
 # ---------------------------------------------------------------------------------------------
 def bench_precision(bgk, dev, n=2048, steps=10000):
-    """Taylor-Green 2048^2, U0 = 0.02, tau = 0.6: 16-bit storage against an FP64 run."""
+    """Taylor-Green 2048^2, U0 = 0.02, tau = 0.6: 16-bit storage against an FP64 run, and the FP64
+    decay of the vortex mode against exp(-nu (kx^2 + ky^2) t).  The mode amplitude is the
+    projection of (u, v) on the initial field, which filters out the acoustic waves (wavenumber
+    2k) that the equilibrium start excites."""
     import numpy as np
     tau, u0 = 0.6, 0.02
     nu = (tau - 0.5) / 3.0
@@ -190,21 +193,22 @@ def bench_precision(bgk, dev, n=2048, steps=10000):
     def run(st):
         with bgk.Solver(n, n, tcase="TGV", storage=st, omega=1.0 / tau, svisc=nu, u0=0.0, init="tgv", tgv_u0=u0,
                         device=dev) as s:
-            e0 = s.diagno()[3]
+            _, ui, vi = s.fields()
             ms = s.step_timed(steps)
-            e1 = s.diagno()[3]
             _, u, v = s.fields()
-        return u, v, ms, e0, e1
+        return ui, vi, u, v, ms
 
-    u64, v64, ms64, e0, e1 = run("f64")
+    ui, vi, u64, v64, ms64 = run("f64")
     k2 = 2 * (2 * np.pi / n) ** 2
-    rate = -np.log(e1 / e0) / (2 * steps)
+    amp = float(np.sum(u64 * ui + v64 * vi) / np.sum(ui * ui + vi * vi))
+    rate = -np.log(amp) / steps
     out = {"workload": f"Taylor-Green {n}x{n}, U0={u0}, tau={tau}, {steps} steps",
+           "fp64_mode_decay_rate": rate, "analytic_rate": nu * k2,
            "fp64_decay_rate_rel_err": float(abs(rate / (nu * k2) - 1)),
            "fp64_GLUPS": round(n * n * steps / (ms64 * 1e-3) / 1e9, 3)}
     den = float(np.sqrt(np.sum(u64 ** 2 + v64 ** 2)))
     for st in ("f32", "f16", "bf16"):
-        u, v, ms, _, _ = run(st)
+        _, _, u, v, ms = run(st)
         err = float(np.sqrt(np.sum((u - u64) ** 2 + (v - v64) ** 2)) / den)
         out[st] = {"velocity_L2_vs_fp64": err, "GLUPS": round(n * n * steps / (ms * 1e-3) / 1e9, 3)}
     return out
@@ -282,7 +286,7 @@ def cfg4_stream(rate, count, seed=1):
     return reqs
 
 
-def bench_serving(bgk, dev, rates=(10.0, 30.0, 100.0), count=40):
+def bench_serving(bgk, dev, rates=(10.0, 30.0, 100.0), count=120):
     out = []
     for rate in rates:
         stream = cfg4_stream(rate, count)

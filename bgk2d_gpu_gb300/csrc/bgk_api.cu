@@ -82,6 +82,19 @@ int fail(bgk_handle *h, int code, const char *fmt, ...)
 #define NOT_IN_BATCH(h) \
     do { if ((h)->batch) return fail(h, BGK_E_INVALID, "handle is attached to a batch; step the batch"); } while (0)
 
+// Stream-ordered allocations: creating or destroying a case does not synchronise the device,
+// so a serving loop can admit and retire cases while other work runs.
+template <typename T>
+cudaError_t dalloc(bgk_handle *h, T **p, size_t bytes)
+{
+    return cudaMallocAsync(reinterpret_cast<void **>(p), bytes, h->st);
+}
+
+void dfree(bgk_handle *h, void *p)
+{
+    if (p) cudaFreeAsync(p, h->st);
+}
+
 bool get_table(int storage, int compute, KernelTable &t)
 {
     if (storage == BGK_STORE_F32 && compute == BGK_COMPUTE_F32) t = table_f32_f32();
@@ -104,10 +117,10 @@ int ensure_stage(bgk_handle *h)
 {
     const size_t need = (size_t)(h->desc.lx + 2) * (size_t)(h->desc.ly + 2) * (size_t)h->host_bytes;
     if (h->stage_bytes >= need) return BGK_OK;
-    if (h->d_stage) cudaFree(h->d_stage);
+    dfree(h, h->d_stage);
     h->d_stage = nullptr;
     h->stage_bytes = 0;
-    if (cudaMalloc(&h->d_stage, need) != cudaSuccess) {
+    if (dalloc(h, &h->d_stage, need) != cudaSuccess) {
         cudaGetLastError();
         return fail(h, BGK_E_NOMEM, "staging buffer of %zu bytes", need);
     }
@@ -217,14 +230,12 @@ void release(bgk_handle *h)
 {
     for (int i = 0; i < 2; ++i)
         if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
-    if (h->d_planes) cudaFree(h->d_planes);
-    if (h->d_mask) cudaFree(h->d_mask);
-    if (h->d_inflow) cudaFree(h->d_inflow);
-    if (h->d_partial) cudaFree(h->d_partial);
-    if (h->d_out) cudaFree(h->d_out);
-    if (h->d_uprev) cudaFree(h->d_uprev);
-    if (h->d_vprev) cudaFree(h->d_vprev);
-    if (h->d_stage) cudaFree(h->d_stage);
+    if (h->st) {
+        for (void *p : {(void *)h->d_planes, (void *)h->d_mask, (void *)h->d_inflow, (void *)h->d_partial,
+                        (void *)h->d_out, (void *)h->d_uprev, (void *)h->d_vprev, h->d_stage})
+            dfree(h, p);
+        cudaStreamSynchronize(h->st);
+    }
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->st) cudaStreamDestroy(h->st);
@@ -308,7 +319,7 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
         cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) {
         release(h); delete h; return BGK_E_CUDA;
     }
-    if (cudaMalloc(&h->d_planes, h->planes_bytes) != cudaSuccess) {
+    if (dalloc(h, &h->d_planes, h->planes_bytes) != cudaSuccess) {
         cudaGetLastError(); release(h); delete h; return BGK_E_NOMEM;
     }
     cudaMemsetAsync(h->d_planes, 0, h->planes_bytes, h->st);
@@ -329,10 +340,11 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
     L.forced = h->cs.forced;
 
     // inflow table
-    if (cudaMalloc(&h->d_inflow, h->cs.inflow.size() * sizeof(double)) != cudaSuccess) {
+    if (dalloc(h, &h->d_inflow, h->cs.inflow.size() * sizeof(double)) != cudaSuccess) {
         cudaGetLastError(); release(h); delete h; return BGK_E_NOMEM;
     }
-    cudaMemcpy(h->d_inflow, h->cs.inflow.data(), h->cs.inflow.size() * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpyAsync(h->d_inflow, h->cs.inflow.data(), h->cs.inflow.size() * sizeof(double), cudaMemcpyHostToDevice,
+                    h->st);
     L.inflow = h->d_inflow;
 
     // obstacle bits, rows 0..m+1, bit x for x = 0..l+1
@@ -342,10 +354,11 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
         for (int i = 1; i <= l; ++i)
             if (h->cs.obs[(size_t)(i - 1) + (size_t)(j - 1) * l] == 1)
                 bits[(size_t)j * L.mask_pitch + (i >> 5)] |= 1u << (i & 31);
-    if (cudaMalloc(&h->d_mask, bits.size() * 4) != cudaSuccess) {
+    if (dalloc(h, &h->d_mask, bits.size() * 4) != cudaSuccess) {
         cudaGetLastError(); release(h); delete h; return BGK_E_NOMEM;
     }
-    cudaMemcpy(h->d_mask, bits.data(), bits.size() * 4, cudaMemcpyHostToDevice);
+    cudaMemcpyAsync(h->d_mask, bits.data(), bits.size() * 4, cudaMemcpyHostToDevice, h->st);
+    cudaStreamSynchronize(h->st);  // `bits` and the inflow table are host temporaries
     L.mask = h->d_mask;
     if (h->cs.has_obs) {
         L.ob_x0 = h->cs.bbox[0] - 1; L.ob_x1 = h->cs.bbox[1] + 1;
@@ -356,8 +369,8 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
 
     // reduction scratch
     h->nb_red = 4 * 152;
-    if (cudaMalloc(&h->d_partial, (size_t)h->nb_red * 4 * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&h->d_out, 4 * sizeof(double)) != cudaSuccess) {
+    if (dalloc(h, &h->d_partial, (size_t)h->nb_red * 4 * sizeof(double)) != cudaSuccess ||
+        dalloc(h, &h->d_out, 4 * sizeof(double)) != cudaSuccess) {
         cudaGetLastError(); release(h); delete h; return BGK_E_NOMEM;
     }
     h->cfg = default_cfg(nvec);
@@ -498,8 +511,8 @@ int bgk_residual(bgk_handle *h, double *out)
     const size_t n = (size_t)h->desc.lx * h->desc.ly;
     bool first = false;
     if (!h->d_uprev) {
-        if (cudaMalloc(&h->d_uprev, n * sizeof(double)) != cudaSuccess ||
-            cudaMalloc(&h->d_vprev, n * sizeof(double)) != cudaSuccess) {
+        if (dalloc(h, &h->d_uprev, n * sizeof(double)) != cudaSuccess ||
+            dalloc(h, &h->d_vprev, n * sizeof(double)) != cudaSuccess) {
             cudaGetLastError();
             return fail(h, BGK_E_NOMEM, "residual snapshot");
         }
@@ -556,7 +569,7 @@ int bgk_fields(bgk_handle *h, double *rho, double *u, double *v)
     if (!rho || !u || !v) return BGK_E_INVALID;
     const size_t n = (size_t)h->desc.lx * h->desc.ly;
     double *d = nullptr;
-    if (cudaMalloc(&d, 3 * n * sizeof(double)) != cudaSuccess) {
+    if (dalloc(h, &d, 3 * n * sizeof(double)) != cudaSuccess) {
         cudaGetLastError();
         return fail(h, BGK_E_NOMEM, "fields buffer");
     }
@@ -565,8 +578,8 @@ int bgk_fields(bgk_handle *h, double *rho, double *u, double *v)
     if (e == cudaSuccess) e = cudaMemcpyAsync(rho, d, n * sizeof(double), cudaMemcpyDeviceToHost, h->st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(u, d + n, n * sizeof(double), cudaMemcpyDeviceToHost, h->st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(v, d + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+    dfree(h, d);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
-    cudaFree(d);
     if (e != cudaSuccess) return fail(h, BGK_E_CUDA, "fields: %s", cudaGetErrorString(e));
     return BGK_OK;
 }

@@ -60,20 +60,20 @@ int rebuild(bgk_batch *b)
             for (int bx = 0; bx < gx; ++bx) tiles.push_back(make_int4((int)i, bx, by, 0));
     }
     if (lats.size() > b->cap_lats) {
-        if (b->d_lats) cudaFree(b->d_lats);
-        if (b->d_cur) cudaFree(b->d_cur);
+        if (b->d_lats) cudaFreeAsync(b->d_lats, b->st);
+        if (b->d_cur) cudaFreeAsync(b->d_cur, b->st);
         b->cap_lats = std::max<size_t>(lats.size(), 2 * b->cap_lats);
-        if (cudaMalloc(&b->d_lats, b->cap_lats * sizeof(Lattice)) != cudaSuccess ||
-            cudaMalloc(&b->d_cur, b->cap_lats * sizeof(int)) != cudaSuccess) {
+        if (cudaMallocAsync((void **)&b->d_lats, b->cap_lats * sizeof(Lattice), b->st) != cudaSuccess ||
+            cudaMallocAsync((void **)&b->d_cur, b->cap_lats * sizeof(int), b->st) != cudaSuccess) {
             cudaGetLastError();
             b->cap_lats = 0;
             return BGK_E_NOMEM;
         }
     }
     if (tiles.size() > b->cap_tiles) {
-        if (b->d_tiles) cudaFree(b->d_tiles);
+        if (b->d_tiles) cudaFreeAsync(b->d_tiles, b->st);
         b->cap_tiles = std::max<size_t>(tiles.size(), 2 * b->cap_tiles);
-        if (cudaMalloc(&b->d_tiles, b->cap_tiles * sizeof(int4)) != cudaSuccess) {
+        if (cudaMallocAsync((void **)&b->d_tiles, b->cap_tiles * sizeof(int4), b->st) != cudaSuccess) {
             cudaGetLastError();
             b->cap_tiles = 0;
             return BGK_E_NOMEM;
@@ -214,9 +214,10 @@ int bgk_batch_destroy(bgk_batch *b)
     cudaStreamSynchronize(b->st);
     for (auto *h : b->members) { h->batch = nullptr; h->wait_ev = nullptr; }
     if (b->graph) cudaGraphExecDestroy(b->graph);
-    if (b->d_lats) cudaFree(b->d_lats);
-    if (b->d_cur) cudaFree(b->d_cur);
-    if (b->d_tiles) cudaFree(b->d_tiles);
+    if (b->d_lats) cudaFreeAsync(b->d_lats, b->st);
+    if (b->d_cur) cudaFreeAsync(b->d_cur, b->st);
+    if (b->d_tiles) cudaFreeAsync(b->d_tiles, b->st);
+    cudaStreamSynchronize(b->st);
     if (b->done) cudaEventDestroy(b->done);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);

@@ -68,10 +68,37 @@ template <> struct Store<double> {
     template <typename K> __device__ __forceinline__ static K getq(double v, int) { return (K)v; }
     template <typename K> __device__ __forceinline__ static double putq(K v, int) { return (double)v; }
 };
+// Stochastic rounding of an FP32 value to a 16-bit kind with D dropped mantissa bits:
+// round-to-nearest of x + (u - 1/2) ulp with u uniform, written as a signed offset on the FP32
+// bit pattern; E[result] = x, so updates below half an ulp are not lost on average.
+// The offset acts on the magnitude bits; magnitudes below it (zero included) are left alone.
+__device__ __forceinline__ float sr_dither(float x, uint32_t r, int dropped)
+{
+    const uint32_t mask = (1u << dropped) - 1u, half = 1u << (dropped - 1);
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t mag = b & 0x7fffffffu;
+    const uint32_t m2 = mag > half ? mag + (r & mask) - half : mag;
+    return __uint_as_float((b & 0x80000000u) | m2);
+}
+
+// 32-bit integer hash (xor-shift / multiply finaliser) for the rounding offsets
+__device__ __forceinline__ uint32_t mix32(uint32_t h)
+{
+    h ^= h >> 16;
+    h *= 0x7feb352du;
+    h ^= h >> 15;
+    h *= 0x846ca68bu;
+    h ^= h >> 16;
+    return h;
+}
+
 template <> struct Store<__half> {
     static constexpr int VEC = 8;
+    static constexpr int DROPPED = 13;  // FP32 -> FP16 mantissa bits
     __device__ __forceinline__ static float raw_get(__half v) { return __half2float(v); }
-    __device__ __forceinline__ static __half raw_put(float v) { return __float2half_rn(v); }
+    __device__ __forceinline__ static __half raw_put(float v) {
+        return __float2half_rn(sr_dither(v, mix32(__float_as_uint(v)), DROPPED));
+    }
     __device__ __forceinline__ static uint32_t pack2(float a, float b) {
         __half2 h = __floats2half2_rn(a, b);
         return *reinterpret_cast<uint32_t *>(&h);
@@ -79,20 +106,22 @@ template <> struct Store<__half> {
     template <typename K, int q> __device__ __forceinline__ static K get(__half v) {
         return (K)(__half2float(v) * (1.0f / scale_of(q)));
     }
-    template <typename K, int q> __device__ __forceinline__ static __half put(K v) {
-        return __float2half_rn((float)v * scale_of(q));
-    }
+    template <typename K, int q> __device__ __forceinline__ static __half put(K v) { return putq<K>(v, q); }
     template <typename K> __device__ __forceinline__ static K getq(__half v, int q) {
         return (K)(__half2float(v) * (1.0f / scale_of(q)));
     }
     template <typename K> __device__ __forceinline__ static __half putq(K v, int q) {
-        return __float2half_rn((float)v * scale_of(q));
+        const float x = (float)v * scale_of(q);
+        return __float2half_rn(sr_dither(x, mix32(__float_as_uint(x) ^ (0x9e3779b9u * (uint32_t)(q + 1))), DROPPED));
     }
 };
 template <> struct Store<__nv_bfloat16> {
     static constexpr int VEC = 8;
+    static constexpr int DROPPED = 16;  // FP32 -> BF16 mantissa bits
     __device__ __forceinline__ static float raw_get(__nv_bfloat16 v) { return __bfloat162float(v); }
-    __device__ __forceinline__ static __nv_bfloat16 raw_put(float v) { return __float2bfloat16_rn(v); }
+    __device__ __forceinline__ static __nv_bfloat16 raw_put(float v) {
+        return __float2bfloat16_rn(sr_dither(v, mix32(__float_as_uint(v)), DROPPED));
+    }
     __device__ __forceinline__ static uint32_t pack2(float a, float b) {
         __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
         return *reinterpret_cast<uint32_t *>(&h);
@@ -100,14 +129,13 @@ template <> struct Store<__nv_bfloat16> {
     template <typename K, int q> __device__ __forceinline__ static K get(__nv_bfloat16 v) {
         return (K)(__bfloat162float(v) * (1.0f / scale_of(q)));
     }
-    template <typename K, int q> __device__ __forceinline__ static __nv_bfloat16 put(K v) {
-        return __float2bfloat16_rn((float)v * scale_of(q));
-    }
+    template <typename K, int q> __device__ __forceinline__ static __nv_bfloat16 put(K v) { return putq<K>(v, q); }
     template <typename K> __device__ __forceinline__ static K getq(__nv_bfloat16 v, int q) {
         return (K)(__bfloat162float(v) * (1.0f / scale_of(q)));
     }
     template <typename K> __device__ __forceinline__ static __nv_bfloat16 putq(K v, int q) {
-        return __float2bfloat16_rn((float)v * scale_of(q));
+        const float x = (float)v * scale_of(q);
+        return __float2bfloat16_rn(sr_dither(x, mix32(__float_as_uint(x) ^ (0x9e3779b9u * (uint32_t)(q + 1))), DROPPED));
     }
 };
 

@@ -153,7 +153,11 @@ __device__ __forceinline__ K outflow_eq(int q, K a01, K a03, K a05, K a08, K a10
 
 // value rounded through the storage kind of plane q (a ghost value lives in storage)
 template <typename S, typename K>
-__device__ __forceinline__ K rnd(int q, K v) { return Store<S>::template getq<K>(Store<S>::template putq<K>(v, q), q); }
+__device__ __forceinline__ K rnd(int q, K v)
+{
+    if constexpr (Is16<S>::value) return (K)(Store<S>::raw_get(S((float)v * scale_of(q))) * (1.0f / scale_of(q)));
+    else return Store<S>::template getq<K>(Store<S>::template putq<K>(v, q), q);
+}
 
 template <typename S, typename K>
 __device__ __forceinline__ K ldq(const S *plane, int64_t i, int q) { return Store<S>::template getq<K>(plane[i], q); }
@@ -318,20 +322,28 @@ __device__ __forceinline__ void relax_vec(K (&x)[9][N], K omega, K fgrad, bool f
 
 // store N values of direction q as one 8- or 16-byte vector
 template <typename S, typename K, int q, bool RAW, int N = vec_of<S>()>
-__device__ __forceinline__ void store_vec(S *p, const K (&v)[N])
+__device__ __forceinline__ void store_vec(S *p, const K (&v)[N], const uint32_t (&rh)[N])
 {
-    if constexpr (RAW && N == 8) {
-        uint4 u;
-        u.x = Store<S>::pack2((float)v[0], (float)v[1]);
-        u.y = Store<S>::pack2((float)v[2], (float)v[3]);
-        u.z = Store<S>::pack2((float)v[4], (float)v[5]);
-        u.w = Store<S>::pack2((float)v[6], (float)v[7]);
-        *reinterpret_cast<uint4 *>(p) = u;
-    } else if constexpr (RAW && N == 4) {
-        uint2 u;
-        u.x = Store<S>::pack2((float)v[0], (float)v[1]);
-        u.y = Store<S>::pack2((float)v[2], (float)v[3]);
-        *reinterpret_cast<uint2 *>(p) = u;
+    if constexpr (RAW) {
+        // stochastic rounding: per-cell hashes `rh` (one 32-bit word per cell), a different
+        // 16-bit window per direction
+        constexpr int D = Store<S>::DROPPED;
+        float w[N];
+#pragma unroll
+        for (int c = 0; c < N; ++c) w[c] = sr_dither((float)v[c], __funnelshift_l(rh[c], rh[c], 3 * q), D);
+        if constexpr (N == 8) {
+            uint4 u;
+            u.x = Store<S>::pack2(w[0], w[1]);
+            u.y = Store<S>::pack2(w[2], w[3]);
+            u.z = Store<S>::pack2(w[4], w[5]);
+            u.w = Store<S>::pack2(w[6], w[7]);
+            *reinterpret_cast<uint4 *>(p) = u;
+        } else {
+            uint2 u;
+            u.x = Store<S>::pack2(w[0], w[1]);
+            u.y = Store<S>::pack2(w[2], w[3]);
+            *reinterpret_cast<uint2 *>(p) = u;
+        }
     } else {
         S o[N];
 #pragma unroll
@@ -421,15 +433,19 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
 
     relax_vec<S, K, RAW, N>(x, (K)L.omega, (K)L.fgrad, L.forced != 0);
     const int64_t me = cell_index<S>(L, xv, y);
-    store_vec<S, K, D01, RAW, N>(dst + D01 * pe + me, x[D01]);
-    store_vec<S, K, D03, RAW, N>(dst + D03 * pe + me, x[D03]);
-    store_vec<S, K, D05, RAW, N>(dst + D05 * pe + me, x[D05]);
-    store_vec<S, K, D08, RAW, N>(dst + D08 * pe + me, x[D08]);
-    store_vec<S, K, D10, RAW, N>(dst + D10 * pe + me, x[D10]);
-    store_vec<S, K, D12, RAW, N>(dst + D12 * pe + me, x[D12]);
-    store_vec<S, K, D14, RAW, N>(dst + D14 * pe + me, x[D14]);
-    store_vec<S, K, D17, RAW, N>(dst + D17 * pe + me, x[D17]);
-    store_vec<S, K, D19, RAW, N>(dst + D19 * pe + me, x[D19]);
+    uint32_t rh[N];
+#pragma unroll
+    for (int c = 0; c < N; ++c)
+        rh[c] = RAW ? mix32(((uint32_t)me + c) * 0x9e3779b9u ^ __float_as_uint((float)x[D19][c])) : 0u;
+    store_vec<S, K, D01, RAW, N>(dst + D01 * pe + me, x[D01], rh);
+    store_vec<S, K, D03, RAW, N>(dst + D03 * pe + me, x[D03], rh);
+    store_vec<S, K, D05, RAW, N>(dst + D05 * pe + me, x[D05], rh);
+    store_vec<S, K, D08, RAW, N>(dst + D08 * pe + me, x[D08], rh);
+    store_vec<S, K, D10, RAW, N>(dst + D10 * pe + me, x[D10], rh);
+    store_vec<S, K, D12, RAW, N>(dst + D12 * pe + me, x[D12], rh);
+    store_vec<S, K, D14, RAW, N>(dst + D14 * pe + me, x[D14], rh);
+    store_vec<S, K, D17, RAW, N>(dst + D17 * pe + me, x[D17], rh);
+    store_vec<S, K, D19, RAW, N>(dst + D19 * pe + me, x[D19], rh);
 
     bool rules = (y == 1) || (y == L.ly) || (k == 0) || (k == nv - 1);
     if (HAS_OBS) rules = rules || (y >= L.ob_y0 && y <= L.ob_y1 && xv + N - 1 >= L.ob_x0 && xv <= L.ob_x1);
@@ -447,25 +463,33 @@ __global__ void __launch_bounds__(TXV *TY) pp_kernel(const Lattice L, const int 
     pp_tile<S, K, TXV, TY, HAS_OBS, N>(L, blockIdx.x, blockIdx.y, parity);
 }
 
-// Persistent ping-pong step over many lattices: block b takes tiles b, b + gridDim.x, ...
-// of the work list (lattice index, tile x, tile y).  Lattice i uses buffer cur[i] ^ parity.
+// Persistent ping-pong step over many lattices.  The work list holds (lattice, tile x, tile y)
+// sorted by lattice; block b takes the contiguous chunk b of it and copies a lattice's
+// descriptor to shared memory only when the lattice changes.  Lattice i uses buffer
+// cur[i] ^ parity.
 template <typename S, typename K, int TXV, int TY, int N>
-__global__ void __launch_bounds__(TXV *TY) batch_pp_kernel(const Lattice *__restrict__ lats,
-                                                           const int *__restrict__ cur,
-                                                           const int4 *__restrict__ tiles, const int ntiles,
-                                                           const int parity)
+__global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && N * sizeof(S) == 8) ? 8 : 1)
+    batch_pp_kernel(const Lattice *__restrict__ lats, const int *__restrict__ cur, const int4 *__restrict__ tiles,
+                    const int ntiles, const int parity)
 {
     __shared__ Lattice sL;
     constexpr int NW = (int)(sizeof(Lattice) / sizeof(int));
     const int tid = threadIdx.y * TXV + threadIdx.x;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int per = (ntiles + gridDim.x - 1) / gridDim.x;
+    const int t0 = blockIdx.x * per, t1 = min(ntiles, t0 + per);
+    int dom = -1, par = 0;
+    for (int t = t0; t < t1; ++t) {
         const int4 tile = __ldg(tiles + t);
-        __syncthreads();
-        const int *srcw = reinterpret_cast<const int *>(lats + tile.x);
-        int *dstw = reinterpret_cast<int *>(&sL);
-        for (int i = tid; i < NW; i += TXV * TY) dstw[i] = __ldg(srcw + i);
-        __syncthreads();
-        pp_tile<S, K, TXV, TY, true, N>(sL, tile.y, tile.z, __ldg(cur + tile.x) ^ parity);
+        if (tile.x != dom) {
+            __syncthreads();
+            const int *srcw = reinterpret_cast<const int *>(lats + tile.x);
+            int *dstw = reinterpret_cast<int *>(&sL);
+            for (int i = tid; i < NW; i += TXV * TY) dstw[i] = __ldg(srcw + i);
+            __syncthreads();
+            dom = tile.x;
+            par = __ldg(cur + dom) ^ parity;
+        }
+        pp_tile<S, K, TXV, TY, true, N>(sL, tile.y, tile.z, par);
     }
 }
 
@@ -762,15 +786,19 @@ __global__ void __launch_bounds__(TXV *TY) aa_l_kernel(const Lattice L)
         }
     }
     relax_vec<S, K, RAW>(x, omega, fgrad, forced);
-    store_vec<S, K, D01, RAW>(base + D12 * pe + me, x[D01]);
-    store_vec<S, K, D03, RAW>(base + D10 * pe + me, x[D03]);
-    store_vec<S, K, D05, RAW>(base + D14 * pe + me, x[D05]);
-    store_vec<S, K, D08, RAW>(base + D17 * pe + me, x[D08]);
-    store_vec<S, K, D10, RAW>(base + D03 * pe + me, x[D10]);
-    store_vec<S, K, D12, RAW>(base + D01 * pe + me, x[D12]);
-    store_vec<S, K, D14, RAW>(base + D05 * pe + me, x[D14]);
-    store_vec<S, K, D17, RAW>(base + D08 * pe + me, x[D17]);
-    store_vec<S, K, D19, RAW>(base + D19 * pe + me, x[D19]);
+    uint32_t rh[VEC];
+#pragma unroll
+    for (int c = 0; c < VEC; ++c)
+        rh[c] = RAW ? mix32(((uint32_t)me + c) * 0x9e3779b9u ^ __float_as_uint((float)x[D19][c])) : 0u;
+    store_vec<S, K, D01, RAW>(base + D12 * pe + me, x[D01], rh);
+    store_vec<S, K, D03, RAW>(base + D10 * pe + me, x[D03], rh);
+    store_vec<S, K, D05, RAW>(base + D14 * pe + me, x[D05], rh);
+    store_vec<S, K, D08, RAW>(base + D17 * pe + me, x[D08], rh);
+    store_vec<S, K, D10, RAW>(base + D03 * pe + me, x[D10], rh);
+    store_vec<S, K, D12, RAW>(base + D01 * pe + me, x[D12], rh);
+    store_vec<S, K, D14, RAW>(base + D05 * pe + me, x[D14], rh);
+    store_vec<S, K, D17, RAW>(base + D08 * pe + me, x[D17], rh);
+    store_vec<S, K, D19, RAW>(base + D19 * pe + me, x[D19], rh);
 }
 
 }  // namespace bgk

@@ -74,7 +74,7 @@ def test_batch_configs_and_tuner_give_same_result(bgk):
             done += 130
         done += b.tune(4)
         tile, bps, g = b.config()
-        assert 0 <= tile < 4 and bps in (2, 4, 8, 16) and g in (8, 32, 128)
+        assert 0 <= tile < 6 and bps in (2, 4, 8, 16) and g in (8, 32, 128)
         for s in ref:
             s.step(done)
         for s, r in zip(members, ref):

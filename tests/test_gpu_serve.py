@@ -31,7 +31,8 @@ def run(bgk, reqs, stagger=0.0, max_slots=64):
         out = []
         for i, rq in zip(ids, reqs):
             r = res[i]
-            r["fields"] = srv.fields(i, r["lx"], r["ly"])
+            if rq.get("keep_fields"):
+                r["fields"] = srv.fields(i, r["lx"], r["ly"])
             out.append(r)
         return out, srv.stats()
 
