@@ -68,75 +68,71 @@ template <> struct Store<double> {
     template <typename K> __device__ __forceinline__ static K getq(double v, int) { return (K)v; }
     template <typename K> __device__ __forceinline__ static double putq(K v, int) { return (double)v; }
 };
-// Stochastic rounding of an FP32 value to a 16-bit kind with D dropped mantissa bits:
-// round-to-nearest of x + (u - 1/2) ulp with u uniform, written as a signed offset on the FP32
-// bit pattern; E[result] = x, so updates below half an ulp are not lost on average.
-// The offset acts on the magnitude bits; magnitudes below it (zero included) are left alone.
-__device__ __forceinline__ float sr_dither(float x, uint32_t r, int dropped)
+// Stochastic rounding to a 16-bit kind with D dropped mantissa bits: round toward zero of
+// |x| + u ulp, u uniform in [0, 1), written as an integer add of r in [0, 2^D) to the FP32 bit
+// pattern followed by a round-toward-zero conversion.  E[result] = x, so updates smaller than
+// half an ulp are not lost on average (round-to-nearest would drop them); zero stays zero.
+__device__ __forceinline__ float sr_add(float x, uint32_t r) { return __int_as_float(__float_as_int(x) + (int)r); }
+
+// per-cell random word: multiplicative hash of the cell index and a value that changes every step
+__device__ __forceinline__ uint32_t cell_hash(uint32_t idx, float v)
 {
-    const uint32_t mask = (1u << dropped) - 1u, half = 1u << (dropped - 1);
-    const uint32_t b = __float_as_uint(x);
-    const uint32_t mag = b & 0x7fffffffu;
-    const uint32_t m2 = mag > half ? mag + (r & mask) - half : mag;
-    return __uint_as_float((b & 0x80000000u) | m2);
+    uint32_t h = idx * 0x9e3779b1u ^ __float_as_uint(v);
+    h ^= h >> 15;
+    return h * 0x85ebca77u;
 }
 
-// 32-bit integer hash (xor-shift / multiply finaliser) for the rounding offsets
-__device__ __forceinline__ uint32_t mix32(uint32_t h)
-{
-    h ^= h >> 16;
-    h *= 0x7feb352du;
-    h ^= h >> 15;
-    h *= 0x846ca68bu;
-    h ^= h >> 16;
-    return h;
-}
+// random bits for a lone value: multiplicative hash of its own bit pattern
+template <int D>
+__device__ __forceinline__ uint32_t self_bits(float x) { return (__float_as_uint(x) * 0x9e3779b1u) >> (32 - D); }
 
 template <> struct Store<__half> {
     static constexpr int VEC = 8;
     static constexpr int DROPPED = 13;  // FP32 -> FP16 mantissa bits
+    static constexpr int POS0 = 19;     // bit window of direction q in a cell's random word: POS0 - q
     __device__ __forceinline__ static float raw_get(__half v) { return __half2float(v); }
     __device__ __forceinline__ static __half raw_put(float v) {
-        return __float2half_rn(sr_dither(v, mix32(__float_as_uint(v)), DROPPED));
+        return __float2half_rz(sr_add(v, self_bits<DROPPED>(v)));
     }
-    __device__ __forceinline__ static uint32_t pack2(float a, float b) {
-        __half2 h = __floats2half2_rn(a, b);
-        return *reinterpret_cast<uint32_t *>(&h);
+    __device__ __forceinline__ static uint32_t pack2_rz(float lo, float hi) {
+        uint32_t r;
+        asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+        return r;
     }
     template <typename K, int q> __device__ __forceinline__ static K get(__half v) {
         return (K)(__half2float(v) * (1.0f / scale_of(q)));
     }
-    template <typename K, int q> __device__ __forceinline__ static __half put(K v) { return putq<K>(v, q); }
     template <typename K> __device__ __forceinline__ static K getq(__half v, int q) {
         return (K)(__half2float(v) * (1.0f / scale_of(q)));
     }
     template <typename K> __device__ __forceinline__ static __half putq(K v, int q) {
-        const float x = (float)v * scale_of(q);
-        return __float2half_rn(sr_dither(x, mix32(__float_as_uint(x) ^ (0x9e3779b9u * (uint32_t)(q + 1))), DROPPED));
+        return raw_put((float)v * scale_of(q));
     }
+    template <typename K, int q> __device__ __forceinline__ static __half put(K v) { return putq<K>(v, q); }
 };
 template <> struct Store<__nv_bfloat16> {
     static constexpr int VEC = 8;
     static constexpr int DROPPED = 16;  // FP32 -> BF16 mantissa bits
+    static constexpr int POS0 = 16;
     __device__ __forceinline__ static float raw_get(__nv_bfloat16 v) { return __bfloat162float(v); }
     __device__ __forceinline__ static __nv_bfloat16 raw_put(float v) {
-        return __float2bfloat16_rn(sr_dither(v, mix32(__float_as_uint(v)), DROPPED));
+        return __float2bfloat16_rz(sr_add(v, self_bits<DROPPED>(v)));
     }
-    __device__ __forceinline__ static uint32_t pack2(float a, float b) {
-        __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-        return *reinterpret_cast<uint32_t *>(&h);
+    __device__ __forceinline__ static uint32_t pack2_rz(float lo, float hi) {
+        uint32_t r;
+        asm("cvt.rz.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+        return r;
     }
     template <typename K, int q> __device__ __forceinline__ static K get(__nv_bfloat16 v) {
         return (K)(__bfloat162float(v) * (1.0f / scale_of(q)));
     }
-    template <typename K, int q> __device__ __forceinline__ static __nv_bfloat16 put(K v) { return putq<K>(v, q); }
     template <typename K> __device__ __forceinline__ static K getq(__nv_bfloat16 v, int q) {
         return (K)(__bfloat162float(v) * (1.0f / scale_of(q)));
     }
     template <typename K> __device__ __forceinline__ static __nv_bfloat16 putq(K v, int q) {
-        const float x = (float)v * scale_of(q);
-        return __float2bfloat16_rn(sr_dither(x, mix32(__float_as_uint(x) ^ (0x9e3779b9u * (uint32_t)(q + 1))), DROPPED));
+        return raw_put((float)v * scale_of(q));
     }
+    template <typename K, int q> __device__ __forceinline__ static __nv_bfloat16 put(K v) { return putq<K>(v, q); }
 };
 
 // One domain as the kernels see it.  Scalars of the compute kind are kept in double and

@@ -327,21 +327,21 @@ __device__ __forceinline__ void store_vec(S *p, const K (&v)[N], const uint32_t 
     if constexpr (RAW) {
         // stochastic rounding: per-cell hashes `rh` (one 32-bit word per cell), a different
         // 16-bit window per direction
-        constexpr int D = Store<S>::DROPPED;
+        constexpr int D = Store<S>::DROPPED, P = Store<S>::POS0 - q;
         float w[N];
 #pragma unroll
-        for (int c = 0; c < N; ++c) w[c] = sr_dither((float)v[c], __funnelshift_l(rh[c], rh[c], 3 * q), D);
+        for (int c = 0; c < N; ++c) w[c] = sr_add((float)v[c], (rh[c] >> P) & ((1u << D) - 1u));
         if constexpr (N == 8) {
             uint4 u;
-            u.x = Store<S>::pack2(w[0], w[1]);
-            u.y = Store<S>::pack2(w[2], w[3]);
-            u.z = Store<S>::pack2(w[4], w[5]);
-            u.w = Store<S>::pack2(w[6], w[7]);
+            u.x = Store<S>::pack2_rz(w[0], w[1]);
+            u.y = Store<S>::pack2_rz(w[2], w[3]);
+            u.z = Store<S>::pack2_rz(w[4], w[5]);
+            u.w = Store<S>::pack2_rz(w[6], w[7]);
             *reinterpret_cast<uint4 *>(p) = u;
         } else {
             uint2 u;
-            u.x = Store<S>::pack2(w[0], w[1]);
-            u.y = Store<S>::pack2(w[2], w[3]);
+            u.x = Store<S>::pack2_rz(w[0], w[1]);
+            u.y = Store<S>::pack2_rz(w[2], w[3]);
             *reinterpret_cast<uint2 *>(p) = u;
         }
     } else {
@@ -397,6 +397,34 @@ __device__ void pp_cell_slow(const Lattice &L, const S *src, S *dst, int x, int 
     for (int q = 0; q < 9; ++q) dst[q * pe + me] = Store<S>::template putq<K>(v[q], q);
 }
 
+// First (x = 1, LOW) or last (x = lx) cell of a row in rows 2..ly-1 away from obstacles: only the
+// three inputs that come from the x ghost column need the boundary rules; they replace the
+// vector-loaded values in place (position C of the thread's N cells, scaled when RAW).
+template <typename S, typename K, bool HAS_OBS, bool RAW, int C, bool LOW, int N>
+__device__ __forceinline__ void pp_edge_pull(const Lattice &L, const S *src, int x, int y, K (&v)[9][N])
+{
+    const int64_t pe = L.plane_elems;
+    const int64_t me = cell_index<S>(L, x, y);
+    auto plane_at = [&](int q, int sx, int sy) -> K { return ldq<S, K>(src + q * pe, cell_index<S>(L, sx, sy), q); };
+    auto own = [&](int q) -> K { return ldq<S, K>(src + q * pe, me, q); };
+    auto ghost_xhi = [&](int q, int sy) -> K {
+        const int l = L.lx;
+        if (L.faces[XHI] == FK_OUTFLOW_ZG) return plane_at(q, l, sy);
+        const int64_t i = cell_index<S>(L, l, sy);
+        K a[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = ldq<S, K>(src + k * pe, i, k);
+        return rnd<S, K>(q, outflow_eq<K>(q, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7]));
+    };
+    constexpr int q0 = LOW ? D01 : D10, q1 = LOW ? D03 : D12, q2 = LOW ? D05 : D14;
+    const K a = pull_rule<S, K, HAS_OBS>(L, q0, x, y, plane_at, own, ghost_xhi);
+    const K b = pull_rule<S, K, HAS_OBS>(L, q1, x, y, plane_at, own, ghost_xhi);
+    const K c = pull_rule<S, K, HAS_OBS>(L, q2, x, y, plane_at, own, ghost_xhi);
+    v[q0][C] = RAW ? (K)((float)a * scale_of(q0)) : a;
+    v[q1][C] = RAW ? (K)((float)b * scale_of(q1)) : b;
+    v[q2][C] = RAW ? (K)((float)c * scale_of(q2)) : c;
+}
+
 // one tile of TXV*VEC x TY cells at tile coordinates (bx, by) of lattice L.  Every lane takes the
 // vector path; cells whose inputs come from the boundary rules are then recomputed one by one
 // and overwritten (the source buffer is read-only during the step, so the recompute sees the
@@ -431,12 +459,20 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
     pull_vec<S, K, D19, W, RAW, N>(L, src + D19 * pe, xv, y, loads, tx, x[D19]);
     if (!active) return;
 
+    const bool rowb = (y == 1) || (y == L.ly);
+    bool obsz = false;
+    if (HAS_OBS) obsz = y >= L.ob_y0 && y <= L.ob_y1 && xv + N - 1 >= L.ob_x0 && xv <= L.ob_x1;
+    const bool left_cell = !rowb && !obsz && k == 0 && nv > 1;
+    const bool right_cell = !rowb && !obsz && k == nv - 1 && nv > 1 && (L.lx % N) == 0;
+    if (left_cell) pp_edge_pull<S, K, HAS_OBS, RAW, 0, true, N>(L, src, xv, y, x);
+    if (right_cell) pp_edge_pull<S, K, HAS_OBS, RAW, N - 1, false, N>(L, src, xv + N - 1, y, x);
+
     relax_vec<S, K, RAW, N>(x, (K)L.omega, (K)L.fgrad, L.forced != 0);
     const int64_t me = cell_index<S>(L, xv, y);
     uint32_t rh[N];
 #pragma unroll
     for (int c = 0; c < N; ++c)
-        rh[c] = RAW ? mix32(((uint32_t)me + c) * 0x9e3779b9u ^ __float_as_uint((float)x[D19][c])) : 0u;
+        rh[c] = RAW ? cell_hash((uint32_t)me + c, (float)x[D19][c]) : 0u;
     store_vec<S, K, D01, RAW, N>(dst + D01 * pe + me, x[D01], rh);
     store_vec<S, K, D03, RAW, N>(dst + D03 * pe + me, x[D03], rh);
     store_vec<S, K, D05, RAW, N>(dst + D05 * pe + me, x[D05], rh);
@@ -447,8 +483,7 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
     store_vec<S, K, D17, RAW, N>(dst + D17 * pe + me, x[D17], rh);
     store_vec<S, K, D19, RAW, N>(dst + D19 * pe + me, x[D19], rh);
 
-    bool rules = (y == 1) || (y == L.ly) || (k == 0) || (k == nv - 1);
-    if (HAS_OBS) rules = rules || (y >= L.ob_y0 && y <= L.ob_y1 && xv + N - 1 >= L.ob_x0 && xv <= L.ob_x1);
+    const bool rules = rowb || obsz || (k == 0 && !left_cell) || (k == nv - 1 && !right_cell);
     if (rules) {
         const int xe = min(xv + N - 1, L.lx);
 #pragma unroll 1
@@ -458,7 +493,7 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
 }
 
 template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N>
-__global__ void __launch_bounds__(TXV *TY) pp_kernel(const Lattice L, const int parity)
+__global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 4 && N == 4) ? 8 : 1) pp_kernel(const Lattice L, const int parity)
 {
     pp_tile<S, K, TXV, TY, HAS_OBS, N>(L, blockIdx.x, blockIdx.y, parity);
 }
@@ -629,6 +664,46 @@ __device__ void aa_p_cell_slow(const Lattice &L, S *base, int x, int y)
     aa_incoming<S, K>(L, base, x, y, g);
 }
 
+// First/last cell of a row in the AA P step, handled inside the vector path (rows 2..ly-1,
+// no obstacle nearby): only the x-face rules apply.  Before the collision the three inputs that
+// come from the x ghost column are replaced; after the vector push the three pushes that leave
+// through the x face are redone with the push rules, and the incoming inflow/outflow values
+// are written.  C is the cell's position in the lane's vector.
+template <typename S, typename K, bool HAS_OBS, bool RAW, int C, bool LOW>
+__device__ __forceinline__ void aa_edge_pull(const Lattice &L, const S *base, int x, int y, K (&v)[9][vec_of<S>()])
+{
+    const int64_t pe = L.plane_elems;
+    const int64_t me = cell_index<S>(L, x, y);
+    auto plane_at = [&](int q, int sx, int sy) -> K {
+        return ldq<S, K>(base + opp_of(q) * pe, cell_index<S>(L, sx, sy), q);
+    };
+    auto own = [&](int q) -> K { return ldq<S, K>(base + opp_of(q) * pe, me, q); };
+    auto ghost_xhi = [&](int q, int sy) -> K { return plane_at(q, L.lx + 1, sy); };
+    constexpr int q0 = LOW ? D01 : D10, q1 = LOW ? D03 : D12, q2 = LOW ? D05 : D14;
+    const K a = pull_rule<S, K, HAS_OBS>(L, q0, x, y, plane_at, own, ghost_xhi);
+    const K b = pull_rule<S, K, HAS_OBS>(L, q1, x, y, plane_at, own, ghost_xhi);
+    const K c = pull_rule<S, K, HAS_OBS>(L, q2, x, y, plane_at, own, ghost_xhi);
+    v[q0][C] = RAW ? (K)((float)a * scale_of(q0)) : a;
+    v[q1][C] = RAW ? (K)((float)b * scale_of(q1)) : b;
+    v[q2][C] = RAW ? (K)((float)c * scale_of(q2)) : c;
+}
+
+template <typename S, typename K, bool HAS_OBS, bool RAW, int C, bool LOW>
+__device__ __forceinline__ void aa_edge_push(const Lattice &L, S *base, int x, int y, const K (&v)[9][vec_of<S>()])
+{
+    K g[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) g[q] = RAW ? (K)((float)v[q][C] * (1.0f / scale_of(q))) : v[q][C];
+    constexpr int q0 = LOW ? D10 : D01, q1 = LOW ? D12 : D03, q2 = LOW ? D14 : D05;
+    aa_push_rule<S, K, HAS_OBS>(L, base, q0, x, y, g[q0]);
+    aa_push_rule<S, K, HAS_OBS>(L, base, q1, x, y, g[q1]);
+    aa_push_rule<S, K, HAS_OBS>(L, base, q2, x, y, g[q2]);
+    K gr[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) gr[q] = rnd<S, K>(q, g[q]);
+    aa_incoming<S, K>(L, base, x, y, gr);
+}
+
 // push VEC values of direction q to (x + c_q) in plane q; lanes at an edge (segment end or a
 // neighbour on the slow path) store the elements that cross into the neighbour's vector.
 template <typename S, typename K, int q, int W, bool RAW = false>
@@ -706,9 +781,14 @@ __global__ void __launch_bounds__(TXV *TY) aa_p_kernel(const Lattice L)
     pull_vec<S, K, D17, W, RAW>(L, base + D08 * pe, xv, y, loads, tx, x[D17]);
     pull_vec<S, K, D19, W, RAW>(L, base + D19 * pe, xv, y, loads, tx, x[D19]);
 
-    bool slow = (y == 1) || (y == L.ly) || (k == 0) || (k >= L.nvec - 1);
+    // lanes on the scalar path: boundary rows, a ragged row end, obstacle surroundings
+    bool slow = (y == 1) || (y == L.ly) || (L.nvec == 1) || (k == L.nvec - 1 && (L.lx % VEC) != 0);
     if (HAS_OBS) slow = slow || (y >= L.ob_y0 && y <= L.ob_y1 && xv + VEC - 1 >= L.ob_x0 && xv <= L.ob_x1);
     slow = slow || !active;
+    const bool left_cell = !slow && k == 0;             // x = 1 is element 0
+    const bool right_cell = !slow && k == L.nvec - 1;   // x = lx is element VEC-1
+    if (left_cell) aa_edge_pull<S, K, HAS_OBS, RAW, 0, true>(L, base, xv, y, x);
+    if (right_cell) aa_edge_pull<S, K, HAS_OBS, RAW, VEC - 1, false>(L, base, xv + VEC - 1, y, x);
     // neighbours on the slow path do not take part in the vector stores
     const bool left_slow = __shfl_up_sync(0xffffffffu, slow ? 1 : 0, 1, W) != 0;
     const bool right_slow = __shfl_down_sync(0xffffffffu, slow ? 1 : 0, 1, W) != 0;
@@ -727,6 +807,8 @@ __global__ void __launch_bounds__(TXV *TY) aa_p_kernel(const Lattice L)
     push_vec<S, K, D14, W, RAW>(L, base + D14 * pe, xv, y, left_edge, right_edge, g[D14], store);
     push_vec<S, K, D17, W, RAW>(L, base + D17 * pe, xv, y, left_edge, right_edge, g[D17], store);
     push_vec<S, K, D19, W, RAW>(L, base + D19 * pe, xv, y, left_edge, right_edge, g[D19], store);
+    if (left_cell) aa_edge_push<S, K, HAS_OBS, RAW, 0, true>(L, base, xv, y, g);
+    if (right_cell) aa_edge_push<S, K, HAS_OBS, RAW, VEC - 1, false>(L, base, xv + VEC - 1, y, g);
     if (!active || !slow) return;
     const int xe = min(xv + VEC - 1, L.lx);
 #pragma unroll 1
@@ -789,7 +871,7 @@ __global__ void __launch_bounds__(TXV *TY) aa_l_kernel(const Lattice L)
     uint32_t rh[VEC];
 #pragma unroll
     for (int c = 0; c < VEC; ++c)
-        rh[c] = RAW ? mix32(((uint32_t)me + c) * 0x9e3779b9u ^ __float_as_uint((float)x[D19][c])) : 0u;
+        rh[c] = RAW ? cell_hash((uint32_t)me + c, (float)x[D19][c]) : 0u;
     store_vec<S, K, D01, RAW>(base + D12 * pe + me, x[D01], rh);
     store_vec<S, K, D03, RAW>(base + D10 * pe + me, x[D03], rh);
     store_vec<S, K, D05, RAW>(base + D14 * pe + me, x[D05], rh);

@@ -46,7 +46,7 @@ def test_tgv_decay_rate_analytic(bgk, storage):
     initial field (the 2k acoustic modes of the equilibrium start are orthogonal to it)."""
     s = tgv(bgk, storage)
     _, ui, vi = s.fields()
-    t = 4000
+    t = int(round(18 * N * np.sqrt(3) / 2))  # whole periods of the 2k acoustic wave
     s.step(t)
     _, u, v = s.fields()
     amp = np.sum(u * ui + v * vi) / np.sum(ui * ui + vi * vi)
