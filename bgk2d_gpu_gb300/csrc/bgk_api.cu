@@ -377,19 +377,25 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
 
     // initial state (SRC/initialize.F90:85-125: init(init_v))
     int rc = BGK_OK;
-    if (d.init_v == BGK_INIT_TGV_REF || d.init_v == BGK_INIT_TGV) {
+    if (d.init_v == BGK_INIT_TGV) {
+        // computed on the device: no host loop over the lattice at admission time
+        if (h->T.init_tgv(h->L, d.tgv_u0, h->st) != cudaSuccess) rc = BGK_E_CUDA;
+        h->launches++;
+        if (rc == BGK_OK && d.scheme == BGK_SCHEME_AA &&
+            (h->cs.faces[XHI] == FK_OUTFLOW_EQ || h->cs.faces[XHI] == FK_OUTFLOW_ZG)) {
+            if (h->T.fill_outflow(h->L, h->st) != cudaSuccess) rc = BGK_E_CUDA;
+        }
+    } else if (d.init_v == BGK_INIT_TGV_REF) {
         const size_t n = (size_t)(l + 2) * (m + 2);
         void *ptrs[9];
         if (h->host_bytes == 8) {
             std::vector<double> a;
-            if (d.init_v == BGK_INIT_TGV) init_tgv<double>(l, m, d.tgv_u0, a);
-            else init_reference<double, double>(l, m, true, a);
+            init_reference<double, double>(l, m, true, a);
             for (int q = 0; q < 9; ++q) ptrs[q] = a.data() + q * n;
             rc = upload_impl(h, ptrs, l + 2);
         } else {
             std::vector<float> a;
-            if (d.init_v == BGK_INIT_TGV) init_tgv<float>(l, m, d.tgv_u0, a);
-            else if (d.compute == BGK_COMPUTE_F64) init_reference<double, float>(l, m, true, a);
+            if (d.compute == BGK_COMPUTE_F64) init_reference<double, float>(l, m, true, a);
             else init_reference<float, float>(l, m, true, a);
             for (int q = 0; q < 9; ++q) ptrs[q] = a.data() + q * n;
             rc = upload_impl(h, ptrs, l + 2);

@@ -46,6 +46,36 @@ __global__ void scatter_plane_kernel(Lattice L, int cur, int q, const H *__restr
     base[p * pe + cell_index<S>(L, x, y)] = Store<S>::template putq<double>((double)v, q);
 }
 
+// Pressure-corrected Taylor-Green start (BGK_INIT_TGV), computed on the device in FP64:
+// u = U0 sin(kx x) cos(ky y), v = -U0 cos(kx x) sin(ky y),
+// rho = 1 - 3 U0^2/4 (cos 2kx x + cos 2ky y), x = i - 1/2, y = j - 1/2, f - w = feq - w.
+template <typename S>
+__global__ void init_tgv_kernel(Lattice L, double u0)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x > L.lx + 1) return;
+    S *base = reinterpret_cast<S *>(L.planes);
+    const int64_t pe = L.plane_elems;
+    const double kx = 2.0 * 3.14159265358979323846 / L.lx, ky = 2.0 * 3.14159265358979323846 / L.ly;
+    const double xx = x - 0.5, yy = y - 0.5;
+    double sx, cx, sy, cy;
+    sincos(kx * xx, &sx, &cx);
+    sincos(ky * yy, &sy, &cy);
+    const double u = u0 * sx * cy, v = -u0 * cx * sy;
+    const double rho = 1.0 - 0.75 * u0 * u0 * ((2.0 * cx * cx - 1.0) + (2.0 * cy * cy - 1.0));
+    const double usq = u * u + v * v;
+    const double w[9] = {1. / 36, 1. / 36, 1. / 9, 1. / 9, 1. / 36, 1. / 36, 1. / 9, 1. / 9, 4. / 9};
+    const int64_t i = cell_index<S>(L, x, y);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const double cu = cx_of(q) * u + cy_of(q) * v;
+        const double f = w[q] * rho * (1.0 + 3.0 * cu + 4.5 * cu * cu - 1.5 * usq) - w[q];
+        const int p = L.scheme == 0 ? q : opp_of(q);
+        base[p * pe + i] = Store<S>::template putq<double>(f, q);
+    }
+}
+
 // device storage -> host-kind staging plane; ghost entries are written as zero
 template <typename S, typename K, typename H, bool HAS_OBS>
 __global__ void gather_plane_kernel(Lattice L, int cur, int phase, int q, H *__restrict__ stage)

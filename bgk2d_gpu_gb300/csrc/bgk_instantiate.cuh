@@ -74,6 +74,14 @@ cudaError_t fill_outflow(const Lattice &L, cudaStream_t st)
     return cudaGetLastError();
 }
 
+template <typename S>
+cudaError_t init_tgv(const Lattice &L, double u0, cudaStream_t st)
+{
+    const dim3 block(256), grid((unsigned)((L.lx + 2 + 255) / 256), (unsigned)(L.ly + 2));
+    init_tgv_kernel<S><<<grid, block, 0, st>>>(L, u0);
+    return cudaGetLastError();
+}
+
 template <typename S, typename K>
 cudaError_t diagno(const Lattice &L, int cur, int phase, int fluid_only, bool obs, double *partial, int nb, cudaStream_t st)
 {
@@ -134,6 +142,7 @@ KernelTable make_table()
     t.scatter = &scatter<S>;
     t.gather = &gather<S, K>;
     t.fill_outflow = &fill_outflow<S, K>;
+    t.init_tgv = &init_tgv<S>;
     t.diagno = &diagno<S, K>;
     t.residual = &residual<S, K>;
     t.draglift = &draglift<S, K>;

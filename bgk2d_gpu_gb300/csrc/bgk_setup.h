@@ -120,33 +120,6 @@ inline void init_reference(int l, int m, bool vortex, std::vector<H> &out)
     }
 }
 
-// BGK_INIT_TGV: u = U0 sin(kx x) cos(ky y), v = -U0 cos(kx x) sin(ky y),
-// rho = 1 - 3 U0^2/4 (cos 2kx x + cos 2ky y), x = i - 1/2, y = j - 1/2; equilibrium in double.
-template <typename H>
-inline void init_tgv(int l, int m, double u0amp, std::vector<H> &out)
-{
-    const size_t n = (size_t)(l + 2) * (size_t)(m + 2);
-    out.assign(9 * n, (H)0);
-    const double kx = 2.0 * M_PI / l, ky = 2.0 * M_PI / m;
-    const double w[9] = {1. / 36, 1. / 36, 1. / 9, 1. / 9, 1. / 36, 1. / 36, 1. / 9, 1. / 9, 4. / 9};
-    for (int j = 0; j <= m + 1; ++j) {
-        const double y = j - 0.5;
-        for (int i = 0; i <= l + 1; ++i) {
-            const double x = i - 0.5;
-            const double u = u0amp * std::sin(kx * x) * std::cos(ky * y);
-            const double v = -u0amp * std::cos(kx * x) * std::sin(ky * y);
-            const double rho = 1.0 - 0.75 * u0amp * u0amp * (std::cos(2 * kx * x) + std::cos(2 * ky * y));
-            const double usq = u * u + v * v;
-            const size_t k = (size_t)i + (size_t)j * (size_t)(l + 2);
-            for (int q = 0; q < 9; ++q) {
-                const double cu = cx_of(q) * u + cy_of(q) * v;
-                const double feq = w[q] * rho * (1.0 + 3.0 * cu + 4.5 * cu * cu - 1.5 * usq);
-                out[(size_t)q * n + k] = (H)(feq - w[q]);
-            }
-        }
-    }
-}
-
 // build_bcond + hencol (SRC/build.bcond.F90:47-56, SRC/hencol.F90:30-50) and the face rules of
 // the reference's boundary routines, in compute kind K.  Returns an empty string on success.
 template <typename K>

@@ -25,6 +25,7 @@ struct KernelTable {
     cudaError_t (*scatter)(const Lattice &L, int cur, int q, const void *stage, cudaStream_t st);
     cudaError_t (*gather)(const Lattice &L, int cur, int phase, int q, void *stage, bool obs, cudaStream_t st);
     cudaError_t (*fill_outflow)(const Lattice &L, cudaStream_t st);
+    cudaError_t (*init_tgv)(const Lattice &L, double u0, cudaStream_t st);
     cudaError_t (*diagno)(const Lattice &L, int cur, int phase, int fluid_only, bool obs, double *partial, int nb,
                           cudaStream_t st);
     cudaError_t (*residual)(const Lattice &L, int cur, int phase, bool obs, double *uprev, double *vprev,

@@ -1,0 +1,46 @@
+"""Multi-rank bench path on CPU (gloo, world size 2): ranks time their own domains, the job time
+is the max over ranks, and the job value sums the ranks' cells."""
+import os
+import socket
+
+import pytest
+
+torch = pytest.importorskip("torch")
+import torch.distributed as dist  # noqa: E402
+import torch.multiprocessing as mp  # noqa: E402
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, q):
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+    t = bench.max_over_ranks(1.0 + rank, dist)       # rank 1 is the slow one
+    g = bench.job_glups(4096 * 4096, 100, t, world)
+    r, w, _ = bench.dist_env()
+    dist.barrier()
+    dist.destroy_process_group()
+    q.put((rank, t, g, r, w))
+
+
+def test_two_ranks_max_and_sum():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(60)
+        assert p.exitcode == 0
+    for rank, t, g, r, w in out:
+        assert t == 2.0 and r == rank and w == 2
+        assert abs(g - 2 * 4096 * 4096 * 100 / 2.0 / 1e9) < 1e-9
