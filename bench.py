@@ -323,7 +323,9 @@ def bench_serving(bgk, dev, rates=(10.0, 30.0, 100.0), count=120):
         out.append({"rate_per_s": rate, "requests": count, "completed": st["completed"], "failed": st["failed"],
                     "GLUPS": round(st["glups"], 3), "p50_s": round(st["p50_s"], 4), "p99_s": round(st["p99_s"], 4),
                     "mean_queue_s": round(st["mean_queue_s"], 4), "peak_resident": st["peak_resident"],
-                    "launches": st["launches"],
+                    "launches": st["launches"], "rounds": st["rounds"],
+                    "mean_round_steps": round(st["mean_round_steps"], 1),
+                    "busy_frac": round(st["busy_s"] / st["wall_s"], 3) if st["wall_s"] else None,
                     "steps": int(sum(r["steps"] for r in res))})
     return out
 

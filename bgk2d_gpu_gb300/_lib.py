@@ -62,7 +62,8 @@ class ServerConfig(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [("submitted", I64), ("admitted", I64), ("completed", I64), ("failed", I64),
                 ("cell_updates", I64), ("busy_s", F64), ("wall_s", F64), ("glups", F64), ("p50_s", F64),
-                ("p99_s", F64), ("mean_queue_s", F64), ("peak_resident", I32), ("launches", I64)]
+                ("p99_s", F64), ("mean_queue_s", F64), ("peak_resident", I32), ("launches", I64),
+                ("rounds", I64), ("mean_round_steps", F64)]
 
 
 class BgkError(RuntimeError):

@@ -493,7 +493,7 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
 }
 
 template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N>
-__global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 4 && N == 4) ? 8 : 1) pp_kernel(const Lattice L, const int parity)
+__global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 || (sizeof(S) == 4 && N == 4)) ? 8 : (sizeof(S) == 2 ? 4 : 1)) pp_kernel(const Lattice L, const int parity)
 {
     pp_tile<S, K, TXV, TY, HAS_OBS, N>(L, blockIdx.x, blockIdx.y, parity);
 }
@@ -503,7 +503,7 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 4 &&
 // descriptor to shared memory only when the lattice changes.  Lattice i uses buffer
 // cur[i] ^ parity.
 template <typename S, typename K, int TXV, int TY, int N>
-__global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && N * sizeof(S) == 8) ? 8 : 1)
+__global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 || (sizeof(S) == 4 && N == 4)) ? 8 : (sizeof(S) == 2 ? 4 : 1))
     batch_pp_kernel(const Lattice *__restrict__ lats, const int *__restrict__ cur, const int4 *__restrict__ tiles,
                     const int ntiles, const int parity)
 {
@@ -754,7 +754,7 @@ __device__ __forceinline__ void push_vec(const Lattice &L, S *plane, int xv, int
 }
 
 template <typename S, typename K, int TXV, int TY, bool HAS_OBS>
-__global__ void __launch_bounds__(TXV *TY) aa_p_kernel(const Lattice L)
+__global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ? 4 : 1) aa_p_kernel(const Lattice L)
 {
     constexpr int VEC = vec_of<S>();
     constexpr int W = TXV < 32 ? TXV : 32;
@@ -817,7 +817,7 @@ __global__ void __launch_bounds__(TXV *TY) aa_p_kernel(const Lattice L)
 
 // L step: local collision, phase 1 -> 0
 template <typename S, typename K, int TXV, int TY, bool HAS_OBS>
-__global__ void __launch_bounds__(TXV *TY) aa_l_kernel(const Lattice L)
+__global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ? 4 : 1) aa_l_kernel(const Lattice L)
 {
     constexpr int VEC = vec_of<S>();
     const int k = blockIdx.x * TXV + threadIdx.x;

@@ -68,6 +68,7 @@ struct bgk_server {
     std::condition_variable cv, done_cv;
     std::deque<std::unique_ptr<Job>> pending;
     std::vector<std::unique_ptr<Job>> active;
+    std::vector<std::unique_ptr<Job>> prepared;    // created, not yet attached to a batch
     std::deque<bgk_result> finished;
     std::map<int64_t, std::unique_ptr<Job>> kept;  // finished jobs holding fields
     std::map<int, bgk_batch *> batches;            // storage kind -> batch
@@ -79,6 +80,7 @@ struct bgk_server {
     // stats
     int64_t submitted = 0, admitted = 0, completed = 0, failed = 0, cell_updates = 0, launches = 0;
     double busy_s = 0, queue_s_sum = 0, first_admit = -1, last_done = 0;
+    int64_t rounds = 0, round_steps = 0;
     int32_t peak = 0;
     std::vector<double> latencies;
 
@@ -173,14 +175,16 @@ void finish(bgk_server *S, std::unique_ptr<Job> j, int status)
     S->done_cv.notify_all();
 }
 
-void admit(bgk_server *S)
+// Create device state for queued requests (FIFO) while slots and HBM allow.  Each new case
+// lives on its own stream, so this overlaps with the batches' kernels.
+void prepare(bgk_server *S)
 {
     for (;;) {
         std::unique_ptr<Job> j;
         {
             std::lock_guard<std::mutex> g(S->mu);
             if (S->pending.empty()) return;
-            if ((int)S->active.size() >= S->cfg.max_slots) return;
+            if ((int)(S->active.size() + S->prepared.size()) >= S->cfg.max_slots) return;
             Job &head = *S->pending.front();
             if (head.bytes > S->budget) {  // can never fit: reject now
                 j = std::move(S->pending.front());
@@ -198,9 +202,20 @@ void admit(bgk_server *S)
             continue;
         }
         int rc = make_handle(S, *j);
-        bgk_batch *b = rc == BGK_OK ? batch_for(S, j->req.storage) : nullptr;
-        if (rc == BGK_OK && !b) rc = BGK_E_CUDA;
-        if (rc == BGK_OK) rc = bgk_batch_add(b, j->h);
+        if (rc != BGK_OK) {
+            finish(S, std::move(j), rc);
+            continue;
+        }
+        S->prepared.push_back(std::move(j));
+    }
+}
+
+// attach prepared cases to the batch of their storage kind (between rounds)
+void attach(bgk_server *S)
+{
+    for (auto &j : S->prepared) {
+        bgk_batch *b = batch_for(S, j->req.storage);
+        int rc = b ? bgk_batch_add(b, j->h) : BGK_E_CUDA;
         if (rc != BGK_OK) {
             finish(S, std::move(j), rc);
             continue;
@@ -213,6 +228,7 @@ void admit(bgk_server *S)
         S->active.push_back(std::move(j));
         S->peak = std::max<int32_t>(S->peak, (int32_t)S->active.size());
     }
+    S->prepared.clear();
 }
 
 int32_t next_event(const Job &j)
@@ -233,12 +249,15 @@ void round_once(bgk_server *S)
         if (members == 0) continue;
         int64_t l0 = 0, l1 = 0;
         bgk_batch_launch_count(kv.second, &l0);
-        bgk_batch_step(kv.second, n);
+        bgk_batch_step(kv.second, n);  // asynchronous
         bgk_batch_launch_count(kv.second, &l1);
         S->launches += l1 - l0;
     }
+    prepare(S);  // new cases are created while the round runs
     for (auto &kv : S->batches) bgk_batch_sync(kv.second);
     S->busy_s += std::chrono::duration<double>(clk::now() - t).count();
+    S->rounds++;
+    S->round_steps += n;
     std::vector<std::unique_ptr<Job>> keep;
     for (auto &j : S->active) {
         j->steps += n;
@@ -258,13 +277,17 @@ void round_once(bgk_server *S)
         else keep.push_back(std::move(j));
     }
     S->active = std::move(keep);
+    attach(S);
 }
 
 void worker_main(bgk_server *S)
 {
     cudaSetDevice(S->cfg.device);
     while (!S->stop.load()) {
-        admit(S);
+        if (S->active.empty()) {
+            prepare(S);
+            attach(S);
+        }
         if (S->active.empty()) {
             std::unique_lock<std::mutex> lk(S->mu);
             S->cv.wait_for(lk, std::chrono::milliseconds(2), [&] { return S->stop.load() || !S->pending.empty(); });
@@ -303,6 +326,8 @@ int bgk_server_destroy(bgk_server *S)
     S->cv.notify_all();
     if (S->worker.joinable()) S->worker.join();
     for (auto &j : S->active)
+        if (j->h) bgk_destroy(j->h);
+    for (auto &j : S->prepared)
         if (j->h) bgk_destroy(j->h);
     for (auto &kv : S->batches) bgk_batch_destroy(kv.second);
     delete S;
@@ -395,6 +420,8 @@ int bgk_server_get_stats(bgk_server *S, bgk_server_stats *o)
     o->mean_queue_s = S->admitted ? S->queue_s_sum / (double)S->admitted : 0.0;
     o->peak_resident = S->peak;
     o->launches = S->launches;
+    o->rounds = S->rounds;
+    o->mean_round_steps = S->rounds ? (double)S->round_steps / (double)S->rounds : 0.0;
     return BGK_OK;
 }
 

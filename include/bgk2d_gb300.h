@@ -186,7 +186,8 @@ int bgk_batch_size(bgk_batch *b, int32_t *members, int64_t *cells);
 int bgk_batch_step(bgk_batch *b, int32_t nsteps);
 int bgk_batch_step_timed(bgk_batch *b, int32_t nsteps, float *ms);
 int bgk_batch_sync(bgk_batch *b);
-/* tile shape (as bgk_set_tile), persistent blocks per SM, steps per CUDA graph (even) */
+/* tile shape (as bgk_set_tile), persistent blocks per SM (0: one block per work-list tile,
+ * no persistent loop), steps per CUDA graph (even) */
 int bgk_batch_set_config(bgk_batch *b, int32_t tile_cfg, int32_t blocks_per_sm, int32_t graph_steps);
 int bgk_batch_get_config(bgk_batch *b, int32_t out[3]);
 /* autotuner: times real steps over tile shapes, grid sizes and graph lengths; keeps the best */
@@ -247,6 +248,8 @@ typedef struct bgk_server_stats {
     double mean_queue_s;      /* mean t_admit - t_submit */
     int32_t peak_resident;
     int64_t launches;         /* kernels launched by the server */
+    int64_t rounds;           /* scheduling rounds */
+    double mean_round_steps;  /* steps per round */
 } bgk_server_stats;
 
 typedef struct bgk_server bgk_server;

@@ -68,13 +68,13 @@ def test_batch_configs_and_tuner_give_same_result(bgk):
         for s in members:
             b.add(s)
         done = 0
-        for cfg in ((0, 2, 8), (1, 16, 32), (3, 4, 2), (2, 8, 128)):
+        for cfg in ((0, 2, 8), (1, 16, 32), (3, 4, 2), (2, 8, 128), (4, 0, 8), (5, 0, 32)):
             b.set_config(*cfg)
             b.step(130)
             done += 130
         done += b.tune(4)
         tile, bps, g = b.config()
-        assert 0 <= tile < 6 and bps in (2, 4, 8, 16) and g in (8, 32, 128)
+        assert 0 <= tile < 6 and bps in (0, 4, 8, 16) and g in (8, 32, 128)
         for s in ref:
             s.step(done)
         for s, r in zip(members, ref):
