@@ -102,7 +102,12 @@ int sync_cur(bgk_batch *b)
     return cudaStreamSynchronize(b->st) == cudaSuccess ? BGK_OK : BGK_E_CUDA;
 }
 
-int grid_of(const bgk_batch *b) { return std::max(1, std::min(b->ntiles, b->blocks_per_sm * b->sms)); }
+// blocks_per_sm == 0 selects one block per tile
+int grid_of(const bgk_batch *b)
+{
+    if (b->blocks_per_sm == 0) return 0;
+    return std::max(1, std::min(b->ntiles, b->blocks_per_sm * b->sms));
+}
 
 int launch_one(bgk_batch *b, int parity)
 {
@@ -297,7 +302,7 @@ int bgk_batch_sync(bgk_batch *b)
 
 int bgk_batch_set_config(bgk_batch *b, int32_t tile_cfg, int32_t blocks_per_sm, int32_t graph_steps)
 {
-    if (!b || tile_cfg < 0 || tile_cfg >= NUM_CFG || blocks_per_sm < 1 || graph_steps < 2 || (graph_steps & 1))
+    if (!b || tile_cfg < 0 || tile_cfg >= NUM_CFG || blocks_per_sm < 0 || graph_steps < 2 || (graph_steps & 1))
         return BGK_E_INVALID;
     if (tile_cfg != b->cfg) b->dirty = true;
     if (tile_cfg != b->cfg || blocks_per_sm != b->blocks_per_sm || graph_steps != b->graph_steps) b->graph_built_for = -1;
@@ -321,7 +326,7 @@ int bgk_batch_tune(bgk_batch *b, int32_t trial_steps, int32_t *steps_run)
     if (!b || trial_steps < 2) return BGK_E_INVALID;
     if (cudaSetDevice(b->dev) != cudaSuccess) return BGK_E_CUDA;
     int64_t run = 0;
-    const int bps_opts[4] = {2, 4, 8, 16};
+    const int bps_opts[4] = {0, 4, 8, 16};
     float best = 1e30f;
     int best_cfg = b->cfg, best_bps = b->blocks_per_sm;
     const int n = trial_steps & ~1;

@@ -883,4 +883,16 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ?
     store_vec<S, K, D19, RAW>(base + D19 * pe + me, x[D19], rh);
 }
 
+// One block per work-list tile (the hardware schedules the blocks); the lattice descriptor is
+// read through the read-only cache.
+template <typename S, typename K, int TXV, int TY, int N>
+__global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 || (sizeof(S) == 4 && N == 4)) ? 8 : (sizeof(S) == 2 ? 4 : 1))
+    batch_pp_flat_kernel(const Lattice *__restrict__ lats, const int *__restrict__ cur, const int4 *__restrict__ tiles,
+                         const int parity)
+{
+    const int4 tile = __ldg(tiles + blockIdx.x);
+    const Lattice &L = lats[tile.x];
+    pp_tile<S, K, TXV, TY, true, N>(L, tile.y, tile.z, __ldg(cur + tile.x) ^ parity);
+}
+
 }  // namespace bgk
