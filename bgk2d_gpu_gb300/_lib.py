@@ -16,9 +16,10 @@ F64 = ctypes.c_double
 VP = ctypes.c_void_p
 
 # status codes
-OK, E_INVALID, E_NOMEM, E_CUDA, E_UNSUPPORTED, E_NUMERIC, E_CANCELLED, E_TIMEOUT, E_NOTFOUND = range(9)
+OK, E_INVALID, E_NOMEM, E_CUDA, E_UNSUPPORTED, E_NUMERIC, E_CANCELLED, E_TIMEOUT, E_NOTFOUND, E_TOOLARGE = range(10)
 STATUS_NAMES = {0: "OK", 1: "BGK_E_INVALID", 2: "BGK_E_NOMEM", 3: "BGK_E_CUDA", 4: "BGK_E_UNSUPPORTED",
-                5: "BGK_E_NUMERIC", 6: "BGK_E_CANCELLED", 7: "BGK_E_TIMEOUT", 8: "BGK_E_NOTFOUND"}
+                5: "BGK_E_NUMERIC", 6: "BGK_E_CANCELLED", 7: "BGK_E_TIMEOUT", 8: "BGK_E_NOTFOUND",
+                9: "BGK_E_TOOLARGE"}
 
 STORE = {"f32": 0, "f64": 1, "f16": 2, "bf16": 3}
 COMPUTE = {"f32": 0, "f64": 1}
@@ -135,6 +136,7 @@ def load(build_if_missing: bool = True):
         "bgk_server_drain": (I32, [VP, F64]),
         "bgk_server_fields": (I32, [VP, I64, P(F64), P(F64), P(F64)]),
         "bgk_server_get_stats": (I32, [VP, P(ServerStats)]),
+        "bgk_diagno_noalloc": (I32, [P(VP), I64, I32, I32, I32, P(F64)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -22,6 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = {
     "bgk_api.cu": ["-fmad=false"],
     "bgk_batch.cu": ["-fmad=false"],
+    "bgk_noalloc.cu": ["-fmad=false"],
     "bgk_inst_f32_f32.cu": ["-fmad=false"],
     "bgk_inst_f32_f64.cu": ["-fmad=false"],
     "bgk_inst_f64_f64.cu": ["-fmad=false"],

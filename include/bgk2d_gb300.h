@@ -44,6 +44,7 @@ extern "C" {
 #define BGK_E_CANCELLED 6    /* work cancelled by the host */
 #define BGK_E_TIMEOUT 7      /* a bounded wait ran out */
 #define BGK_E_NOTFOUND 8     /* unknown id */
+#define BGK_E_TOOLARGE 9     /* size beyond a fixed limit of the entry point */
 
 /* storage kind of the populations in HBM (SRC/precision.F90:13-47, `mystorage`) */
 #define BGK_STORE_F32 0   /* SINGLE / MIXED2 */
@@ -169,6 +170,23 @@ int bgk_footprint(bgk_handle *h, int64_t *device_bytes, int32_t *bytes_per_cell)
 int bgk_launch_count(bgk_handle *h, int64_t *launches);
 int bgk_last_error(bgk_handle *h, char *buf, size_t len);
 const char *bgk_version(void);
+
+/* diagno sums without any allocation.  No counterpart in the reference.
+ * For callers that cannot let the library allocate device memory: a Fortran OpenACC or
+ * OpenMP-offload build whose populations live in data regions owned by the compiler's runtime,
+ * or a program running under a fixed device-memory budget.  The caller passes device pointers
+ * to its own nine population arrays (reference layout and direction order, leading dimension
+ * ld >= lx+2, deviations f - w, float for BGK_STORE_F32 or double for BGK_STORE_F64) and a
+ * host array for out = <u>, <v>, <rho>, <|u|^2> (SRC/diagno.F90 per-cell arithmetic, FP64
+ * sums).  The partial sums go to one static device array of 128 KiB that every GPU loading the
+ * library holds until exit; lx*ly may be at most 16,777,216 (4096^2), larger domains return
+ * BGK_E_TOOLARGE.  Nothing is allocated: no cudaMalloc/cudaFree, no pools.  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress), so make that first
+ * call before any stream capture.  Runs on the legacy default stream and returns when the
+ * means are on the host; the caller makes sure the arrays are ready.  All calls share the
+ * array: calls that overlap on the GPU (from several host threads) race on it. */
+int bgk_diagno_noalloc(const void *const pops[9], int64_t ld, int32_t lx, int32_t ly, int32_t storage,
+                       double out[4]);
 
 /* ---------------------------------------------------------------------------------------------
  * Batches: many independent ping-pong cases of one (storage, compute) kind advanced together,
