@@ -68,11 +68,12 @@ template <> struct Store<double> {
     template <typename K> __device__ __forceinline__ static K getq(double v, int) { return (K)v; }
     template <typename K> __device__ __forceinline__ static double putq(K v, int) { return (double)v; }
 };
-// Stochastic rounding to a 16-bit kind with D dropped mantissa bits: round toward zero of
-// |x| + u ulp, u uniform in [0, 1), written as an integer add of r in [0, 2^D) to the FP32 bit
-// pattern followed by a round-toward-zero conversion.  E[result] = x, so updates smaller than
-// half an ulp are not lost on average (round-to-nearest would drop them); zero stays zero.
-__device__ __forceinline__ float sr_add(float x, uint32_t r) { return __int_as_float(__float_as_int(x) + (int)r); }
+// Stochastic rounding FP32 -> 16 bits with the conversion instruction's own random-bits operand
+// (`cvt.rs`, Blackwell): each value goes to one of its two neighbouring representable values,
+// with the probabilities that make the expected result equal to the input, so updates smaller
+// than half an ulp are not lost on average (round-to-nearest would drop them).  Zero stays zero.
+// The random bits come from a per-cell hash (vector stores) or a hash of the value's own bit
+// pattern (lone values).
 
 // per-cell random word: multiplicative hash of the cell index and a value that changes every step
 __device__ __forceinline__ uint32_t cell_hash(uint32_t idx, float v)
@@ -82,22 +83,26 @@ __device__ __forceinline__ uint32_t cell_hash(uint32_t idx, float v)
     return h * 0x85ebca77u;
 }
 
-// random bits for a lone value: multiplicative hash of its own bit pattern
-template <int D>
-__device__ __forceinline__ uint32_t self_bits(float x) { return (__float_as_uint(x) * 0x9e3779b1u) >> (32 - D); }
+// random word for a lone value: the well-mixed upper half of a multiplicative hash of its bit
+// pattern, in both halves of the word
+__device__ __forceinline__ uint32_t lone_bits(float x) { return __byte_perm(__float_as_uint(x) * 0x9e3779b1u, 0u, 0x3232); }
+
+// direction q's random word for the pair of cells whose words are lo, hi: a 32-bit window of the
+// 64-bit concatenation at a direction-dependent offset
+template <int q>
+__device__ __forceinline__ uint32_t pair_bits(uint32_t lo, uint32_t hi) { return __funnelshift_l(lo, hi, 3 * q + 2); }
 
 template <> struct Store<__half> {
     static constexpr int VEC = 8;
-    static constexpr int DROPPED = 13;  // FP32 -> FP16 mantissa bits
-    static constexpr int POS0 = 19;     // bit window of direction q in a cell's random word: POS0 - q
     __device__ __forceinline__ static float raw_get(__half v) { return __half2float(v); }
-    __device__ __forceinline__ static __half raw_put(float v) {
-        return __float2half_rz(sr_add(v, self_bits<DROPPED>(v)));
-    }
-    __device__ __forceinline__ static uint32_t pack2_rz(float lo, float hi) {
+    // lo in the low half, hi in the high half of the result
+    __device__ __forceinline__ static uint32_t pack2_rs(float lo, float hi, uint32_t rbits) {
         uint32_t r;
-        asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+        asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(r) : "f"(hi), "f"(lo), "r"(rbits));
         return r;
+    }
+    __device__ __forceinline__ static __half raw_put(float v) {
+        return __ushort_as_half((unsigned short)(pack2_rs(v, 0.0f, lone_bits(v)) & 0xffffu));
     }
     template <typename K, int q> __device__ __forceinline__ static K get(__half v) {
         return (K)(__half2float(v) * (1.0f / scale_of(q)));
@@ -112,16 +117,14 @@ template <> struct Store<__half> {
 };
 template <> struct Store<__nv_bfloat16> {
     static constexpr int VEC = 8;
-    static constexpr int DROPPED = 16;  // FP32 -> BF16 mantissa bits
-    static constexpr int POS0 = 16;
     __device__ __forceinline__ static float raw_get(__nv_bfloat16 v) { return __bfloat162float(v); }
-    __device__ __forceinline__ static __nv_bfloat16 raw_put(float v) {
-        return __float2bfloat16_rz(sr_add(v, self_bits<DROPPED>(v)));
-    }
-    __device__ __forceinline__ static uint32_t pack2_rz(float lo, float hi) {
+    __device__ __forceinline__ static uint32_t pack2_rs(float lo, float hi, uint32_t rbits) {
         uint32_t r;
-        asm("cvt.rz.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+        asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(r) : "f"(hi), "f"(lo), "r"(rbits));
         return r;
+    }
+    __device__ __forceinline__ static __nv_bfloat16 raw_put(float v) {
+        return __ushort_as_bfloat16((unsigned short)(pack2_rs(v, 0.0f, lone_bits(v)) & 0xffffu));
     }
     template <typename K, int q> __device__ __forceinline__ static K get(__nv_bfloat16 v) {
         return (K)(__bfloat162float(v) * (1.0f / scale_of(q)));

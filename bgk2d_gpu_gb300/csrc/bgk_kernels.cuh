@@ -325,23 +325,19 @@ template <typename S, typename K, int q, bool RAW, int N = vec_of<S>()>
 __device__ __forceinline__ void store_vec(S *p, const K (&v)[N], const uint32_t (&rh)[N])
 {
     if constexpr (RAW) {
-        // stochastic rounding: per-cell hashes `rh` (one 32-bit word per cell), a different
-        // 16-bit window per direction
-        constexpr int D = Store<S>::DROPPED, P = Store<S>::POS0 - q;
-        float w[N];
-#pragma unroll
-        for (int c = 0; c < N; ++c) w[c] = sr_add((float)v[c], (rh[c] >> P) & ((1u << D) - 1u));
+        // stochastic rounding of each pair of cells with a direction-dependent window of their
+        // two hash words `rh`
         if constexpr (N == 8) {
             uint4 u;
-            u.x = Store<S>::pack2_rz(w[0], w[1]);
-            u.y = Store<S>::pack2_rz(w[2], w[3]);
-            u.z = Store<S>::pack2_rz(w[4], w[5]);
-            u.w = Store<S>::pack2_rz(w[6], w[7]);
+            u.x = Store<S>::pack2_rs((float)v[0], (float)v[1], pair_bits<q>(rh[0], rh[1]));
+            u.y = Store<S>::pack2_rs((float)v[2], (float)v[3], pair_bits<q>(rh[2], rh[3]));
+            u.z = Store<S>::pack2_rs((float)v[4], (float)v[5], pair_bits<q>(rh[4], rh[5]));
+            u.w = Store<S>::pack2_rs((float)v[6], (float)v[7], pair_bits<q>(rh[6], rh[7]));
             *reinterpret_cast<uint4 *>(p) = u;
         } else {
             uint2 u;
-            u.x = Store<S>::pack2_rz(w[0], w[1]);
-            u.y = Store<S>::pack2_rz(w[2], w[3]);
+            u.x = Store<S>::pack2_rs((float)v[0], (float)v[1], pair_bits<q>(rh[0], rh[1]));
+            u.y = Store<S>::pack2_rs((float)v[2], (float)v[3], pair_bits<q>(rh[2], rh[3]));
             *reinterpret_cast<uint2 *>(p) = u;
         }
     } else {
@@ -706,9 +702,12 @@ __device__ __forceinline__ void aa_edge_push(const Lattice &L, S *base, int x, i
 
 // push VEC values of direction q to (x + c_q) in plane q; lanes at an edge (segment end or a
 // neighbour on the slow path) store the elements that cross into the neighbour's vector.
+// 16-bit kinds (RAW) round the shifted vector in pairs, as it is stored, with the lane's cell
+// hash words `rh`; lone elements at an edge use the lone-value rounding.
 template <typename S, typename K, int q, int W, bool RAW = false>
 __device__ __forceinline__ void push_vec(const Lattice &L, S *plane, int xv, int y, bool left_edge,
-                                         bool right_edge, const K (&g)[vec_of<S>()], bool store)
+                                         bool right_edge, const K (&g)[vec_of<S>()], bool store,
+                                         const uint32_t (&rh)[vec_of<S>()])
 {
     constexpr int VEC = vec_of<S>();
     constexpr int cx = cx_of(q), cy = cy_of(q);
@@ -717,6 +716,40 @@ __device__ __forceinline__ void push_vec(const Lattice &L, S *plane, int xv, int
         if constexpr (RAW) return Store<S>::raw_put((float)v);
         else return Store<S>::template put<K, q>(v);
     };
+    if constexpr (RAW) {
+        static_assert(VEC == 8, "16-bit vectors hold 8 elements");
+        K sh[VEC];  // the vector as stored at idx
+        if (cx == 0) {
+#pragma unroll
+            for (int c = 0; c < VEC; ++c) sh[c] = g[c];
+        } else if (cx == 1) {
+            sh[0] = shfl_up(g[VEC - 1], W);
+#pragma unroll
+            for (int c = 1; c < VEC; ++c) sh[c] = g[c - 1];
+        } else {
+#pragma unroll
+            for (int c = 0; c < VEC - 1; ++c) sh[c] = g[c + 1];
+            sh[VEC - 1] = shfl_down(g[0], W);
+        }
+        if (!store) return;
+        if (cx == 0 || (cx == 1 && !left_edge) || (cx == -1 && !right_edge)) {
+            uint4 u;
+            u.x = Store<S>::pack2_rs((float)sh[0], (float)sh[1], pair_bits<q>(rh[0], rh[1]));
+            u.y = Store<S>::pack2_rs((float)sh[2], (float)sh[3], pair_bits<q>(rh[2], rh[3]));
+            u.z = Store<S>::pack2_rs((float)sh[4], (float)sh[5], pair_bits<q>(rh[4], rh[5]));
+            u.w = Store<S>::pack2_rs((float)sh[6], (float)sh[7], pair_bits<q>(rh[6], rh[7]));
+            *reinterpret_cast<uint4 *>(plane + idx) = u;
+        } else if (cx == 1) {
+#pragma unroll
+            for (int c = 0; c < VEC - 1; ++c) plane[idx + 1 + c] = cvt(g[c]);
+        } else {
+#pragma unroll
+            for (int c = 1; c < VEC; ++c) plane[idx - 1 + c] = cvt(g[c]);
+        }
+        if (cx == 1 && right_edge) plane[idx + VEC] = cvt(g[VEC - 1]);
+        if (cx == -1 && left_edge) plane[idx - 1] = cvt(g[0]);
+        return;
+    }
     S s[VEC];
 #pragma unroll
     for (int c = 0; c < VEC; ++c) s[c] = cvt(g[c]);
@@ -798,15 +831,19 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ?
     relax_vec<S, K, RAW>(x, (K)L.omega, (K)L.fgrad, L.forced != 0);
     K (&g)[9][VEC] = x;
     const bool store = !slow;
-    push_vec<S, K, D01, W, RAW>(L, base + D01 * pe, xv, y, left_edge, right_edge, g[D01], store);
-    push_vec<S, K, D03, W, RAW>(L, base + D03 * pe, xv, y, left_edge, right_edge, g[D03], store);
-    push_vec<S, K, D05, W, RAW>(L, base + D05 * pe, xv, y, left_edge, right_edge, g[D05], store);
-    push_vec<S, K, D08, W, RAW>(L, base + D08 * pe, xv, y, left_edge, right_edge, g[D08], store);
-    push_vec<S, K, D10, W, RAW>(L, base + D10 * pe, xv, y, left_edge, right_edge, g[D10], store);
-    push_vec<S, K, D12, W, RAW>(L, base + D12 * pe, xv, y, left_edge, right_edge, g[D12], store);
-    push_vec<S, K, D14, W, RAW>(L, base + D14 * pe, xv, y, left_edge, right_edge, g[D14], store);
-    push_vec<S, K, D17, W, RAW>(L, base + D17 * pe, xv, y, left_edge, right_edge, g[D17], store);
-    push_vec<S, K, D19, W, RAW>(L, base + D19 * pe, xv, y, left_edge, right_edge, g[D19], store);
+    uint32_t rh[VEC];
+    const uint32_t me = (uint32_t)cell_index<S>(L, xv, y);
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) rh[c] = RAW ? cell_hash(me + c, (float)g[D19][c]) : 0u;
+    push_vec<S, K, D01, W, RAW>(L, base + D01 * pe, xv, y, left_edge, right_edge, g[D01], store, rh);
+    push_vec<S, K, D03, W, RAW>(L, base + D03 * pe, xv, y, left_edge, right_edge, g[D03], store, rh);
+    push_vec<S, K, D05, W, RAW>(L, base + D05 * pe, xv, y, left_edge, right_edge, g[D05], store, rh);
+    push_vec<S, K, D08, W, RAW>(L, base + D08 * pe, xv, y, left_edge, right_edge, g[D08], store, rh);
+    push_vec<S, K, D10, W, RAW>(L, base + D10 * pe, xv, y, left_edge, right_edge, g[D10], store, rh);
+    push_vec<S, K, D12, W, RAW>(L, base + D12 * pe, xv, y, left_edge, right_edge, g[D12], store, rh);
+    push_vec<S, K, D14, W, RAW>(L, base + D14 * pe, xv, y, left_edge, right_edge, g[D14], store, rh);
+    push_vec<S, K, D17, W, RAW>(L, base + D17 * pe, xv, y, left_edge, right_edge, g[D17], store, rh);
+    push_vec<S, K, D19, W, RAW>(L, base + D19 * pe, xv, y, left_edge, right_edge, g[D19], store, rh);
     if (left_cell) aa_edge_push<S, K, HAS_OBS, RAW, 0, true>(L, base, xv, y, g);
     if (right_cell) aa_edge_push<S, K, HAS_OBS, RAW, VEC - 1, false>(L, base, xv + VEC - 1, y, g);
     if (!active || !slow) return;
