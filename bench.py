@@ -166,7 +166,8 @@ def run_reference(args):
 
 
 def run_profile(args):
-    """Small case for ncu captures: warm-up steps, then `--steps` steps, nothing printed but a tag."""
+    """Small case for ncu captures (or a quick timing of one tile shape): warm-up steps, then
+    `--steps` device-timed steps; prints one tag line with the time per step."""
     import bgk2d_gpu_gb300 as bgk
     scheme, storage = args.profile.split("_")
     compute = "f64" if storage == "f64" else "f32"
@@ -175,9 +176,11 @@ def run_profile(args):
         if args.tile >= 0:
             s.set_tile(args.tile)
         s.step(args.warmup)
-        s.step(args.steps)
         s.sync()
-    print(f"profile run {args.profile} {args.size}^2 tile={args.tile} warmup={args.warmup} steps={args.steps}")
+        ms = s.step_timed(args.steps)
+    per = ms / args.steps
+    print(f"profile run {args.profile} {args.size}^2 tile={args.tile} warmup={args.warmup} steps={args.steps} "
+          f"ms/step={per:.4f} GLUPS={args.size * args.size / (per * 1e-3) / 1e9:.2f}")
     return 0
 
 
@@ -438,7 +441,8 @@ def main():
                        "parallelism": f"{world} independent cavities" if world > 1 else "single domain"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": kt, "peak_kind": peak_kind,
-                         "kernel": "bgk::pp_kernel<float,float,...> (tile config %d)" % tile_cfg,
+                         "kernel": ("bgk::pp_staged_kernel<float,float,...> (tile config %d)" if tile_cfg >= 6 else
+                                    "bgk::pp_kernel<float,float,...> (tile config %d)") % tile_cfg,
                          "bytes_per_cell": 72},
             "e2e": e2e,
             "gpu_launches": launches,

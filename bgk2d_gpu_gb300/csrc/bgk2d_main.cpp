@@ -7,8 +7,10 @@
 // drag.lift.dat, save.XXXXXXXX.bin checkpoints (Fortran unformatted sequential records, as
 // SRC/save_raw.F90) and bgk.perf.  VTK output is not produced.
 //
-//   bgk2d_gb300 [--input bgk.input] [--case LDC|TGV|POF|VKS|COU] [--prec single|double|mixed2|f16|bf16]
-//               [--scheme pingpong|aa] [--dir OUTDIR]
+//   bgk2d_gb300 [--input bgk.input] [--case LDC|TGV|POF|VKS|COU|BFS] [--prec single|double|mixed2|f16|bf16]
+//               [--scheme pingpong|aa] [--les 0|1] [--dir OUTDIR]
+// `--les 1` stands for the reference's -DLES build (Smagorinsky constant from the namelist key cteS).
+#include <cctype>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -74,6 +76,7 @@ std::map<std::string, std::string> read_namelist(const std::string &path)
         if (v.empty() && i + 1 < toks.size()) v = toks[++i];
         for (char &c : v)
             if (c == 'd' || c == 'D') c = 'e';
+        for (char &c : k) c = (char)std::tolower((unsigned char)c);  // namelist names ignore case
         kv[k] = v;
     }
     return kv;
@@ -168,7 +171,7 @@ int die(const char *what, int rc)
 
 int main(int argc, char **argv)
 {
-    std::string input = "bgk.input", tcase = "LDC", prec = "single", scheme = "pingpong", dir = ".";
+    std::string input = "bgk.input", tcase = "LDC", prec = "single", scheme = "pingpong", dir = ".", les = "0";
     for (int i = 1; i + 1 < argc; i += 2) {
         std::string k = argv[i], v = argv[i + 1];
         if (k == "--input") input = v;
@@ -176,6 +179,7 @@ int main(int argc, char **argv)
         else if (k == "--prec") prec = v;
         else if (k == "--scheme") scheme = v;
         else if (k == "--dir") dir = v;
+        else if (k == "--les") les = v;
     }
     auto kv = read_namelist(input);
     if (kv.empty()) { std::fprintf(stderr, "bgk2d_gb300: no &parameters namelist in %s\n", input.c_str()); return 1; }
@@ -195,13 +199,15 @@ int main(int argc, char **argv)
     d.svisc = getd("svisc", 0.1);
     d.u0 = getd("u0", 0.1);
     d.radius = geti("radius", 16);
+    d.les = les == "1";
+    d.cte_s = getd("ctes", 0.1);
     d.scheme = scheme == "aa" ? BGK_SCHEME_AA : BGK_SCHEME_PINGPONG;
     if (prec == "double") { d.storage = BGK_STORE_F64; d.compute = BGK_COMPUTE_F64; }
     else if (prec == "mixed2") { d.storage = BGK_STORE_F32; d.compute = BGK_COMPUTE_F64; }
     else if (prec == "f16") d.storage = BGK_STORE_F16;
     else if (prec == "bf16") d.storage = BGK_STORE_BF16;
     const std::map<std::string, int> cases = {{"LDC", BGK_CASE_LDC}, {"TGV", BGK_CASE_TGV}, {"POF", BGK_CASE_POF},
-                                              {"VKS", BGK_CASE_VKS}, {"COU", BGK_CASE_COU}};
+                                              {"VKS", BGK_CASE_VKS}, {"COU", BGK_CASE_COU}, {"BFS", BGK_CASE_BFS}};
     if (!cases.count(tcase)) { std::fprintf(stderr, "bgk2d_gb300: unknown case %s\n", tcase.c_str()); return 1; }
     d.tcase = cases.at(tcase);
     if (d.tcase == BGK_CASE_TGV) d.init_v = BGK_INIT_TGV_REF;

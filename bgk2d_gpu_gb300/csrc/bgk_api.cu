@@ -157,6 +157,10 @@ int upload_impl(bgk_handle *h, const void *const pops[9], int64_t ld)
 int launch_step(bgk_handle *h)
 {
     if (h->L.scheme == BGK_SCHEME_PINGPONG) {
+        if (h->cs.bfs) {  // the step's boundary routine writes the source buffer's ghosts first
+            CK(h, h->T.bcond_step(h->L, h->cur, h->cs.stepx, h->cs.stepy, h->st));
+            h->launches++;
+        }
         CK(h, h->T.step(STEP_PP, h->L, h->cur, h->cs.has_obs, h->cfg, h->st));
         h->cur ^= 1;
     } else {
@@ -208,12 +212,26 @@ int steps_impl(bgk_handle *h, int32_t n)
         const int slot = h->L.scheme == BGK_SCHEME_PINGPONG ? h->cur : 0;
         if (!h->graph[slot] && (rc = build_graph(h, slot))) return rc;
         CK(h, cudaGraphLaunch(h->graph[slot], h->st));
-        h->launches += h->graph_steps;
+        h->launches += (int64_t)h->graph_steps * (h->cs.bfs ? 2 : 1);
         h->itime += h->graph_steps;
         n -= h->graph_steps;
     }
     while (n-- > 0)
         if ((rc = launch_step(h))) return rc;
+    return BGK_OK;
+}
+
+// Status word of the step kernels, read once the stream is idle: non-zero when a bounded wait
+// inside a kernel ran out, which leaves the state undefined (the handle stays failed).
+int check_status(bgk_handle *h)
+{
+    uint32_t s = 0;
+    CK(h, cudaMemcpyAsync(&s, h->d_status, sizeof(s), cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    if (s != 0) {
+        h->sticky = BGK_E_TIMEOUT;
+        return fail(h, BGK_E_TIMEOUT, "step kernel: a wait for staged rows ran out (status 0x%x)", s);
+    }
     return BGK_OK;
 }
 
@@ -223,7 +241,7 @@ int reduce4(bgk_handle *h, double out[4])
     h->launches++;
     CK(h, cudaMemcpyAsync(out, h->d_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
     CK(h, cudaStreamSynchronize(h->st));
-    return BGK_OK;
+    return check_status(h);
 }
 
 void release(bgk_handle *h)
@@ -232,7 +250,7 @@ void release(bgk_handle *h)
         if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
     if (h->st) {
         for (void *p : {(void *)h->d_planes, (void *)h->d_mask, (void *)h->d_inflow, (void *)h->d_partial,
-                        (void *)h->d_out, (void *)h->d_uprev, (void *)h->d_vprev, h->d_stage})
+                        (void *)h->d_out, (void *)h->d_status, (void *)h->d_uprev, (void *)h->d_vprev, h->d_stage})
             dfree(h, p);
         cudaStreamSynchronize(h->st);
     }
@@ -265,6 +283,7 @@ int bgk_default_desc(bgk_case_desc *d)
     d->obs_icoord = -1;
     d->obs_jcoord = -1;
     d->tgv_u0 = 0.02;
+    d->cte_s = 0.1;
     return BGK_OK;
 }
 
@@ -338,6 +357,8 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
     L.omega = h->cs.omega;
     L.fgrad = h->cs.fgrad;
     L.forced = h->cs.forced;
+    L.les = h->cs.les;
+    L.cte_s = h->cs.cte_s;
 
     // inflow table
     if (dalloc(h, &h->d_inflow, h->cs.inflow.size() * sizeof(double)) != cudaSuccess) {
@@ -370,9 +391,12 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
     // reduction scratch
     h->nb_red = 4 * 152;
     if (dalloc(h, &h->d_partial, (size_t)h->nb_red * 4 * sizeof(double)) != cudaSuccess ||
-        dalloc(h, &h->d_out, 4 * sizeof(double)) != cudaSuccess) {
+        dalloc(h, &h->d_out, 4 * sizeof(double)) != cudaSuccess ||
+        dalloc(h, &h->d_status, sizeof(uint32_t)) != cudaSuccess) {
         cudaGetLastError(); release(h); delete h; return BGK_E_NOMEM;
     }
+    cudaMemsetAsync(h->d_status, 0, sizeof(uint32_t), h->st);
+    L.status = h->d_status;
     h->cfg = default_cfg(nvec);
 
     // initial state (SRC/initialize.F90:85-125: init(init_v))
@@ -484,14 +508,14 @@ int bgk_step_timed(bgk_handle *h, int32_t nsteps, float *ms)
     CK(h, cudaEventRecord(h->ev1, h->st));
     CK(h, cudaEventSynchronize(h->ev1));
     CK(h, cudaEventElapsedTime(ms, h->ev0, h->ev1));
-    return BGK_OK;
+    return check_status(h);
 }
 
 int bgk_sync(bgk_handle *h)
 {
     CHECK_HANDLE(h);
     CK(h, cudaStreamSynchronize(h->st));
-    return BGK_OK;
+    return check_status(h);
 }
 
 int bgk_diagno(bgk_handle *h, int32_t fluid_only, double out[4])
@@ -617,7 +641,8 @@ int bgk_footprint(bgk_handle *h, int64_t *device_bytes, int32_t *bytes_per_cell)
 int bgk_set_tile(bgk_handle *h, int32_t tile_cfg)
 {
     CHECK_HANDLE(h);
-    if (tile_cfg < 0 || tile_cfg >= NUM_CFG) return fail(h, BGK_E_INVALID, "tile configuration %d", tile_cfg);
+    const int ncfg = h->L.scheme == BGK_SCHEME_PINGPONG ? NUM_STEP_CFG : NUM_CFG;
+    if (tile_cfg < 0 || tile_cfg >= ncfg) return fail(h, BGK_E_INVALID, "tile configuration %d", tile_cfg);
     if (tile_cfg != h->cfg) {
         for (int i = 0; i < 2; ++i)
             if (h->graph[i]) { cudaGraphExecDestroy(h->graph[i]); h->graph[i] = nullptr; }
@@ -635,7 +660,8 @@ int bgk_tune(bgk_handle *h, int32_t trial_steps, int32_t *tile_cfg, int32_t *ste
     float best = 1e30f;
     int best_cfg = h->cfg, rc;
     int64_t run = 0;
-    for (int c = 0; c < NUM_CFG; ++c) {
+    const int ncfg = h->L.scheme == BGK_SCHEME_PINGPONG ? NUM_STEP_CFG : NUM_CFG;
+    for (int c = 0; c < ncfg; ++c) {
         if ((rc = bgk_set_tile(h, c))) return rc;
         for (int s = 0; s < 2; ++s)
             if ((rc = launch_step(h))) return rc;

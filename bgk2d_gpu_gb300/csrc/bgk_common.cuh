@@ -36,7 +36,8 @@ __host__ __device__ constexpr int opp_of(int q) {
 }
 
 enum Face { XLO = 0, XHI = 1, YLO = 2, YHI = 3 };
-enum FaceKind { FK_WALL = 0, FK_PERIODIC = 1, FK_INFLOW = 2, FK_OUTFLOW_EQ = 3, FK_OUTFLOW_ZG = 4 };
+enum FaceKind { FK_WALL = 0, FK_PERIODIC = 1, FK_INFLOW = 2, FK_OUTFLOW_EQ = 3, FK_OUTFLOW_ZG = 4,
+                FK_STORED = 5 };  // STORED: ghost values written into the source buffer before the step
 
 // 16-bit storage keeps (f_q - w_q) * s_q with a power-of-two s_q close to 1/w_q, so the
 // scaling is exact and only the 16-bit rounding loses information.
@@ -151,10 +152,13 @@ struct Lattice {
     double wt[4][9];         // wall term added to the bounced population, per face and direction
     double omega, fgrad;     // relaxation rate and body-force gradient (compute kind)
     int32_t forced;          // 1 when the x body force fgrad*rho is applied (CHANNEL)
+    int32_t les;             // 1: Smagorinsky eddy viscosity in the collision (-DLES)
+    double cte_s;            // Smagorinsky constant cteS (compute kind)
     const double *inflow;    // [3][ly+2] equilibrium deviations of 01,03,05 at the x_lo inflow
     const uint32_t *mask;    // obstacle bits, row y (0..ly+1) at mask + y*mask_pitch, bit x
     int32_t mask_pitch;      // 32-bit words per mask row
     int32_t ob_x0, ob_x1, ob_y0, ob_y1;  // cells whose pull may touch an obstacle
+    uint32_t *status;        // device word set by a kernel whose bounded wait ran out (0: fine)
 };
 
 template <typename S> __host__ __device__ constexpr int vec_of() { return 16 / (int)sizeof(S); }

@@ -27,6 +27,7 @@ struct bgk_handle {
     double *d_inflow = nullptr;
     double *d_partial = nullptr;
     double *d_out = nullptr;
+    uint32_t *d_status = nullptr;  // kernel-side failure word (Lattice::status)
     int nb_red = 0;
     double *d_uprev = nullptr, *d_vprev = nullptr;
     int64_t res_itime = -1;

@@ -2,7 +2,10 @@
 // Each bgk_inst_*.cu translation unit includes this once, so the pairs compile in parallel.
 #pragma once
 
+#include <algorithm>
+
 #include "bgk_aux.cuh"
+#include "bgk_staged.cuh"
 #include "bgk_table.h"
 
 namespace bgk {
@@ -27,9 +30,56 @@ cudaError_t step_cfg(int kind, const Lattice &L, int parity, cudaStream_t st)
     return cudaGetLastError();
 }
 
+// ping-pong step through shared-memory staging: one wave of blocks, each a band of T*N columns
+// and a stripe of rows
+template <typename S, typename K, int T, int STAGES, bool OBS>
+cudaError_t step_staged(const Lattice &L, int parity, cudaStream_t st)
+{
+    constexpr int N = vec_of<S>() / 2;
+    constexpr size_t smem = staged_smem_bytes<S, T, N, STAGES>();
+    auto kern = pp_staged_kernel<S, K, T, N, STAGES, OBS>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, occ = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, T, smem)) != cudaSuccess) return e;
+    const int bands = (L.lx + T * N - 1) / (T * N);
+    int stripes = std::max(1, std::max(1, occ) * sms / bands);
+    stripes = std::min(stripes, L.ly);
+    const int rows = (L.ly + stripes - 1) / stripes;
+    stripes = (L.ly + rows - 1) / rows;
+    kern<<<dim3((unsigned)bands, (unsigned)stripes), T, smem, st>>>(L, parity, rows);
+    return cudaGetLastError();
+}
+
+// steps with the Smagorinsky collision: their own instantiation (128 x 1 threads, a whole vector
+// per thread), so that the eddy-viscosity code takes no registers from the plain kernels
+template <typename S, typename K, bool OBS>
+cudaError_t step_les(int kind, const Lattice &L, int parity, cudaStream_t st)
+{
+    const dim3 block(128, 1);
+    if (kind == STEP_PP) {
+        constexpr int N = vec_of<S>();
+        const int nv = (L.lx + N - 1) / N;
+        pp_kernel<S, K, 128, 1, OBS, N, true><<<dim3((unsigned)((nv + 127) / 128), (unsigned)L.ly), block, 0, st>>>(L, parity);
+    } else {
+        const dim3 grid((unsigned)((L.nvec + 127) / 128), (unsigned)L.ly);
+        if (kind == STEP_AA_P) aa_p_kernel<S, K, 128, 1, OBS, true><<<grid, block, 0, st>>>(L);
+        else aa_l_kernel<S, K, 128, 1, OBS, true><<<grid, block, 0, st>>>(L);
+    }
+    return cudaGetLastError();
+}
+
 template <typename S, typename K, bool OBS>
 cudaError_t step_obs(int kind, const Lattice &L, int parity, int cfg, cudaStream_t st)
 {
+    if (L.les) return step_les<S, K, OBS>(kind, L, parity, st);
+    if (kind == STEP_PP && cfg >= NUM_CFG) {
+        if (cfg == 6) return step_staged<S, K, 128, 3, OBS>(L, parity, st);
+        if (cfg == 7) return step_staged<S, K, 128, 4, OBS>(L, parity, st);
+        return step_staged<S, K, 256, 3, OBS>(L, parity, st);
+    }
     switch (cfg) {
     case 0: return step_cfg<S, K, 32, 4, OBS, 1>(kind, L, parity, st);
     case 1: return step_cfg<S, K, 64, 2, OBS, 1>(kind, L, parity, st);
@@ -71,6 +121,13 @@ template <typename S, typename K>
 cudaError_t fill_outflow(const Lattice &L, cudaStream_t st)
 {
     aa_fill_outflow_kernel<S, K><<<(L.ly + 127) / 128, 128, 0, st>>>(L);
+    return cudaGetLastError();
+}
+
+template <typename S, typename K>
+cudaError_t bcond_step(const Lattice &L, int cur, int stepx, int stepy, cudaStream_t st)
+{
+    bfs_bcond_kernel<S, K><<<1, 1024, 0, st>>>(L, cur, stepx, stepy);
     return cudaGetLastError();
 }
 
@@ -151,6 +208,7 @@ KernelTable make_table()
     t.scatter = &scatter<S>;
     t.gather = &gather<S, K>;
     t.fill_outflow = &fill_outflow<S, K>;
+    t.bcond_step = &bcond_step<S, K>;
     t.init_tgv = &init_tgv<S>;
     t.diagno = &diagno<S, K>;
     t.residual = &residual<S, K>;

@@ -26,8 +26,24 @@ namespace bgk {
 // ---------------------------------------------------------------------------------------------
 // collision: SRC/col_MC.F90:128-176 (equilibrium) and :285-293 (relaxation + body force)
 // ---------------------------------------------------------------------------------------------
+// Smagorinsky eddy viscosity (SRC/col_MC.F90:178-248): the relaxation rate from the
+// non-equilibrium momentum flux n_q = x_q - e_q; the molecular rate omega1 equals omega
+// (hencol.F90:30-31).
 template <typename K>
-__device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced)
+__device__ __forceinline__ K les_omega(K n01, K n03, K n05, K n08, K n10, K n12, K n14, K n17, K omega1, K cte_s)
+{
+    const K uno = (K)1;
+    const K pxx = ((((n01 + n03) + n05) + n10) + n12) + n14;
+    const K pyy = ((((n01 + n03) + n08) + n10) + n12) + n17;
+    const K pxy = (((-n01) + n03) + n10) - n12;
+    const K ptotal = sqrt(((pxx * pxx) + (((K)2 * pxy) * pxy)) + (pyy * pyy));
+    const K r = uno / omega1;
+    const K ts = uno / ((K)2 * omega1) + sqrt((((K)18 * (cte_s * cte_s)) * ptotal) + (r * r)) / (K)2;
+    return uno / ts;
+}
+
+template <typename K, bool LES = false>
+__device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced, K cte_s = (K)0)
 {
     const K uno = (K)1, cte1 = (K)1, cte0 = uno - cte1;
     const K tre = (K)3, qf = (K)1.5, rf = (K)3;
@@ -64,6 +80,8 @@ __device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced
     K e14 = rp1 * (-vx + qx) + cte1 * (rp1 - p1);
     K e17 = rp1 * (-vy + qy) + cte1 * (rp1 - p1);
     K e19 = rp0 * (q0) + cte1 * (rp0 - p0);
+    if constexpr (LES) omega = les_omega<K>(x01 - e01, x03 - e03, x05 - e05, x08 - e08, x10 - e10, x12 - e12, x14 - e14,
+                                  x17 - e17, omega, cte_s);
     K fx = (K)0, fy = (K)0;
     if (forced) fx = fgrad * rho;
     x[0] = (x01 - omega * (x01 - e01)) + (fx - fy);
@@ -115,10 +133,12 @@ __device__ __forceinline__ void collide_scaled(float (&D)[9], float omega, float
 }
 
 // collision on unscaled deviations in compute kind K, for any storage kind
-template <typename S, typename K>
-__device__ __forceinline__ void collide_stored(K (&v)[9], K omega, K fgrad, bool forced)
+template <typename S, typename K, bool LES = false>
+__device__ __forceinline__ void collide_stored(K (&v)[9], K omega, K fgrad, bool forced, K cte_s)
 {
-    if constexpr (Is16<S>::value) {
+    if constexpr (Is16<S>::value && LES) {
+        collide<K, true>(v, omega, fgrad, forced, cte_s);
+    } else if constexpr (Is16<S>::value) {
         float D[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) D[q] = (float)v[q] * scale_of(q);  // exact: powers of two
@@ -126,7 +146,7 @@ __device__ __forceinline__ void collide_stored(K (&v)[9], K omega, K fgrad, bool
 #pragma unroll
         for (int q = 0; q < 9; ++q) v[q] = (K)(D[q] * (1.0f / scale_of(q)));
     } else {
-        collide<K>(v, omega, fgrad, forced);
+        collide<K, LES>(v, omega, fgrad, forced, cte_s);
     }
 }
 
@@ -273,7 +293,9 @@ __device__ __forceinline__ K pull_rule(const Lattice &L, int q, int x, int y, Pl
     const int oq = opp_of(q);
     if (sy < 1 || sy > m) {
         const int f = sy < 1 ? YLO : YHI;
-        if (L.faces[f] == FK_PERIODIC) {
+        if (L.faces[f] == FK_STORED) {
+            return plane_at(q, sx, sy);
+        } else if (L.faces[f] == FK_PERIODIC) {
             sy = (sy < 1) ? m : 1;
         } else {
             K v = own(oq);
@@ -284,7 +306,9 @@ __device__ __forceinline__ K pull_rule(const Lattice &L, int q, int x, int y, Pl
     if (sx < 1 || sx > l) {
         const int f = sx < 1 ? XLO : XHI;
         const int kind = L.faces[f];
-        if (kind == FK_PERIODIC) {
+        if (kind == FK_STORED) {
+            return plane_at(q, sx, sy);
+        } else if (kind == FK_PERIODIC) {
             sx = (sx < 1) ? l : 1;
         } else if (kind == FK_WALL) {
             K v = own(oq);
@@ -305,16 +329,27 @@ __device__ __forceinline__ K pull_rule(const Lattice &L, int q, int x, int y, Pl
 }
 
 // relax N cells in place: x[q][c] holds direction q of cell c (scaled 16-bit units when RAW)
-template <typename S, typename K, bool RAW, int N = vec_of<S>()>
-__device__ __forceinline__ void relax_vec(K (&x)[9][N], K omega, K fgrad, bool forced)
+template <typename S, typename K, bool RAW, int N = vec_of<S>(), bool LES = false>
+__device__ __forceinline__ void relax_vec(K (&x)[9][N], K omega, K fgrad, bool forced, K cte_s)
 {
 #pragma unroll
     for (int c = 0; c < N; ++c) {
         K v[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) v[q] = x[q][c];
-        if constexpr (RAW) collide_scaled(v, (float)omega, (float)fgrad, forced);
-        else collide<K>(v, omega, fgrad, forced);
+        if constexpr (RAW) {
+            if constexpr (LES) {  // eddy viscosity on unscaled deviations, as the 32/64-bit kinds
+#pragma unroll
+                for (int q = 0; q < 9; ++q) v[q] *= (1.0f / scale_of(q));
+                collide<K, true>(v, omega, fgrad, forced, cte_s);
+#pragma unroll
+                for (int q = 0; q < 9; ++q) v[q] *= scale_of(q);
+            } else {
+                collide_scaled(v, (float)omega, (float)fgrad, forced);
+            }
+        } else {
+            collide<K, LES>(v, omega, fgrad, forced, cte_s);
+        }
 #pragma unroll
         for (int q = 0; q < 9; ++q) x[q][c] = v[q];
     }
@@ -368,7 +403,7 @@ __device__ __forceinline__ bool needs_rule(const Lattice &L, int x, int y)
 }
 
 // one cell with the boundary rules: reads the source buffer only, writes the destination
-template <typename S, typename K, bool HAS_OBS>
+template <typename S, typename K, bool HAS_OBS, bool LES = false>
 __device__ void pp_cell_slow(const Lattice &L, const S *src, S *dst, int x, int y)
 {
     const int64_t pe = L.plane_elems;
@@ -388,7 +423,7 @@ __device__ void pp_cell_slow(const Lattice &L, const S *src, S *dst, int x, int 
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) v[q] = pull_rule<S, K, HAS_OBS>(L, q, x, y, plane_at, own, ghost_xhi);
     v[8] = ldq<S, K>(src + D19 * pe, me, D19);
-    collide_stored<S, K>(v, (K)L.omega, (K)L.fgrad, L.forced != 0);
+    collide_stored<S, K, LES>(v, (K)L.omega, (K)L.fgrad, L.forced != 0, (K)L.cte_s);
 #pragma unroll
     for (int q = 0; q < 9; ++q) dst[q * pe + me] = Store<S>::template putq<K>(v[q], q);
 }
@@ -425,7 +460,7 @@ __device__ __forceinline__ void pp_edge_pull(const Lattice &L, const S *src, int
 // vector path; cells whose inputs come from the boundary rules are then recomputed one by one
 // and overwritten (the source buffer is read-only during the step, so the recompute sees the
 // same inputs).
-template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N = vec_of<S>()>
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N = vec_of<S>(), bool LES = false>
 __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const int by, const int parity)
 {
     constexpr int W = TXV < 32 ? TXV : 32;
@@ -463,7 +498,7 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
     if (left_cell) pp_edge_pull<S, K, HAS_OBS, RAW, 0, true, N>(L, src, xv, y, x);
     if (right_cell) pp_edge_pull<S, K, HAS_OBS, RAW, N - 1, false, N>(L, src, xv + N - 1, y, x);
 
-    relax_vec<S, K, RAW, N>(x, (K)L.omega, (K)L.fgrad, L.forced != 0);
+    relax_vec<S, K, RAW, N, LES>(x, (K)L.omega, (K)L.fgrad, L.forced != 0, (K)L.cte_s);
     const int64_t me = cell_index<S>(L, xv, y);
     uint32_t rh[N];
 #pragma unroll
@@ -484,14 +519,14 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
         const int xe = min(xv + N - 1, L.lx);
 #pragma unroll 1
         for (int xc = xv; xc <= xe; ++xc)
-            if (needs_rule<HAS_OBS>(L, xc, y)) pp_cell_slow<S, K, HAS_OBS>(L, src, dst, xc, y);
+            if (needs_rule<HAS_OBS>(L, xc, y)) pp_cell_slow<S, K, HAS_OBS, LES>(L, src, dst, xc, y);
     }
 }
 
-template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N>
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N, bool LES = false>
 __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 || (sizeof(S) == 4 && N == 4)) ? 8 : (sizeof(S) == 2 ? 4 : 1)) pp_kernel(const Lattice L, const int parity)
 {
-    pp_tile<S, K, TXV, TY, HAS_OBS, N>(L, blockIdx.x, blockIdx.y, parity);
+    pp_tile<S, K, TXV, TY, HAS_OBS, N, LES>(L, blockIdx.x, blockIdx.y, parity);
 }
 
 // Persistent ping-pong step over many lattices.  The work list holds (lattice, tile x, tile y)
@@ -631,7 +666,7 @@ __device__ __forceinline__ void aa_outflow_ghost(const Lattice &L, S *base, int 
     }
 }
 
-template <typename S, typename K, bool HAS_OBS>
+template <typename S, typename K, bool HAS_OBS, bool LES = false>
 __device__ void aa_p_cell_slow(const Lattice &L, S *base, int x, int y)
 {
     const int64_t pe = L.plane_elems;
@@ -650,7 +685,7 @@ __device__ void aa_p_cell_slow(const Lattice &L, S *base, int x, int y)
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) v[q] = pull_rule<S, K, HAS_OBS>(L, q, x, y, plane_at, own, ghost_xhi);
     v[8] = ldq<S, K>(base + D19 * pe, me, D19);
-    collide_stored<S, K>(v, (K)L.omega, (K)L.fgrad, L.forced != 0);
+    collide_stored<S, K, LES>(v, (K)L.omega, (K)L.fgrad, L.forced != 0, (K)L.cte_s);
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) aa_push_rule<S, K, HAS_OBS>(L, base, q, x, y, v[q]);
     base[D19 * pe + me] = Store<S>::template putq<K>(v[8], D19);
@@ -748,45 +783,45 @@ __device__ __forceinline__ void push_vec(const Lattice &L, S *plane, int xv, int
         }
         if (cx == 1 && right_edge) plane[idx + VEC] = cvt(g[VEC - 1]);
         if (cx == -1 && left_edge) plane[idx - 1] = cvt(g[0]);
-        return;
-    }
-    S s[VEC];
-#pragma unroll
-    for (int c = 0; c < VEC; ++c) s[c] = cvt(g[c]);
-    if (cx == 0) {
-        if (store) stv<S>(plane + idx, s);
-    } else if (cx == 1) {
-        K fl = shfl_up(g[VEC - 1], W);
-        if (!store) return;
-        if (!left_edge) {
-            S v[VEC];
-            v[0] = cvt(fl);
-#pragma unroll
-            for (int c = 1; c < VEC; ++c) v[c] = s[c - 1];
-            stv<S>(plane + idx, v);
-        } else {
-#pragma unroll
-            for (int c = 0; c < VEC - 1; ++c) plane[idx + 1 + c] = s[c];
-        }
-        if (right_edge) plane[idx + VEC] = s[VEC - 1];
     } else {
-        K fr = shfl_down(g[0], W);
-        if (!store) return;
-        if (!right_edge) {
-            S v[VEC];
+        S s[VEC];
 #pragma unroll
-            for (int c = 0; c < VEC - 1; ++c) v[c] = s[c + 1];
-            v[VEC - 1] = cvt(fr);
-            stv<S>(plane + idx, v);
+        for (int c = 0; c < VEC; ++c) s[c] = cvt(g[c]);
+        if (cx == 0) {
+            if (store) stv<S>(plane + idx, s);
+        } else if (cx == 1) {
+            K fl = shfl_up(g[VEC - 1], W);
+            if (!store) return;
+            if (!left_edge) {
+                S v[VEC];
+                v[0] = cvt(fl);
+#pragma unroll
+                for (int c = 1; c < VEC; ++c) v[c] = s[c - 1];
+                stv<S>(plane + idx, v);
+            } else {
+#pragma unroll
+                for (int c = 0; c < VEC - 1; ++c) plane[idx + 1 + c] = s[c];
+            }
+            if (right_edge) plane[idx + VEC] = s[VEC - 1];
         } else {
+            K fr = shfl_down(g[0], W);
+            if (!store) return;
+            if (!right_edge) {
+                S v[VEC];
 #pragma unroll
-            for (int c = 1; c < VEC; ++c) plane[idx - 1 + c] = s[c];
+                for (int c = 0; c < VEC - 1; ++c) v[c] = s[c + 1];
+                v[VEC - 1] = cvt(fr);
+                stv<S>(plane + idx, v);
+            } else {
+#pragma unroll
+                for (int c = 1; c < VEC; ++c) plane[idx - 1 + c] = s[c];
+            }
+            if (left_edge) plane[idx - 1] = s[0];
         }
-        if (left_edge) plane[idx - 1] = s[0];
     }
 }
 
-template <typename S, typename K, int TXV, int TY, bool HAS_OBS>
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS, bool LES = false>
 __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ? 4 : 1) aa_p_kernel(const Lattice L)
 {
     constexpr int VEC = vec_of<S>();
@@ -828,7 +863,7 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ?
     const bool left_edge = (tx % W) == 0 || left_slow;
     const bool right_edge = (tx % W) == W - 1 || right_slow;
 
-    relax_vec<S, K, RAW>(x, (K)L.omega, (K)L.fgrad, L.forced != 0);
+    relax_vec<S, K, RAW, VEC, LES>(x, (K)L.omega, (K)L.fgrad, L.forced != 0, (K)L.cte_s);
     K (&g)[9][VEC] = x;
     const bool store = !slow;
     uint32_t rh[VEC];
@@ -849,11 +884,11 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ?
     if (!active || !slow) return;
     const int xe = min(xv + VEC - 1, L.lx);
 #pragma unroll 1
-    for (int xc = xv; xc <= xe; ++xc) aa_p_cell_slow<S, K, HAS_OBS>(L, base, xc, y);
+    for (int xc = xv; xc <= xe; ++xc) aa_p_cell_slow<S, K, HAS_OBS, LES>(L, base, xc, y);
 }
 
 // L step: local collision, phase 1 -> 0
-template <typename S, typename K, int TXV, int TY, bool HAS_OBS>
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS, bool LES = false>
 __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ? 4 : 1) aa_l_kernel(const Lattice L)
 {
     constexpr int VEC = vec_of<S>();
@@ -880,7 +915,7 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ?
             K v[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) v[q] = ldq<S, K>(base + q * pe, i, q);
-            collide_stored<S, K>(v, omega, fgrad, forced);
+            collide_stored<S, K, LES>(v, omega, fgrad, forced, (K)L.cte_s);
             K g[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) {
@@ -904,7 +939,7 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ?
             else x[q][c] = Store<S>::template getq<K>(v[c], q);
         }
     }
-    relax_vec<S, K, RAW>(x, omega, fgrad, forced);
+    relax_vec<S, K, RAW, VEC, LES>(x, omega, fgrad, forced, (K)L.cte_s);
     uint32_t rh[VEC];
 #pragma unroll
     for (int c = 0; c < VEC; ++c)

@@ -19,6 +19,10 @@ struct CaseSetup {
     double wt[4][9];
     double omega, fgrad, u00, u0;   // values of the compute kind
     int forced;
+    int bfs = 0;                    // backward-facing step: boundary kernel before each step
+    int stepx = 0, stepy = 0;       // step corner (SRC/input.F90:74-75)
+    int les;                        // Smagorinsky eddy viscosity on
+    double cte_s;                   // Smagorinsky constant (compute kind)
     double u_inflow;                // compute-kind inflow speed (peak for the parabolic profile)
     std::vector<double> inflow;     // [3][ly+2] equilibrium deviations of 01,03,05 at x_lo
     std::vector<int32_t> obs;       // obs(1:lx,1:ly), i fastest
@@ -134,6 +138,8 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
     if (d.omega > 0) omega = (K)d.omega;
     const K fgrad = (((K)4 * u0) * svisc) / (((K)3 * (K)m) * (K)m);
     cs.omega = (double)omega;
+    cs.les = d.les != 0;
+    cs.cte_s = (double)(K)d.cte_s;  // namelist value read in mykind
     cs.fgrad = (double)fgrad;
     cs.u00 = (double)u00;
     cs.u0 = (double)u0;
@@ -165,6 +171,15 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
         cs.wt[YHI][D01] = (double)force;
         cs.wt[YHI][D10] = (double)(-force);
         break;
+    case BGK_CASE_BFS:
+        // every ghost value is written by the step's boundary kernel (SRC/bcond.step.F90)
+        cs.faces[XLO] = cs.faces[XHI] = cs.faces[YLO] = cs.faces[YHI] = FK_STORED;
+        cs.bfs = 1;
+        cs.stepx = l / 20;
+        cs.stepy = m / 2;
+        if (cs.stepx < 2 || m < 4) return "backward-facing step needs lx >= 40 and ly >= 4";
+        if (d.scheme != BGK_SCHEME_PINGPONG) return "backward-facing step: ping-pong scheme only";
+        break;
     case BGK_CASE_CUSTOM:
         for (int f = 0; f < 4; ++f) cs.faces[f] = d.faces[f];
         for (int f = 0; f < 4; ++f) {
@@ -179,18 +194,29 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
         return "unknown test case";
     }
     for (int f = 0; f < 4; ++f)
-        if (cs.faces[f] < FK_WALL || cs.faces[f] > FK_OUTFLOW_ZG) return "unknown face kind";
+        if ((cs.faces[f] < FK_WALL || cs.faces[f] > FK_OUTFLOW_ZG) && !cs.bfs) return "unknown face kind";
     if ((cs.faces[XLO] == FK_PERIODIC) != (cs.faces[XHI] == FK_PERIODIC)) return "x faces: periodic must pair";
     if ((cs.faces[YLO] == FK_PERIODIC) != (cs.faces[YHI] == FK_PERIODIC)) return "y faces: periodic must pair";
     if (cs.faces[XHI] == FK_INFLOW) return "inflow is supported on the x_lo face only";
     if (cs.faces[XLO] == FK_OUTFLOW_EQ || cs.faces[XLO] == FK_OUTFLOW_ZG) return "outflow is supported on the x_hi face only";
     for (int f = YLO; f <= YHI; ++f)
-        if (cs.faces[f] != FK_WALL && cs.faces[f] != FK_PERIODIC) return "y faces must be walls or periodic";
+        if (cs.faces[f] != FK_WALL && cs.faces[f] != FK_PERIODIC && !cs.bfs) return "y faces must be walls or periodic";
 
     // inflow table (u_inflow=0.1 is a default-real literal in SRC/bcond.inflow.F90:190)
     const K uin = d.u_inflow > 0 ? (K)d.u_inflow : (K)0.1f;
     cs.u_inflow = (double)uin;
     cs.inflow.assign(3 * (size_t)(m + 2), 0.0);
+    if (cs.bfs) {
+        // parabolic inflow above the step, u = 0.1 (j-stepy)(m-j) / ((m-stepy)^2/4) with the
+        // reference's float() conversions and integer division (SRC/bcond.step.F90:133-136)
+        const int sy = cs.stepy;
+        for (int j = sy; j <= m + 1; ++j) {
+            const K xj = ((uin * (K)(float)(j - sy)) * (K)(float)(m - j)) / (K)(float)(((m - sy) * (m - sy)) / 4);
+            K e[3];
+            inflow_eq<K>(xj, e);
+            for (int t = 0; t < 3; ++t) cs.inflow[(size_t)t * (m + 2) + j] = (double)e[t];
+        }
+    }
     if (cs.faces[XLO] == FK_INFLOW) {
         for (int j = 0; j <= m + 1; ++j) {
             K u = uin;

@@ -17,6 +17,10 @@ enum StepKind { STEP_PP = 0, STEP_AA_P = 1, STEP_AA_L = 2 };
 struct TileCfg { int txv, ty, cdiv; };
 constexpr int NUM_CFG = 6;
 constexpr TileCfg TILE_CFGS[NUM_CFG] = {{32, 4, 1}, {64, 2, 1}, {128, 1, 1}, {128, 2, 1}, {32, 4, 2}, {128, 1, 2}};
+// Single-domain ping-pong only: configurations NUM_CFG .. NUM_STEP_CFG-1 select the kernel whose
+// source rows are staged in shared memory by bulk async copies (8 bytes of each plane per thread):
+// 6 = 128 threads, 3 rows in flight; 7 = 128 threads, 4 rows; 8 = 256 threads, 3 rows.
+constexpr int NUM_STEP_CFG = 9;
 
 struct KernelTable {
     int vec;  // cells per 16-byte vector
@@ -25,6 +29,7 @@ struct KernelTable {
     cudaError_t (*scatter)(const Lattice &L, int cur, int q, const void *stage, cudaStream_t st);
     cudaError_t (*gather)(const Lattice &L, int cur, int phase, int q, void *stage, bool obs, cudaStream_t st);
     cudaError_t (*fill_outflow)(const Lattice &L, cudaStream_t st);
+    cudaError_t (*bcond_step)(const Lattice &L, int cur, int stepx, int stepy, cudaStream_t st);
     cudaError_t (*init_tgv)(const Lattice &L, double u0, cudaStream_t st);
     cudaError_t (*diagno)(const Lattice &L, int cur, int phase, int fluid_only, bool obs, double *partial, int nb,
                           cudaStream_t st);

@@ -66,6 +66,8 @@ extern "C" {
 #define BGK_CASE_POF 2     /* bcond_channel + body force fgrad */
 #define BGK_CASE_VKS 3     /* bcond_inflow (+ obstacle, drag/lift) */
 #define BGK_CASE_COU 4     /* bcond_couette */
+#define BGK_CASE_BFS 5     /* bcond_step: backward-facing step, stepx = lx/20, stepy = ly/2
+                              (SRC/input.F90:74-75); ping-pong only, lx >= 40 */
 #define BGK_CASE_CUSTOM 9  /* faces[] and wall_u[] given explicitly */
 
 /* face kinds for BGK_CASE_CUSTOM; faces are x_lo (i=0), x_hi (i=lx+1), y_lo, y_hi */
@@ -109,7 +111,11 @@ typedef struct bgk_case_desc {
     int32_t init_v;           /* BGK_INIT_* applied by bgk_create */
     double tgv_u0;            /* amplitude for BGK_INIT_TGV */
     int32_t device;           /* CUDA device ordinal */
-    int32_t reserved[7];
+    int32_t les;              /* 1: Smagorinsky eddy viscosity in the collision (-DLES,
+                                 SRC/col_MC.F90:178-248); such a handle steps with its own
+                                 128x1 kernels and cannot join a batch */
+    double cte_s;             /* Smagorinsky constant cteS (namelist, SRC/input.F90:55; default 0.1) */
+    int32_t reserved[4];
 } bgk_case_desc;
 
 typedef struct bgk_handle bgk_handle;
@@ -159,7 +165,10 @@ int bgk_get_scalars(bgk_handle *h, double out[4], int64_t *itime);
 /* thread-block tile shape of the step kernels (no reference counterpart):
  *   0 = 32x4 threads, 1 = 64x2, 2 = 128x1, 3 = 128x2, each thread updating one 16-byte vector
  *   of cells per plane; 4 = 32x4 and 5 = 128x1 with half a vector (8 bytes) per thread in the
- *   ping-pong kernels.  Results do not depend on the choice. */
+ *   ping-pong kernels.  Ping-pong only: 6, 7, 8 stage the source rows in shared memory with bulk
+ *   async copies (128 threads and 3 rows in flight, 128 and 4, 256 and 3; 8 bytes per thread);
+ *   such a step reports BGK_E_TIMEOUT at the next synchronisation if a copy never completed.
+ *   Results do not depend on the choice. */
 int bgk_set_tile(bgk_handle *h, int32_t tile_cfg);
 /* time `trial_steps` real steps per tile shape (the state advances) and keep the fastest */
 int bgk_tune(bgk_handle *h, int32_t trial_steps, int32_t *tile_cfg, int32_t *steps_run);
@@ -253,7 +262,8 @@ typedef struct bgk_server_config {
     int32_t max_slots;       /* concurrently resident requests */
     int64_t hbm_budget;      /* bytes the server may hold; <= 0: free HBM minus 4 GiB */
     int32_t chunk_steps;     /* steps per scheduling round (upper bound) */
-    int32_t tile_cfg;        /* batch tile shape (bgk_set_tile numbering); < 0 selects 32x4 */
+    int32_t tile_cfg;        /* batch tile shape (bgk_set_tile numbering, 0..5); < 0 selects 32x4,
+                                with 8 bytes per thread for the 16-bit kinds */
 } bgk_server_config;
 
 typedef struct bgk_server_stats {

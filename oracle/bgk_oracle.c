@@ -37,12 +37,14 @@ struct orc_state {
 #define K float
 #define FN(x) x##_ss
 #define SIN sinf
+#define SQRT sqrtf
 #define COS cosf
 #include "bgk_oracle_body.h"
 #undef S
 #undef K
 #undef FN
 #undef SIN
+#undef SQRT
 #undef COS
 
 /* DOUBLE: mystorage = mykind = REAL(8) */
@@ -50,12 +52,14 @@ struct orc_state {
 #define K double
 #define FN(x) x##_dd
 #define SIN sin
+#define SQRT sqrt
 #define COS cos
 #include "bgk_oracle_body.h"
 #undef S
 #undef K
 #undef FN
 #undef SIN
+#undef SQRT
 #undef COS
 
 /* MIXED2: mystorage = REAL(4), mykind = REAL(8) */
@@ -63,12 +67,14 @@ struct orc_state {
 #define K double
 #define FN(x) x##_sd
 #define SIN sin
+#define SQRT sqrt
 #define COS cos
 #include "bgk_oracle_body.h"
 #undef S
 #undef K
 #undef FN
 #undef SIN
+#undef SQRT
 #undef COS
 
 #define DISPATCH(s, fn, args)                              \

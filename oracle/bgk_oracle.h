@@ -53,6 +53,8 @@ typedef struct {
     int init_v;        /* 0 rest flow; TGV cases use the periodic init */
     double svisc;      /* namelist svisc, rounded to mykind */
     double u0;         /* namelist u0, rounded to mykind */
+    int les;           /* 1: Smagorinsky eddy viscosity (-DLES, SRC/col_MC.F90:178-264) */
+    double cte_s;      /* namelist cteS (SRC/input.F90:55), rounded to mykind */
 } orc_params;
 
 orc_state *orc_create(const orc_params *p);

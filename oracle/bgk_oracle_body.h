@@ -355,7 +355,7 @@ static void FN(boundaries)(orc_state *s)
 
 /* col_MC.F90:114-176 / col.F90:90-152 (equilibrium) and :285-293 / :229-237 (relaxation);
  * x[] holds x01..x19, out[] receives the nine post-collision values in mykind */
-static inline void FN(collide)(const K *x, K omega, K fgrad, int forced, K *out)
+static inline void FN(collide)(const K *x, K omega, K fgrad, int forced, int les, K cte_s, K *out)
 {
     const K cte1 = UNO, cte0 = UNO - cte1;
     K x01 = x[0], x03 = x[1], x05 = x[2], x08 = x[3], x10 = x[4];
@@ -390,6 +390,22 @@ static inline void FN(collide)(const K *x, K omega, K fgrad, int forced, K *out)
     K e14 = rp1 * (-vx + qx) + cte1 * (rp1 - P1);
     K e17 = rp1 * (-vy + qy) + cte1 * (rp1 - P1);
     K e19 = rp0 * (+q0) + cte1 * (rp0 - P0);
+    if (les) {
+        /* col_MC.F90:178-248: non-equilibrium stress, then omega = 1/Ts with the Smagorinsky
+         * eddy viscosity; omega1 is the molecular rate (hencol.F90:31, equal to omega).
+         * `18.0` and `1.0` are default-real literals, exact in either kind. */
+        const K omega1 = omega;
+        K n01 = x01 - e01, n03 = x03 - e03, n05 = x05 - e05, n08 = x08 - e08;
+        K n10 = x10 - e10, n12 = x12 - e12, n14 = x14 - e14, n17 = x17 - e17;
+        K pxx = ((((n01 + n03) + n05) + n10) + n12) + n14;
+        K pyy = ((((n01 + n03) + n08) + n10) + n12) + n17;
+        K pxy = (((-n01) + n03) + n10) - n12;
+        K pyx = pxy;
+        K ptotal = SQRT(((pxx * pxx) + (((K)2 * pxy) * pyx)) + (pyy * pyy));
+        K r = UNO / omega1;
+        K ts = UNO / ((K)2 * omega1) + SQRT((((K)18 * (cte_s * cte_s)) * ptotal) + (r * r)) / (K)2;
+        omega = UNO / ts;
+    }
     K forcex = ZERO, forcey = ZERO;
     if (forced) forcex = fgrad * rho;
     out[0] = (x01 - omega * (x01 - e01)) + (forcex - forcey);
@@ -407,8 +423,8 @@ static inline void FN(collide)(const K *x, K omega, K fgrad, int forced, K *out)
 static void FN(col_MC_rows)(orc_state *s, int j0, int j1)
 {
     const int l = s->l;
-    const K omega = (K)s->omega, fgrad = (K)s->fgrad;
-    const int forced = (s->p.tcase == ORC_POF);
+    const K omega = (K)s->omega, fgrad = (K)s->fgrad, cte_s = (K)s->p.cte_s;
+    const int forced = (s->p.tcase == ORC_POF), les = s->p.les;
     K x[9], o[9];
     for (int j = j0; j <= j1; ++j) {
         for (int i = 1; i <= l; ++i) {
@@ -421,7 +437,7 @@ static void FN(col_MC_rows)(orc_state *s, int j0, int j1)
             x[6] = RA(6, i + 1, j);
             x[7] = RA(7, i, j + 1);
             x[8] = RA(8, i, j);
-            FN(collide)(x, omega, fgrad, forced, o);
+            FN(collide)(x, omega, fgrad, forced, les, cte_s, o);
             for (int q = 0; q < 8; ++q) B_(q, i, j) = (S)o[q];
             A_(8, i, j) = (S)o[8];
         }
@@ -437,8 +453,8 @@ static void FN(swap)(orc_state *s)
 static void FN(movef_col)(orc_state *s)
 {
     const int l = s->l, m = s->m;
-    const K omega = (K)s->omega, fgrad = (K)s->fgrad;
-    const int forced = (s->p.tcase == ORC_POF);
+    const K omega = (K)s->omega, fgrad = (K)s->fgrad, cte_s = (K)s->p.cte_s;
+    const int forced = (s->p.tcase == ORC_POF), les = s->p.les;
     for (int j = 1; j <= m; ++j) {
         for (int i = 1; i <= l; ++i) {
             B_(0, i, j) = A_(0, i - 1, j + 1);
@@ -456,7 +472,7 @@ static void FN(movef_col)(orc_state *s)
         for (int i = 1; i <= l; ++i) {
             for (int q = 0; q < 8; ++q) x[q] = RB(q, i, j);
             x[8] = RA(8, i, j);
-            FN(collide)(x, omega, fgrad, forced, o);
+            FN(collide)(x, omega, fgrad, forced, les, cte_s, o);
             for (int q = 0; q < 9; ++q) A_(q, i, j) = (S)o[q];
         }
     }

@@ -182,3 +182,59 @@ def test_4096_first_steps_bit_exact(oracle_mod, bgk, prec):
     finally:
         a.close()
         b.close()
+
+
+@pytest.mark.parametrize("scheme", ["pingpong", "aa"])
+@pytest.mark.parametrize("prec", ["single", "double", "mixed2"])
+@pytest.mark.parametrize("case", ["ldc", "tgv", "vks"])
+def test_les_bit_exact(oracle_mod, bgk, case, prec, scheme):
+    """Smagorinsky eddy viscosity (-DLES, SRC/col_MC.F90:178-248), cteS = 0.2."""
+    tc, lx, ly, svisc, u0, okw, skw = CASES[case]
+    oprec, st, cp = PRECS[prec]
+    o = oracle_mod.Oracle(lx, ly, prec=oprec, tcase=ORACLE_CASE[tc], svisc=svisc / 4, u0=u0,
+                          obs_order=oracle_mod.OBS_SNAPSHOT, les=True, cte_s=0.2, **okw)
+    with bgk.Solver(lx, ly, tcase=tc, svisc=svisc / 4, u0=u0, storage=st, compute=cp, scheme=scheme,
+                    les=True, cte_s=0.2, **skw) as s:
+        for n in (1, 2, 40, 75):
+            s.step(n)
+            o.step(n)
+            assert_same(o, s, scheme)
+
+
+def _bfs_fluid(a, lx, ly):
+    """Interior populations outside the step block x < lx/20, y < ly/2 (SRC/input.F90:74-75)."""
+    sx, sy = lx // 20, ly // 2
+    g = a[:, 1:ly + 1, 1:lx + 1]
+    keep = np.ones((ly, lx), bool)
+    keep[:sy - 1, :sx - 1] = False
+    return g[:, keep]
+
+
+@pytest.mark.parametrize("tile", [2, 6])
+@pytest.mark.parametrize("prec", ["single", "double", "mixed2"])
+def test_bfs_bit_exact(oracle_mod, bgk, prec, tile):
+    """Backward-facing step (SRC/bcond.step.F90): outflow, parabolic inflow above the step, no-slip
+    walls and the step faces written by a boundary kernel before each fused step.  The solid block
+    holds values nobody reads back (the reference poisons its second buffer with huge(), this
+    code with zeros), so the fluid cells are compared."""
+    oprec, st, cp = PRECS[prec]
+    lx, ly = 200, 64
+    o = oracle_mod.Oracle(lx, ly, prec=oprec, tcase=oracle_mod.BFS, svisc=0.02, u0=0.1)
+    with bgk.Solver(lx, ly, tcase="BFS", svisc=0.02, u0=0.1, storage=st, compute=cp) as s:
+        s.set_tile(tile)
+        for n in (1, 2, 40, 75):
+            s.step(n)
+            o.step(n)
+            g, r = _bfs_fluid(s.download(), lx, ly), _bfs_fluid(o.raw(), lx, ly)
+            bad = np.flatnonzero(g != r)
+            assert bad.size == 0, f"{bad.size} populations differ after {n}"
+
+
+def test_bfs_rejects_aa_and_batches(bgk):
+    from bgk2d_gpu_gb300 import _lib
+    with pytest.raises(bgk.BgkError):
+        bgk.Solver(200, 64, tcase="BFS", scheme="aa")
+    with bgk.Solver(200, 64, tcase="BFS") as s, bgk.Batch("f32") as b:
+        with pytest.raises(bgk.BgkError) as e:
+            b.add(s)
+        assert e.value.code == _lib.E_UNSUPPORTED
