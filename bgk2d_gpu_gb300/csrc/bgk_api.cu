@@ -397,6 +397,8 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
     }
     cudaMemsetAsync(h->d_status, 0, sizeof(uint32_t), h->st);
     L.status = h->d_status;
+    const char *stall = std::getenv("BGK_FAULT_INJECT_STALL");
+    L.inject_stall = (stall && stall[0] == '1') ? 1 : 0;
     h->cfg = default_cfg(nvec);
 
     // initial state (SRC/initialize.F90:85-125: init(init_v))

@@ -13,7 +13,7 @@
 // the same arithmetic per cell, the same hash words for the stochastic rounding, and the same
 // boundary-rule recomputation from the source buffer afterwards.
 //
-// Every wait on an mbarrier is bounded.  When a wait runs out, the warp sets the lattice's status
+// Every wait on an mbarrier is bounded (0.5 s).  When a wait runs out, the warp sets the lattice's status
 // word and leaves the row loop; the other warps then run out too (nobody refills the stage they
 // wait for), and the block waits (bounded again) for its own copies still in flight before it
 // returns.  The host reads the status word at the next synchronisation, and later launches return
@@ -24,8 +24,9 @@
 
 namespace bgk {
 
-constexpr uint32_t STAGED_WAIT_LIMIT = 1u << 20;  // try_wait polls before a wait gives up
-constexpr uint32_t STAGED_TIMEOUT = 0x5747u;      // status word value written on a timeout
+constexpr uint64_t STAGED_WAIT_NS = 500000000ull;  // a wait gives up after 0.5 s (global timer)
+constexpr uint32_t STAGED_WAIT_POLLS = 1u << 26;    // and after this many polls in any case
+constexpr uint32_t STAGED_TIMEOUT = 0x5747u;        // status word value written on a timeout
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -49,11 +50,19 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
                  : "memory");
 }
 
-// bounded wait for the phase with parity `par` of `bar` to complete
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// bounded wait for the phase with parity `par` of `bar` to complete: false after 0.5 s
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t par)
 {
     const uint32_t a = smem_u32(bar);
-    for (uint32_t i = 0; i < STAGED_WAIT_LIMIT; ++i) {
+    uint64_t t0 = 0;
+    for (uint32_t i = 0; i < STAGED_WAIT_POLLS; ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -63,6 +72,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t par)
             : "r"(a), "r"(par)
             : "memory");
         if (done) return true;
+        if ((i & 63u) == 63u) {
+            const uint64_t t = global_ns();
+            if (t0 == 0) t0 = t;
+            else if (t - t0 > STAGED_WAIT_NS) return false;
+        }
     }
     return false;
 }
@@ -139,7 +153,8 @@ __global__ void __launch_bounds__(T, ((N * sizeof(S) <= 8) ? 1024 : 512) / T)
     __shared__ int uses[STAGES];  // rows issued into each stage so far
     auto issue = [&](int y, int s) {
         uses[s] += 1;
-        mbar_expect_tx(&full[s], 9u * row_bytes);
+        // (a test hook declares 16 bytes that never arrive, so that the waits run out)
+        mbar_expect_tx(&full[s], 9u * row_bytes + (L.inject_stall ? 16u : 0u));
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
             const int ry = y - cy_of(q);

@@ -78,3 +78,29 @@ def test_staged_les_bit_exact(oracle_mod, bgk, prec):
         s.step(50)
         o.step(50)
         assert_same(o, s, "pingpong")
+
+
+def test_staged_wait_timeout_reports_status(oracle_mod, bgk, monkeypatch):
+    """A staged row that never completes (the test hook declares 16 bytes more than the copies
+    bring): every wait gives up after 0.5 s, the step reports BGK_E_TIMEOUT at the next
+    synchronisation, the handle stays failed, and the context stays usable for new handles."""
+    from bgk2d_gpu_gb300 import _lib
+    monkeypatch.setenv("BGK_FAULT_INJECT_STALL", "1")
+    s = bgk.Solver(1024, 256, tcase="LDC", svisc=0.05, u0=0.1)
+    monkeypatch.delenv("BGK_FAULT_INJECT_STALL")
+    try:
+        s.set_tile(6)
+        s.step(1)
+        with pytest.raises(bgk.BgkError) as e:
+            s.sync()
+        assert e.value.code == _lib.E_TIMEOUT
+        with pytest.raises(bgk.BgkError):
+            s.step(1)
+    finally:
+        s.close()
+    o = oracle_mod.Oracle(200, 90, prec=0, tcase=0, svisc=0.05, u0=0.1)
+    with bgk.Solver(200, 90, tcase="LDC", svisc=0.05, u0=0.1) as t:
+        t.set_tile(6)
+        t.step(5)
+        o.step(5)
+        assert_same(o, t, "pingpong")
