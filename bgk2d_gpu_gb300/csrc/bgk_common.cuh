@@ -73,8 +73,8 @@ template <> struct Store<double> {
 // (`cvt.rs`, Blackwell): each value goes to one of its two neighbouring representable values,
 // with the probabilities that make the expected result equal to the input, so updates smaller
 // than half an ulp are not lost on average (round-to-nearest would drop them).  Zero stays zero.
-// The random bits come from a per-cell hash (vector stores) or a hash of the value's own bit
-// pattern (lone values).
+// The random bits come from a hash per pair of cells (vector stores) or a hash of the value's own
+// bit pattern (lone values).
 
 // per-cell random word: multiplicative hash of the cell index and a value that changes every step
 __device__ __forceinline__ uint32_t cell_hash(uint32_t idx, float v)
@@ -88,10 +88,13 @@ __device__ __forceinline__ uint32_t cell_hash(uint32_t idx, float v)
 // pattern, in both halves of the word
 __device__ __forceinline__ uint32_t lone_bits(float x) { return __byte_perm(__float_as_uint(x) * 0x9e3779b1u, 0u, 0x3232); }
 
-// direction q's random word for the pair of cells whose words are lo, hi: a 32-bit window of the
-// 64-bit concatenation at a direction-dependent offset
+// hash words held by a thread of N cells: one per pair (at least one)
+template <int N> __host__ __device__ constexpr int npair() { return N > 1 ? N / 2 : 1; }
+
+// direction q's random word for a pair of cells with hash word h: h rotated by a
+// direction-dependent amount
 template <int q>
-__device__ __forceinline__ uint32_t pair_bits(uint32_t lo, uint32_t hi) { return __funnelshift_l(lo, hi, 3 * q + 2); }
+__device__ __forceinline__ uint32_t pair_bits(uint32_t h) { return __funnelshift_l(h, h, 3 * q + 2); }
 
 template <> struct Store<__half> {
     static constexpr int VEC = 8;

@@ -114,17 +114,20 @@ __device__ __forceinline__ void collide_scaled(float (&D)[9], float omega, float
     const float ux = jx * rinv, uy = jy * rinv;
     const float A = fmaf(-1.5f, fmaf(jx, ux, jy * uy), rho1);
     const float omc = 1.0f - omega, k = omega * (8.0f / 9.0f);
-    auto pair = [&](int qp, int qm, float cj, float cu) {
-        const float t = fmaf(4.5f * cj, cu, A);
-        const float s3 = 3.0f * cj;
-        D[qp] = fmaf(omc, D[qp], k * (t + s3));
-        D[qm] = fmaf(omc, D[qm], k * (t - s3));
+    // k folded into A and j, 4.5 into u: per direction pair (q, opp q) with kcj = k c.j and
+    // cu45 = 4.5 c.u,  D' = (1 - omega) D + kA + kcj cu45 +- 3 kcj
+    const float kA = k * A, kjx = k * jx, kjy = k * jy;
+    const float ux45 = 4.5f * ux, uy45 = 4.5f * uy;
+    auto pair = [&](int qp, int qm, float kcj, float cu45) {
+        const float t = fmaf(kcj, cu45, kA);
+        D[qp] = fmaf(omc, D[qp], fmaf(3.0f, kcj, t));
+        D[qm] = fmaf(omc, D[qm], fmaf(-3.0f, kcj, t));
     };
-    pair(D05, D14, jx, ux);
-    pair(D08, D17, jy, uy);
-    pair(D03, D10, jx + jy, ux + uy);
-    pair(D01, D12, jx - jy, ux - uy);
-    D[D19] = fmaf(omc, D[D19], k * A);
+    pair(D05, D14, kjx, ux45);
+    pair(D08, D17, kjy, uy45);
+    pair(D03, D10, kjx + kjy, ux45 + uy45);
+    pair(D01, D12, kjx - kjy, ux45 - uy45);
+    D[D19] = fmaf(omc, D[D19], kA);
     if (forced) {
         const float F = fgrad * rho;  // +F on 01,03,05 and -F on 10,12,14 (SRC/col_MC.F90:285-291)
         D[D01] += 32.0f * F; D[D03] += 32.0f * F; D[D05] += 8.0f * F;
@@ -357,22 +360,22 @@ __device__ __forceinline__ void relax_vec(K (&x)[9][N], K omega, K fgrad, bool f
 
 // store N values of direction q as one 8- or 16-byte vector
 template <typename S, typename K, int q, bool RAW, int N = vec_of<S>()>
-__device__ __forceinline__ void store_vec(S *p, const K (&v)[N], const uint32_t (&rh)[N])
+__device__ __forceinline__ void store_vec(S *p, const K (&v)[N], const uint32_t (&rh)[npair<N>()])
 {
     if constexpr (RAW) {
-        // stochastic rounding of each pair of cells with a direction-dependent window of their
-        // two hash words `rh`
+        // stochastic rounding of each pair of cells with a direction-dependent rotation of the
+        // pair's hash word rh[j]
         if constexpr (N == 8) {
             uint4 u;
-            u.x = Store<S>::pack2_rs((float)v[0], (float)v[1], pair_bits<q>(rh[0], rh[1]));
-            u.y = Store<S>::pack2_rs((float)v[2], (float)v[3], pair_bits<q>(rh[2], rh[3]));
-            u.z = Store<S>::pack2_rs((float)v[4], (float)v[5], pair_bits<q>(rh[4], rh[5]));
-            u.w = Store<S>::pack2_rs((float)v[6], (float)v[7], pair_bits<q>(rh[6], rh[7]));
+            u.x = Store<S>::pack2_rs((float)v[0], (float)v[1], pair_bits<q>(rh[0]));
+            u.y = Store<S>::pack2_rs((float)v[2], (float)v[3], pair_bits<q>(rh[1]));
+            u.z = Store<S>::pack2_rs((float)v[4], (float)v[5], pair_bits<q>(rh[2]));
+            u.w = Store<S>::pack2_rs((float)v[6], (float)v[7], pair_bits<q>(rh[3]));
             *reinterpret_cast<uint4 *>(p) = u;
         } else {
             uint2 u;
-            u.x = Store<S>::pack2_rs((float)v[0], (float)v[1], pair_bits<q>(rh[0], rh[1]));
-            u.y = Store<S>::pack2_rs((float)v[2], (float)v[3], pair_bits<q>(rh[2], rh[3]));
+            u.x = Store<S>::pack2_rs((float)v[0], (float)v[1], pair_bits<q>(rh[0]));
+            u.y = Store<S>::pack2_rs((float)v[2], (float)v[3], pair_bits<q>(rh[1]));
             *reinterpret_cast<uint2 *>(p) = u;
         }
     } else {
@@ -500,10 +503,10 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
 
     relax_vec<S, K, RAW, N, LES>(x, (K)L.omega, (K)L.fgrad, L.forced != 0, (K)L.cte_s);
     const int64_t me = cell_index<S>(L, xv, y);
-    uint32_t rh[N];
+    uint32_t rh[npair<N>()] = {};
 #pragma unroll
-    for (int c = 0; c < N; ++c)
-        rh[c] = RAW ? cell_hash((uint32_t)me + c, (float)x[D19][c]) : 0u;
+    for (int j = 0; j < N / 2; ++j)
+        rh[j] = RAW ? cell_hash((uint32_t)me + 2 * j, (float)x[D19][2 * j]) : 0u;
     store_vec<S, K, D01, RAW, N>(dst + D01 * pe + me, x[D01], rh);
     store_vec<S, K, D03, RAW, N>(dst + D03 * pe + me, x[D03], rh);
     store_vec<S, K, D05, RAW, N>(dst + D05 * pe + me, x[D05], rh);
@@ -737,12 +740,12 @@ __device__ __forceinline__ void aa_edge_push(const Lattice &L, S *base, int x, i
 
 // push VEC values of direction q to (x + c_q) in plane q; lanes at an edge (segment end or a
 // neighbour on the slow path) store the elements that cross into the neighbour's vector.
-// 16-bit kinds (RAW) round the shifted vector in pairs, as it is stored, with the lane's cell
+// 16-bit kinds (RAW) round the shifted vector in pairs, as it is stored, with the lane's pair
 // hash words `rh`; lone elements at an edge use the lone-value rounding.
 template <typename S, typename K, int q, int W, bool RAW = false>
 __device__ __forceinline__ void push_vec(const Lattice &L, S *plane, int xv, int y, bool left_edge,
                                          bool right_edge, const K (&g)[vec_of<S>()], bool store,
-                                         const uint32_t (&rh)[vec_of<S>()])
+                                         const uint32_t (&rh)[npair<vec_of<S>()>()])
 {
     constexpr int VEC = vec_of<S>();
     constexpr int cx = cx_of(q), cy = cy_of(q);
@@ -769,10 +772,10 @@ __device__ __forceinline__ void push_vec(const Lattice &L, S *plane, int xv, int
         if (!store) return;
         if (cx == 0 || (cx == 1 && !left_edge) || (cx == -1 && !right_edge)) {
             uint4 u;
-            u.x = Store<S>::pack2_rs((float)sh[0], (float)sh[1], pair_bits<q>(rh[0], rh[1]));
-            u.y = Store<S>::pack2_rs((float)sh[2], (float)sh[3], pair_bits<q>(rh[2], rh[3]));
-            u.z = Store<S>::pack2_rs((float)sh[4], (float)sh[5], pair_bits<q>(rh[4], rh[5]));
-            u.w = Store<S>::pack2_rs((float)sh[6], (float)sh[7], pair_bits<q>(rh[6], rh[7]));
+            u.x = Store<S>::pack2_rs((float)sh[0], (float)sh[1], pair_bits<q>(rh[0]));
+            u.y = Store<S>::pack2_rs((float)sh[2], (float)sh[3], pair_bits<q>(rh[1]));
+            u.z = Store<S>::pack2_rs((float)sh[4], (float)sh[5], pair_bits<q>(rh[2]));
+            u.w = Store<S>::pack2_rs((float)sh[6], (float)sh[7], pair_bits<q>(rh[3]));
             *reinterpret_cast<uint4 *>(plane + idx) = u;
         } else if (cx == 1) {
 #pragma unroll
@@ -866,10 +869,10 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ?
     relax_vec<S, K, RAW, VEC, LES>(x, (K)L.omega, (K)L.fgrad, L.forced != 0, (K)L.cte_s);
     K (&g)[9][VEC] = x;
     const bool store = !slow;
-    uint32_t rh[VEC];
+    uint32_t rh[npair<VEC>()] = {};
     const uint32_t me = (uint32_t)cell_index<S>(L, xv, y);
 #pragma unroll
-    for (int c = 0; c < VEC; ++c) rh[c] = RAW ? cell_hash(me + c, (float)g[D19][c]) : 0u;
+    for (int j = 0; j < VEC / 2; ++j) rh[j] = RAW ? cell_hash(me + 2 * j, (float)g[D19][2 * j]) : 0u;
     push_vec<S, K, D01, W, RAW>(L, base + D01 * pe, xv, y, left_edge, right_edge, g[D01], store, rh);
     push_vec<S, K, D03, W, RAW>(L, base + D03 * pe, xv, y, left_edge, right_edge, g[D03], store, rh);
     push_vec<S, K, D05, W, RAW>(L, base + D05 * pe, xv, y, left_edge, right_edge, g[D05], store, rh);
@@ -940,10 +943,10 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ?
         }
     }
     relax_vec<S, K, RAW, VEC, LES>(x, omega, fgrad, forced, (K)L.cte_s);
-    uint32_t rh[VEC];
+    uint32_t rh[npair<VEC>()] = {};
 #pragma unroll
-    for (int c = 0; c < VEC; ++c)
-        rh[c] = RAW ? cell_hash((uint32_t)me + c, (float)x[D19][c]) : 0u;
+    for (int j = 0; j < VEC / 2; ++j)
+        rh[j] = RAW ? cell_hash((uint32_t)me + 2 * j, (float)x[D19][2 * j]) : 0u;
     store_vec<S, K, D01, RAW>(base + D12 * pe + me, x[D01], rh);
     store_vec<S, K, D03, RAW>(base + D10 * pe + me, x[D03], rh);
     store_vec<S, K, D05, RAW>(base + D14 * pe + me, x[D05], rh);

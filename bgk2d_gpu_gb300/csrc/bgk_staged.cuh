@@ -232,9 +232,9 @@ __global__ void __launch_bounds__(T, ((N * sizeof(S) <= 8) ? 1024 : 512) / T)
 
             relax_vec<S, K, RAW, N>(x, omega, fgrad, forced, (K)0);
             const int64_t me = cell_index<S>(L, xv, y);
-            uint32_t rh[N];
+            uint32_t rh[npair<N>()] = {};
 #pragma unroll
-            for (int c = 0; c < N; ++c) rh[c] = RAW ? cell_hash((uint32_t)me + c, (float)x[D19][c]) : 0u;
+            for (int j = 0; j < N / 2; ++j) rh[j] = RAW ? cell_hash((uint32_t)me + 2 * j, (float)x[D19][2 * j]) : 0u;
             store_vec<S, K, D01, RAW, N>(dst + D01 * pe + me, x[D01], rh);
             store_vec<S, K, D03, RAW, N>(dst + D03 * pe + me, x[D03], rh);
             store_vec<S, K, D05, RAW, N>(dst + D05 * pe + me, x[D05], rh);
