@@ -175,11 +175,13 @@ def run_profile(args):
                     compute=compute, scheme=scheme) as s:
         if args.tile >= 0:
             s.set_tile(args.tile)
+        s.set_prefetch(args.prefetch)
         s.step(args.warmup)
         s.sync()
         ms = s.step_timed(args.steps)
     per = ms / args.steps
-    print(f"profile run {args.profile} {args.size}^2 tile={args.tile} warmup={args.warmup} steps={args.steps} "
+    print(f"profile run {args.profile} {args.size}^2 tile={args.tile} prefetch={args.prefetch} "
+          f"warmup={args.warmup} steps={args.steps} "
           f"ms/step={per:.4f} GLUPS={args.size * args.size / (per * 1e-3) / 1e9:.2f}")
     return 0
 
@@ -189,11 +191,12 @@ def measure_variant(bgk, storage, scheme, steps, warmup, dev, tune=True):
     with bgk.Solver(LX, LY, tcase="LDC", svisc=SVISC, u0=U0, storage=storage, compute=compute, scheme=scheme,
                     device=dev) as s:
         cfg = s.tune(4 if storage == "f64" else 10)[0] if tune else None
+        pf = s.prefetch()
         s.step(warmup)
         s.sync()
         ms = s.step_timed(steps)
     glups = LX * LY * steps / (ms * 1e-3) / 1e9
-    return glups, ms / steps, cfg
+    return glups, ms / steps, cfg, pf
 
 
 # ---------------------------------------------------------------------------------------------
@@ -346,6 +349,7 @@ def main():
                     help="run only <scheme>_<storage> (e.g. pingpong_f32) on a --size^2 cavity, for ncu")
     ap.add_argument("--size", type=int, default=2048)
     ap.add_argument("--tile", type=int, default=-1, help="tile configuration for --profile")
+    ap.add_argument("--prefetch", type=int, default=0, help="L2 prefetch distance in blocks for --profile")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -368,6 +372,7 @@ def main():
     # ---- device-timed value: K steps from HBM-resident state --------------------------------
     s = bgk.Solver(LX, LY, tcase="LDC", svisc=SVISC, u0=U0, storage="f32", scheme="pingpong", device=local)
     tile_cfg, _ = s.tune(10)
+    prefetch = s.prefetch()
     s.step(args.warmup)
     s.sync()
     if dist:
@@ -415,10 +420,11 @@ def main():
                               ("pingpong_bf16", "bf16", "pingpong"), ("pingpong_f64", "f64", "pingpong"),
                               ("aa_f64", "f64", "aa")):
             n = vsteps if st != "f64" else max(10, vsteps // 4)
-            g, msv, cfg = measure_variant(bgk, st, sch, n, 5, local)
+            g, msv, cfg, pf = measure_variant(bgk, st, sch, n, 5, local)
             bw = BYTES_PER_CELL[st] * LX * LY / (msv * 1e-3) / 1e9
             variants[name] = {"GLUPS": round(g, 3), "ms_per_step": round(msv, 4), "algorithmic_GBps": round(bw, 1),
-                              "hbm_frac": round(bw / peak, 4), "steps": n, "tile_cfg": cfg}
+                              "hbm_frac": round(bw / peak, 4), "steps": n, "tile_cfg": cfg,
+                              "prefetch_blocks": pf}
 
     forms = {}
     if rank == 0 and not args.no_forms:
@@ -438,7 +444,8 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (rest-state start, no dataset)",
             "config": {"workload": WORKLOAD, "lx": LX, "ly": LY, "scheme": "pingpong", "storage": "f32",
                        "l2": "inputs larger than L2: 1.21 GB of populations per step",
-                       "parallelism": f"{world} independent cavities" if world > 1 else "single domain"},
+                       "parallelism": f"{world} independent cavities" if world > 1 else "single domain",
+                       "tile_cfg": tile_cfg, "prefetch_blocks": prefetch},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": kt, "peak_kind": peak_kind,
                          "kernel": ("bgk::pp_staged_kernel<float,float,...> (tile config %d)" if tile_cfg >= 6 else

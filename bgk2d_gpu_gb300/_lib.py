@@ -117,6 +117,8 @@ def load(build_if_missing: bool = True):
         "bgk_version": (ctypes.c_char_p, []),
         "bgk_set_tile": (I32, [H, I32]),
         "bgk_tune": (I32, [H, I32, P(I32), P(I32)]),
+        "bgk_set_prefetch": (I32, [H, I32]),
+        "bgk_get_prefetch": (I32, [H, P(I32)]),
         "bgk_batch_create": (I32, [I32, I32, I32, P(VP)]),
         "bgk_batch_destroy": (I32, [VP]),
         "bgk_batch_add": (I32, [VP, H]),

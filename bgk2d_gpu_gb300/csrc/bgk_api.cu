@@ -399,6 +399,7 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
     L.status = h->d_status;
     const char *stall = std::getenv("BGK_FAULT_INJECT_STALL");
     L.inject_stall = (stall && stall[0] == '1') ? 1 : 0;
+    L.pf_ahead = 0;
     h->cfg = default_cfg(nvec);
 
     // initial state (SRC/initialize.F90:85-125: init(init_v))
@@ -653,6 +654,25 @@ int bgk_set_tile(bgk_handle *h, int32_t tile_cfg)
     return BGK_OK;
 }
 
+int bgk_set_prefetch(bgk_handle *h, int32_t blocks_ahead)
+{
+    CHECK_HANDLE(h);
+    if (blocks_ahead < 0) return fail(h, BGK_E_INVALID, "negative prefetch distance");
+    if (blocks_ahead != h->L.pf_ahead) {
+        for (int i = 0; i < 2; ++i)
+            if (h->graph[i]) { cudaGraphExecDestroy(h->graph[i]); h->graph[i] = nullptr; }
+        h->L.pf_ahead = blocks_ahead;
+    }
+    return BGK_OK;
+}
+
+int bgk_get_prefetch(bgk_handle *h, int32_t *blocks_ahead)
+{
+    if (!h || !blocks_ahead) return BGK_E_INVALID;
+    *blocks_ahead = h->L.pf_ahead;
+    return BGK_OK;
+}
+
 int bgk_tune(bgk_handle *h, int32_t trial_steps, int32_t *tile_cfg, int32_t *steps_run)
 {
     CHECK_HANDLE(h);
@@ -660,24 +680,32 @@ int bgk_tune(bgk_handle *h, int32_t trial_steps, int32_t *tile_cfg, int32_t *ste
     if (trial_steps < 2) return fail(h, BGK_E_INVALID, "trial_steps < 2");
     const int n = trial_steps & ~1;
     float best = 1e30f;
-    int best_cfg = h->cfg, rc;
+    int best_cfg = h->cfg, best_pf = h->L.pf_ahead, rc;
     int64_t run = 0;
+    int sms = 0;
+    CK(h, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->dev));
+    // L2 prefetch distances for the register-vector ping-pong kernels: off, half a wave and one
+    // wave of 8 resident blocks per SM ahead
+    const int pfs[3] = {0, 4 * sms, 8 * sms};
     const int ncfg = h->L.scheme == BGK_SCHEME_PINGPONG ? NUM_STEP_CFG : NUM_CFG;
     for (int c = 0; c < ncfg; ++c) {
-        if ((rc = bgk_set_tile(h, c))) return rc;
-        for (int s = 0; s < 2; ++s)
-            if ((rc = launch_step(h))) return rc;
-        float ms = 0;
-        CK(h, cudaEventRecord(h->ev0, h->st));
-        for (int s = 0; s < n; ++s)
-            if ((rc = launch_step(h))) return rc;
-        CK(h, cudaEventRecord(h->ev1, h->st));
-        CK(h, cudaEventSynchronize(h->ev1));
-        CK(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
-        run += n + 2;
-        if (ms < best) { best = ms; best_cfg = c; }
+        const int npf = (h->L.scheme == BGK_SCHEME_PINGPONG && c < NUM_CFG && !h->L.les) ? 3 : 1;
+        for (int p = 0; p < npf; ++p) {
+            if ((rc = bgk_set_tile(h, c)) || (rc = bgk_set_prefetch(h, pfs[p]))) return rc;
+            for (int s = 0; s < 2; ++s)
+                if ((rc = launch_step(h))) return rc;
+            float ms = 0;
+            CK(h, cudaEventRecord(h->ev0, h->st));
+            for (int s = 0; s < n; ++s)
+                if ((rc = launch_step(h))) return rc;
+            CK(h, cudaEventRecord(h->ev1, h->st));
+            CK(h, cudaEventSynchronize(h->ev1));
+            CK(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+            run += n + 2;
+            if (ms < best) { best = ms; best_cfg = c; best_pf = pfs[p]; }
+        }
     }
-    if ((rc = bgk_set_tile(h, best_cfg))) return rc;
+    if ((rc = bgk_set_tile(h, best_cfg)) || (rc = bgk_set_prefetch(h, best_pf))) return rc;
     if (tile_cfg) *tile_cfg = best_cfg;
     if (steps_run) *steps_run = (int32_t)run;
     return BGK_OK;

@@ -163,6 +163,7 @@ struct Lattice {
     int32_t ob_x0, ob_x1, ob_y0, ob_y1;  // cells whose pull may touch an obstacle
     uint32_t *status;        // device word set by a kernel whose bounded wait ran out (0: fine)
     int32_t inject_stall;    // test hook (BGK_FAULT_INJECT_STALL=1): staged copies never complete
+    int32_t pf_ahead;        // ping-pong kernels: L2 prefetch of the block this many places ahead (0: off)
 };
 
 template <typename S> __host__ __device__ constexpr int vec_of() { return 16 / (int)sizeof(S); }

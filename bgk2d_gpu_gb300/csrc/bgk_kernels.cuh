@@ -526,9 +526,34 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
     }
 }
 
+// Bulk prefetch into L2 of the source segments of the block L.pf_ahead places further on in
+// launch order (one row of one plane per thread, 9 * TY threads): by the time that block runs,
+// its loads hit L2 instead of HBM.
+template <typename S, int TXV, int TY, int N>
+__device__ __forceinline__ void prefetch_tile(const Lattice &L, const int parity)
+{
+    constexpr int VEC = vec_of<S>();
+    const int t = threadIdx.x + threadIdx.y * TXV;
+    if (t >= 9 * TY) return;
+    const long long lin = (long long)blockIdx.y * gridDim.x + blockIdx.x + L.pf_ahead;
+    if (lin >= (long long)gridDim.x * gridDim.y) return;
+    const int bx = (int)(lin % gridDim.x), by = (int)(lin / gridDim.x);
+    const int q = t % 9, y = by * TY + t / 9 + 1;
+    if (y > L.ly) return;
+    const int row = y - cy_of(q);
+    const int x0 = 1 + bx * TXV * N;
+    const int x1 = min(x0 + TXV * N, L.lx + 1);
+    const int64_t rs = (int64_t)row * L.pitch;
+    const int64_t lo = (cell_index<S>(L, x0 - 1, row) - rs) / VEC * VEC;
+    const int64_t hi = min((int64_t)L.pitch, (cell_index<S>(L, x1, row) - rs) / VEC * VEC + VEC);
+    const S *p = reinterpret_cast<const S *>(L.planes) + ((parity ? 9 : 0) + q) * L.plane_elems + rs + lo;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"((uint32_t)((hi - lo) * sizeof(S))) : "memory");
+}
+
 template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N, bool LES = false>
 __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 || (sizeof(S) == 4 && N == 4)) ? 8 : (sizeof(S) == 2 ? 4 : 1)) pp_kernel(const Lattice L, const int parity)
 {
+    if (L.pf_ahead > 0) prefetch_tile<S, TXV, TY, N>(L, parity);
     pp_tile<S, K, TXV, TY, HAS_OBS, N, LES>(L, blockIdx.x, blockIdx.y, parity);
 }
 

@@ -212,6 +212,14 @@ class Solver:
     def set_tile(self, cfg):
         self._check(self._L.bgk_set_tile(self._h, int(cfg)), "set_tile")
 
+    def set_prefetch(self, blocks_ahead):
+        self._check(self._L.bgk_set_prefetch(self._h, int(blocks_ahead)), "set_prefetch")
+
+    def prefetch(self):
+        n = ctypes.c_int32()
+        self._check(self._L.bgk_get_prefetch(self._h, ctypes.byref(n)), "get_prefetch")
+        return n.value
+
     def tune(self, trial_steps=20):
         """Time real steps per tile shape (the state advances); returns (tile_cfg, steps_run)."""
         c, n = ctypes.c_int32(), ctypes.c_int32()

@@ -238,3 +238,17 @@ def test_bfs_rejects_aa_and_batches(bgk):
         with pytest.raises(bgk.BgkError) as e:
             b.add(s)
         assert e.value.code == _lib.E_UNSUPPORTED
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_prefetch_does_not_change_results(bgk, storage):
+    """The L2 prefetch only moves data earlier; populations are identical with and without it."""
+    out = []
+    for pf in (0, 64, 1216):
+        with bgk.Solver(700, 300, tcase="LDC", svisc=0.02, u0=0.1, storage=storage) as s:
+            s.set_tile(5)
+            s.set_prefetch(pf)
+            assert s.prefetch() == pf
+            s.step(70)
+            out.append(s.download())
+    assert np.array_equal(out[0], out[1]) and np.array_equal(out[0], out[2])

@@ -63,7 +63,9 @@ def test_staged_tuner_may_pick_it(bgk):
     """The autotuner times the staged configurations too; whichever wins, the result is exact."""
     with bgk.Solver(1024, 512, tcase="LDC", svisc=0.05, u0=0.1, storage="f16") as s:
         cfg, run = s.tune(4)
-        assert 0 <= cfg <= 8 and run == 9 * 6
+        # 6 register-vector shapes x 3 prefetch distances + 3 staged shapes, 6 steps each
+        assert 0 <= cfg <= 8 and run == (6 * 3 + 3) * 6
+        assert s.prefetch() == 0 or cfg < 6
         s.step(10)
         s.sync()
 
