@@ -437,7 +437,7 @@ def main():
         cpu = cpu_reference(steps_budget_s=12.0)
 
     if rank == 0:
-        kt = traffic_from_profiles("pp_kernel_f32_ldc4096")
+        kt = traffic_from_profiles(f"pp_kernel_f32_ldc4096_t{tile_cfg}_pf{prefetch}")
         line = {
             "metric": "GLUPS", "value": round(glups, 3), "unit": "GLUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 5), "higher_is_better": True, "scaling": "weak",
@@ -448,6 +448,8 @@ def main():
                        "tile_cfg": tile_cfg, "prefetch_blocks": prefetch},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": kt, "peak_kind": peak_kind,
+                         "traffic_source": "profiles/dram_traffic.txt, same tile configuration and prefetch"
+                         if kt is not None else "no capture of this configuration",
                          "kernel": ("bgk::pp_staged_kernel<float,float,...> (tile config %d)" if tile_cfg >= 6 else
                                     "bgk::pp_kernel<float,float,...> (tile config %d)") % tile_cfg,
                          "bytes_per_cell": 72},
