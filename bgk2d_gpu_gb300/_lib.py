@@ -13,6 +13,7 @@ from . import build as _build
 I32 = ctypes.c_int32
 I64 = ctypes.c_int64
 F64 = ctypes.c_double
+F32 = ctypes.c_float
 VP = ctypes.c_void_p
 
 # status codes
@@ -109,6 +110,7 @@ def load(build_if_missing: bool = True):
         "bgk_draglift": (I32, [H, P(F64)]),
         "bgk_residual": (I32, [H, P(F64)]),
         "bgk_fields": (I32, [H, P(F64), P(F64), P(F64)]),
+        "bgk_vtk_fields": (I32, [H, P(F32), P(F32), P(F32), P(F32), P(F32)]),
         "bgk_get_obs": (I32, [H, P(I32), P(I32)]),
         "bgk_get_scalars": (I32, [H, P(F64), P(I64)]),
         "bgk_footprint": (I32, [H, P(I64), P(I32)]),

@@ -5,7 +5,8 @@
 // collision are one fused step on the device) and writes the reference's text outputs at its
 // diagnostic cadence (SRC/diagnostic.F90): diagno.dat, probe.dat, prof_i.dat, prof_j.dat,
 // drag.lift.dat, save.XXXXXXXX.bin checkpoints (Fortran unformatted sequential records, as
-// SRC/save_raw.F90) and bgk.perf.  VTK output is not produced.
+// SRC/save_raw.F90), tec_xy/tec_om VTK files (SRC/vtk_xy.binary.F90, SRC/vtk_om.binary.F90, from
+// fields computed on the device) and bgk.perf.
 //
 //   bgk2d_gb300 [--input bgk.input] [--case LDC|TGV|POF|VKS|COU|BFS] [--prec single|double|mixed2|f16|bf16]
 //               [--scheme pingpong|aa] [--les 0|1] [--dir OUTDIR]
@@ -161,6 +162,69 @@ bool read_record(FILE *f, void *data, uint32_t bytes)
     return std::fread(&b, 4, 1, f) == 1 && b == bytes;
 }
 
+// Big-endian float32 stream (Fortran access='STREAM', CONVERT="BIG_ENDIAN")
+void write_be(FILE *f, const float *v, size_t n)
+{
+    std::vector<unsigned char> b(4 * n);
+    for (size_t i = 0; i < n; ++i) {
+        uint32_t u;
+        std::memcpy(&u, v + i, 4);
+        b[4 * i] = (unsigned char)(u >> 24); b[4 * i + 1] = (unsigned char)(u >> 16);
+        b[4 * i + 2] = (unsigned char)(u >> 8); b[4 * i + 3] = (unsigned char)u;
+    }
+    std::fwrite(b.data(), 1, b.size(), f);
+}
+
+// Fortran Aw output of a shorter string: right-justified with leading blanks
+std::string fa(const char *s, int w)
+{
+    std::string t(s);
+    return (int)t.size() >= w ? t.substr(0, w) : std::string(w - t.size(), ' ') + t;
+}
+
+// tec_xy.XXXXXXXX.vtk and tec_om.XXXXXXXX.vtk as SRC/vtk_xy.binary.F90 and SRC/vtk_om.binary.F90
+// write them (serial build: offsets 0), from the fields computed on the device
+int write_vtk(bgk_handle *h, const std::string &dir, int itime, int lx, int ly)
+{
+    const size_t n = (size_t)lx * ly, n2 = (size_t)(lx - 2) * (ly - 2);
+    std::vector<float> u(n), w(n), rho(n), om(n2), st(n2);
+    int rc = bgk_vtk_fields(h, u.data(), w.data(), rho.data(), om.data(), st.data());
+    if (rc) return rc;
+    auto header = [&](FILE *f, int nx, int ny, int org) {
+        std::fprintf(f, "# vtk DataFile Version 2.0\nCampo\nBINARY\nDATASET STRUCTURED_POINTS\n");
+        std::fprintf(f, "DIMENSIONS %10d %10d %10d\n", nx, ny, 1);
+        std::fprintf(f, "ORIGIN %10d %10d %10d\n", org, org, 1);
+        std::fprintf(f, "SPACING %10d %10d %10d\n", 1, 1, 1);
+        std::fprintf(f, "POINT_DATA%10d\n", nx * ny);  // (A10,I10) keeps 10 of 'POINT_DATA '
+    };
+    char name[64];
+    std::snprintf(name, sizeof(name), "/tec_xy.%08d.vtk", itime);
+    FILE *f = std::fopen((dir + name).c_str(), "wb");
+    if (!f) return BGK_E_INVALID;
+    header(f, lx, ly, 1);
+    std::fprintf(f, "%s\n", fa("VECTORS velocity float", 23).c_str());
+    std::vector<float> vec(3 * n, 0.0f);
+    for (size_t k = 0; k < n; ++k) { vec[3 * k] = u[k]; vec[3 * k + 1] = w[k]; }
+    write_be(f, vec.data(), vec.size());
+    std::fprintf(f, "%s\n%s\n", fa("SCALARS w float", 21).c_str(), fa("LOOKUP_TABLE default", 20).c_str());
+    write_be(f, w.data(), n);
+    std::fprintf(f, "%s\n%s\n", fa("SCALARS u float", 21).c_str(), fa("LOOKUP_TABLE default", 20).c_str());
+    write_be(f, u.data(), n);
+    std::fprintf(f, "%s\n%s\n", fa("SCALARS rho float", 21).c_str(), fa("LOOKUP_TABLE default", 20).c_str());
+    write_be(f, rho.data(), n);
+    std::fclose(f);
+    std::snprintf(name, sizeof(name), "/tec_om.%08d.vtk", itime);
+    f = std::fopen((dir + name).c_str(), "wb");
+    if (!f) return BGK_E_INVALID;
+    header(f, lx - 2, ly - 2, 2);
+    std::fprintf(f, "%s\n%s\n", fa("SCALARS vorticity float", 24).c_str(), fa("LOOKUP_TABLE default", 20).c_str());
+    write_be(f, om.data(), n2);
+    std::fprintf(f, "%s\n%s\n", fa("SCALARS stream float", 25).c_str(), fa("LOOKUP_TABLE default", 20).c_str());
+    write_be(f, st.data(), n2);
+    std::fclose(f);
+    return BGK_OK;
+}
+
 int die(const char *what, int rc)
 {
     std::fprintf(stderr, "bgk2d_gb300: %s failed (status %d)\n", what, rc);
@@ -188,7 +252,6 @@ int main(int argc, char **argv)
     const int lx = geti("lx", 0), ly = geti("ly", 0), itfin = geti("itfin", 0);
     const int ivtim = geti("ivtim", 1 << 30), isignal = geti("isignal", 1 << 30), itsave = geti("itsave", 1 << 30);
     const int icheck = geti("icheck", 1 << 30), irestart = geti("irestart", 0), init_v = geti("init_v", 0);
-    (void)ivtim;
 
     bgk_case_desc d;
     bgk_default_desc(&d);
@@ -266,10 +329,12 @@ int main(int argc, char **argv)
     while (itime < itfin) {
         // advance to the next diagnostic, save or signal step
         int next = itfin;
-        for (int every : {icheck, itsave, isignal})
+        for (int every : {icheck, itsave, isignal, ivtim})
             if (every > 0) next = std::min(next, (itime / every + 1) * every);
         if ((rc = bgk_step(h, next - itime))) return die("bgk_step", rc);
         itime = next;
+        if (itime % ivtim == 0 && lx > 2 && ly > 2 && (rc = write_vtk(h, dir, itime, lx, ly)))  // SRC/diagnostic.F90:32-57
+            return die("vtk", rc);
         if (itime % icheck == 0 && (rc = diagnostic(itime))) return die("diagnostic", rc);
         if (itime % itsave == 0) {  // SRC/save_raw.F90
             if ((rc = bgk_download(h, pops.p, lx + 2))) return die("bgk_download", rc);

@@ -6,6 +6,8 @@
 // collides; steps are replayed from CUDA graphs; reductions run in FP64 on the device.
 #include <cuda_runtime.h>
 
+#include <utility>
+
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -614,6 +616,32 @@ int bgk_fields(bgk_handle *h, double *rho, double *u, double *v)
     dfree(h, d);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
     if (e != cudaSuccess) return fail(h, BGK_E_CUDA, "fields: %s", cudaGetErrorString(e));
+    return BGK_OK;
+}
+
+int bgk_vtk_fields(bgk_handle *h, float *u, float *w, float *rho, float *vort, float *stream)
+{
+    CHECK_HANDLE(h);
+    NOT_IN_BATCH(h);
+    const int l = h->desc.lx, m = h->desc.ly;
+    if (l < 3 || m < 3) return fail(h, BGK_E_INVALID, "vtk fields need lx, ly >= 3");
+    const size_t n = (size_t)l * m, n2 = (size_t)(l - 2) * (m - 2);
+    float *d = nullptr;
+    if (dalloc(h, &d, (3 * n + 2 * n2 + (size_t)m + 2) * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(h, BGK_E_NOMEM, "vtk fields buffer");
+    }
+    float *du = d, *dw = d + n, *dr = d + 2 * n, *dv = d + 3 * n, *ds = dv + n2, *dphi = ds + n2;
+    cudaError_t e = h->T.vtk(h->L, h->cur, h->phase, h->cs.has_obs, du, dw, dr, dv, ds, dphi, h->st);
+    h->launches += 3;
+    const std::pair<float *, const float *> out[5] = {{u, du}, {w, dw}, {rho, dr}, {vort, dv}, {stream, ds}};
+    for (int k = 0; k < 5 && e == cudaSuccess; ++k)
+        if (out[k].first)
+            e = cudaMemcpyAsync(out[k].first, out[k].second, (k < 3 ? n : n2) * sizeof(float), cudaMemcpyDeviceToHost,
+                                h->st);
+    dfree(h, d);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (e != cudaSuccess) return fail(h, BGK_E_CUDA, "vtk fields: %s", cudaGetErrorString(e));
     return BGK_OK;
 }
 

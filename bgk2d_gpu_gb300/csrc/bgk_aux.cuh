@@ -290,6 +290,94 @@ __global__ void fields_kernel(Lattice L, int cur, int phase, double *rho, double
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Fields of the reference's VTK writers (SRC/vtk_xy.binary.F90:75-140, SRC/vtk_om.binary.F90:62-150),
+// in their real(sp) arithmetic: sums of stored values in the storage kind (FP32 for the 16-bit
+// kinds), rounded to single precision; the vorticity's quotients divide a storage-kind numerator by
+// a single-precision density in the wider kind.
+template <typename S> struct VtkSum { using T = S; };
+template <> struct VtkSum<__half> { using T = float; };
+template <> struct VtkSum<__nv_bfloat16> { using T = float; };
+
+template <typename S, typename K, bool HAS_OBS>
+__device__ __forceinline__ void vtk_sums(const Lattice &L, int cur, int phase, int x, int y, float &den,
+                                         typename VtkSum<S>::T &u, typename VtkSum<S>::T &v)
+{
+    using T = typename VtkSum<S>::T;
+    T a[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) a[q] = (T)post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
+    const T t = ((((((((a[0] + a[1]) + a[2]) + a[3]) + a[4]) + a[5]) + a[6]) + a[7]) + a[8]);
+    den = (float)(t + (T)1.0f);
+    u = ((((a[D01] + a[D03]) + a[D05]) - a[D10]) - a[D12]) - a[D14];
+    v = ((((a[D03] + a[D08]) + a[D12]) - a[D01]) - a[D10]) - a[D17];
+}
+
+// u/rho, w/rho, rho over the interior and the vorticity over 2..lx-1 x 2..ly-1, one cell per thread
+template <typename S, typename K, bool HAS_OBS>
+__global__ void vtk_cells_kernel(Lattice L, int cur, int phase, float *u, float *w, float *rho, float *vort)
+{
+    using T = typename VtkSum<S>::T;
+    const int l = L.lx, m = L.ly;
+    const int64_t n = (int64_t)l * m;
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        const int x = (int)(c % l) + 1, y = (int)(c / l) + 1;
+        float den;
+        T su, sv;
+        vtk_sums<S, K, HAS_OBS>(L, cur, phase, x, y, den, su, sv);
+        u[c] = (float)su / den;
+        w[c] = (float)sv / den;
+        rho[c] = den;
+        if (x >= 2 && x <= l - 1 && y >= 2 && y <= m - 1) {
+            float d_up, d_down, d_left, d_right;
+            T u_up, u_down, v_left, v_right, unused;
+            vtk_sums<S, K, HAS_OBS>(L, cur, phase, x, y + 1, d_up, u_up, unused);
+            vtk_sums<S, K, HAS_OBS>(L, cur, phase, x, y - 1, d_down, u_down, unused);
+            vtk_sums<S, K, HAS_OBS>(L, cur, phase, x - 1, y, d_left, unused, v_left);
+            vtk_sums<S, K, HAS_OBS>(L, cur, phase, x + 1, y, d_right, unused, v_right);
+            const float up1 = (float)(u_up / (T)d_up), down1 = (float)(u_down / (T)d_down);
+            const float left1 = (float)(v_left / (T)d_left), right1 = (float)(v_right / (T)d_right);
+            vort[(int64_t)(y - 2) * (l - 2) + (x - 2)] = 0.5f * (up1 - down1) - 0.5f * (right1 - left1);
+        }
+    }
+}
+
+// stream function: the column integral of u at x = 1 from row 1 up (one thread, in row order),
+// then each row's running sum of -v/rho along x (one thread per row, in column order)
+template <typename S, typename K, bool HAS_OBS>
+__global__ void vtk_stream_kernel(Lattice L, int cur, int phase, float *phi)
+{
+    using T = typename VtkSum<S>::T;
+    const int m = L.ly;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        float prev = 0.0f;
+        for (int y = 1; y <= m; ++y) {
+            float den;
+            T su, sv;
+            vtk_sums<S, K, HAS_OBS>(L, cur, phase, 1, y, den, su, sv);
+            prev = prev + (float)su / den;
+            phi[y] = prev;
+        }
+    }
+}
+
+template <typename S, typename K, bool HAS_OBS>
+__global__ void vtk_stream_rows_kernel(Lattice L, int cur, int phase, const float *phi, float *stream)
+{
+    using T = typename VtkSum<S>::T;
+    const int l = L.lx, m = L.ly;
+    const int y = 2 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (y > m - 1) return;
+    float p = phi[y];
+    for (int x = 2; x <= l - 1; ++x) {
+        float den;
+        T su, sv;
+        vtk_sums<S, K, HAS_OBS>(L, cur, phase, x, y, den, su, sv);
+        p = p - (float)sv / den;
+        stream[(int64_t)(y - 2) * (l - 2) + (x - 2)] = p;
+    }
+}
+
 // fixed-order sum of nb partial 4-vectors (deterministic)
 __global__ void finalize4_kernel(const double *partial, int nb, double *out);
 

@@ -173,6 +173,24 @@ cudaError_t fields(const Lattice &L, int cur, int phase, bool obs, double *rho, 
     return cudaGetLastError();
 }
 
+template <typename S, typename K, bool OBS>
+void vtk_launch(const Lattice &L, int cur, int phase, float *u, float *w, float *rho, float *vort, float *stream,
+                float *phi, cudaStream_t st)
+{
+    vtk_cells_kernel<S, K, OBS><<<4 * 152, 256, 0, st>>>(L, cur, phase, u, w, rho, vort);
+    vtk_stream_kernel<S, K, OBS><<<1, 32, 0, st>>>(L, cur, phase, phi);
+    if (L.ly > 2) vtk_stream_rows_kernel<S, K, OBS><<<(L.ly - 2 + 127) / 128, 128, 0, st>>>(L, cur, phase, phi, stream);
+}
+
+template <typename S, typename K>
+cudaError_t vtk(const Lattice &L, int cur, int phase, bool obs, float *u, float *w, float *rho, float *vort,
+                float *stream, float *phi, cudaStream_t st)
+{
+    if (obs) vtk_launch<S, K, true>(L, cur, phase, u, w, rho, vort, stream, phi, st);
+    else vtk_launch<S, K, false>(L, cur, phase, u, w, rho, vort, stream, phi, st);
+    return cudaGetLastError();
+}
+
 template <typename S, typename K, int TXV, int TY, int N>
 void batch_launch(const Lattice *lats, const int *cur, const int4 *tiles, int ntiles, int parity, int grid,
                   cudaStream_t st)
@@ -214,6 +232,7 @@ KernelTable make_table()
     t.residual = &residual<S, K>;
     t.draglift = &draglift<S, K>;
     t.fields = &fields<S, K>;
+    t.vtk = &vtk<S, K>;
     t.batch_step = &batch_step<S, K>;
     return t;
 }

@@ -41,6 +41,8 @@ struct KernelTable {
                               int grid, cudaStream_t st);
     cudaError_t (*fields)(const Lattice &L, int cur, int phase, bool obs, double *rho, double *u, double *v,
                           cudaStream_t st);
+    cudaError_t (*vtk)(const Lattice &L, int cur, int phase, bool obs, float *u, float *w, float *rho, float *vort,
+                       float *stream, float *phi, cudaStream_t st);
 };
 
 KernelTable table_f32_f32();

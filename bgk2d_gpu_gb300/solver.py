@@ -212,6 +212,16 @@ class Solver:
     def set_tile(self, cfg):
         self._check(self._L.bgk_set_tile(self._h, int(cfg)), "set_tile")
 
+    def vtk_fields(self):
+        """The VTK writers' float32 fields computed on the device: (u, w, rho) as (ly, lx) and
+        (vorticity, stream) as (ly-2, lx-2) (SRC/vtk_xy.binary.F90, SRC/vtk_om.binary.F90)."""
+        lx, ly = self.lx, self.ly
+        u = np.empty((ly, lx), np.float32); w = np.empty_like(u); r = np.empty_like(u)
+        om = np.empty((ly - 2, lx - 2), np.float32); st = np.empty_like(om)
+        fp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        self._check(self._L.bgk_vtk_fields(self._h, fp(u), fp(w), fp(r), fp(om), fp(st)), "vtk_fields")
+        return u, w, r, om, st
+
     def set_prefetch(self, blocks_ahead):
         self._check(self._L.bgk_set_prefetch(self._h, int(blocks_ahead)), "set_prefetch")
 

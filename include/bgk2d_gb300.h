@@ -159,6 +159,15 @@ int bgk_residual(bgk_handle *h, double *out);
 int bgk_fields(bgk_handle *h, double *rho, double *u, double *v);
 /* obstacle mask obs(1:lx,1:ly) and imin,imax,jmin,jmax,nobs (SRC/build.obs.F90) */
 int bgk_get_obs(bgk_handle *h, int32_t *mask, int32_t bbox[5]);
+/* The fields the reference's VTK writers compute on the host after a device-to-host update
+ * (SRC/vtk_xy.binary.F90:75-140, SRC/vtk_om.binary.F90:62-150), computed on the device in their
+ * single-precision arithmetic, so that 5 float fields cross the bus instead of 9 populations:
+ * u/rho, w/rho, rho over the interior (lx*ly each, x fastest), vorticity and stream function over
+ * x = 2..lx-1, y = 2..ly-1 ((lx-2)*(ly-2) each).  The stream function integrates from row 1: the
+ * reference starts at ghost row 0, whose values the fused step keeps nowhere (in the reference's
+ * FUSED build that term reads the ghost row of the buffer written two steps earlier).  Any
+ * output pointer may be NULL. */
+int bgk_vtk_fields(bgk_handle *h, float *u, float *w, float *rho, float *vort, float *stream);
 /* omega, fgrad, u00, u0 after build_bcond + hencol, and the step counter */
 int bgk_get_scalars(bgk_handle *h, double out[4], int64_t *itime);
 

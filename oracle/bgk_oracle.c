@@ -173,3 +173,7 @@ void orc_prof_j(const orc_state *s, int icoord, double *u, double *v, double *de
     DISPATCH(s, prof_j, (s, icoord, u, v, den));
 }
 void orc_fields(const orc_state *s, double *rho, double *u, double *v) { DISPATCH(s, fields, (s, rho, u, v)); }
+void orc_vtk(const orc_state *s, int from_ghost_row, float *u, float *w, float *rho, float *vort, float *stream)
+{
+    DISPATCH(s, vtk, (s, from_ghost_row, u, w, rho, vort, stream));
+}

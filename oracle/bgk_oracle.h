@@ -90,6 +90,11 @@ void orc_draglift(const orc_state *s, int mode, double out[2]);
 void orc_prof_j(const orc_state *s, int icoord, double *u, double *v, double *den);
 /* macroscopic fields over the interior, l*m each, i fastest (diagno's per-cell arithmetic) */
 void orc_fields(const orc_state *s, double *rho, double *u, double *v);
+/* the VTK writers' single-precision fields (SRC/vtk_xy.binary.F90, SRC/vtk_om.binary.F90): u, w,
+ * rho over 1..l x 1..m (l*m each); vorticity and stream function over 2..l-1 x 2..m-1
+ * ((l-2)*(m-2) each); i fastest.  from_ghost_row = 1 integrates the stream function from ghost
+ * row 0 as the reference does, 0 from row 1 */
+void orc_vtk(const orc_state *s, int from_ghost_row, float *u, float *w, float *rho, float *vort, float *stream);
 
 #ifdef __cplusplus
 }

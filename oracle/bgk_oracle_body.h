@@ -599,6 +599,62 @@ static void FN(prof_j)(const orc_state *s, int icoord, double *u, double *v, dou
     }
 }
 
+/* SRC/vtk_xy.binary.F90:75-140 and SRC/vtk_om.binary.F90:62-150: the VTK writers' fields in
+ * real(sp).  Sums of stored values run in the storage kind S (mystorage, not mykind: float in
+ * MIXED2) and are then rounded to sp; the
+ * vorticity's quotients divide a storage-kind numerator by an sp denominator in the wider kind. */
+static inline float FN(vtk_den)(const orc_state *s, int i, int j)
+{
+    S t = ((((((((A_(0, i, j) + A_(1, i, j)) + A_(2, i, j)) + A_(3, i, j)) + A_(4, i, j)) + A_(5, i, j)) + A_(6, i, j)) +
+            A_(7, i, j)) + A_(8, i, j));
+    return (float)(t + (S)1.0f);
+}
+static inline S FN(vtk_u)(const orc_state *s, int i, int j)
+{
+    return ((((A_(0, i, j) + A_(1, i, j)) + A_(2, i, j)) - A_(4, i, j)) - A_(5, i, j)) - A_(6, i, j);
+}
+static inline S FN(vtk_v)(const orc_state *s, int i, int j)
+{
+    return ((((A_(1, i, j) + A_(3, i, j)) + A_(5, i, j)) - A_(0, i, j)) - A_(4, i, j)) - A_(7, i, j);
+}
+static void FN(vtk)(const orc_state *s, int from_ghost_row, float *u, float *w, float *rho, float *vort, float *stream)
+{
+    const int l = s->l, m = s->m;
+    for (int j = 1; j <= m; ++j)
+        for (int i = 1; i <= l; ++i) {
+            const size_t k = (size_t)(i - 1) + (size_t)(j - 1) * (size_t)l;
+            const float den = FN(vtk_den)(s, i, j);
+            u[k] = (float)FN(vtk_u)(s, i, j) / den;
+            w[k] = (float)FN(vtk_v)(s, i, j) / den;
+            rho[k] = den;
+        }
+    float *phi = (float *)malloc(sizeof(float) * (size_t)(m + 2));
+    float prev = 0.0f;
+    phi[0] = 0.0f;
+    for (int j = from_ghost_row ? 0 : 1; j <= m; ++j) {  /* column integral of u at i = 1 */
+        const float den = FN(vtk_den)(s, 1, j);
+        const float uv = (float)FN(vtk_u)(s, 1, j);
+        phi[j] = prev + uv / den;
+        prev = phi[j];
+    }
+    for (int j = 2; j <= m - 1; ++j)
+        for (int i = 2; i <= l - 1; ++i) {
+            const size_t k = (size_t)(i - 2) + (size_t)(j - 2) * (size_t)(l - 2);
+            const float d_up = FN(vtk_den)(s, i, j + 1), d_down = FN(vtk_den)(s, i, j - 1);
+            const float d_left = FN(vtk_den)(s, i - 1, j), d_right = FN(vtk_den)(s, i + 1, j);
+            const float up1 = (float)(FN(vtk_u)(s, i, j + 1) / (S)d_up);
+            const float down1 = (float)(FN(vtk_u)(s, i, j - 1) / (S)d_down);
+            const float left1 = (float)(FN(vtk_v)(s, i - 1, j) / (S)d_left);
+            const float right1 = (float)(FN(vtk_v)(s, i + 1, j) / (S)d_right);
+            vort[k] = 0.5f * (up1 - down1) - 0.5f * (right1 - left1);
+            const float den = FN(vtk_den)(s, i, j);
+            const float vv = (float)FN(vtk_v)(s, i, j);
+            phi[j] = phi[j] - vv / den;
+            stream[k] = phi[j];
+        }
+    free(phi);
+}
+
 static void FN(fields)(const orc_state *s, double *rho, double *u, double *v)
 {
     for (int j = 1; j <= s->m; ++j) {

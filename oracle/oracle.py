@@ -77,6 +77,8 @@ def lib():
         L.orc_draglift.argtypes = [P, ctypes.c_int, dp]
         L.orc_prof_j.argtypes = [P, ctypes.c_int, dp, dp, dp]
         L.orc_fields.argtypes = [P, dp, dp, dp]
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.orc_vtk.argtypes = [P, ctypes.c_int, fp, fp, fp, fp, fp]
         _lib = L
     return _lib
 
@@ -174,6 +176,17 @@ class Oracle:
         lib().orc_fields(self._h, _dp(r), _dp(u), _dp(v))
         sh = (self.m, self.l)
         return r.reshape(sh), u.reshape(sh), v.reshape(sh)
+
+
+    def vtk(self, from_ghost_row=True):
+        """The VTK writers' float32 fields: u, w, rho as (m, l); vorticity, stream as (m-2, l-2)."""
+        l, m = self.l, self.m
+        u = np.empty(l * m, np.float32); w = np.empty_like(u); r = np.empty_like(u)
+        om = np.empty((l - 2) * (m - 2), np.float32); st = np.empty_like(om)
+        fp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        lib().orc_vtk(self._h, int(from_ghost_row), fp(u), fp(w), fp(r), fp(om), fp(st))
+        return (u.reshape(m, l), w.reshape(m, l), r.reshape(m, l), om.reshape(m - 2, l - 2),
+                st.reshape(m - 2, l - 2))
 
 
 def build_obs(l, m, shape, radius, icoord=-1, jcoord=-1, prec=SINGLE):

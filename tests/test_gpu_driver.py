@@ -14,7 +14,7 @@ ly = {ly}
 svisc={svisc}
 u0=0.1
 itfin={itfin}
-ivtim=1000000
+ivtim={ivtim}
 isignal={isignal}
 itsave={itsave}
 icheck={icheck}
@@ -28,7 +28,7 @@ def run_driver(bgk, tmp, case="LDC", prec="single", **kw):
     from bgk2d_gpu_gb300 import build
     exe = build.EXE_PATH
     assert os.path.exists(exe)
-    p = dict(lx=64, ly=48, svisc=0.0384, itfin=300, isignal=100, itsave=150, icheck=100, irestart=0)
+    p = dict(lx=64, ly=48, svisc=0.0384, itfin=300, isignal=100, itsave=150, icheck=100, irestart=0, ivtim=1000000)
     p.update(kw)
     (tmp / "bgk.input").write_text(NAMELIST.format(**p))
     r = subprocess.run([exe, "--input", str(tmp / "bgk.input"), "--case", case, "--prec", prec, "--dir", str(tmp)],
@@ -76,3 +76,48 @@ def test_driver_vks_writes_drag_lift(bgk, tmp_path):
     run_driver(bgk, tmp_path, case="VKS", lx=160, ly=62, svisc=0.05, itfin=200, itsave=1000000)
     rows = [ln.split() for ln in (tmp_path / "drag.lift.dat").read_text().splitlines()]
     assert len(rows) == 3 and all(np.isfinite(float(x)) for r in rows for x in r[1:])
+
+
+def _vtk_sections(path):
+    """(header lines, {section name: float32 array}) of a legacy binary VTK file as written by
+    SRC/vtk_xy.binary.F90 / vtk_om.binary.F90."""
+    data = path.read_bytes()
+    head = data.split(b"POINT_DATA", 1)
+    lines = head[0].decode().splitlines()
+    rest = b"POINT_DATA" + head[1]
+    eol = rest.index(b"\n")
+    npts = int(rest[10:eol])
+    rest = rest[eol + 1:]
+    out = {}
+    while rest:
+        eol = rest.index(b"\n")
+        title = rest[:eol].decode().strip()
+        rest = rest[eol + 1:]
+        count = npts
+        if title.startswith("SCALARS"):
+            eol = rest.index(b"\n")
+            assert rest[:eol].decode().strip() == "LOOKUP_TABLE default"
+            rest = rest[eol + 1:]
+        else:
+            count = 3 * npts
+        out[title.split()[1]] = np.frombuffer(rest[:4 * count], dtype=">f4")
+        rest = rest[4 * count:]
+    return lines, npts, out
+
+
+def test_driver_vtk_files(bgk, tmp_path):
+    """tec_xy / tec_om files at the ivtim cadence, with the reference writers' header and the
+    device-computed fields (big-endian float32)."""
+    p = run_driver(bgk, tmp_path, itfin=200, ivtim=100)
+    lx, ly = p["lx"], p["ly"]
+    lines, npts, xy = _vtk_sections(tmp_path / "tec_xy.00000200.vtk")
+    assert lines[:4] == ["# vtk DataFile Version 2.0", "Campo", "BINARY", "DATASET STRUCTURED_POINTS"]
+    assert lines[4] == "DIMENSIONS %10d %10d %10d" % (lx, ly, 1) and npts == lx * ly
+    _, npts2, om = _vtk_sections(tmp_path / "tec_om.00000200.vtk")
+    assert npts2 == (lx - 2) * (ly - 2) and (tmp_path / "tec_xy.00000100.vtk").exists()
+    with bgk.Solver(lx, ly, tcase="LDC", svisc=p["svisc"], u0=0.1) as s:
+        s.step(200)
+        u, w, r, vort, st = s.vtk_fields()
+    assert np.array_equal(xy["u"], u.ravel()) and np.array_equal(xy["rho"], r.ravel())
+    assert np.array_equal(xy["velocity"][1::3], w.ravel())
+    assert np.array_equal(om["vorticity"], vort.ravel()) and np.array_equal(om["stream"], st.ravel())
