@@ -712,12 +712,12 @@ int bgk_tune(bgk_handle *h, int32_t trial_steps, int32_t *tile_cfg, int32_t *ste
     int64_t run = 0;
     int sms = 0;
     CK(h, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->dev));
-    // L2 prefetch distances for the register-vector ping-pong kernels: off, half a wave and one
-    // wave of 8 resident blocks per SM ahead
+    // L2 prefetch distances for the register-vector ping-pong and AA kernels: off, half a wave
+    // and one wave of 8 resident blocks per SM ahead
     const int pfs[3] = {0, 4 * sms, 8 * sms};
     const int ncfg = h->L.scheme == BGK_SCHEME_PINGPONG ? NUM_STEP_CFG : NUM_CFG;
     for (int c = 0; c < ncfg; ++c) {
-        const int npf = (h->L.scheme == BGK_SCHEME_PINGPONG && c < NUM_CFG && !h->L.les) ? 3 : 1;
+        const int npf = (c < NUM_CFG && !h->L.les) ? 3 : 1;
         for (int p = 0; p < npf; ++p) {
             if ((rc = bgk_set_tile(h, c)) || (rc = bgk_set_prefetch(h, pfs[p]))) return rc;
             for (int s = 0; s < 2; ++s)

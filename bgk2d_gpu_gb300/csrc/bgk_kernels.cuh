@@ -528,8 +528,12 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
 
 // Bulk prefetch into L2 of the source segments of the block L.pf_ahead places further on in
 // launch order (one row of one plane per thread, 9 * TY threads): by the time that block runs,
-// its loads hit L2 instead of HBM.
-template <typename S, int TXV, int TY, int N>
+// its loads hit L2 instead of HBM.  Which plane and row a direction reads: ping-pong, plane q of
+// the source buffer at row y - c_q.y; AA P step, plane opp(q) at row y - c_q.y; AA L step, plane q
+// at row y.
+enum PrefetchKind { PF_PP = 0, PF_AA_P = 1, PF_AA_L = 2 };
+
+template <typename S, int TXV, int TY, int N, int KIND>
 __device__ __forceinline__ void prefetch_tile(const Lattice &L, const int parity)
 {
     constexpr int VEC = vec_of<S>();
@@ -540,20 +544,21 @@ __device__ __forceinline__ void prefetch_tile(const Lattice &L, const int parity
     const int bx = (int)(lin % gridDim.x), by = (int)(lin / gridDim.x);
     const int q = t % 9, y = by * TY + t / 9 + 1;
     if (y > L.ly) return;
-    const int row = y - cy_of(q);
+    const int row = KIND == PF_AA_L ? y : y - cy_of(q);
+    const int plane = KIND == PF_PP ? (parity ? 9 : 0) + q : KIND == PF_AA_P ? opp_of(q) : q;
     const int x0 = 1 + bx * TXV * N;
     const int x1 = min(x0 + TXV * N, L.lx + 1);
     const int64_t rs = (int64_t)row * L.pitch;
     const int64_t lo = (cell_index<S>(L, x0 - 1, row) - rs) / VEC * VEC;
     const int64_t hi = min((int64_t)L.pitch, (cell_index<S>(L, x1, row) - rs) / VEC * VEC + VEC);
-    const S *p = reinterpret_cast<const S *>(L.planes) + ((parity ? 9 : 0) + q) * L.plane_elems + rs + lo;
+    const S *p = reinterpret_cast<const S *>(L.planes) + plane * L.plane_elems + rs + lo;
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"((uint32_t)((hi - lo) * sizeof(S))) : "memory");
 }
 
 template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N, bool LES = false>
 __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 || (sizeof(S) == 4 && N == 4)) ? 8 : (sizeof(S) == 2 ? 4 : 1)) pp_kernel(const Lattice L, const int parity)
 {
-    if (L.pf_ahead > 0) prefetch_tile<S, TXV, TY, N>(L, parity);
+    if (L.pf_ahead > 0) prefetch_tile<S, TXV, TY, N, PF_PP>(L, parity);
     pp_tile<S, K, TXV, TY, HAS_OBS, N, LES>(L, blockIdx.x, blockIdx.y, parity);
 }
 
@@ -854,6 +859,7 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ?
 {
     constexpr int VEC = vec_of<S>();
     constexpr int W = TXV < 32 ? TXV : 32;
+    if (L.pf_ahead > 0) prefetch_tile<S, TXV, TY, VEC, PF_AA_P>(L, 0);
     const int tx = threadIdx.x;
     const int k = blockIdx.x * TXV + tx;
     const int y = blockIdx.y * TY + threadIdx.y + 1;
@@ -920,6 +926,7 @@ template <typename S, typename K, int TXV, int TY, bool HAS_OBS, bool LES = fals
 __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ? 4 : 1) aa_l_kernel(const Lattice L)
 {
     constexpr int VEC = vec_of<S>();
+    if (L.pf_ahead > 0) prefetch_tile<S, TXV, TY, VEC, PF_AA_L>(L, 0);
     const int k = blockIdx.x * TXV + threadIdx.x;
     const int y = blockIdx.y * TY + threadIdx.y + 1;
     if (y > L.ly || k >= L.nvec) return;

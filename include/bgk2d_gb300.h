@@ -179,9 +179,9 @@ int bgk_get_scalars(bgk_handle *h, double out[4], int64_t *itime);
  *   such a step reports BGK_E_TIMEOUT at the next synchronisation if a copy never completed.
  *   Results do not depend on the choice. */
 int bgk_set_tile(bgk_handle *h, int32_t tile_cfg);
-/* ping-pong configurations 0-5: each block first asks for an L2 prefetch (bulk, no registers)
- * of the source rows of the block `blocks_ahead` places further on in launch order; 0 = off
- * (no reference counterpart).  Results do not depend on it. */
+/* configurations 0-5 (ping-pong and AA): each block first asks for an L2 prefetch (bulk, no
+ * registers) of the source rows of the block `blocks_ahead` places further on in launch order;
+ * 0 = off (no reference counterpart).  Results do not depend on it. */
 int bgk_set_prefetch(bgk_handle *h, int32_t blocks_ahead);
 int bgk_get_prefetch(bgk_handle *h, int32_t *blocks_ahead);
 /* time `trial_steps` real steps per tile shape and prefetch distance (the state advances) and

@@ -240,12 +240,13 @@ def test_bfs_rejects_aa_and_batches(bgk):
         assert e.value.code == _lib.E_UNSUPPORTED
 
 
+@pytest.mark.parametrize("scheme", ["pingpong", "aa"])
 @pytest.mark.parametrize("storage", ["f32", "f16"])
-def test_prefetch_does_not_change_results(bgk, storage):
+def test_prefetch_does_not_change_results(bgk, storage, scheme):
     """The L2 prefetch only moves data earlier; populations are identical with and without it."""
     out = []
     for pf in (0, 64, 1216):
-        with bgk.Solver(700, 300, tcase="LDC", svisc=0.02, u0=0.1, storage=storage) as s:
+        with bgk.Solver(700, 300, tcase="LDC", svisc=0.02, u0=0.1, storage=storage, scheme=scheme) as s:
             s.set_tile(5)
             s.set_prefetch(pf)
             assert s.prefetch() == pf
