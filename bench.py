@@ -214,8 +214,13 @@ def bench_precision(bgk, dev, n=2048, steps=10000):
     t_dec = int(round(int(steps / (n * np.sqrt(3) / 2)) * n * np.sqrt(3) / 2))
 
     def run(st):
-        with bgk.Solver(n, n, tcase="TGV", storage=st, omega=1.0 / tau, svisc=nu, u0=0.0, init="tgv", tgv_u0=u0,
-                        device=dev) as s:
+        kw = dict(tcase="TGV", storage=st, omega=1.0 / tau, svisc=nu, u0=0.0, init="tgv", tgv_u0=u0, device=dev)
+        with bgk.Solver(n, n, **kw) as t:  # tuned on a separate copy: the measured run keeps its step count
+            cfg, _ = t.tune(4 if st == "f64" else 8)
+            pf = t.prefetch()
+        with bgk.Solver(n, n, **kw) as s:
+            s.set_tile(cfg)
+            s.set_prefetch(pf)
             _, ui, vi = s.fields()
             ms = s.step_timed(t_dec)
             _, ud, vd = s.fields()

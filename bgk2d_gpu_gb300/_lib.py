@@ -130,6 +130,7 @@ def load(build_if_missing: bool = True):
         "bgk_batch_step_timed": (I32, [VP, I32, P(ctypes.c_float)]),
         "bgk_batch_sync": (I32, [VP]),
         "bgk_batch_set_config": (I32, [VP, I32, I32, I32]),
+        "bgk_batch_set_prefetch": (I32, [VP, I32]),
         "bgk_batch_get_config": (I32, [VP, P(I32)]),
         "bgk_batch_tune": (I32, [VP, I32, P(I32)]),
         "bgk_batch_launch_count": (I32, [VP, P(I64)]),

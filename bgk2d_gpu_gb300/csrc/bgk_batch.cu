@@ -33,6 +33,7 @@ struct bgk_batch {
     int cfg = 2;                    // tile shape index (TILE_CFGS)
     int blocks_per_sm = 8;
     int graph_steps = 32;           // even
+    int pf = 0;                     // one-block-per-tile kernel: L2 prefetch this many tiles ahead
     int sms = 152;
     int64_t launches = 0;
     int64_t steps = 0;
@@ -112,7 +113,8 @@ int grid_of(const bgk_batch *b)
 int launch_one(bgk_batch *b, int parity)
 {
     if (b->ntiles == 0) return BGK_OK;
-    if (b->T.batch_step(b->d_lats, b->d_cur, b->d_tiles, b->ntiles, parity, b->cfg, grid_of(b), b->st) != cudaSuccess)
+    if (b->T.batch_step(b->d_lats, b->d_cur, b->d_tiles, b->ntiles, parity, b->cfg, grid_of(b), b->pf, b->st) !=
+        cudaSuccess)
         return BGK_E_CUDA;
     b->launches++;
     return BGK_OK;
@@ -314,6 +316,14 @@ int bgk_batch_set_config(bgk_batch *b, int32_t tile_cfg, int32_t blocks_per_sm, 
     return BGK_OK;
 }
 
+int bgk_batch_set_prefetch(bgk_batch *b, int32_t tiles_ahead)
+{
+    if (!b || tiles_ahead < 0) return BGK_E_INVALID;
+    if (tiles_ahead != b->pf) b->graph_built_for = -1;
+    b->pf = tiles_ahead;
+    return BGK_OK;
+}
+
 int bgk_batch_get_config(bgk_batch *b, int32_t out[3])
 {
     if (!b || !out) return BGK_E_INVALID;
@@ -321,8 +331,9 @@ int bgk_batch_get_config(bgk_batch *b, int32_t out[3])
     return BGK_OK;
 }
 
-// Autotuner: times `trial_steps` real steps (they advance the members) for every tile shape
-// and persistent grid size, then the steps-per-graph candidates, and keeps the fastest.
+// Autotuner: times `trial_steps` real steps (they advance the members) for every tile shape and
+// persistent grid size (and, with one block per tile, L2 prefetch distance), then the
+// steps-per-graph candidates, and keeps the fastest.
 int bgk_batch_tune(bgk_batch *b, int32_t trial_steps, int32_t *steps_run)
 {
     if (!b || trial_steps < 2) return BGK_E_INVALID;
@@ -330,12 +341,14 @@ int bgk_batch_tune(bgk_batch *b, int32_t trial_steps, int32_t *steps_run)
     int64_t run = 0;
     const int bps_opts[4] = {0, 4, 8, 16};
     float best = 1e30f;
-    int best_cfg = b->cfg, best_bps = b->blocks_per_sm;
+    int best_cfg = b->cfg, best_bps = b->blocks_per_sm, best_pf = b->pf;
     const int n = trial_steps & ~1;
+    const int pf_opts[3] = {0, 4 * b->sms, 8 * b->sms};
     for (int c = 0; c < NUM_CFG; ++c) {
-        for (int bi = 0; bi < 4; ++bi) {
-            int rc = bgk_batch_set_config(b, c, bps_opts[bi], b->graph_steps);
-            if (rc) return rc;
+        for (int bi = 0; bi < 6; ++bi) {
+            const int bps = bps_opts[bi < 3 ? 0 : bi - 2], pf = bi < 3 ? pf_opts[bi] : 0;
+            int rc = bgk_batch_set_config(b, c, bps, b->graph_steps);
+            if (rc || (rc = bgk_batch_set_prefetch(b, pf))) return rc;
             if ((rc = rebuild(b))) return rc;
             if ((rc = step_impl(b, 2, false))) return rc;  // warm-up at this shape
             run += 2;
@@ -346,12 +359,13 @@ int bgk_batch_tune(bgk_batch *b, int32_t trial_steps, int32_t *steps_run)
             if (cudaEventRecord(b->ev1, b->st) != cudaSuccess || cudaEventSynchronize(b->ev1) != cudaSuccess ||
                 cudaEventElapsedTime(&ms, b->ev0, b->ev1) != cudaSuccess)
                 return BGK_E_CUDA;
-            if (ms < best) { best = ms; best_cfg = c; best_bps = bps_opts[bi]; }
+            if (ms < best) { best = ms; best_cfg = c; best_bps = bps; best_pf = pf; }
         }
     }
     const int g_opts[3] = {8, 32, 128};
     float gbest = 1e30f;
     int best_g = b->graph_steps;
+    if (int rc = bgk_batch_set_prefetch(b, best_pf)) return rc;
     for (int gi = 0; gi < 3; ++gi) {
         int rc = bgk_batch_set_config(b, best_cfg, best_bps, g_opts[gi]);
         if (rc) return rc;

@@ -192,26 +192,27 @@ cudaError_t vtk(const Lattice &L, int cur, int phase, bool obs, float *u, float 
 }
 
 template <typename S, typename K, int TXV, int TY, int N>
-void batch_launch(const Lattice *lats, const int *cur, const int4 *tiles, int ntiles, int parity, int grid,
+void batch_launch(const Lattice *lats, const int *cur, const int4 *tiles, int ntiles, int parity, int grid, int pf,
                   cudaStream_t st)
 {
-    if (grid <= 0) batch_pp_flat_kernel<S, K, TXV, TY, N><<<ntiles, dim3(TXV, TY), 0, st>>>(lats, cur, tiles, parity);
+    if (grid <= 0)
+        batch_pp_flat_kernel<S, K, TXV, TY, N><<<ntiles, dim3(TXV, TY), 0, st>>>(lats, cur, tiles, ntiles, parity, pf);
     else batch_pp_kernel<S, K, TXV, TY, N><<<grid, dim3(TXV, TY), 0, st>>>(lats, cur, tiles, ntiles, parity);
 }
 
 // grid <= 0: one block per tile; otherwise a persistent grid walking contiguous chunks
 template <typename S, typename K>
 cudaError_t batch_step(const Lattice *lats, const int *cur, const int4 *tiles, int ntiles, int parity, int cfg, int grid,
-                       cudaStream_t st)
+                       int pf, cudaStream_t st)
 {
     constexpr int V = vec_of<S>();
     switch (cfg) {
-    case 0: batch_launch<S, K, 32, 4, V>(lats, cur, tiles, ntiles, parity, grid, st); break;
-    case 1: batch_launch<S, K, 64, 2, V>(lats, cur, tiles, ntiles, parity, grid, st); break;
-    case 3: batch_launch<S, K, 128, 2, V>(lats, cur, tiles, ntiles, parity, grid, st); break;
-    case 4: batch_launch<S, K, 32, 4, V / 2>(lats, cur, tiles, ntiles, parity, grid, st); break;
-    case 5: batch_launch<S, K, 128, 1, V / 2>(lats, cur, tiles, ntiles, parity, grid, st); break;
-    default: batch_launch<S, K, 128, 1, V>(lats, cur, tiles, ntiles, parity, grid, st); break;
+    case 0: batch_launch<S, K, 32, 4, V>(lats, cur, tiles, ntiles, parity, grid, pf, st); break;
+    case 1: batch_launch<S, K, 64, 2, V>(lats, cur, tiles, ntiles, parity, grid, pf, st); break;
+    case 3: batch_launch<S, K, 128, 2, V>(lats, cur, tiles, ntiles, parity, grid, pf, st); break;
+    case 4: batch_launch<S, K, 32, 4, V / 2>(lats, cur, tiles, ntiles, parity, grid, pf, st); break;
+    case 5: batch_launch<S, K, 128, 1, V / 2>(lats, cur, tiles, ntiles, parity, grid, pf, st); break;
+    default: batch_launch<S, K, 128, 1, V>(lats, cur, tiles, ntiles, parity, grid, pf, st); break;
     }
     return cudaGetLastError();
 }

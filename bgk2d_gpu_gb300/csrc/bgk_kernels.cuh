@@ -533,15 +533,12 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
 // at row y.
 enum PrefetchKind { PF_PP = 0, PF_AA_P = 1, PF_AA_L = 2 };
 
+// segment of thread t (< 9 * TY) of tile (bx, by) of lattice L
 template <typename S, int TXV, int TY, int N, int KIND>
-__device__ __forceinline__ void prefetch_tile(const Lattice &L, const int parity)
+__device__ __forceinline__ void prefetch_segment(const Lattice &L, const int parity, const int t, const int bx,
+                                                 const int by)
 {
     constexpr int VEC = vec_of<S>();
-    const int t = threadIdx.x + threadIdx.y * TXV;
-    if (t >= 9 * TY) return;
-    const long long lin = (long long)blockIdx.y * gridDim.x + blockIdx.x + L.pf_ahead;
-    if (lin >= (long long)gridDim.x * gridDim.y) return;
-    const int bx = (int)(lin % gridDim.x), by = (int)(lin / gridDim.x);
     const int q = t % 9, y = by * TY + t / 9 + 1;
     if (y > L.ly) return;
     const int row = KIND == PF_AA_L ? y : y - cy_of(q);
@@ -553,6 +550,16 @@ __device__ __forceinline__ void prefetch_tile(const Lattice &L, const int parity
     const int64_t hi = min((int64_t)L.pitch, (cell_index<S>(L, x1, row) - rs) / VEC * VEC + VEC);
     const S *p = reinterpret_cast<const S *>(L.planes) + plane * L.plane_elems + rs + lo;
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"((uint32_t)((hi - lo) * sizeof(S))) : "memory");
+}
+
+template <typename S, int TXV, int TY, int N, int KIND>
+__device__ __forceinline__ void prefetch_tile(const Lattice &L, const int parity)
+{
+    const int t = threadIdx.x + threadIdx.y * TXV;
+    if (t >= 9 * TY) return;
+    const long long lin = (long long)blockIdx.y * gridDim.x + blockIdx.x + L.pf_ahead;
+    if (lin >= (long long)gridDim.x * gridDim.y) return;
+    prefetch_segment<S, TXV, TY, N, KIND>(L, parity, t, (int)(lin % gridDim.x), (int)(lin / gridDim.x));
 }
 
 template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N, bool LES = false>
@@ -995,8 +1002,16 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ?
 template <typename S, typename K, int TXV, int TY, int N>
 __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 || (sizeof(S) == 4 && N == 4)) ? 8 : (sizeof(S) == 2 ? 4 : 1))
     batch_pp_flat_kernel(const Lattice *__restrict__ lats, const int *__restrict__ cur, const int4 *__restrict__ tiles,
-                         const int parity)
+                         const int ntiles, const int parity, const int pf)
 {
+    if (pf > 0) {  // L2 prefetch of the work-list entry pf places ahead (see prefetch_tile)
+        const int t = threadIdx.x + threadIdx.y * TXV;
+        const int ahead = blockIdx.x + pf;
+        if (t < 9 * TY && ahead < ntiles) {
+            const int4 ta = __ldg(tiles + ahead);
+            prefetch_segment<S, TXV, TY, N, PF_PP>(lats[ta.x], __ldg(cur + ta.x) ^ parity, t, ta.y, ta.z);
+        }
+    }
     const int4 tile = __ldg(tiles + blockIdx.x);
     const Lattice &L = lats[tile.x];
     pp_tile<S, K, TXV, TY, true, N>(L, tile.y, tile.z, __ldg(cur + tile.x) ^ parity);

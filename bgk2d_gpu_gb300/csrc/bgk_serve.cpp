@@ -135,11 +135,14 @@ bgk_batch *batch_for(bgk_server *S, int storage)
     bgk_batch *b = nullptr;
     const int compute = storage == BGK_STORE_F64 ? BGK_COMPUTE_F64 : BGK_COMPUTE_F32;
     if (bgk_batch_create(storage, compute, S->cfg.device, &b) != BGK_OK) return nullptr;
-    // one block per work-list tile; 8 bytes per thread for the 16-bit kinds (measured on a mixed
-    // cavity / cylinder / Taylor-Green batch: FP32 89 GLUPS, FP16 142, against 54 and 62 with
-    // the persistent grid)
+    // one block per work-list tile with an L2 prefetch of the tile half a wave (FP32) or a wave
+    // (16-bit, 8 bytes per thread) ahead: on a mixed cavity / cylinder / Taylor-Green batch FP32
+    // 90.7 GLUPS and FP16 148.6, against 54 and 62 with the persistent grid
     const bool half = storage == BGK_STORE_F16 || storage == BGK_STORE_BF16;
-    bgk_batch_set_config(b, S->cfg.tile_cfg >= 0 ? S->cfg.tile_cfg : (half ? 4 : 0), 0, 32);
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, S->cfg.device);
+    bgk_batch_set_config(b, S->cfg.tile_cfg >= 0 ? S->cfg.tile_cfg : (half ? 5 : 1), 0, 32);
+    bgk_batch_set_prefetch(b, (half ? 8 : 4) * sms);
     S->batches[storage] = b;
     return b;
 }

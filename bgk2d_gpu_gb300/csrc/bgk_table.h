@@ -38,7 +38,7 @@ struct KernelTable {
     cudaError_t (*draglift)(const Lattice &L, int cur, int phase, int i0, int i1, int j0, int j1, double *partial,
                             int nb, cudaStream_t st);
     cudaError_t (*batch_step)(const Lattice *lats, const int *cur, const int4 *tiles, int ntiles, int parity, int cfg,
-                              int grid, cudaStream_t st);
+                              int grid, int pf, cudaStream_t st);
     cudaError_t (*fields)(const Lattice &L, int cur, int phase, bool obs, double *rho, double *u, double *v,
                           cudaStream_t st);
     cudaError_t (*vtk)(const Lattice &L, int cur, int phase, bool obs, float *u, float *w, float *rho, float *vort,

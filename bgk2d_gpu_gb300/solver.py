@@ -313,6 +313,9 @@ class Batch:
         self._check(self._L.bgk_batch_set_config(self._b, int(tile_cfg), int(blocks_per_sm), int(graph_steps)),
                     "batch_set_config")
 
+    def set_prefetch(self, tiles_ahead):
+        self._check(self._L.bgk_batch_set_prefetch(self._b, int(tiles_ahead)), "batch_set_prefetch")
+
     def config(self):
         out = (ctypes.c_int32 * 3)()
         self._check(self._L.bgk_batch_get_config(self._b, out), "batch_get_config")

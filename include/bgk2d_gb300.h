@@ -231,6 +231,9 @@ int bgk_batch_sync(bgk_batch *b);
 /* tile shape (as bgk_set_tile), persistent blocks per SM (0: one block per work-list tile,
  * no persistent loop), steps per CUDA graph (even) */
 int bgk_batch_set_config(bgk_batch *b, int32_t tile_cfg, int32_t blocks_per_sm, int32_t graph_steps);
+/* one block per tile (blocks_per_sm = 0): L2 prefetch of the work-list entry `tiles_ahead` places
+ * further on (0 = off); the autotuner sets it */
+int bgk_batch_set_prefetch(bgk_batch *b, int32_t tiles_ahead);
 int bgk_batch_get_config(bgk_batch *b, int32_t out[3]);
 /* autotuner: times real steps over tile shapes, grid sizes and graph lengths; keeps the best */
 int bgk_batch_tune(bgk_batch *b, int32_t trial_steps, int32_t *steps_run);
@@ -277,8 +280,8 @@ typedef struct bgk_server_config {
     int32_t max_slots;       /* concurrently resident requests */
     int64_t hbm_budget;      /* bytes the server may hold; <= 0: free HBM minus 4 GiB */
     int32_t chunk_steps;     /* steps per scheduling round (upper bound) */
-    int32_t tile_cfg;        /* batch tile shape (bgk_set_tile numbering, 0..5); < 0 selects 32x4,
-                                with 8 bytes per thread for the 16-bit kinds */
+    int32_t tile_cfg;        /* batch tile shape (bgk_set_tile numbering, 0..5); < 0 selects 64x2
+                                (FP32/FP64) or 128x1 with 8 bytes per thread (16-bit) */
 } bgk_server_config;
 
 typedef struct bgk_server_stats {
