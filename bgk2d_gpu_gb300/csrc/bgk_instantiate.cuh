@@ -23,9 +23,11 @@ cudaError_t step_cfg(int kind, const Lattice &L, int parity, cudaStream_t st)
         const dim3 grid((unsigned)((nv + TXV - 1) / TXV), (unsigned)((L.ly + TY - 1) / TY));
         pp_kernel<S, K, TXV, TY, OBS, N><<<grid, block, 0, st>>>(L, parity);
     } else {
-        const dim3 grid((unsigned)((L.nvec + TXV - 1) / TXV), (unsigned)((L.ly + TY - 1) / TY));
-        if (kind == STEP_AA_P) aa_p_kernel<S, K, TXV, TY, OBS><<<grid, block, 0, st>>>(L);
-        else aa_l_kernel<S, K, TXV, TY, OBS><<<grid, block, 0, st>>>(L);
+        constexpr int N = vec_of<S>() / CDIV;
+        const int nv = (L.lx + N - 1) / N;
+        const dim3 grid((unsigned)((nv + TXV - 1) / TXV), (unsigned)((L.ly + TY - 1) / TY));
+        if (kind == STEP_AA_P) aa_p_kernel<S, K, TXV, TY, OBS, false, N><<<grid, block, 0, st>>>(L);
+        else aa_l_kernel<S, K, TXV, TY, OBS, false, N><<<grid, block, 0, st>>>(L);
     }
     return cudaGetLastError();
 }
@@ -84,12 +86,8 @@ cudaError_t step_obs(int kind, const Lattice &L, int parity, int cfg, cudaStream
     case 0: return step_cfg<S, K, 32, 4, OBS, 1>(kind, L, parity, st);
     case 1: return step_cfg<S, K, 64, 2, OBS, 1>(kind, L, parity, st);
     case 3: return step_cfg<S, K, 128, 2, OBS, 1>(kind, L, parity, st);
-    case 4:
-        if (kind == STEP_PP) return step_cfg<S, K, 32, 4, OBS, 2>(kind, L, parity, st);
-        return step_cfg<S, K, 32, 4, OBS, 1>(kind, L, parity, st);
-    case 5:
-        if (kind == STEP_PP) return step_cfg<S, K, 128, 1, OBS, 2>(kind, L, parity, st);
-        return step_cfg<S, K, 128, 1, OBS, 1>(kind, L, parity, st);
+    case 4: return step_cfg<S, K, 32, 4, OBS, 2>(kind, L, parity, st);
+    case 5: return step_cfg<S, K, 128, 1, OBS, 2>(kind, L, parity, st);
     default: return step_cfg<S, K, 128, 1, OBS, 1>(kind, L, parity, st);
     }
 }

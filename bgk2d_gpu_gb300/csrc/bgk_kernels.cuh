@@ -740,8 +740,8 @@ __device__ void aa_p_cell_slow(const Lattice &L, S *base, int x, int y)
 // come from the x ghost column are replaced; after the vector push the three pushes that leave
 // through the x face are redone with the push rules, and the incoming inflow/outflow values
 // are written.  C is the cell's position in the lane's vector.
-template <typename S, typename K, bool HAS_OBS, bool RAW, int C, bool LOW>
-__device__ __forceinline__ void aa_edge_pull(const Lattice &L, const S *base, int x, int y, K (&v)[9][vec_of<S>()])
+template <typename S, typename K, bool HAS_OBS, bool RAW, int C, bool LOW, int N>
+__device__ __forceinline__ void aa_edge_pull(const Lattice &L, const S *base, int x, int y, K (&v)[9][N])
 {
     const int64_t pe = L.plane_elems;
     const int64_t me = cell_index<S>(L, x, y);
@@ -759,8 +759,8 @@ __device__ __forceinline__ void aa_edge_pull(const Lattice &L, const S *base, in
     v[q2][C] = RAW ? (K)((float)c * scale_of(q2)) : c;
 }
 
-template <typename S, typename K, bool HAS_OBS, bool RAW, int C, bool LOW>
-__device__ __forceinline__ void aa_edge_push(const Lattice &L, S *base, int x, int y, const K (&v)[9][vec_of<S>()])
+template <typename S, typename K, bool HAS_OBS, bool RAW, int C, bool LOW, int N>
+__device__ __forceinline__ void aa_edge_push(const Lattice &L, S *base, int x, int y, const K (&v)[9][N])
 {
     K g[9];
 #pragma unroll
@@ -775,16 +775,15 @@ __device__ __forceinline__ void aa_edge_push(const Lattice &L, S *base, int x, i
     aa_incoming<S, K>(L, base, x, y, gr);
 }
 
-// push VEC values of direction q to (x + c_q) in plane q; lanes at an edge (segment end or a
+// push N values of direction q to (x + c_q) in plane q; lanes at an edge (segment end or a
 // neighbour on the slow path) store the elements that cross into the neighbour's vector.
 // 16-bit kinds (RAW) round the shifted vector in pairs, as it is stored, with the lane's pair
 // hash words `rh`; lone elements at an edge use the lone-value rounding.
-template <typename S, typename K, int q, int W, bool RAW = false>
+template <typename S, typename K, int q, int W, bool RAW, int N>
 __device__ __forceinline__ void push_vec(const Lattice &L, S *plane, int xv, int y, bool left_edge,
-                                         bool right_edge, const K (&g)[vec_of<S>()], bool store,
-                                         const uint32_t (&rh)[npair<vec_of<S>()>()])
+                                         bool right_edge, const K (&g)[N], bool store,
+                                         const uint32_t (&rh)[npair<N>()])
 {
-    constexpr int VEC = vec_of<S>();
     constexpr int cx = cx_of(q), cy = cy_of(q);
     const int64_t idx = cell_index<S>(L, xv, y + cy);
     auto cvt = [](K v) -> S {
@@ -792,87 +791,89 @@ __device__ __forceinline__ void push_vec(const Lattice &L, S *plane, int xv, int
         else return Store<S>::template put<K, q>(v);
     };
     if constexpr (RAW) {
-        static_assert(VEC == 8, "16-bit vectors hold 8 elements");
-        K sh[VEC];  // the vector as stored at idx
+        static_assert(N == 4 || N == 8, "16-bit vectors hold 4 or 8 elements");
+        K sh[N];  // the vector as stored at idx
         if (cx == 0) {
 #pragma unroll
-            for (int c = 0; c < VEC; ++c) sh[c] = g[c];
+            for (int c = 0; c < N; ++c) sh[c] = g[c];
         } else if (cx == 1) {
-            sh[0] = shfl_up(g[VEC - 1], W);
+            sh[0] = shfl_up(g[N - 1], W);
 #pragma unroll
-            for (int c = 1; c < VEC; ++c) sh[c] = g[c - 1];
+            for (int c = 1; c < N; ++c) sh[c] = g[c - 1];
         } else {
 #pragma unroll
-            for (int c = 0; c < VEC - 1; ++c) sh[c] = g[c + 1];
-            sh[VEC - 1] = shfl_down(g[0], W);
+            for (int c = 0; c < N - 1; ++c) sh[c] = g[c + 1];
+            sh[N - 1] = shfl_down(g[0], W);
         }
         if (!store) return;
         if (cx == 0 || (cx == 1 && !left_edge) || (cx == -1 && !right_edge)) {
-            uint4 u;
-            u.x = Store<S>::pack2_rs((float)sh[0], (float)sh[1], pair_bits<q>(rh[0]));
-            u.y = Store<S>::pack2_rs((float)sh[2], (float)sh[3], pair_bits<q>(rh[1]));
-            u.z = Store<S>::pack2_rs((float)sh[4], (float)sh[5], pair_bits<q>(rh[2]));
-            u.w = Store<S>::pack2_rs((float)sh[6], (float)sh[7], pair_bits<q>(rh[3]));
-            *reinterpret_cast<uint4 *>(plane + idx) = u;
+            using U = typename VecT<S, N>::U;
+            union { U u; uint32_t w[N / 2]; } t;
+#pragma unroll
+            for (int j = 0; j < N / 2; ++j)
+                t.w[j] = Store<S>::pack2_rs((float)sh[2 * j], (float)sh[2 * j + 1], pair_bits<q>(rh[j]));
+            *reinterpret_cast<U *>(plane + idx) = t.u;
         } else if (cx == 1) {
 #pragma unroll
-            for (int c = 0; c < VEC - 1; ++c) plane[idx + 1 + c] = cvt(g[c]);
+            for (int c = 0; c < N - 1; ++c) plane[idx + 1 + c] = cvt(g[c]);
         } else {
 #pragma unroll
-            for (int c = 1; c < VEC; ++c) plane[idx - 1 + c] = cvt(g[c]);
+            for (int c = 1; c < N; ++c) plane[idx - 1 + c] = cvt(g[c]);
         }
-        if (cx == 1 && right_edge) plane[idx + VEC] = cvt(g[VEC - 1]);
+        if (cx == 1 && right_edge) plane[idx + N] = cvt(g[N - 1]);
         if (cx == -1 && left_edge) plane[idx - 1] = cvt(g[0]);
     } else {
-        S s[VEC];
+        S s[N];
 #pragma unroll
-        for (int c = 0; c < VEC; ++c) s[c] = cvt(g[c]);
+        for (int c = 0; c < N; ++c) s[c] = cvt(g[c]);
         if (cx == 0) {
-            if (store) stv<S>(plane + idx, s);
+            if (store) stn<S, N>(plane + idx, s);
         } else if (cx == 1) {
-            K fl = shfl_up(g[VEC - 1], W);
+            K fl = shfl_up(g[N - 1], W);
             if (!store) return;
             if (!left_edge) {
-                S v[VEC];
+                S v[N];
                 v[0] = cvt(fl);
 #pragma unroll
-                for (int c = 1; c < VEC; ++c) v[c] = s[c - 1];
-                stv<S>(plane + idx, v);
+                for (int c = 1; c < N; ++c) v[c] = s[c - 1];
+                stn<S, N>(plane + idx, v);
             } else {
 #pragma unroll
-                for (int c = 0; c < VEC - 1; ++c) plane[idx + 1 + c] = s[c];
+                for (int c = 0; c < N - 1; ++c) plane[idx + 1 + c] = s[c];
             }
-            if (right_edge) plane[idx + VEC] = s[VEC - 1];
+            if (right_edge) plane[idx + N] = s[N - 1];
         } else {
             K fr = shfl_down(g[0], W);
             if (!store) return;
             if (!right_edge) {
-                S v[VEC];
+                S v[N];
 #pragma unroll
-                for (int c = 0; c < VEC - 1; ++c) v[c] = s[c + 1];
-                v[VEC - 1] = cvt(fr);
-                stv<S>(plane + idx, v);
+                for (int c = 0; c < N - 1; ++c) v[c] = s[c + 1];
+                v[N - 1] = cvt(fr);
+                stn<S, N>(plane + idx, v);
             } else {
 #pragma unroll
-                for (int c = 1; c < VEC; ++c) plane[idx - 1 + c] = s[c];
+                for (int c = 1; c < N; ++c) plane[idx - 1 + c] = s[c];
             }
             if (left_edge) plane[idx - 1] = s[0];
         }
     }
 }
 
-template <typename S, typename K, int TXV, int TY, bool HAS_OBS, bool LES = false>
-__global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ? 4 : 1) aa_p_kernel(const Lattice L)
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS, bool LES = false, int N = vec_of<S>()>
+__global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 ? (sizeof(S) == 2 ? 6 : 8) : (sizeof(S) == 2 ? 4 : 1)))
+    aa_p_kernel(const Lattice L)
 {
-    constexpr int VEC = vec_of<S>();
+    constexpr int VEC = N;  // cells per thread
     constexpr int W = TXV < 32 ? TXV : 32;
     if (L.pf_ahead > 0) prefetch_tile<S, TXV, TY, VEC, PF_AA_P>(L, 0);
+    const int nv = (L.lx + VEC - 1) / VEC;
     const int tx = threadIdx.x;
     const int k = blockIdx.x * TXV + tx;
     const int y = blockIdx.y * TY + threadIdx.y + 1;
     const bool in_rows = y <= L.ly;
-    const bool loads = in_rows && k <= L.nvec;
-    const bool active = in_rows && k < L.nvec;
+    const bool loads = in_rows && k <= nv;
+    const bool active = in_rows && k < nv;
     const int xv = 1 + k * VEC;
     const int64_t pe = L.plane_elems;
     S *base = reinterpret_cast<S *>(L.planes);
@@ -880,24 +881,24 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ?
     // pull f*_q from plane opp(q) at x - c_q
     constexpr bool RAW = Is16<S>::value;
     K x[9][VEC];
-    pull_vec<S, K, D01, W, RAW>(L, base + D12 * pe, xv, y, loads, tx, x[D01]);
-    pull_vec<S, K, D03, W, RAW>(L, base + D10 * pe, xv, y, loads, tx, x[D03]);
-    pull_vec<S, K, D05, W, RAW>(L, base + D14 * pe, xv, y, loads, tx, x[D05]);
-    pull_vec<S, K, D08, W, RAW>(L, base + D17 * pe, xv, y, loads, tx, x[D08]);
-    pull_vec<S, K, D10, W, RAW>(L, base + D03 * pe, xv, y, loads, tx, x[D10]);
-    pull_vec<S, K, D12, W, RAW>(L, base + D01 * pe, xv, y, loads, tx, x[D12]);
-    pull_vec<S, K, D14, W, RAW>(L, base + D05 * pe, xv, y, loads, tx, x[D14]);
-    pull_vec<S, K, D17, W, RAW>(L, base + D08 * pe, xv, y, loads, tx, x[D17]);
-    pull_vec<S, K, D19, W, RAW>(L, base + D19 * pe, xv, y, loads, tx, x[D19]);
+    pull_vec<S, K, D01, W, RAW, VEC>(L, base + D12 * pe, xv, y, loads, tx, x[D01]);
+    pull_vec<S, K, D03, W, RAW, VEC>(L, base + D10 * pe, xv, y, loads, tx, x[D03]);
+    pull_vec<S, K, D05, W, RAW, VEC>(L, base + D14 * pe, xv, y, loads, tx, x[D05]);
+    pull_vec<S, K, D08, W, RAW, VEC>(L, base + D17 * pe, xv, y, loads, tx, x[D08]);
+    pull_vec<S, K, D10, W, RAW, VEC>(L, base + D03 * pe, xv, y, loads, tx, x[D10]);
+    pull_vec<S, K, D12, W, RAW, VEC>(L, base + D01 * pe, xv, y, loads, tx, x[D12]);
+    pull_vec<S, K, D14, W, RAW, VEC>(L, base + D05 * pe, xv, y, loads, tx, x[D14]);
+    pull_vec<S, K, D17, W, RAW, VEC>(L, base + D08 * pe, xv, y, loads, tx, x[D17]);
+    pull_vec<S, K, D19, W, RAW, VEC>(L, base + D19 * pe, xv, y, loads, tx, x[D19]);
 
     // lanes on the scalar path: boundary rows, a ragged row end, obstacle surroundings
-    bool slow = (y == 1) || (y == L.ly) || (L.nvec == 1) || (k == L.nvec - 1 && (L.lx % VEC) != 0);
+    bool slow = (y == 1) || (y == L.ly) || (nv == 1) || (k == nv - 1 && (L.lx % VEC) != 0);
     if (HAS_OBS) slow = slow || (y >= L.ob_y0 && y <= L.ob_y1 && xv + VEC - 1 >= L.ob_x0 && xv <= L.ob_x1);
     slow = slow || !active;
     const bool left_cell = !slow && k == 0;             // x = 1 is element 0
-    const bool right_cell = !slow && k == L.nvec - 1;   // x = lx is element VEC-1
-    if (left_cell) aa_edge_pull<S, K, HAS_OBS, RAW, 0, true>(L, base, xv, y, x);
-    if (right_cell) aa_edge_pull<S, K, HAS_OBS, RAW, VEC - 1, false>(L, base, xv + VEC - 1, y, x);
+    const bool right_cell = !slow && k == nv - 1;       // x = lx is element VEC-1
+    if (left_cell) aa_edge_pull<S, K, HAS_OBS, RAW, 0, true, VEC>(L, base, xv, y, x);
+    if (right_cell) aa_edge_pull<S, K, HAS_OBS, RAW, VEC - 1, false, VEC>(L, base, xv + VEC - 1, y, x);
     // neighbours on the slow path do not take part in the vector stores
     const bool left_slow = __shfl_up_sync(0xffffffffu, slow ? 1 : 0, 1, W) != 0;
     const bool right_slow = __shfl_down_sync(0xffffffffu, slow ? 1 : 0, 1, W) != 0;
@@ -911,17 +912,17 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ?
     const uint32_t me = (uint32_t)cell_index<S>(L, xv, y);
 #pragma unroll
     for (int j = 0; j < VEC / 2; ++j) rh[j] = RAW ? cell_hash(me + 2 * j, (float)g[D19][2 * j]) : 0u;
-    push_vec<S, K, D01, W, RAW>(L, base + D01 * pe, xv, y, left_edge, right_edge, g[D01], store, rh);
-    push_vec<S, K, D03, W, RAW>(L, base + D03 * pe, xv, y, left_edge, right_edge, g[D03], store, rh);
-    push_vec<S, K, D05, W, RAW>(L, base + D05 * pe, xv, y, left_edge, right_edge, g[D05], store, rh);
-    push_vec<S, K, D08, W, RAW>(L, base + D08 * pe, xv, y, left_edge, right_edge, g[D08], store, rh);
-    push_vec<S, K, D10, W, RAW>(L, base + D10 * pe, xv, y, left_edge, right_edge, g[D10], store, rh);
-    push_vec<S, K, D12, W, RAW>(L, base + D12 * pe, xv, y, left_edge, right_edge, g[D12], store, rh);
-    push_vec<S, K, D14, W, RAW>(L, base + D14 * pe, xv, y, left_edge, right_edge, g[D14], store, rh);
-    push_vec<S, K, D17, W, RAW>(L, base + D17 * pe, xv, y, left_edge, right_edge, g[D17], store, rh);
-    push_vec<S, K, D19, W, RAW>(L, base + D19 * pe, xv, y, left_edge, right_edge, g[D19], store, rh);
-    if (left_cell) aa_edge_push<S, K, HAS_OBS, RAW, 0, true>(L, base, xv, y, g);
-    if (right_cell) aa_edge_push<S, K, HAS_OBS, RAW, VEC - 1, false>(L, base, xv + VEC - 1, y, g);
+    push_vec<S, K, D01, W, RAW, VEC>(L, base + D01 * pe, xv, y, left_edge, right_edge, g[D01], store, rh);
+    push_vec<S, K, D03, W, RAW, VEC>(L, base + D03 * pe, xv, y, left_edge, right_edge, g[D03], store, rh);
+    push_vec<S, K, D05, W, RAW, VEC>(L, base + D05 * pe, xv, y, left_edge, right_edge, g[D05], store, rh);
+    push_vec<S, K, D08, W, RAW, VEC>(L, base + D08 * pe, xv, y, left_edge, right_edge, g[D08], store, rh);
+    push_vec<S, K, D10, W, RAW, VEC>(L, base + D10 * pe, xv, y, left_edge, right_edge, g[D10], store, rh);
+    push_vec<S, K, D12, W, RAW, VEC>(L, base + D12 * pe, xv, y, left_edge, right_edge, g[D12], store, rh);
+    push_vec<S, K, D14, W, RAW, VEC>(L, base + D14 * pe, xv, y, left_edge, right_edge, g[D14], store, rh);
+    push_vec<S, K, D17, W, RAW, VEC>(L, base + D17 * pe, xv, y, left_edge, right_edge, g[D17], store, rh);
+    push_vec<S, K, D19, W, RAW, VEC>(L, base + D19 * pe, xv, y, left_edge, right_edge, g[D19], store, rh);
+    if (left_cell) aa_edge_push<S, K, HAS_OBS, RAW, 0, true, VEC>(L, base, xv, y, g);
+    if (right_cell) aa_edge_push<S, K, HAS_OBS, RAW, VEC - 1, false, VEC>(L, base, xv + VEC - 1, y, g);
     if (!active || !slow) return;
     const int xe = min(xv + VEC - 1, L.lx);
 #pragma unroll 1
@@ -929,20 +930,22 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ?
 }
 
 // L step: local collision, phase 1 -> 0
-template <typename S, typename K, int TXV, int TY, bool HAS_OBS, bool LES = false>
-__global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ? 4 : 1) aa_l_kernel(const Lattice L)
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS, bool LES = false, int N = vec_of<S>()>
+__global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 ? (sizeof(S) == 2 ? 6 : 8) : (sizeof(S) == 2 ? 4 : 1)))
+    aa_l_kernel(const Lattice L)
 {
-    constexpr int VEC = vec_of<S>();
+    constexpr int VEC = N;  // cells per thread
     if (L.pf_ahead > 0) prefetch_tile<S, TXV, TY, VEC, PF_AA_L>(L, 0);
+    const int nv = (L.lx + VEC - 1) / VEC;
     const int k = blockIdx.x * TXV + threadIdx.x;
     const int y = blockIdx.y * TY + threadIdx.y + 1;
-    if (y > L.ly || k >= L.nvec) return;
+    if (y > L.ly || k >= nv) return;
     const int xv = 1 + k * VEC;
     const int64_t pe = L.plane_elems;
     S *base = reinterpret_cast<S *>(L.planes);
     const int64_t me = cell_index<S>(L, xv, y);
     const bool outflow = L.faces[XHI] == FK_OUTFLOW_EQ || L.faces[XHI] == FK_OUTFLOW_ZG;
-    bool slow = (k == L.nvec - 1) && ((L.lx % VEC) != 0 || outflow);
+    bool slow = (k == nv - 1) && ((L.lx % VEC) != 0 || outflow);
     if (HAS_OBS) slow = slow || (y >= L.ob_y0 && y <= L.ob_y1 && xv + VEC - 1 >= L.ob_x0 && xv <= L.ob_x1);
     const K omega = (K)L.omega, fgrad = (K)L.fgrad;
     const bool forced = L.forced != 0;
@@ -974,7 +977,7 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ?
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         S v[VEC];
-        ldv<S>(base + q * pe + me, v);
+        ldn<S, VEC>(base + q * pe + me, v);
 #pragma unroll
         for (int c = 0; c < VEC; ++c) {
             if constexpr (RAW) x[q][c] = (K)Store<S>::raw_get(v[c]);
@@ -986,15 +989,15 @@ __global__ void __launch_bounds__(TXV *TY, (TXV * TY == 128 && sizeof(S) == 2) ?
 #pragma unroll
     for (int j = 0; j < VEC / 2; ++j)
         rh[j] = RAW ? cell_hash((uint32_t)me + 2 * j, (float)x[D19][2 * j]) : 0u;
-    store_vec<S, K, D01, RAW>(base + D12 * pe + me, x[D01], rh);
-    store_vec<S, K, D03, RAW>(base + D10 * pe + me, x[D03], rh);
-    store_vec<S, K, D05, RAW>(base + D14 * pe + me, x[D05], rh);
-    store_vec<S, K, D08, RAW>(base + D17 * pe + me, x[D08], rh);
-    store_vec<S, K, D10, RAW>(base + D03 * pe + me, x[D10], rh);
-    store_vec<S, K, D12, RAW>(base + D01 * pe + me, x[D12], rh);
-    store_vec<S, K, D14, RAW>(base + D05 * pe + me, x[D14], rh);
-    store_vec<S, K, D17, RAW>(base + D08 * pe + me, x[D17], rh);
-    store_vec<S, K, D19, RAW>(base + D19 * pe + me, x[D19], rh);
+    store_vec<S, K, D01, RAW, VEC>(base + D12 * pe + me, x[D01], rh);
+    store_vec<S, K, D03, RAW, VEC>(base + D10 * pe + me, x[D03], rh);
+    store_vec<S, K, D05, RAW, VEC>(base + D14 * pe + me, x[D05], rh);
+    store_vec<S, K, D08, RAW, VEC>(base + D17 * pe + me, x[D08], rh);
+    store_vec<S, K, D10, RAW, VEC>(base + D03 * pe + me, x[D10], rh);
+    store_vec<S, K, D12, RAW, VEC>(base + D01 * pe + me, x[D12], rh);
+    store_vec<S, K, D14, RAW, VEC>(base + D05 * pe + me, x[D14], rh);
+    store_vec<S, K, D17, RAW, VEC>(base + D08 * pe + me, x[D17], rh);
+    store_vec<S, K, D19, RAW, VEC>(base + D19 * pe + me, x[D19], rh);
 }
 
 // One block per work-list tile (the hardware schedules the blocks); the lattice descriptor is

@@ -12,8 +12,7 @@ struct Lattice;
 enum StepKind { STEP_PP = 0, STEP_AA_P = 1, STEP_AA_L = 2 };
 
 // thread-block shapes: threads along a row segment x rows, and cells per thread as a divisor of
-// the 16-byte vector (1: a thread updates 16 bytes of each plane, 2: 8 bytes).  The AA kernels
-// always use a whole vector per thread.
+// the 16-byte vector (1: a thread updates 16 bytes of each plane, 2: 8 bytes).
 struct TileCfg { int txv, ty, cdiv; };
 constexpr int NUM_CFG = 6;
 constexpr TileCfg TILE_CFGS[NUM_CFG] = {{32, 4, 1}, {64, 2, 1}, {128, 1, 1}, {128, 2, 1}, {32, 4, 2}, {128, 1, 2}};

@@ -173,8 +173,7 @@ int bgk_get_scalars(bgk_handle *h, double out[4], int64_t *itime);
 
 /* thread-block tile shape of the step kernels (no reference counterpart):
  *   0 = 32x4 threads, 1 = 64x2, 2 = 128x1, 3 = 128x2, each thread updating one 16-byte vector
- *   of cells per plane; 4 = 32x4 and 5 = 128x1 with half a vector (8 bytes) per thread in the
- *   ping-pong kernels.  Ping-pong only: 6, 7, 8 stage the source rows in shared memory with bulk
+ *   of cells per plane; 4 = 32x4 and 5 = 128x1 with half a vector (8 bytes) per thread.  Ping-pong only: 6, 7, 8 stage the source rows in shared memory with bulk
  *   async copies (128 threads and 3 rows in flight, 128 and 4, 256 and 3; 8 bytes per thread);
  *   such a step reports BGK_E_TIMEOUT at the next synchronisation if a copy never completed.
  *   Results do not depend on the choice. */

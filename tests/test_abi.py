@@ -39,8 +39,9 @@ def test_desc_layout_matches_c():
 #include <stdio.h>
 #include <stddef.h>
 #include "bgk2d_gb300.h"
-int main(void){printf("%zu %zu %zu %zu %zu\n", sizeof(bgk_case_desc), offsetof(bgk_case_desc, svisc),
- offsetof(bgk_case_desc, obs_mask), offsetof(bgk_case_desc, tgv_u0), offsetof(bgk_case_desc, device));return 0;}
+int main(void){printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(bgk_case_desc), offsetof(bgk_case_desc, svisc),
+ offsetof(bgk_case_desc, obs_mask), offsetof(bgk_case_desc, tgv_u0), offsetof(bgk_case_desc, device),
+ offsetof(bgk_case_desc, les), offsetof(bgk_case_desc, cte_s));return 0;}
 '''
     exe = os.path.join(ROOT, "bgk2d_gpu_gb300", "_build", "desc_layout")
     os.makedirs(os.path.dirname(exe), exist_ok=True)
@@ -49,7 +50,8 @@ int main(void){printf("%zu %zu %zu %zu %zu\n", sizeof(bgk_case_desc), offsetof(b
     assert r.returncode == 0, r.stderr
     vals = [int(x) for x in subprocess.run([exe], capture_output=True, text=True).stdout.split()]
     C = _lib.CaseDesc
-    assert vals == [ctypes.sizeof(C), C.svisc.offset, C.obs_mask.offset, C.tgv_u0.offset, C.device.offset]
+    assert vals == [ctypes.sizeof(C), C.svisc.offset, C.obs_mask.offset, C.tgv_u0.offset, C.device.offset,
+                    C.les.offset, C.cte_s.offset]
 
 
 def test_no_device_means_loud_error(bgk):

@@ -271,3 +271,34 @@ def test_vtk_fields_bit_exact(oracle_mod, bgk, case, prec, scheme):
     want = o.vtk(from_ghost_row=False)
     for name, g, w in zip(("u", "w", "rho", "vorticity", "stream"), got, want):
         assert np.array_equal(g, w), f"{name}: {int(np.sum(g != w))} values differ, max |d| {np.abs(g - w).max()}"
+
+
+@pytest.mark.parametrize("tile", [0, 1, 3, 4, 5])
+@pytest.mark.parametrize("prec", ["single", "double", "mixed2"])
+@pytest.mark.parametrize("case", ["ldc", "pof", "vks"])
+def test_aa_tile_shapes_bit_exact(oracle_mod, bgk, case, prec, tile):
+    """AA steps with every tile shape, 16 or 8 bytes per thread (configurations 4, 5)."""
+    o, s = make_pair(oracle_mod, bgk, case, prec, "aa")
+    with s:
+        s.set_tile(tile)
+        for n in (1, 2, 40, 75):
+            s.step(n)
+            o.step(n)
+            assert_same(o, s, "aa")
+
+
+@pytest.mark.parametrize("tile", [4, 5])
+@pytest.mark.parametrize("storage", ["f16", "bf16"])
+def test_aa_16bit_half_vector_accuracy(bgk, storage, tile):
+    """16-bit AA with 8 bytes per thread stays as close to FP32 as the whole-vector kernels."""
+    errs = []
+    for t in (0, tile):
+        with bgk.Solver(300, 200, tcase="LDC", svisc=0.02, u0=0.1, storage=storage, scheme="aa") as s, \
+                bgk.Solver(300, 200, tcase="LDC", svisc=0.02, u0=0.1, storage="f32", scheme="aa") as r:
+            s.set_tile(t)
+            s.step(400)
+            r.step(400)
+            _, u, v = s.fields()
+            _, ur, vr = r.fields()
+        errs.append(float(np.sqrt(np.sum((u - ur) ** 2 + (v - vr) ** 2) / np.sum(ur ** 2 + vr ** 2))))
+    assert errs[1] < max(2 * errs[0], 1e-3), errs
