@@ -361,6 +361,9 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
     L.forced = h->cs.forced;
     L.les = h->cs.les;
     L.cte_s = h->cs.cte_s;
+    L.omega_f = (float)L.omega;  // exact when the compute kind is FP32 (the values were computed in it)
+    L.fgrad_f = (float)L.fgrad;
+    L.cte_s_f = (float)L.cte_s;
 
     // inflow table
     if (dalloc(h, &h->d_inflow, h->cs.inflow.size() * sizeof(double)) != cudaSuccess) {

@@ -157,6 +157,8 @@ struct Lattice {
     int32_t forced;          // 1 when the x body force fgrad*rho is applied (CHANNEL)
     int32_t les;             // 1: Smagorinsky eddy viscosity in the collision (-DLES)
     double cte_s;            // Smagorinsky constant cteS (compute kind)
+    float omega_f, fgrad_f, cte_s_f;  // the same three in single precision (exact for FP32 compute),
+                                      // so that FP32 kernels convert nothing on the FP64 pipe
     const double *inflow;    // [3][ly+2] equilibrium deviations of 01,03,05 at the x_lo inflow
     const uint32_t *mask;    // obstacle bits, row y (0..ly+1) at mask + y*mask_pitch, bit x
     int32_t mask_pitch;      // 32-bit words per mask row
@@ -167,6 +169,17 @@ struct Lattice {
 };
 
 template <typename S> __host__ __device__ constexpr int vec_of() { return 16 / (int)sizeof(S); }
+
+// relaxation scalars of a lattice in the compute kind K
+template <typename K> __device__ __forceinline__ K lat_omega(const Lattice &L);
+template <> __device__ __forceinline__ float lat_omega<float>(const Lattice &L) { return L.omega_f; }
+template <> __device__ __forceinline__ double lat_omega<double>(const Lattice &L) { return L.omega; }
+template <typename K> __device__ __forceinline__ K lat_fgrad(const Lattice &L);
+template <> __device__ __forceinline__ float lat_fgrad<float>(const Lattice &L) { return L.fgrad_f; }
+template <> __device__ __forceinline__ double lat_fgrad<double>(const Lattice &L) { return L.fgrad; }
+template <typename K> __device__ __forceinline__ K lat_cte_s(const Lattice &L);
+template <> __device__ __forceinline__ float lat_cte_s<float>(const Lattice &L) { return L.cte_s_f; }
+template <> __device__ __forceinline__ double lat_cte_s<double>(const Lattice &L) { return L.cte_s; }
 
 template <typename S>
 __device__ __forceinline__ int64_t cell_index(const Lattice &L, int x, int y) {

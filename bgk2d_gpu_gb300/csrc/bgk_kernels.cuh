@@ -426,7 +426,7 @@ __device__ void pp_cell_slow(const Lattice &L, const S *src, S *dst, int x, int 
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) v[q] = pull_rule<S, K, HAS_OBS>(L, q, x, y, plane_at, own, ghost_xhi);
     v[8] = ldq<S, K>(src + D19 * pe, me, D19);
-    collide_stored<S, K, LES>(v, (K)L.omega, (K)L.fgrad, L.forced != 0, (K)L.cte_s);
+    collide_stored<S, K, LES>(v, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
 #pragma unroll
     for (int q = 0; q < 9; ++q) dst[q * pe + me] = Store<S>::template putq<K>(v[q], q);
 }
@@ -501,7 +501,7 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
     if (left_cell) pp_edge_pull<S, K, HAS_OBS, RAW, 0, true, N>(L, src, xv, y, x);
     if (right_cell) pp_edge_pull<S, K, HAS_OBS, RAW, N - 1, false, N>(L, src, xv + N - 1, y, x);
 
-    relax_vec<S, K, RAW, N, LES>(x, (K)L.omega, (K)L.fgrad, L.forced != 0, (K)L.cte_s);
+    relax_vec<S, K, RAW, N, LES>(x, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
     const int64_t me = cell_index<S>(L, xv, y);
     uint32_t rh[npair<N>()] = {};
 #pragma unroll
@@ -725,7 +725,7 @@ __device__ void aa_p_cell_slow(const Lattice &L, S *base, int x, int y)
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) v[q] = pull_rule<S, K, HAS_OBS>(L, q, x, y, plane_at, own, ghost_xhi);
     v[8] = ldq<S, K>(base + D19 * pe, me, D19);
-    collide_stored<S, K, LES>(v, (K)L.omega, (K)L.fgrad, L.forced != 0, (K)L.cte_s);
+    collide_stored<S, K, LES>(v, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) aa_push_rule<S, K, HAS_OBS>(L, base, q, x, y, v[q]);
     base[D19 * pe + me] = Store<S>::template putq<K>(v[8], D19);
@@ -905,7 +905,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
     const bool left_edge = (tx % W) == 0 || left_slow;
     const bool right_edge = (tx % W) == W - 1 || right_slow;
 
-    relax_vec<S, K, RAW, VEC, LES>(x, (K)L.omega, (K)L.fgrad, L.forced != 0, (K)L.cte_s);
+    relax_vec<S, K, RAW, VEC, LES>(x, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
     K (&g)[9][VEC] = x;
     const bool store = !slow;
     uint32_t rh[npair<VEC>()] = {};
@@ -947,7 +947,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
     const bool outflow = L.faces[XHI] == FK_OUTFLOW_EQ || L.faces[XHI] == FK_OUTFLOW_ZG;
     bool slow = (k == nv - 1) && ((L.lx % VEC) != 0 || outflow);
     if (HAS_OBS) slow = slow || (y >= L.ob_y0 && y <= L.ob_y1 && xv + VEC - 1 >= L.ob_x0 && xv <= L.ob_x1);
-    const K omega = (K)L.omega, fgrad = (K)L.fgrad;
+    const K omega = lat_omega<K>(L), fgrad = lat_fgrad<K>(L);
     const bool forced = L.forced != 0;
     if (slow) {
         const int xe = min(xv + VEC - 1, L.lx);
@@ -960,7 +960,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
             K v[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) v[q] = ldq<S, K>(base + q * pe, i, q);
-            collide_stored<S, K, LES>(v, omega, fgrad, forced, (K)L.cte_s);
+            collide_stored<S, K, LES>(v, omega, fgrad, forced, lat_cte_s<K>(L));
             K g[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) {
@@ -984,7 +984,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
             else x[q][c] = Store<S>::template getq<K>(v[c], q);
         }
     }
-    relax_vec<S, K, RAW, VEC, LES>(x, omega, fgrad, forced, (K)L.cte_s);
+    relax_vec<S, K, RAW, VEC, LES>(x, omega, fgrad, forced, lat_cte_s<K>(L));
     uint32_t rh[npair<VEC>()] = {};
 #pragma unroll
     for (int j = 0; j < VEC / 2; ++j)

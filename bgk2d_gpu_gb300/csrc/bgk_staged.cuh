@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(T, ((N * sizeof(S) <= 8) ? 1024 : 512) / T)
     const bool active = k < nv;
     const int xv = 1 + k * N;
     const int i0 = VEC + t * N;  // staged index of the thread's first cell
-    const K omega = (K)L.omega, fgrad = (K)L.fgrad;
+    const K omega = lat_omega<K>(L), fgrad = lat_fgrad<K>(L);
     const bool forced = L.forced != 0;
     constexpr int NW = T / 32;
 
