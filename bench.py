@@ -423,10 +423,11 @@ def main():
         for name, st, sch in (("pingpong_f32", "f32", "pingpong"), ("aa_f32", "f32", "aa"),
                               ("pingpong_f16", "f16", "pingpong"), ("aa_f16", "f16", "aa"),
                               ("pingpong_bf16", "bf16", "pingpong"), ("pingpong_f64", "f64", "pingpong"),
-                              ("aa_f64", "f64", "aa")):
+                              ("aa_f64", "f64", "aa"), ("original_f32", "f32", "original")):
             n = vsteps if st != "f64" else max(10, vsteps // 4)
             g, msv, cfg, pf = measure_variant(bgk, st, sch, n, 5, local)
-            bw = BYTES_PER_CELL[st] * LX * LY / (msv * 1e-3) / 1e9
+            # the two-pass form moves every population twice per step (stream, then collide)
+            bw = BYTES_PER_CELL[st] * (2 if sch == "original" else 1) * LX * LY / (msv * 1e-3) / 1e9
             variants[name] = {"GLUPS": round(g, 3), "ms_per_step": round(msv, 4), "algorithmic_GBps": round(bw, 1),
                               "hbm_frac": round(bw / peak, 4), "steps": n, "tile_cfg": cfg,
                               "prefetch_blocks": pf}

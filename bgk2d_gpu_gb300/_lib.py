@@ -24,7 +24,7 @@ STATUS_NAMES = {0: "OK", 1: "BGK_E_INVALID", 2: "BGK_E_NOMEM", 3: "BGK_E_CUDA", 
 
 STORE = {"f32": 0, "f64": 1, "f16": 2, "bf16": 3}
 COMPUTE = {"f32": 0, "f64": 1}
-SCHEME = {"pingpong": 0, "aa": 1}
+SCHEME = {"pingpong": 0, "aa": 1, "original": 2}
 CASE = {"LDC": 0, "TGV": 1, "POF": 2, "VKS": 3, "COU": 4, "BFS": 5, "CUSTOM": 9}
 FACE = {"wall": 0, "periodic": 1, "inflow": 2, "outflow_eq": 3, "outflow_zg": 4}
 OBS = {None: 0, "none": 0, "circle": 1, "square": 2, "half_circle": 3, "mask": 4}

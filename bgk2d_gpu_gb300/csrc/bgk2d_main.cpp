@@ -9,7 +9,7 @@
 // fields computed on the device) and bgk.perf.
 //
 //   bgk2d_gb300 [--input bgk.input] [--case LDC|TGV|POF|VKS|COU|BFS] [--prec single|double|mixed2|f16|bf16]
-//               [--scheme pingpong|aa] [--les 0|1] [--dir OUTDIR]
+//               [--scheme pingpong|aa|original] [--les 0|1] [--dir OUTDIR]
 // `--les 1` stands for the reference's -DLES build (Smagorinsky constant from the namelist key cteS).
 #include <cctype>
 #include <chrono>
@@ -264,7 +264,7 @@ int main(int argc, char **argv)
     d.radius = geti("radius", 16);
     d.les = les == "1";
     d.cte_s = getd("ctes", 0.1);
-    d.scheme = scheme == "aa" ? BGK_SCHEME_AA : BGK_SCHEME_PINGPONG;
+    d.scheme = scheme == "aa" ? BGK_SCHEME_AA : scheme == "original" ? BGK_SCHEME_ORIGINAL : BGK_SCHEME_PINGPONG;
     if (prec == "double") { d.storage = BGK_STORE_F64; d.compute = BGK_COMPUTE_F64; }
     else if (prec == "mixed2") { d.storage = BGK_STORE_F32; d.compute = BGK_COMPUTE_F64; }
     else if (prec == "f16") d.storage = BGK_STORE_F16;

@@ -163,7 +163,13 @@ int launch_step(bgk_handle *h)
             CK(h, h->T.bcond_step(h->L, h->cur, h->cs.stepx, h->cs.stepy, h->st));
             h->launches++;
         }
-        CK(h, h->T.step(STEP_PP, h->L, h->cur, h->cs.has_obs, h->cfg, h->st));
+        if (h->two_pass) {
+            CK(h, h->T.step(STEP_STREAM, h->L, h->cur, h->cs.has_obs, h->cfg, h->st));
+            CK(h, h->T.step(STEP_COLLIDE, h->L, h->cur ^ 1, h->cs.has_obs, h->cfg, h->st));
+            h->launches++;
+        } else {
+            CK(h, h->T.step(STEP_PP, h->L, h->cur, h->cs.has_obs, h->cfg, h->st));
+        }
         h->cur ^= 1;
     } else {
         CK(h, h->T.step(h->phase == 0 ? STEP_AA_P : STEP_AA_L, h->L, 0, h->cs.has_obs, h->cfg, h->st));
@@ -204,6 +210,7 @@ int build_graph(bgk_handle *h, int start)
 int steps_impl(bgk_handle *h, int32_t n)
 {
     if (n < 0) return fail(h, BGK_E_INVALID, "negative step count");
+    if (h->streamed) return fail(h, BGK_E_INVALID, "two-pass step half done: call bgk_collision first");
     int rc;
     // AA graphs start at phase 0; the odd step that brings phase 1 back to 0 runs directly
     if (h->L.scheme == BGK_SCHEME_AA && h->phase == 1 && n > 0) {
@@ -214,7 +221,7 @@ int steps_impl(bgk_handle *h, int32_t n)
         const int slot = h->L.scheme == BGK_SCHEME_PINGPONG ? h->cur : 0;
         if (!h->graph[slot] && (rc = build_graph(h, slot))) return rc;
         CK(h, cudaGraphLaunch(h->graph[slot], h->st));
-        h->launches += (int64_t)h->graph_steps * (h->cs.bfs ? 2 : 1);
+        h->launches += (int64_t)h->graph_steps * (1 + (h->cs.bfs ? 1 : 0) + (h->two_pass ? 1 : 0));
         h->itime += h->graph_steps;
         n -= h->graph_steps;
     }
@@ -295,7 +302,8 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
     *out = nullptr;
     const bgk_case_desc &d = *desc;
     if (d.lx < 2 || d.ly < 2 || d.ipad < 0 || d.jpad < 0) return BGK_E_INVALID;
-    if (d.scheme != BGK_SCHEME_PINGPONG && d.scheme != BGK_SCHEME_AA) return BGK_E_INVALID;
+    if (d.scheme != BGK_SCHEME_PINGPONG && d.scheme != BGK_SCHEME_AA && d.scheme != BGK_SCHEME_ORIGINAL)
+        return BGK_E_INVALID;
     KernelTable T;
     if (!get_table(d.storage, d.compute, T)) return BGK_E_INVALID;
 
@@ -323,7 +331,7 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
     pitch = (pitch + row_align - 1) / row_align * row_align;
     int64_t plane = pitch * (m + 2);
     plane = (plane + 256 / eb - 1) / (256 / eb) * (256 / eb);
-    const int nplanes = d.scheme == BGK_SCHEME_PINGPONG ? 18 : 9;
+    const int nplanes = d.scheme == BGK_SCHEME_AA ? 9 : 18;
     h->planes_bytes = (size_t)plane * nplanes * eb;
 
     // admission against free HBM (populations + staging plane + mask + reduction scratch)
@@ -351,7 +359,8 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
     L.pitch = (int32_t)pitch;
     L.lx = l; L.ly = m;
     L.nvec = nvec;
-    L.scheme = d.scheme;
+    L.scheme = d.scheme == BGK_SCHEME_AA ? BGK_SCHEME_AA : BGK_SCHEME_PINGPONG;  // layout
+    h->two_pass = d.scheme == BGK_SCHEME_ORIGINAL;
     for (int f = 0; f < 4; ++f) {
         L.faces[f] = h->cs.faces[f];
         for (int q = 0; q < 9; ++q) L.wt[f][q] = h->cs.wt[f][q];
@@ -481,13 +490,24 @@ int bgk_download(bgk_handle *h, void *const pops[9], int64_t ld)
 int bgk_boundaries(bgk_handle *h)
 {
     CHECK_HANDLE(h);
-    return BGK_OK;  // folded into the fused step launched by bgk_collision
+    return BGK_OK;  // folded into the step launched by bgk_propagation / bgk_collision
 }
 
 int bgk_propagation(bgk_handle *h)
 {
     CHECK_HANDLE(h);
-    return BGK_OK;  // the pull streaming is part of the fused step
+    NOT_IN_BATCH(h);
+    if (!h->two_pass || h->streamed) return BGK_OK;  // fused: the pull streaming is part of the step
+    // two-pass: the streaming pass (and the step's boundary kernel) now, the collision in
+    // bgk_collision, as SRC/propagation.F90 and SRC/collision.F90 split them
+    if (h->cs.bfs) {
+        CK(h, h->T.bcond_step(h->L, h->cur, h->cs.stepx, h->cs.stepy, h->st));
+        h->launches++;
+    }
+    CK(h, h->T.step(STEP_STREAM, h->L, h->cur, h->cs.has_obs, h->cfg, h->st));
+    h->launches++;
+    h->streamed = true;
+    return BGK_OK;
 }
 
 int bgk_collision(bgk_handle *h, int32_t itime)
@@ -495,6 +515,14 @@ int bgk_collision(bgk_handle *h, int32_t itime)
     CHECK_HANDLE(h);
     NOT_IN_BATCH(h);
     (void)itime;
+    if (h->two_pass && h->streamed) {
+        CK(h, h->T.step(STEP_COLLIDE, h->L, h->cur ^ 1, h->cs.has_obs, h->cfg, h->st));
+        h->launches++;
+        h->streamed = false;
+        h->cur ^= 1;
+        h->itime++;
+        return BGK_OK;
+    }
     return launch_step(h);
 }
 
@@ -675,7 +703,7 @@ int bgk_footprint(bgk_handle *h, int64_t *device_bytes, int32_t *bytes_per_cell)
 int bgk_set_tile(bgk_handle *h, int32_t tile_cfg)
 {
     CHECK_HANDLE(h);
-    const int ncfg = h->L.scheme == BGK_SCHEME_PINGPONG ? NUM_STEP_CFG : NUM_CFG;
+    const int ncfg = (h->L.scheme == BGK_SCHEME_PINGPONG && !h->two_pass) ? NUM_STEP_CFG : NUM_CFG;
     if (tile_cfg < 0 || tile_cfg >= ncfg) return fail(h, BGK_E_INVALID, "tile configuration %d", tile_cfg);
     if (tile_cfg != h->cfg) {
         for (int i = 0; i < 2; ++i)
@@ -718,7 +746,7 @@ int bgk_tune(bgk_handle *h, int32_t trial_steps, int32_t *tile_cfg, int32_t *ste
     // L2 prefetch distances for the register-vector ping-pong and AA kernels: off, half a wave
     // and one wave of 8 resident blocks per SM ahead
     const int pfs[3] = {0, 4 * sms, 8 * sms};
-    const int ncfg = h->L.scheme == BGK_SCHEME_PINGPONG ? NUM_STEP_CFG : NUM_CFG;
+    const int ncfg = (h->L.scheme == BGK_SCHEME_PINGPONG && !h->two_pass) ? NUM_STEP_CFG : NUM_CFG;
     for (int c = 0; c < ncfg; ++c) {
         const int npf = (c < NUM_CFG && !h->L.les) ? 3 : 1;
         for (int p = 0; p < npf; ++p) {

@@ -241,7 +241,7 @@ int bgk_batch_add(bgk_batch *b, bgk_handle *h)
         h->L.scheme != BGK_SCHEME_PINGPONG)
         return BGK_E_INVALID;
     // the batch kernels carry the plain BGK collision and the folded boundary rules only
-    if (h->L.les || h->cs.bfs) return BGK_E_UNSUPPORTED;
+    if (h->L.les || h->cs.bfs || h->two_pass) return BGK_E_UNSUPPORTED;
     if (h->sticky) return h->sticky;
     cudaSetDevice(b->dev);
     if (cudaStreamSynchronize(h->st) != cudaSuccess || cudaStreamSynchronize(b->st) != cudaSuccess) return BGK_E_CUDA;

@@ -42,6 +42,8 @@ struct bgk_handle {
     int64_t itime = 0;
     int64_t launches = 0;
     int cfg = 2;
+    bool two_pass = false;  // BGK_SCHEME_ORIGINAL: ping-pong layout, streaming then collision
+    bool streamed = false;  // two-pass: bgk_propagation has run, bgk_collision completes the step
     int host_bytes = 4;
     int sticky = BGK_OK;
     void *batch = nullptr;   // owning batch while attached (steps go through the batch)

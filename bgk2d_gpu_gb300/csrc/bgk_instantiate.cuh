@@ -17,11 +17,13 @@ template <typename S, typename K, int TXV, int TY, bool OBS, int CDIV>
 cudaError_t step_cfg(int kind, const Lattice &L, int parity, cudaStream_t st)
 {
     const dim3 block(TXV, TY);
-    if (kind == STEP_PP) {
+    if (kind == STEP_PP || kind == STEP_STREAM || kind == STEP_COLLIDE) {
         constexpr int N = vec_of<S>() / CDIV;
         const int nv = (L.lx + N - 1) / N;
         const dim3 grid((unsigned)((nv + TXV - 1) / TXV), (unsigned)((L.ly + TY - 1) / TY));
-        pp_kernel<S, K, TXV, TY, OBS, N><<<grid, block, 0, st>>>(L, parity);
+        if (kind == STEP_PP) pp_kernel<S, K, TXV, TY, OBS, N><<<grid, block, 0, st>>>(L, parity);
+        else if (kind == STEP_STREAM) pp_kernel<S, K, TXV, TY, OBS, N, false, false><<<grid, block, 0, st>>>(L, parity);
+        else col_kernel<S, K, TXV, TY, N><<<grid, block, 0, st>>>(L, parity);
     } else {
         constexpr int N = vec_of<S>() / CDIV;
         const int nv = (L.lx + N - 1) / N;
@@ -61,10 +63,13 @@ template <typename S, typename K, bool OBS>
 cudaError_t step_les(int kind, const Lattice &L, int parity, cudaStream_t st)
 {
     const dim3 block(128, 1);
-    if (kind == STEP_PP) {
+    if (kind == STEP_PP || kind == STEP_STREAM || kind == STEP_COLLIDE) {
         constexpr int N = vec_of<S>();
         const int nv = (L.lx + N - 1) / N;
-        pp_kernel<S, K, 128, 1, OBS, N, true><<<dim3((unsigned)((nv + 127) / 128), (unsigned)L.ly), block, 0, st>>>(L, parity);
+        const dim3 grid((unsigned)((nv + 127) / 128), (unsigned)L.ly);
+        if (kind == STEP_PP) pp_kernel<S, K, 128, 1, OBS, N, true><<<grid, block, 0, st>>>(L, parity);
+        else if (kind == STEP_STREAM) pp_kernel<S, K, 128, 1, OBS, N, false, false><<<grid, block, 0, st>>>(L, parity);
+        else col_kernel<S, K, 128, 1, N, true><<<grid, block, 0, st>>>(L, parity);
     } else {
         const dim3 grid((unsigned)((L.nvec + 127) / 128), (unsigned)L.ly);
         if (kind == STEP_AA_P) aa_p_kernel<S, K, 128, 1, OBS, true><<<grid, block, 0, st>>>(L);

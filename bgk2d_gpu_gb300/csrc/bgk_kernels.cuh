@@ -406,7 +406,7 @@ __device__ __forceinline__ bool needs_rule(const Lattice &L, int x, int y)
 }
 
 // one cell with the boundary rules: reads the source buffer only, writes the destination
-template <typename S, typename K, bool HAS_OBS, bool LES = false>
+template <typename S, typename K, bool HAS_OBS, bool LES = false, bool COLLIDE = true>
 __device__ void pp_cell_slow(const Lattice &L, const S *src, S *dst, int x, int y)
 {
     const int64_t pe = L.plane_elems;
@@ -426,7 +426,7 @@ __device__ void pp_cell_slow(const Lattice &L, const S *src, S *dst, int x, int 
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) v[q] = pull_rule<S, K, HAS_OBS>(L, q, x, y, plane_at, own, ghost_xhi);
     v[8] = ldq<S, K>(src + D19 * pe, me, D19);
-    collide_stored<S, K, LES>(v, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
+    if constexpr (COLLIDE) collide_stored<S, K, LES>(v, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
 #pragma unroll
     for (int q = 0; q < 9; ++q) dst[q * pe + me] = Store<S>::template putq<K>(v[q], q);
 }
@@ -463,7 +463,8 @@ __device__ __forceinline__ void pp_edge_pull(const Lattice &L, const S *src, int
 // vector path; cells whose inputs come from the boundary rules are then recomputed one by one
 // and overwritten (the source buffer is read-only during the step, so the recompute sees the
 // same inputs).
-template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N = vec_of<S>(), bool LES = false>
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N = vec_of<S>(), bool LES = false,
+          bool COLLIDE = true>
 __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const int by, const int parity)
 {
     constexpr int W = TXV < 32 ? TXV : 32;
@@ -501,7 +502,7 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
     if (left_cell) pp_edge_pull<S, K, HAS_OBS, RAW, 0, true, N>(L, src, xv, y, x);
     if (right_cell) pp_edge_pull<S, K, HAS_OBS, RAW, N - 1, false, N>(L, src, xv + N - 1, y, x);
 
-    relax_vec<S, K, RAW, N, LES>(x, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
+    if constexpr (COLLIDE) relax_vec<S, K, RAW, N, LES>(x, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
     const int64_t me = cell_index<S>(L, xv, y);
     uint32_t rh[npair<N>()] = {};
 #pragma unroll
@@ -522,7 +523,7 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
         const int xe = min(xv + N - 1, L.lx);
 #pragma unroll 1
         for (int xc = xv; xc <= xe; ++xc)
-            if (needs_rule<HAS_OBS>(L, xc, y)) pp_cell_slow<S, K, HAS_OBS, LES>(L, src, dst, xc, y);
+            if (needs_rule<HAS_OBS>(L, xc, y)) pp_cell_slow<S, K, HAS_OBS, LES, COLLIDE>(L, src, dst, xc, y);
     }
 }
 
@@ -562,11 +563,13 @@ __device__ __forceinline__ void prefetch_tile(const Lattice &L, const int parity
     prefetch_segment<S, TXV, TY, N, KIND>(L, parity, t, (int)(lin % gridDim.x), (int)(lin / gridDim.x));
 }
 
-template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N, bool LES = false>
+// COLLIDE = false: the streaming half of the two-pass form (SRC/movef.F90 with the boundary
+// rules folded in, the rest population copied); the collision then runs in col_kernel.
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N, bool LES = false, bool COLLIDE = true>
 __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 || (sizeof(S) == 4 && N == 4)) ? 8 : (sizeof(S) == 2 ? 4 : 1)) pp_kernel(const Lattice L, const int parity)
 {
     if (L.pf_ahead > 0) prefetch_tile<S, TXV, TY, N, PF_PP>(L, parity);
-    pp_tile<S, K, TXV, TY, HAS_OBS, N, LES>(L, blockIdx.x, blockIdx.y, parity);
+    pp_tile<S, K, TXV, TY, HAS_OBS, N, LES, COLLIDE>(L, blockIdx.x, blockIdx.y, parity);
 }
 
 // Persistent ping-pong step over many lattices.  The work list holds (lattice, tile x, tile y)
@@ -1018,6 +1021,63 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
     const int4 tile = __ldg(tiles + blockIdx.x);
     const Lattice &L = lats[tile.x];
     pp_tile<S, K, TXV, TY, true, N>(L, tile.y, tile.z, __ldg(cur + tile.x) ^ parity);
+}
+
+// Collision half of the two-pass form (SRC/col.F90): every interior cell of buffer `parity`
+// relaxes in place, obstacle cells included, as the reference's col loop does.
+template <typename S, typename K, int TXV, int TY, int N, bool LES = false>
+__global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 || (sizeof(S) == 4 && N == 4)) ? 8 : (sizeof(S) == 2 ? 4 : 1))
+    col_kernel(const Lattice L, const int parity)
+{
+    const int nv = (L.lx + N - 1) / N;
+    const int k = blockIdx.x * TXV + threadIdx.x;
+    const int y = blockIdx.y * TY + threadIdx.y + 1;
+    if (y > L.ly || k >= nv) return;
+    const int xv = 1 + k * N;
+    const int64_t pe = L.plane_elems;
+    S *base = reinterpret_cast<S *>(L.planes) + (parity ? 9 : 0) * pe;
+    const int64_t me = cell_index<S>(L, xv, y);
+    const K omega = lat_omega<K>(L), fgrad = lat_fgrad<K>(L);
+    const bool forced = L.forced != 0;
+    if (k == nv - 1 && (L.lx % N) != 0) {  // ragged row end: the cells up to lx one by one
+        const int xe = L.lx;
+#pragma unroll 1
+        for (int xc = xv; xc <= xe; ++xc) {
+            const int64_t i = cell_index<S>(L, xc, y);
+            K v[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) v[q] = ldq<S, K>(base + q * pe, i, q);
+            collide_stored<S, K, LES>(v, omega, fgrad, forced, lat_cte_s<K>(L));
+#pragma unroll
+            for (int q = 0; q < 9; ++q) base[q * pe + i] = Store<S>::template putq<K>(v[q], q);
+        }
+        return;
+    }
+    constexpr bool RAW = Is16<S>::value;
+    K x[9][N];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        S v[N];
+        ldn<S, N>(base + q * pe + me, v);
+#pragma unroll
+        for (int c = 0; c < N; ++c) {
+            if constexpr (RAW) x[q][c] = (K)Store<S>::raw_get(v[c]);
+            else x[q][c] = Store<S>::template getq<K>(v[c], q);
+        }
+    }
+    relax_vec<S, K, RAW, N, LES>(x, omega, fgrad, forced, lat_cte_s<K>(L));
+    uint32_t rh[npair<N>()] = {};
+#pragma unroll
+    for (int j = 0; j < N / 2; ++j) rh[j] = RAW ? cell_hash((uint32_t)me + 2 * j, (float)x[D19][2 * j]) : 0u;
+    store_vec<S, K, D01, RAW, N>(base + D01 * pe + me, x[D01], rh);
+    store_vec<S, K, D03, RAW, N>(base + D03 * pe + me, x[D03], rh);
+    store_vec<S, K, D05, RAW, N>(base + D05 * pe + me, x[D05], rh);
+    store_vec<S, K, D08, RAW, N>(base + D08 * pe + me, x[D08], rh);
+    store_vec<S, K, D10, RAW, N>(base + D10 * pe + me, x[D10], rh);
+    store_vec<S, K, D12, RAW, N>(base + D12 * pe + me, x[D12], rh);
+    store_vec<S, K, D14, RAW, N>(base + D14 * pe + me, x[D14], rh);
+    store_vec<S, K, D17, RAW, N>(base + D17 * pe + me, x[D17], rh);
+    store_vec<S, K, D19, RAW, N>(base + D19 * pe + me, x[D19], rh);
 }
 
 }  // namespace bgk

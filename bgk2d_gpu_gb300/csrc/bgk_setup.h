@@ -178,7 +178,7 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
         cs.stepx = l / 20;
         cs.stepy = m / 2;
         if (cs.stepx < 2 || m < 4) return "backward-facing step needs lx >= 40 and ly >= 4";
-        if (d.scheme != BGK_SCHEME_PINGPONG) return "backward-facing step: ping-pong scheme only";
+        if (d.scheme == BGK_SCHEME_AA) return "backward-facing step: ping-pong or two-pass scheme only";
         break;
     case BGK_CASE_CUSTOM:
         for (int f = 0; f < 4; ++f) cs.faces[f] = d.faces[f];

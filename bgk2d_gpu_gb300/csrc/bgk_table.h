@@ -9,7 +9,9 @@ namespace bgk {
 struct Lattice;
 
 // step kinds
-enum StepKind { STEP_PP = 0, STEP_AA_P = 1, STEP_AA_L = 2 };
+enum StepKind { STEP_PP = 0, STEP_AA_P = 1, STEP_AA_L = 2, STEP_STREAM = 3, STEP_COLLIDE = 4 };
+// STEP_STREAM and STEP_COLLIDE are the two halves of the two-pass form (SRC/movef.F90 then
+// SRC/col.F90): parity = the source buffer for STREAM, the buffer collided in place for COLLIDE.
 
 // thread-block shapes: threads along a row segment x rows, and cells per thread as a divisor of
 // the 16-byte vector (1: a thread updates 16 bytes of each plane, 2: 8 bytes).

@@ -59,6 +59,9 @@ extern "C" {
 /* scheme */
 #define BGK_SCHEME_PINGPONG 0  /* fused pull stream+collide, two buffers (SRC/col_MC.F90) */
 #define BGK_SCHEME_AA 1        /* fused, one buffer, alternating even/odd access pattern */
+#define BGK_SCHEME_ORIGINAL 2  /* two passes per step, as the ORIGINAL build: streaming (SRC/movef.F90)
+                                  into the second buffer, then collision in place (SRC/col.F90);
+                                  same results as ping-pong, twice its HBM traffic */
 
 /* test case presets: the reference's compile-time case flags (SRC/Makefile:155-187) */
 #define BGK_CASE_LDC 0     /* bcond_driven: walls + moving lid at y = ly+1 */

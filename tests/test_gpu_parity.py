@@ -302,3 +302,56 @@ def test_aa_16bit_half_vector_accuracy(bgk, storage, tile):
             _, ur, vr = r.fields()
         errs.append(float(np.sqrt(np.sum((u - ur) ** 2 + (v - vr) ** 2) / np.sum(ur ** 2 + vr ** 2))))
     assert errs[1] < max(2 * errs[0], 1e-3), errs
+
+
+@pytest.mark.parametrize("prec", ["single", "double", "mixed2"])
+@pytest.mark.parametrize("case", list(CASES))
+def test_original_two_pass_bit_exact(oracle_mod, bgk, case, prec):
+    """BGK_SCHEME_ORIGINAL: streaming (SRC/movef.F90) then collision (SRC/col.F90) as two kernels,
+    against the oracle's ORIGINAL form (movef + col)."""
+    tc, lx, ly, svisc, u0, okw, skw = CASES[case]
+    oprec, st, cp = PRECS[prec]
+    o = oracle_mod.Oracle(lx, ly, prec=oprec, tcase=ORACLE_CASE[tc], svisc=svisc, u0=u0, fused=False,
+                          obs_order=oracle_mod.OBS_SNAPSHOT, **okw)
+    with bgk.Solver(lx, ly, tcase=tc, svisc=svisc, u0=u0, storage=st, compute=cp, scheme="original", **skw) as s:
+        for n in (1, 2, 40, 75):
+            s.step(n)
+            o.step(n)
+            assert_same(o, s, "original")
+        n0 = s.launches()
+        s.step(64)
+        assert s.launches() - n0 == 128  # two kernels per step
+
+
+def test_original_reference_call_sequence(oracle_mod, bgk):
+    """boundaries / propagation / collision(itime) split the two passes like the reference."""
+    o = oracle_mod.Oracle(70, 37, prec=0, tcase=0, svisc=0.05, u0=0.1, fused=False)
+    with bgk.Solver(70, 37, tcase="LDC", svisc=0.05, u0=0.1, scheme="original") as s:
+        for it in range(1, 6):
+            s.boundaries()
+            s.propagation()
+            s.collision(it)
+        o.step(5)
+        assert_same(o, s, "original")
+        s.propagation()
+        with pytest.raises(bgk.BgkError):
+            s.step(1)  # half a step pending
+        s.collision(6)
+        s.step(3)
+        o.step(4)
+        assert_same(o, s, "original")
+
+
+def test_original_bfs_and_les(oracle_mod, bgk):
+    lx, ly = 200, 64
+    o = oracle_mod.Oracle(lx, ly, prec=0, tcase=oracle_mod.BFS, svisc=0.02, u0=0.1, fused=False)
+    with bgk.Solver(lx, ly, tcase="BFS", svisc=0.02, u0=0.1, scheme="original") as s:
+        s.step(45)
+        o.step(45)
+        assert np.array_equal(_bfs_fluid(s.download(), lx, ly), _bfs_fluid(o.raw(), lx, ly))
+    o = oracle_mod.Oracle(70, 37, prec=1, tcase=0, svisc=0.01, u0=0.1, fused=False, les=True, cte_s=0.2)
+    with bgk.Solver(70, 37, tcase="LDC", svisc=0.01, u0=0.1, storage="f64", scheme="original", les=True,
+                    cte_s=0.2) as s:
+        s.step(45)
+        o.step(45)
+        assert_same(o, s, "original")
