@@ -303,7 +303,7 @@ int main(int argc, char **argv)
     const bool dbl = d.storage == BGK_STORE_F64;
     auto diagnostic = [&](int itime) -> int {
         double dg[4];
-        int r = bgk_diagno(h, 0, dg);
+        int r = bgk_diagno(h, BGK_DIAGNO_REFERENCE, dg);  // the reference's own sums (diagno.dat)
         if (r && r != BGK_E_NUMERIC) return r;
         std::fprintf(fdiag, "%8d%s %s %s %s \n", itime, fortran_e(dg[0]).c_str(), fortran_e(dg[1]).c_str(),
                      fortran_e(dg[2]).c_str(), fortran_e(dg[3]).c_str());

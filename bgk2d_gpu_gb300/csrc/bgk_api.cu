@@ -557,7 +557,17 @@ int bgk_sync(bgk_handle *h)
 int bgk_diagno(bgk_handle *h, int32_t fluid_only, double out[4])
 {
     CHECK_HANDLE(h);
-    if (!out) return BGK_E_INVALID;
+    if (!out || fluid_only < BGK_DIAGNO_ALL || fluid_only > BGK_DIAGNO_REFERENCE) return BGK_E_INVALID;
+    if (fluid_only == BGK_DIAGNO_REFERENCE) {
+        CK(h, h->T.diagno_seq(h->L, h->cur, h->phase, h->cs.has_obs, h->d_out, h->st));
+        h->launches++;
+        CK(h, cudaMemcpyAsync(out, h->d_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        CK(h, cudaStreamSynchronize(h->st));
+        if (int rc = check_status(h)) return rc;
+        for (int i = 0; i < 4; ++i)
+            if (!std::isfinite(out[i])) return fail(h, BGK_E_NUMERIC, "diagno: non-finite mean");
+        return BGK_OK;
+    }
     CK(h, h->T.diagno(h->L, h->cur, h->phase, fluid_only, h->cs.has_obs, h->d_partial, h->nb_red, h->st));
     h->launches++;
     double s[4];

@@ -214,6 +214,50 @@ __global__ void __launch_bounds__(RED_NT) diagno_kernel(Lattice L, int cur, int 
     block_sum4<RED_NT>(acc, partial + 4 * blockIdx.x);
 }
 
+// diagno in the reference's own arithmetic (SRC/diagno.F90:63-101): sums in the compute kind K,
+// in the serial j-outer / i-inner order, then (sum / l) / m.  The per-cell moments of a chunk of
+// 1024 cells are computed in parallel; one thread adds them in order.  One block.
+template <typename S, typename K, bool HAS_OBS>
+__global__ void __launch_bounds__(1024) diagno_seq_kernel(Lattice L, int cur, int phase, double *out)
+{
+    __shared__ K sh[4][1024];
+    const int64_t n = (int64_t)L.lx * L.ly;
+    K rtot = (K)0, xtot = (K)0, ytot = (K)0, stot = (K)0;
+    for (int64_t c0 = 0; c0 < n; c0 += 1024) {
+        const int64_t c = c0 + threadIdx.x;
+        if (c < n) {
+            const int x = (int)(c % L.lx) + 1, y = (int)(c / L.lx) + 1;
+            K a[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) a[q] = post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
+            K rho, xj, yj;
+            moments<K>(a, rho, xj, yj);
+            sh[0][threadIdx.x] = rho;
+            sh[1][threadIdx.x] = xj;
+            sh[2][threadIdx.x] = yj;
+            sh[3][threadIdx.x] = xj * xj + yj * yj;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int cnt = (int)min((int64_t)1024, n - c0);
+            for (int k = 0; k < cnt; ++k) {
+                rtot = rtot + sh[0][k];
+                xtot = xtot + sh[1][k];
+                ytot = ytot + sh[2][k];
+                stot = stot + sh[3][k];
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const K fl = (K)(float)L.lx, fm = (K)(float)L.ly;  // float(l), float(m)
+        out[0] = (double)((xtot / fl) / fm);
+        out[1] = (double)((ytot / fl) / fm);
+        out[2] = (double)((rtot / fl) / fm);
+        out[3] = (double)((stot / fl) / fm);
+    }
+}
+
 // residual: sum |u - u_prev|^2 and |u|^2 (FP64); the snapshot is refreshed
 template <typename S, typename K, bool HAS_OBS>
 __global__ void __launch_bounds__(RED_NT) residual_kernel(Lattice L, int cur, int phase, double *uprev, double *vprev,

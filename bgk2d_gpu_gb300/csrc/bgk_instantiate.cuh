@@ -151,6 +151,14 @@ cudaError_t diagno(const Lattice &L, int cur, int phase, int fluid_only, bool ob
 }
 
 template <typename S, typename K>
+cudaError_t diagno_seq(const Lattice &L, int cur, int phase, bool obs, double *out, cudaStream_t st)
+{
+    if (obs) diagno_seq_kernel<S, K, true><<<1, 1024, 0, st>>>(L, cur, phase, out);
+    else diagno_seq_kernel<S, K, false><<<1, 1024, 0, st>>>(L, cur, phase, out);
+    return cudaGetLastError();
+}
+
+template <typename S, typename K>
 cudaError_t residual(const Lattice &L, int cur, int phase, bool obs, double *uprev, double *vprev, double *partial, int nb,
                      cudaStream_t st)
 {
@@ -233,6 +241,7 @@ KernelTable make_table()
     t.bcond_step = &bcond_step<S, K>;
     t.init_tgv = &init_tgv<S>;
     t.diagno = &diagno<S, K>;
+    t.diagno_seq = &diagno_seq<S, K>;
     t.residual = &residual<S, K>;
     t.draglift = &draglift<S, K>;
     t.fields = &fields<S, K>;

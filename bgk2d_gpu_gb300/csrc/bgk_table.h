@@ -34,6 +34,7 @@ struct KernelTable {
     cudaError_t (*init_tgv)(const Lattice &L, double u0, cudaStream_t st);
     cudaError_t (*diagno)(const Lattice &L, int cur, int phase, int fluid_only, bool obs, double *partial, int nb,
                           cudaStream_t st);
+    cudaError_t (*diagno_seq)(const Lattice &L, int cur, int phase, bool obs, double *out, cudaStream_t st);
     cudaError_t (*residual)(const Lattice &L, int cur, int phase, bool obs, double *uprev, double *vprev,
                             double *partial, int nb, cudaStream_t st);
     cudaError_t (*draglift)(const Lattice &L, int cur, int phase, int i0, int i1, int j0, int j1, double *partial,

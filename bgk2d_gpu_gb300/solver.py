@@ -162,10 +162,12 @@ class Solver:
         self._check(self._L.bgk_upload(self._h, self._ptrs(a), self.lx + 2), "upload")
 
     # -- reductions (FP64 on the device) ------------------------------------------------------
-    def diagno(self, fluid_only=False):
-        """(<u>, <v>, <rho>, <|u|^2>) as written to diagno.dat (SRC/diagno.F90:327)."""
+    def diagno(self, mode=0):
+        """(<u>, <v>, <rho>, <|u|^2>) (SRC/diagno.F90:63-101).  mode 0: FP64 sums over all cells;
+        1 (or True): fluid cells only; 2: the reference's own sums in the compute kind and order,
+        the values it writes to diagno.dat."""
         out = np.zeros(4)
-        self._check(self._L.bgk_diagno(self._h, int(bool(fluid_only)),
+        self._check(self._L.bgk_diagno(self._h, int(mode),
                                        out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))), "diagno")
         return out
 

@@ -151,8 +151,14 @@ int bgk_step(bgk_handle *h, int32_t nsteps);
 int bgk_step_timed(bgk_handle *h, int32_t nsteps, float *ms);
 int bgk_sync(bgk_handle *h);
 
-/* Reductions over the interior in FP64 (synchronise).
- * diagno (SRC/diagno.F90:282-320): out = <u>, <v>, <rho>, <|u|^2>; fluid_only skips obstacle cells. */
+/* Reductions over the interior (synchronise).
+ * diagno (SRC/diagno.F90:63-101): out = <u>, <v>, <rho>, <|u|^2>.  mode BGK_DIAGNO_ALL sums in FP64
+ * over all cells, BGK_DIAGNO_FLUID skips obstacle cells, BGK_DIAGNO_REFERENCE sums in the compute
+ * kind in the reference's sequential j/i order and divides as it does, so the means equal the
+ * values the reference writes to diagno.dat (one block on the GPU: slower, for output files). */
+#define BGK_DIAGNO_ALL 0
+#define BGK_DIAGNO_FLUID 1
+#define BGK_DIAGNO_REFERENCE 2
 int bgk_diagno(bgk_handle *h, int32_t fluid_only, double out[4]);
 /* momentum-exchange drag/lift (SRC/draglift.F90:383-444): out = Fx*norm, Fy*norm */
 int bgk_draglift(bgk_handle *h, double out[2]);
