@@ -2,8 +2,11 @@
 //
 // The reference keeps its populations in `module storage` and runs boundaries, propagation
 // and collision as separate directive loops (SRC/bgk2d.F90:100-102).  Here a handle owns the
-// populations in HBM; one fused kernel per time step applies the boundary rules, streams and
-// collides; steps are replayed from CUDA graphs; reductions run in FP64 on the device.
+// populations in HBM.  One fused kernel per time step applies the boundary rules, streams and
+// collides (ping-pong or AA); the two-pass scheme streams and collides in two kernels as the
+// ORIGINAL build does; the backward-facing step adds its boundary kernel in front.  Steps are
+// replayed from CUDA graphs, the tile shape and L2 prefetch distance come from the autotuner,
+// and reductions run on the device (FP64, or the reference's own order for diagno).
 #include <cuda_runtime.h>
 
 #include <utility>

@@ -1,10 +1,12 @@
 // bgk_batch.cu -- many independent lattices advanced by one persistent launch per time step.
 //
 // The reference advances one domain per run (SRC/bgk2d.F90:92-113).  A batch keeps any number
-// of ping-pong handles of the same (storage, compute) kind resident; one persistent kernel per
-// time step walks a work list of row-segment tiles over all of them (batch_pp_kernel), and the
-// step loop is replayed from CUDA graphs.  Tile shape, persistent grid size and steps per
-// graph are chosen by bgk_batch_tune from timed trial steps.
+// of ping-pong handles of the same (storage, compute) kind resident; one kernel per time step
+// covers a work list of row-segment tiles over all of them, either as one block per tile
+// (batch_pp_flat_kernel, with an L2 prefetch of the tile a set distance ahead) or as a
+// persistent grid walking contiguous chunks (batch_pp_kernel), and the step loop is replayed
+// from CUDA graphs.  Tile shape, grid form, prefetch distance and steps per graph are chosen by
+// bgk_batch_tune from timed trial steps.
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -14,6 +14,14 @@
 // and returns to phase 0.  Every cell reads and writes the same nine slots, so the update is
 // in place.  Boundary rules are applied in the P step when pulling and when pushing.
 //
+// Two-pass (ORIGINAL, SRC/movef.F90 + SRC/col.F90): the ping-pong kernel without its collision
+// streams into the second buffer, and col_kernel relaxes that buffer in place.
+//
+// Each thread updates N consecutive cells of a row with 8- or 16-byte vector accesses; the +-x
+// neighbours come from adjacent lanes.  A block may first ask for an L2 prefetch of the rows of
+// the block a set distance ahead in launch order (prefetch_tile).  The collision with the
+// Smagorinsky eddy viscosity is a template parameter (LES), instantiated separately.
+//
 // All arithmetic is one IEEE operation per reference operation: this file is compiled with
 // -fmad=false for the FP32/FP64 kinds so that results are bit-identical to the reference's
 // serial arithmetic; the 16-bit storage kernels are compiled with contraction enabled.
