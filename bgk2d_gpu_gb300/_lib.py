@@ -108,6 +108,7 @@ def load(build_if_missing: bool = True):
         "bgk_sync": (I32, [H]),
         "bgk_diagno": (I32, [H, I32, P(F64)]),
         "bgk_draglift": (I32, [H, P(F64)]),
+        "bgk_draglift_reference": (I32, [H, P(F64)]),
         "bgk_residual": (I32, [H, P(F64)]),
         "bgk_fields": (I32, [H, P(F64), P(F64), P(F64)]),
         "bgk_vtk_fields": (I32, [H, P(F32), P(F32), P(F32), P(F32), P(F32)]),

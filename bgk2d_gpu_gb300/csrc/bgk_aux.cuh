@@ -316,6 +316,34 @@ __global__ void __launch_bounds__(RED_NT) draglift_kernel(Lattice L, int cur, in
     block_sum4<RED_NT>(acc, partial + 4 * blockIdx.x);
 }
 
+// drag/lift in the reference's own arithmetic (SRC/draglift.F90:41-100): the x then the y sum in
+// the compute kind, in the serial j/i order over the box, then times norm = 1/(u_in^2 R).  One
+// thread (the box is (2R+7)^2 cells); cells of the box outside the interior are skipped.
+template <typename S, typename K, bool HAS_OBS>
+__global__ void draglift_seq_kernel(Lattice L, int cur, int phase, int i0, int i1, int j0, int j1, K norm, double *out)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    K f[2] = {(K)0, (K)0};
+    for (int comp = 0; comp < 2; ++comp) {
+        for (int y = j0; y <= j1; ++y) {
+            for (int x = i0; x <= i1; ++x) {
+                if (obs_bit(L, x, y)) continue;
+                K t[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int ox = x + cx_of(q), oy = y + cy_of(q);
+                    const bool ob = ox >= 1 && ox <= L.lx && oy >= 1 && oy <= L.ly && obs_bit(L, ox, oy);
+                    const K c = (K)(comp == 0 ? cx_of(q) : cy_of(q));
+                    t[q] = (((K)2 * c) * post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y)) * (ob ? (K)1 : (K)0);
+                }
+                f[comp] = f[comp] + (((((((t[0] + t[1]) + t[2]) + t[3]) + t[4]) + t[5]) + t[6]) + t[7]);
+            }
+        }
+    }
+    out[0] = (double)(f[0] * norm);
+    out[1] = (double)(f[1] * norm);
+}
+
 // rho, u, v fields of the interior (double), i fastest
 template <typename S, typename K, bool HAS_OBS>
 __global__ void fields_kernel(Lattice L, int cur, int phase, double *rho, double *u, double *v)

@@ -176,6 +176,14 @@ cudaError_t draglift(const Lattice &L, int cur, int phase, int i0, int i1, int j
 }
 
 template <typename S, typename K>
+cudaError_t draglift_seq(const Lattice &L, int cur, int phase, int i0, int i1, int j0, int j1, double norm, double *out,
+                         cudaStream_t st)
+{
+    draglift_seq_kernel<S, K, true><<<1, 32, 0, st>>>(L, cur, phase, i0, i1, j0, j1, (K)norm, out);
+    return cudaGetLastError();
+}
+
+template <typename S, typename K>
 cudaError_t fields(const Lattice &L, int cur, int phase, bool obs, double *rho, double *u, double *v, cudaStream_t st)
 {
     const int nb = 4 * 152;
@@ -244,6 +252,7 @@ KernelTable make_table()
     t.diagno_seq = &diagno_seq<S, K>;
     t.residual = &residual<S, K>;
     t.draglift = &draglift<S, K>;
+    t.draglift_seq = &draglift_seq<S, K>;
     t.fields = &fields<S, K>;
     t.vtk = &vtk<S, K>;
     t.batch_step = &batch_step<S, K>;

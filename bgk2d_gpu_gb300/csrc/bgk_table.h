@@ -39,6 +39,8 @@ struct KernelTable {
                             double *partial, int nb, cudaStream_t st);
     cudaError_t (*draglift)(const Lattice &L, int cur, int phase, int i0, int i1, int j0, int j1, double *partial,
                             int nb, cudaStream_t st);
+    cudaError_t (*draglift_seq)(const Lattice &L, int cur, int phase, int i0, int i1, int j0, int j1, double norm,
+                                double *out, cudaStream_t st);
     cudaError_t (*batch_step)(const Lattice *lats, const int *cur, const int4 *tiles, int ntiles, int parity, int cfg,
                               int grid, int pf, cudaStream_t st);
     cudaError_t (*fields)(const Lattice &L, int cur, int phase, bool obs, double *rho, double *u, double *v,

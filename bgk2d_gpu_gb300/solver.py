@@ -171,10 +171,12 @@ class Solver:
                                        out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))), "diagno")
         return out
 
-    def draglift(self):
+    def draglift(self, reference=False):
+        """(drag, lift) by momentum exchange (SRC/draglift.F90); reference=True: the reference's
+        own compute-kind sums in its order (the values it writes to drag.lift)."""
         out = np.zeros(2)
-        self._check(self._L.bgk_draglift(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
-                    "draglift")
+        fn = self._L.bgk_draglift_reference if reference else self._L.bgk_draglift
+        self._check(fn(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))), "draglift")
         return out
 
     def residual(self):

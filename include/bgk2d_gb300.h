@@ -162,6 +162,10 @@ int bgk_sync(bgk_handle *h);
 int bgk_diagno(bgk_handle *h, int32_t fluid_only, double out[4]);
 /* momentum-exchange drag/lift (SRC/draglift.F90:383-444): out = Fx*norm, Fy*norm */
 int bgk_draglift(bgk_handle *h, double out[2]);
+/* the same in the reference's own arithmetic and order (compute-kind sums over the box, serial
+ * j/i, x then y; SRC/draglift.F90:41-100), the values it writes to drag.lift; box cells outside
+ * the interior are skipped */
+int bgk_draglift_reference(bgk_handle *h, double out[2]);
 /* steady-state residual: ||u - u_prev||_2 / ||u||_2 since the previous call (first call: 1) */
 int bgk_residual(bgk_handle *h, double *out);
 /* macroscopic fields rho, u, v of the interior to host arrays of lx*ly doubles, i fastest */

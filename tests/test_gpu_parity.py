@@ -371,3 +371,14 @@ def test_diagno_reference_order_bit_exact(oracle_mod, bgk, case, prec, scheme):
         o.step(41)
         got = s.diagno(2)
     assert list(got) == list(o.diagno(0))
+
+
+@pytest.mark.parametrize("scheme", ["pingpong", "aa"])
+@pytest.mark.parametrize("prec", ["single", "double", "mixed2"])
+def test_draglift_reference_order_bit_exact(oracle_mod, bgk, prec, scheme):
+    """bgk_draglift_reference: SRC/draglift.F90's compute-kind sums in its order (oracle mode 0)."""
+    o, s = make_pair(oracle_mod, bgk, "vks", prec, scheme)
+    with s:
+        s.step(37)
+        o.step(37)
+        assert list(s.draglift(reference=True)) == list(o.draglift(0))
