@@ -81,3 +81,34 @@ def test_batch_configs_and_tuner_give_same_result(bgk):
             assert np.array_equal(s.download(), r.download())
     for s in members + ref:
         s.close()
+
+
+@pytest.mark.parametrize("tile,pf", [(1, 64), (5, 608), (4, 1216)])
+def test_batch_prefetch_does_not_change_results(bgk, tile, pf):
+    """One block per tile with an L2 prefetch of the work-list entry pf places ahead: the same
+    populations as the cases stepped alone."""
+    members, cases = make_cases(bgk, "f32")
+    alone = [bgk.Solver(storage="f32", **c) for c in cases]
+    with bgk.Batch("f32") as b:
+        for s in members:
+            b.add(s)
+        b.set_config(tile, 0, 8)
+        b.set_prefetch(pf)
+        b.step(21)
+        for s in alone:
+            s.step(21)
+        for s, a in zip(members, alone):
+            assert np.array_equal(s.download(), a.download())
+    for s in members + alone:
+        s.close()
+
+
+def test_unsupported_members_are_rejected(bgk):
+    """LES, backward-facing-step and two-pass handles carry steps the batch kernel does not."""
+    from bgk2d_gpu_gb300 import _lib
+    for kw in (dict(tcase="LDC", les=True), dict(tcase="BFS", lx=200), dict(tcase="LDC", scheme="original")):
+        lx = kw.pop("lx", 64)
+        with bgk.Solver(lx, 64, **kw) as s, bgk.Batch("f32") as b:
+            with pytest.raises(bgk.BgkError) as e:
+                b.add(s)
+            assert e.value.code == _lib.E_UNSUPPORTED

@@ -382,3 +382,14 @@ def test_draglift_reference_order_bit_exact(oracle_mod, bgk, prec, scheme):
         s.step(37)
         o.step(37)
         assert list(s.draglift(reference=True)) == list(o.draglift(0))
+
+
+def test_tuning_knobs_validate(bgk):
+    with bgk.Solver(64, 48) as s:
+        with pytest.raises(bgk.BgkError):
+            s.set_prefetch(-1)
+        with pytest.raises(bgk.BgkError):
+            s.set_tile(9)
+    with bgk.Solver(64, 48, scheme="aa") as s:
+        with pytest.raises(bgk.BgkError):
+            s.set_tile(6)  # staged rows exist for ping-pong only
