@@ -64,7 +64,7 @@ int fail(bgk_handle *h, int code, const char *fmt, ...)
     vsnprintf(buf, sizeof(buf), fmt, ap);
     va_end(ap);
     if (h) {
-        if (h->err.empty()) h->err = buf;
+        h->err = buf;  // the most recent failure (bgk_last_error)
         if (code == BGK_E_CUDA) h->sticky = code;
     }
     return code;

@@ -13,8 +13,8 @@
  *
  * Conventions
  *  - Every entry point returns an int status: BGK_OK (0) or a BGK_E_* code.  After an error
- *    the handle keeps the first message; read it with bgk_last_error.  CUDA errors are
- *    sticky for the handle.
+ *    the handle keeps its message (the most recent one); read it with bgk_last_error.  CUDA
+ *    errors and kernel-side timeouts are sticky for the handle.
  *  - Host population arrays use the reference layout (SRC/alloca.F90:220-238): nine
  *    column-major arrays (0:lx+1+ipad, 0:ly+1+jpad), i fastest, leading dimension
  *    ld = lx+2+ipad, direction order 01,03,05,08,10,12,14,17,19 (SRC/bgk2d.F90:29-39),
