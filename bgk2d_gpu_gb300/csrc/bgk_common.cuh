@@ -170,6 +170,14 @@ struct Lattice {
 
 template <typename S> __host__ __device__ constexpr int vec_of() { return 16 / (int)sizeof(S); }
 
+// Row of tiles processed by grid row b of gy: the last row of the domain (whose cells take the
+// slow boundary-rule path) runs second instead of last, so its blocks overlap with the bulk of
+// the launch instead of forming its tail.  A bijection of 0..gy-1.
+__device__ __forceinline__ int tile_row(int b, int gy)
+{
+    return (gy < 2 || b == 0) ? b : (b == 1 ? gy - 1 : b - 1);
+}
+
 // relaxation scalars of a lattice in the compute kind K
 template <typename K> __device__ __forceinline__ K lat_omega(const Lattice &L);
 template <> __device__ __forceinline__ float lat_omega<float>(const Lattice &L) { return L.omega_f; }

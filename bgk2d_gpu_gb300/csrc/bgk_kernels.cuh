@@ -568,7 +568,8 @@ __device__ __forceinline__ void prefetch_tile(const Lattice &L, const int parity
     if (t >= 9 * TY) return;
     const long long lin = (long long)blockIdx.y * gridDim.x + blockIdx.x + L.pf_ahead;
     if (lin >= (long long)gridDim.x * gridDim.y) return;
-    prefetch_segment<S, TXV, TY, N, KIND>(L, parity, t, (int)(lin % gridDim.x), (int)(lin / gridDim.x));
+    prefetch_segment<S, TXV, TY, N, KIND>(L, parity, t, (int)(lin % gridDim.x),
+                                          tile_row((int)(lin / gridDim.x), (int)gridDim.y));
 }
 
 // COLLIDE = false: the streaming half of the two-pass form (SRC/movef.F90 with the boundary
@@ -577,7 +578,7 @@ template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N, bool LES
 __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 || (sizeof(S) == 4 && N == 4)) ? 8 : (sizeof(S) == 2 ? 4 : 1)) pp_kernel(const Lattice L, const int parity)
 {
     if (L.pf_ahead > 0) prefetch_tile<S, TXV, TY, N, PF_PP>(L, parity);
-    pp_tile<S, K, TXV, TY, HAS_OBS, N, LES, COLLIDE>(L, blockIdx.x, blockIdx.y, parity);
+    pp_tile<S, K, TXV, TY, HAS_OBS, N, LES, COLLIDE>(L, blockIdx.x, tile_row(blockIdx.y, gridDim.y), parity);
 }
 
 // Persistent ping-pong step over many lattices.  The work list holds (lattice, tile x, tile y)
@@ -881,7 +882,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
     const int nv = (L.lx + VEC - 1) / VEC;
     const int tx = threadIdx.x;
     const int k = blockIdx.x * TXV + tx;
-    const int y = blockIdx.y * TY + threadIdx.y + 1;
+    const int y = tile_row(blockIdx.y, gridDim.y) * TY + threadIdx.y + 1;
     const bool in_rows = y <= L.ly;
     const bool loads = in_rows && k <= nv;
     const bool active = in_rows && k < nv;
@@ -949,7 +950,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
     if (L.pf_ahead > 0) prefetch_tile<S, TXV, TY, VEC, PF_AA_L>(L, 0);
     const int nv = (L.lx + VEC - 1) / VEC;
     const int k = blockIdx.x * TXV + threadIdx.x;
-    const int y = blockIdx.y * TY + threadIdx.y + 1;
+    const int y = tile_row(blockIdx.y, gridDim.y) * TY + threadIdx.y + 1;
     if (y > L.ly || k >= nv) return;
     const int xv = 1 + k * VEC;
     const int64_t pe = L.plane_elems;
@@ -1039,7 +1040,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
 {
     const int nv = (L.lx + N - 1) / N;
     const int k = blockIdx.x * TXV + threadIdx.x;
-    const int y = blockIdx.y * TY + threadIdx.y + 1;
+    const int y = tile_row(blockIdx.y, gridDim.y) * TY + threadIdx.y + 1;
     if (y > L.ly || k >= nv) return;
     const int xv = 1 + k * N;
     const int64_t pe = L.plane_elems;
