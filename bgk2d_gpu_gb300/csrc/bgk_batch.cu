@@ -59,8 +59,12 @@ int rebuild(bgk_batch *b)
         const int n = b->T.vec / tc.cdiv;
         const int nv = (h->L.lx + n - 1) / n;
         const int gx = (nv + tc.txv - 1) / tc.txv, gy = (h->L.ly + tc.ty - 1) / tc.ty;
-        for (int by = 0; by < gy; ++by)
+        // the lattice's last tile row (boundary-rule cells) second, as tile_row() orders single
+        // domains, so that it does not trail its lattice's work
+        for (int b = 0; b < gy; ++b) {
+            const int by = (gy < 2 || b == 0) ? b : (b == 1 ? gy - 1 : b - 1);
             for (int bx = 0; bx < gx; ++bx) tiles.push_back(make_int4((int)i, bx, by, 0));
+        }
     }
     if (lats.size() > b->cap_lats) {
         if (b->d_lats) cudaFreeAsync(b->d_lats, b->st);

@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(T, ((N * sizeof(S) <= 8) ? 1024 : 512) / T)
 
     const int t = threadIdx.x;
     const int band = blockIdx.x;
-    const int ya = 1 + blockIdx.y * rows;
+    const int ya = 1 + tile_row(blockIdx.y, gridDim.y) * rows;  // the last stripe runs second
     const int yb = min(L.ly, ya + rows - 1);  // inclusive
     if (ya > L.ly) return;
     const int64_t pe = L.plane_elems;
