@@ -393,3 +393,19 @@ def test_tuning_knobs_validate(bgk):
     with bgk.Solver(64, 48, scheme="aa") as s:
         with pytest.raises(bgk.BgkError):
             s.set_tile(6)  # staged rows exist for ping-pong only
+
+
+@pytest.mark.parametrize("scheme", ["pingpong", "aa", "original"])
+@pytest.mark.parametrize("lx,ly", [(2, 2), (3, 5), (5, 3), (9, 2), (17, 7), (33, 4), (130, 3)])
+def test_tiny_domains_every_tile_shape(oracle_mod, bgk, scheme, lx, ly):
+    """Domains narrower than one vector, a warp or a block, and one or two tile rows, in every
+    tile shape (block-row order, ragged vectors, single-vector rows)."""
+    for prec in ("single", "double"):
+        oprec, st, cp = PRECS[prec]
+        o = oracle_mod.Oracle(lx, ly, prec=oprec, tcase=0, svisc=0.05, u0=0.1, fused=scheme != "original")
+        with bgk.Solver(lx, ly, tcase="LDC", svisc=0.05, u0=0.1, storage=st, compute=cp, scheme=scheme) as s:
+            for tile in range(6):
+                s.set_tile(tile)
+                s.step(3)
+                o.step(3)
+                assert_same(o, s, scheme)
