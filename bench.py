@@ -402,6 +402,11 @@ def main():
     L = bgk.load()
     ptr_in = (ctypes.c_void_p * 9)(*[host[q].data_ptr() for q in range(9)])
     ptr_out = (ctypes.c_void_p * 9)(*[out[q].data_ptr() for q in range(9)])
+    # one-time setup outside the timed region: the step graphs of both buffer parities
+    s.step(32)
+    s.step(1)
+    s.step(32)
+    s.sync()
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
