@@ -873,7 +873,7 @@ __device__ __forceinline__ void push_vec(const Lattice &L, S *plane, int xv, int
 }
 
 template <typename S, typename K, int TXV, int TY, bool HAS_OBS, bool LES = false, int N = vec_of<S>()>
-__global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 ? (sizeof(S) == 2 ? 6 : 8) : (sizeof(S) == 2 ? 4 : 1)))
+__global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 ? 8 : (sizeof(S) == 2 ? 4 : 1)))
     aa_p_kernel(const Lattice L)
 {
     constexpr int VEC = N;  // cells per thread
@@ -943,7 +943,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
 
 // L step: local collision, phase 1 -> 0
 template <typename S, typename K, int TXV, int TY, bool HAS_OBS, bool LES = false, int N = vec_of<S>()>
-__global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 ? (sizeof(S) == 2 ? 6 : 8) : (sizeof(S) == 2 ? 4 : 1)))
+__global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 ? 8 : (sizeof(S) == 2 ? 4 : 1)))
     aa_l_kernel(const Lattice L)
 {
     constexpr int VEC = N;  // cells per thread
