@@ -817,23 +817,39 @@ __device__ __forceinline__ void push_vec(const Lattice &L, S *plane, int xv, int
             for (int c = 0; c < N - 1; ++c) sh[c] = g[c + 1];
             sh[N - 1] = shfl_down(g[0], W);
         }
-        if (!store) return;
-        if (cx == 0 || (cx == 1 && !left_edge) || (cx == -1 && !right_edge)) {
-            using U = typename VecT<S, N>::U;
-            union { U u; uint32_t w[N / 2]; } t;
+        // Every lane rounds its shifted vector in pairs.  A lane at an edge stores only the part
+        // of it that it owns (the element from the neighbouring lane is missing or belongs to a
+        // slow neighbour): halves and words of the same rounded pairs, as predicated stores, so
+        // the warp runs no divergent branch here.  The one element that crosses into the next
+        // segment is rounded alone.
+        using U = typename VecT<S, N>::U;
+        union { U u; uint32_t w[N / 2]; } t;
 #pragma unroll
-            for (int j = 0; j < N / 2; ++j)
-                t.w[j] = Store<S>::pack2_rs((float)sh[2 * j], (float)sh[2 * j + 1], pair_bits<q>(rh[j]));
-            *reinterpret_cast<U *>(plane + idx) = t.u;
-        } else if (cx == 1) {
-#pragma unroll
-            for (int c = 0; c < N - 1; ++c) plane[idx + 1 + c] = cvt(g[c]);
-        } else {
-#pragma unroll
-            for (int c = 1; c < N; ++c) plane[idx - 1 + c] = cvt(g[c]);
+        for (int j = 0; j < N / 2; ++j)
+            t.w[j] = Store<S>::pack2_rs((float)sh[2 * j], (float)sh[2 * j + 1], pair_bits<q>(rh[j]));
+        const bool full = cx == 0 || (cx == 1 ? !left_edge : !right_edge);
+        if (store && full) *reinterpret_cast<U *>(plane + idx) = t.u;
+        if constexpr (cx == 1) {
+            // owned: elements 1 .. N-1 of the vector at idx
+            if (store && left_edge) {
+                reinterpret_cast<uint16_t *>(plane)[idx + 1] = (uint16_t)(t.w[0] >> 16);
+                reinterpret_cast<uint32_t *>(plane + idx + 2)[0] = t.w[1];
+                if constexpr (N == 8) *reinterpret_cast<uint2 *>(plane + idx + 4) = make_uint2(t.w[2], t.w[3]);
+            }
+            if (store && right_edge) plane[idx + N] = cvt(g[N - 1]);
+        } else if constexpr (cx == -1) {
+            // owned: elements 0 .. N-2 of the vector at idx
+            if (store && right_edge) {
+                if constexpr (N == 8) {
+                    *reinterpret_cast<uint2 *>(plane + idx) = make_uint2(t.w[0], t.w[1]);
+                    reinterpret_cast<uint32_t *>(plane + idx + 4)[0] = t.w[2];
+                } else {
+                    reinterpret_cast<uint32_t *>(plane + idx)[0] = t.w[0];
+                }
+                reinterpret_cast<uint16_t *>(plane)[idx + N - 2] = (uint16_t)(t.w[N / 2 - 1] & 0xffffu);
+            }
+            if (store && left_edge) plane[idx - 1] = cvt(g[0]);
         }
-        if (cx == 1 && right_edge) plane[idx + N] = cvt(g[N - 1]);
-        if (cx == -1 && left_edge) plane[idx - 1] = cvt(g[0]);
     } else {
         S s[N];
 #pragma unroll
