@@ -248,12 +248,12 @@ __device__ __forceinline__ K shfl_up(K v, int w) { return __shfl_up_sync(0xfffff
 template <typename K>
 __device__ __forceinline__ K shfl_down(K v, int w) { return __shfl_down_sync(0xffffffffu, v, 1, w); }
 
-// Load VEC consecutive values of direction q pulled from (x - c_q): aligned 16-byte load of
-// row y - cy at the thread's own columns; the +-1 column shift comes from the neighbouring
-// lane, or from one scalar load at a segment edge.
-template <typename S, typename K, int q, int W, bool RAW = false, int N = vec_of<S>()>
+// Load N consecutive values of direction q pulled from (x - c_q): an aligned 8- or 16-byte load
+// of row y - cy at the thread's own columns; for a +-1 column shift, one scalar load of the
+// element beside the vector (it sits in the neighbouring lane's vector, so it comes from L1).
+template <typename S, typename K, int q, bool RAW = false, int N = vec_of<S>()>
 __device__ __forceinline__ void pull_vec(const Lattice &L, const S *plane, int xv, int y, bool loads,
-                                         int seg_lane, K (&out)[N])
+                                         K (&out)[N])
 {
     auto cvt = [](S v) -> K {
         if constexpr (RAW) return (K)Store<S>::raw_get(v);
@@ -274,17 +274,13 @@ __device__ __forceinline__ void pull_vec(const Lattice &L, const S *plane, int x
 #pragma unroll
         for (int c = 0; c < N; ++c) out[c] = kv[c];
     } else if (sx == -1) {
-        K left = shfl_up(kv[N - 1], W);
-        if ((seg_lane % W) == 0 && loads) left = cvt(plane[idx - 1]);
-        out[0] = left;
+        out[0] = loads ? cvt(plane[idx - 1]) : K(0);
 #pragma unroll
         for (int c = 1; c < N; ++c) out[c] = kv[c - 1];
     } else {
-        K right = shfl_down(kv[0], W);
-        if ((seg_lane % W) == W - 1 && loads) right = cvt(plane[idx + N]);
 #pragma unroll
         for (int c = 0; c < N - 1; ++c) out[c] = kv[c + 1];
-        out[N - 1] = right;
+        out[N - 1] = loads ? cvt(plane[idx + N]) : K(0);
     }
 }
 
@@ -475,31 +471,35 @@ template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N = vec_of<
           bool COLLIDE = true>
 __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const int by, const int parity)
 {
-    constexpr int W = TXV < 32 ? TXV : 32;
     const int nv = (L.lx + N - 1) / N;
     const int tx = threadIdx.x;
     const int k = bx * TXV + tx;
     const int y = by * TY + threadIdx.y + 1;
+    static_assert(TXV % 32 == 0, "a warp covers one row segment");
+    constexpr bool RAW = Is16<S>::value;
     const bool in_rows = y <= L.ly;
-    const bool loads = in_rows && k <= nv;
+    // 16-bit kinds: whole warps past the last row leave, and lanes past the row end load the
+    // last vector (their values are not used) instead of predicating the loads
+    if (RAW && !in_rows) return;
+    const bool loads = RAW || (in_rows && k <= nv);
     const bool active = in_rows && k < nv;
     const int xv = 1 + k * N;
+    const int xl = RAW ? 1 + min(k, nv) * N : xv;
     const int64_t pe = L.plane_elems;
     S *base = reinterpret_cast<S *>(L.planes);
     const S *src = base + (parity ? 9 : 0) * pe;
     S *dst = base + (parity ? 0 : 9) * pe;
 
-    constexpr bool RAW = Is16<S>::value;
     K x[9][N];
-    pull_vec<S, K, D01, W, RAW, N>(L, src + D01 * pe, xv, y, loads, tx, x[D01]);
-    pull_vec<S, K, D03, W, RAW, N>(L, src + D03 * pe, xv, y, loads, tx, x[D03]);
-    pull_vec<S, K, D05, W, RAW, N>(L, src + D05 * pe, xv, y, loads, tx, x[D05]);
-    pull_vec<S, K, D08, W, RAW, N>(L, src + D08 * pe, xv, y, loads, tx, x[D08]);
-    pull_vec<S, K, D10, W, RAW, N>(L, src + D10 * pe, xv, y, loads, tx, x[D10]);
-    pull_vec<S, K, D12, W, RAW, N>(L, src + D12 * pe, xv, y, loads, tx, x[D12]);
-    pull_vec<S, K, D14, W, RAW, N>(L, src + D14 * pe, xv, y, loads, tx, x[D14]);
-    pull_vec<S, K, D17, W, RAW, N>(L, src + D17 * pe, xv, y, loads, tx, x[D17]);
-    pull_vec<S, K, D19, W, RAW, N>(L, src + D19 * pe, xv, y, loads, tx, x[D19]);
+    pull_vec<S, K, D01, RAW, N>(L, src + D01 * pe, xl, y, loads, x[D01]);
+    pull_vec<S, K, D03, RAW, N>(L, src + D03 * pe, xl, y, loads, x[D03]);
+    pull_vec<S, K, D05, RAW, N>(L, src + D05 * pe, xl, y, loads, x[D05]);
+    pull_vec<S, K, D08, RAW, N>(L, src + D08 * pe, xl, y, loads, x[D08]);
+    pull_vec<S, K, D10, RAW, N>(L, src + D10 * pe, xl, y, loads, x[D10]);
+    pull_vec<S, K, D12, RAW, N>(L, src + D12 * pe, xl, y, loads, x[D12]);
+    pull_vec<S, K, D14, RAW, N>(L, src + D14 * pe, xl, y, loads, x[D14]);
+    pull_vec<S, K, D17, RAW, N>(L, src + D17 * pe, xl, y, loads, x[D17]);
+    pull_vec<S, K, D19, RAW, N>(L, src + D19 * pe, xl, y, loads, x[D19]);
     if (!active) return;
 
     const bool rowb = (y == 1) || (y == L.ly);
@@ -899,25 +899,28 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
     const int tx = threadIdx.x;
     const int k = blockIdx.x * TXV + tx;
     const int y = tile_row(blockIdx.y, gridDim.y) * TY + threadIdx.y + 1;
+    static_assert(TXV % 32 == 0, "a warp covers one row segment");
+    constexpr bool RAW = Is16<S>::value;
     const bool in_rows = y <= L.ly;
-    const bool loads = in_rows && k <= nv;
+    if (RAW && !in_rows) return;  // as in pp_tile
+    const bool loads = RAW || (in_rows && k <= nv);
     const bool active = in_rows && k < nv;
     const int xv = 1 + k * VEC;
+    const int xl = RAW ? 1 + min(k, nv) * VEC : xv;
     const int64_t pe = L.plane_elems;
     S *base = reinterpret_cast<S *>(L.planes);
 
     // pull f*_q from plane opp(q) at x - c_q
-    constexpr bool RAW = Is16<S>::value;
     K x[9][VEC];
-    pull_vec<S, K, D01, W, RAW, VEC>(L, base + D12 * pe, xv, y, loads, tx, x[D01]);
-    pull_vec<S, K, D03, W, RAW, VEC>(L, base + D10 * pe, xv, y, loads, tx, x[D03]);
-    pull_vec<S, K, D05, W, RAW, VEC>(L, base + D14 * pe, xv, y, loads, tx, x[D05]);
-    pull_vec<S, K, D08, W, RAW, VEC>(L, base + D17 * pe, xv, y, loads, tx, x[D08]);
-    pull_vec<S, K, D10, W, RAW, VEC>(L, base + D03 * pe, xv, y, loads, tx, x[D10]);
-    pull_vec<S, K, D12, W, RAW, VEC>(L, base + D01 * pe, xv, y, loads, tx, x[D12]);
-    pull_vec<S, K, D14, W, RAW, VEC>(L, base + D05 * pe, xv, y, loads, tx, x[D14]);
-    pull_vec<S, K, D17, W, RAW, VEC>(L, base + D08 * pe, xv, y, loads, tx, x[D17]);
-    pull_vec<S, K, D19, W, RAW, VEC>(L, base + D19 * pe, xv, y, loads, tx, x[D19]);
+    pull_vec<S, K, D01, RAW, VEC>(L, base + D12 * pe, xl, y, loads, x[D01]);
+    pull_vec<S, K, D03, RAW, VEC>(L, base + D10 * pe, xl, y, loads, x[D03]);
+    pull_vec<S, K, D05, RAW, VEC>(L, base + D14 * pe, xl, y, loads, x[D05]);
+    pull_vec<S, K, D08, RAW, VEC>(L, base + D17 * pe, xl, y, loads, x[D08]);
+    pull_vec<S, K, D10, RAW, VEC>(L, base + D03 * pe, xl, y, loads, x[D10]);
+    pull_vec<S, K, D12, RAW, VEC>(L, base + D01 * pe, xl, y, loads, x[D12]);
+    pull_vec<S, K, D14, RAW, VEC>(L, base + D05 * pe, xl, y, loads, x[D14]);
+    pull_vec<S, K, D17, RAW, VEC>(L, base + D08 * pe, xl, y, loads, x[D17]);
+    pull_vec<S, K, D19, RAW, VEC>(L, base + D19 * pe, xl, y, loads, x[D19]);
 
     // lanes on the scalar path: boundary rows, a ragged row end, obstacle surroundings
     bool slow = (y == 1) || (y == L.ly) || (nv == 1) || (k == nv - 1 && (L.lx % VEC) != 0);
