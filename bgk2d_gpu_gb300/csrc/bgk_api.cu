@@ -790,7 +790,11 @@ int bgk_tune(bgk_handle *h, int32_t trial_steps, int32_t *tile_cfg, int32_t *ste
     // and one wave of 8 resident blocks per SM ahead
     const int pfs[3] = {0, 4 * sms, 8 * sms};
     const int ncfg = (h->L.scheme == BGK_SCHEME_PINGPONG && !h->two_pass) ? NUM_STEP_CFG : NUM_CFG;
-    for (int c = 0; c < ncfg; ++c) {
+    // AA with 16-bit storage rounds each value that crosses a warp edge on its own, and where
+    // the warp edges fall depends on the bytes per thread.  Only the 8-byte shapes (4, 5) are
+    // tried, so the populations of a tuned run do not depend on which of them wins.
+    const bool aa16 = h->L.scheme == BGK_SCHEME_AA && h->T.elem_bytes == 2;
+    for (int c = aa16 ? 4 : 0; c < ncfg; ++c) {
         const int npf = (c < NUM_CFG && !h->L.les) ? 3 : 1;
         for (int p = 0; p < npf; ++p) {
             if ((rc = bgk_set_tile(h, c)) || (rc = bgk_set_prefetch(h, pfs[p]))) return rc;

@@ -189,7 +189,9 @@ int bgk_get_scalars(bgk_handle *h, double out[4], int64_t *itime);
  *   of cells per plane; 4 = 32x4 and 5 = 128x1 with half a vector (8 bytes) per thread.  Ping-pong only: 6, 7, 8 stage the source rows in shared memory with bulk
  *   async copies (128 threads and 3 rows in flight, 128 and 4, 256 and 3; 8 bytes per thread);
  *   such a step reports BGK_E_TIMEOUT at the next synchronisation if a copy never completed.
- *   Results do not depend on the choice. */
+ *   Results do not depend on the choice, with one exception: AA with 16-bit storage rounds
+ *   each value that crosses a warp edge on its own, so shapes 0-3 and shapes 4-5 give slightly
+ *   different populations (identical within each group). */
 int bgk_set_tile(bgk_handle *h, int32_t tile_cfg);
 /* configurations 0-5 (ping-pong and AA): each block first asks for an L2 prefetch (bulk, no
  * registers) of the source rows of the block `blocks_ahead` places further on in launch order;
@@ -197,7 +199,8 @@ int bgk_set_tile(bgk_handle *h, int32_t tile_cfg);
 int bgk_set_prefetch(bgk_handle *h, int32_t blocks_ahead);
 int bgk_get_prefetch(bgk_handle *h, int32_t *blocks_ahead);
 /* time `trial_steps` real steps per tile shape and prefetch distance (the state advances) and
- * keep the fastest */
+ * keep the fastest.  AA with 16-bit storage tries shapes 4 and 5 only, so the populations of a
+ * tuned run do not depend on which shape wins. */
 int bgk_tune(bgk_handle *h, int32_t trial_steps, int32_t *tile_cfg, int32_t *steps_run);
 
 /* bytes of HBM the handle holds, and the algorithmic bytes moved per lattice update */
