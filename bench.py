@@ -155,7 +155,8 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    cb = cpu_reference(steps_budget_s=max(5.0, 2.0 * args.steps / 2000 * 5), max_steps=max(args.steps, 3))
+    # a bounded sample: 5 s per 1000 requested steps, between 5 s and 60 s of host time
+    cb = cpu_reference(steps_budget_s=min(60.0, max(5.0, 5.0 * args.steps / 1000)), max_steps=max(args.steps, 3))
     line = {"metric": "GLUPS", "value": cb["value"], "unit": "GLUPS", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": LX * LY / (cb["value"] * 1e9) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
