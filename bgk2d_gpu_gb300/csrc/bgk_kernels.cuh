@@ -103,43 +103,103 @@ __device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced
     x[8] = x19 - omega * (x19 - e19);
 }
 
+// Exact IEEE operations for the 16-bit kinds' collision, on one value (float) or on the values
+// of two cells at once (F2: the packed FP32 pair instructions add/sub/mul/fma .f32x2 of sm_100 and
+// later, one instruction for both cells).  The intrinsics are never contracted, so the scalar
+// and the packed collision round identically and give the same bits for the same inputs.
+struct F2 {
+    unsigned long long v;
+};
+__device__ __forceinline__ F2 f2_pack(float lo, float hi)
+{
+    F2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(F2 a, float &lo, float &hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
+}
+__device__ __forceinline__ float op_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float op_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float op_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float op_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float op_rcp(float a) { return __fdividef(1.0f, a); }
+__device__ __forceinline__ F2 op_add(F2 a, F2 b)
+{
+    F2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ F2 op_sub(F2 a, F2 b)
+{
+    F2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ F2 op_mul(F2 a, F2 b)
+{
+    F2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ F2 op_fma(F2 a, F2 b, F2 c)
+{
+    F2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+    return r;
+}
+__device__ __forceinline__ F2 op_rcp(F2 a)
+{
+    float lo, hi;
+    f2_unpack(a, lo, hi);
+    return f2_pack(__fdividef(1.0f, lo), __fdividef(1.0f, hi));
+}
+template <typename T> __device__ __forceinline__ T splat(float a);
+template <> __device__ __forceinline__ float splat<float>(float a) { return a; }
+template <> __device__ __forceinline__ F2 splat<F2>(float a) { return f2_pack(a, a); }
+
 // Collision of the 16-bit storage kernels, on scaled deviations D_q = s_q (f_q - w_q) in FP32.
 // Same BGK relaxation as collide<K> rewritten for throughput: with j = rho u and
 // A = (rho - 1) - 1.5 j.u, the equilibrium deviation is w_q (A + 3 c.j + 4.5 (c.j)(c.u)); the
 // scales satisfy s_q w_q = 8/9 for every q, so D_q' = (1 - omega) D_q + (8/9) omega (...).
-__device__ __forceinline__ void collide_scaled(float (&D)[9], float omega, float fgrad, bool forced)
+// T = float: one cell; T = F2: two cells.
+template <typename T>
+__device__ __forceinline__ void collide_scaled(T (&D)[9], float omega, float fgrad, bool forced)
 {
-    const float i32 = 1.0f / 32.0f, i8 = 1.0f / 8.0f;
-    const float sd = (D[D01] + D[D03]) + (D[D10] + D[D12]);
-    const float sa = (D[D05] + D[D08]) + (D[D14] + D[D17]);
-    const float rho1 = fmaf(sd, i32, fmaf(sa, i8, D[D19] * 0.5f));
-    const float rho = 1.0f + rho1;
-    const float dpp = D[D03] - D[D10];  // c = (1, 1)
-    const float dpm = D[D01] - D[D12];  // c = (1,-1)
-    const float jx = fmaf(dpp + dpm, i32, (D[D05] - D[D14]) * i8);
-    const float jy = fmaf(dpp - dpm, i32, (D[D08] - D[D17]) * i8);
-    const float rinv = __fdividef(1.0f, rho);
-    const float ux = jx * rinv, uy = jy * rinv;
-    const float A = fmaf(-1.5f, fmaf(jx, ux, jy * uy), rho1);
-    const float omc = 1.0f - omega, k = omega * (8.0f / 9.0f);
+    const T i32 = splat<T>(1.0f / 32.0f), i8 = splat<T>(1.0f / 8.0f);
+    const T sd = op_add(op_add(D[D01], D[D03]), op_add(D[D10], D[D12]));
+    const T sa = op_add(op_add(D[D05], D[D08]), op_add(D[D14], D[D17]));
+    const T rho1 = op_fma(sd, i32, op_fma(sa, i8, op_mul(D[D19], splat<T>(0.5f))));
+    const T rho = op_add(splat<T>(1.0f), rho1);
+    const T dpp = op_sub(D[D03], D[D10]);  // c = (1, 1)
+    const T dpm = op_sub(D[D01], D[D12]);  // c = (1,-1)
+    const T jx = op_fma(op_add(dpp, dpm), i32, op_mul(op_sub(D[D05], D[D14]), i8));
+    const T jy = op_fma(op_sub(dpp, dpm), i32, op_mul(op_sub(D[D08], D[D17]), i8));
+    const T rinv = op_rcp(rho);
+    const T ux = op_mul(jx, rinv), uy = op_mul(jy, rinv);
+    const T A = op_fma(splat<T>(-1.5f), op_fma(jx, ux, op_mul(jy, uy)), rho1);
+    const T omc = splat<T>(__fsub_rn(1.0f, omega)), k = splat<T>(__fmul_rn(omega, 8.0f / 9.0f));
     // k folded into A and j, 4.5 into u: per direction pair (q, opp q) with kcj = k c.j and
     // cu45 = 4.5 c.u,  D' = (1 - omega) D + kA + kcj cu45 +- 3 kcj
-    const float kA = k * A, kjx = k * jx, kjy = k * jy;
-    const float ux45 = 4.5f * ux, uy45 = 4.5f * uy;
-    auto pair = [&](int qp, int qm, float kcj, float cu45) {
-        const float t = fmaf(kcj, cu45, kA);
-        D[qp] = fmaf(omc, D[qp], fmaf(3.0f, kcj, t));
-        D[qm] = fmaf(omc, D[qm], fmaf(-3.0f, kcj, t));
+    const T kA = op_mul(k, A), kjx = op_mul(k, jx), kjy = op_mul(k, jy);
+    const T ux45 = op_mul(splat<T>(4.5f), ux), uy45 = op_mul(splat<T>(4.5f), uy);
+    auto pair = [&](int qp, int qm, T kcj, T cu45) {
+        const T t = op_fma(kcj, cu45, kA);
+        D[qp] = op_fma(omc, D[qp], op_fma(splat<T>(3.0f), kcj, t));
+        D[qm] = op_fma(omc, D[qm], op_fma(splat<T>(-3.0f), kcj, t));
     };
     pair(D05, D14, kjx, ux45);
     pair(D08, D17, kjy, uy45);
-    pair(D03, D10, kjx + kjy, ux45 + uy45);
-    pair(D01, D12, kjx - kjy, ux45 - uy45);
-    D[D19] = fmaf(omc, D[D19], kA);
+    pair(D03, D10, op_add(kjx, kjy), op_add(ux45, uy45));
+    pair(D01, D12, op_sub(kjx, kjy), op_sub(ux45, uy45));
+    D[D19] = op_fma(omc, D[D19], kA);
     if (forced) {
-        const float F = fgrad * rho;  // +F on 01,03,05 and -F on 10,12,14 (SRC/col_MC.F90:285-291)
-        D[D01] += 32.0f * F; D[D03] += 32.0f * F; D[D05] += 8.0f * F;
-        D[D10] -= 32.0f * F; D[D12] -= 32.0f * F; D[D14] -= 8.0f * F;
+        // +F on 01,03,05 and -F on 10,12,14 (SRC/col_MC.F90:285-291); 32 F and 8 F are exact
+        const T F = op_mul(splat<T>(fgrad), rho);
+        const T F32 = op_mul(splat<T>(32.0f), F), F8 = op_mul(splat<T>(8.0f), F);
+        D[D01] = op_add(D[D01], F32); D[D03] = op_add(D[D03], F32); D[D05] = op_add(D[D05], F8);
+        D[D10] = op_sub(D[D10], F32); D[D12] = op_sub(D[D12], F32); D[D14] = op_sub(D[D14], F8);
     }
 }
 
@@ -153,7 +213,7 @@ __device__ __forceinline__ void collide_stored(K (&v)[9], K omega, K fgrad, bool
         float D[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) D[q] = (float)v[q] * scale_of(q);  // exact: powers of two
-        collide_scaled(D, (float)omega, (float)fgrad, forced);
+        collide_scaled<float>(D, (float)omega, (float)fgrad, forced);
 #pragma unroll
         for (int q = 0; q < 9; ++q) v[q] = (K)(D[q] * (1.0f / scale_of(q)));
     } else {
@@ -339,6 +399,20 @@ __device__ __forceinline__ K pull_rule(const Lattice &L, int q, int x, int y, Pl
 template <typename S, typename K, bool RAW, int N = vec_of<S>(), bool LES = false>
 __device__ __forceinline__ void relax_vec(K (&x)[9][N], K omega, K fgrad, bool forced, K cte_s)
 {
+    if constexpr (RAW && !LES) {
+        // two cells per packed FP32 instruction
+        static_assert(N % 2 == 0, "16-bit vectors hold an even number of cells");
+#pragma unroll
+        for (int c = 0; c < N; c += 2) {
+            F2 v[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) v[q] = f2_pack(x[q][c], x[q][c + 1]);
+            collide_scaled<F2>(v, (float)omega, (float)fgrad, forced);
+#pragma unroll
+            for (int q = 0; q < 9; ++q) f2_unpack(v[q], x[q][c], x[q][c + 1]);
+        }
+        return;
+    }
 #pragma unroll
     for (int c = 0; c < N; ++c) {
         K v[9];
@@ -352,7 +426,7 @@ __device__ __forceinline__ void relax_vec(K (&x)[9][N], K omega, K fgrad, bool f
 #pragma unroll
                 for (int q = 0; q < 9; ++q) v[q] *= scale_of(q);
             } else {
-                collide_scaled(v, (float)omega, (float)fgrad, forced);
+                collide_scaled<float>(v, (float)omega, (float)fgrad, forced);
             }
         } else {
             collide<K, LES>(v, omega, fgrad, forced, cte_s);
