@@ -583,7 +583,7 @@ int bgk_diagno(bgk_handle *h, int32_t fluid_only, double out[4])
     int rc = reduce4(h, s);
     if (rc) return rc;
     const double l = h->desc.lx, m = h->desc.ly;
-    for (int i = 0; i < 4; ++i) out[i] = (s[i] / l) / m;  // SRC/diagno.F90:317-320
+    for (int i = 0; i < 4; ++i) out[i] = (s[i] / l) / m;  // SRC/diagno.F90:98-101
     for (int i = 0; i < 4; ++i)
         if (!std::isfinite(s[i])) return fail(h, BGK_E_NUMERIC, "diagno: non-finite sum");
     return BGK_OK;

@@ -152,7 +152,7 @@ __global__ void bfs_bcond_kernel(const Lattice L, const int cur, const int stepx
     }
 }
 
-// moments with the reference's per-cell arithmetic (SRC/diagno.F90:285-307)
+// moments with the reference's per-cell arithmetic (SRC/diagno.F90:82-93)
 template <typename K>
 __device__ __forceinline__ void moments(const K (&a)[9], K &rho, K &xj, K &yj)
 {
@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(RED_NT) residual_kernel(Lattice L, int cur, in
     block_sum4<RED_NT>(acc, partial + 4 * blockIdx.x);
 }
 
-// momentum-exchange force on the obstacle (SRC/draglift.F90:405-441) over a box of cells
+// momentum-exchange force on the obstacle (SRC/draglift.F90:62-100) over a box of cells
 template <typename S, typename K, bool HAS_OBS>
 __global__ void __launch_bounds__(RED_NT) draglift_kernel(Lattice L, int cur, int phase, int i0, int i1, int j0, int j1,
                                                           double *partial)
@@ -363,7 +363,7 @@ __global__ void fields_kernel(Lattice L, int cur, int phase, double *rho, double
 }
 
 // ---------------------------------------------------------------------------------------------
-// Fields of the reference's VTK writers (SRC/vtk_xy.binary.F90:75-140, SRC/vtk_om.binary.F90:62-150),
+// Fields of the reference's VTK writers (SRC/vtk_xy.binary.F90:75-140, SRC/vtk_om.binary.F90:61-155),
 // in their real(sp) arithmetic: sums of stored values in the storage kind (FP32 for the 16-bit
 // kinds), rounded to single precision; the vorticity's quotients divide a storage-kind numerator by
 // a single-precision density in the wider kind.

@@ -221,7 +221,7 @@ __device__ __forceinline__ void collide_stored(K (&v)[9], K omega, K fgrad, bool
     }
 }
 
-// equilibrium deviation of the outflow ghost (rho = 1, local u): bcond.inflow.F90:211-230
+// equilibrium deviation of the outflow ghost (rho = 1, local u): bcond.inflow.F90:80-99
 template <typename K>
 __device__ __forceinline__ K outflow_eq(int q, K a01, K a03, K a05, K a08, K a10, K a12, K a14, K a17)
 {

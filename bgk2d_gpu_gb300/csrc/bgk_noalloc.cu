@@ -32,7 +32,7 @@ struct Planes {
     const void *p[9];
 };
 
-// per-cell moments as SRC/diagno.F90:285-307, in the storage kind T
+// per-cell moments as SRC/diagno.F90:82-93, in the storage kind T
 template <typename T>
 __global__ void __launch_bounds__(NA_THREADS) noalloc_diagno_kernel(Planes P, long long ld, int lx, int ly,
                                                                     double *scratch)
@@ -127,7 +127,7 @@ extern "C" int bgk_diagno_noalloc(const void *const pops[9], int64_t ld, int32_t
     if (cudaGetLastError() != cudaSuccess) return BGK_E_CUDA;
     double s[4];
     if (cudaMemcpy(s, scratch + 4 * NA_MAX_CHUNKS, sizeof(s), cudaMemcpyDeviceToHost) != cudaSuccess) return BGK_E_CUDA;
-    for (int q = 0; q < 4; ++q) out[q] = (s[q] / (double)lx) / (double)ly;  // SRC/diagno.F90:317-320
+    for (int q = 0; q < 4; ++q) out[q] = (s[q] / (double)lx) / (double)ly;  // SRC/diagno.F90:98-101
     for (int q = 0; q < 4; ++q)
         if (!(s[q] == s[q]) || s[q] - s[q] != 0.0) return BGK_E_NUMERIC;
     return BGK_OK;

@@ -32,7 +32,7 @@ struct CaseSetup {
 };
 
 // equilibrium deviation of an inflow ghost at velocity (xj, 0) with rho = 1
-// (SRC/bcond.inflow.F90:233-244).  The `3.d0` literal promotes that sub-expression to double
+// (SRC/bcond.inflow.F90:101-113).  The `3.d0` literal promotes that sub-expression to double
 // even in a single-precision build, which is kept here.
 template <typename K>
 inline void inflow_eq(K xj, K out[3])
@@ -202,7 +202,7 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
     for (int f = YLO; f <= YHI; ++f)
         if (cs.faces[f] != FK_WALL && cs.faces[f] != FK_PERIODIC && !cs.bfs) return "y faces must be walls or periodic";
 
-    // inflow table (u_inflow=0.1 is a default-real literal in SRC/bcond.inflow.F90:190)
+    // inflow table (u_inflow=0.1 is a default-real literal in SRC/bcond.inflow.F90:59)
     const K uin = d.u_inflow > 0 ? (K)d.u_inflow : (K)0.1f;
     cs.u_inflow = (double)uin;
     cs.inflow.assign(3 * (size_t)(m + 2), 0.0);

@@ -260,7 +260,7 @@ class Solver:
         return u, v, den
 
     def probe(self, i0, j0, pops=None):
-        """u, v, rho at one node (SRC/probe.F90:57-66)."""
+        """u, v, rho at one node (SRC/probe.F90:46-62)."""
         a = self.download() if pops is None else pops
         x = a[:, j0, i0]
         k = a.dtype.type

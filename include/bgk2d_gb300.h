@@ -15,7 +15,7 @@
  *  - Every entry point returns an int status: BGK_OK (0) or a BGK_E_* code.  After an error
  *    the handle keeps its message (the most recent one); read it with bgk_last_error.  CUDA
  *    errors and kernel-side timeouts are sticky for the handle.
- *  - Host population arrays use the reference layout (SRC/alloca.F90:220-238): nine
+ *  - Host population arrays use the reference layout (SRC/alloca.F90:113-121): nine
  *    column-major arrays (0:lx+1+ipad, 0:ly+1+jpad), i fastest, leading dimension
  *    ld = lx+2+ipad, direction order 01,03,05,08,10,12,14,17,19 (SRC/bgk2d.F90:29-39),
  *    holding the deviations f_i - w_i (the reference's default "shifted" storage).
@@ -76,8 +76,8 @@ extern "C" {
 /* face kinds for BGK_CASE_CUSTOM; faces are x_lo (i=0), x_hi (i=lx+1), y_lo, y_hi */
 #define BGK_FACE_WALL 0         /* half-way bounce-back, optional wall velocity */
 #define BGK_FACE_PERIODIC 1
-#define BGK_FACE_INFLOW 2       /* x faces: equilibrium at rho=1, prescribed u (bcond.inflow.F90:233-244) */
-#define BGK_FACE_OUTFLOW_EQ 3   /* x_hi: equilibrium at rho=1 and the local u (bcond.inflow.F90:211-230) */
+#define BGK_FACE_INFLOW 2       /* x faces: equilibrium at rho=1, prescribed u (bcond.inflow.F90:101-113) */
+#define BGK_FACE_OUTFLOW_EQ 3   /* x_hi: equilibrium at rho=1 and the local u (bcond.inflow.F90:80-99) */
 #define BGK_FACE_OUTFLOW_ZG 4   /* x_hi: zero-gradient copy of column lx */
 
 /* obstacle shapes (SRC/build.obs.F90) */
@@ -160,7 +160,7 @@ int bgk_sync(bgk_handle *h);
 #define BGK_DIAGNO_FLUID 1
 #define BGK_DIAGNO_REFERENCE 2
 int bgk_diagno(bgk_handle *h, int32_t fluid_only, double out[4]);
-/* momentum-exchange drag/lift (SRC/draglift.F90:383-444): out = Fx*norm, Fy*norm */
+/* momentum-exchange drag/lift (SRC/draglift.F90:41-100): out = Fx*norm, Fy*norm */
 int bgk_draglift(bgk_handle *h, double out[2]);
 /* the same in the reference's own arithmetic and order (compute-kind sums over the box, serial
  * j/i, x then y; SRC/draglift.F90:41-100), the values it writes to drag.lift; box cells outside
@@ -173,7 +173,7 @@ int bgk_fields(bgk_handle *h, double *rho, double *u, double *v);
 /* obstacle mask obs(1:lx,1:ly) and imin,imax,jmin,jmax,nobs (SRC/build.obs.F90) */
 int bgk_get_obs(bgk_handle *h, int32_t *mask, int32_t bbox[5]);
 /* The fields the reference's VTK writers compute on the host after a device-to-host update
- * (SRC/vtk_xy.binary.F90:75-140, SRC/vtk_om.binary.F90:62-150), computed on the device in their
+ * (SRC/vtk_xy.binary.F90:75-140, SRC/vtk_om.binary.F90:61-155), computed on the device in their
  * single-precision arithmetic, so that 5 float fields cross the bus instead of 9 populations:
  * u/rho, w/rho, rho over the interior (lx*ly each, x fastest), vorticity and stream function over
  * x = 2..lx-1, y = 2..ly-1 ((lx-2)*(ly-2) each).  The stream function integrates from row 1: the

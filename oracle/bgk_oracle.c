@@ -99,7 +99,7 @@ orc_state *orc_create(const orc_params *p)
     for (int q = 0; q < 9; ++q) {
         s->A[q] = malloc(s->n * (size_t)s->ssize);
         s->B[q] = malloc(s->n * (size_t)s->ssize);
-        /* alloca.F90:240-258 poisons every array with huge(mykind) */
+        /* alloca.F90:133-151 poisons every array with huge(mykind) */
         for (size_t k = 0; k < s->n; ++k) {
             if (s->ssize == 8) { ((double *)s->A[q])[k] = DBL_MAX; ((double *)s->B[q])[k] = DBL_MAX; }
             else { ((float *)s->A[q])[k] = FLT_MAX; ((float *)s->B[q])[k] = FLT_MAX; }

@@ -16,7 +16,7 @@
  * Fortran operation is one IEEE operation.
  *
  * Arrays use the reference layout: population q is a column-major array
- * (0:l+1, 0:m+1), i fastest (SRC/alloca.F90:220-238, ipad=jpad=0), and the
+ * (0:l+1, 0:m+1), i fastest (SRC/alloca.F90:113-121, ipad=jpad=0), and the
  * direction order is 01,03,05,08,10,12,14,17,19 (SRC/bgk2d.F90:29-39).
  */
 #ifndef BGK_ORACLE_H

@@ -188,7 +188,7 @@ static void FN(bcond_channel)(orc_state *s)
     }
 }
 
-/* outflow equilibrium shared by bcond.inflow.F90:211-230 and bcond.step.F90:82-101 */
+/* outflow equilibrium shared by bcond.inflow.F90:80-99 and bcond.step.F90:82-101 */
 static void FN(outflow_col)(orc_state *s, int j)
 {
     const int l = s->l, l1 = l + 1;
@@ -204,7 +204,7 @@ static void FN(outflow_col)(orc_state *s, int j)
     A_(6, l1, j) = (S)((crho * P1) * (cte1 + cx14));
 }
 
-/* inflow equilibrium at velocity (xj, 0): bcond.inflow.F90:233-244, bcond.step.F90:135-150 */
+/* inflow equilibrium at velocity (xj, 0): bcond.inflow.F90:101-113, bcond.step.F90:135-150 */
 static void FN(inflow_cell)(orc_state *s, int j, K xj)
 {
     const K crho = UNO, cte1 = ZERO;
@@ -219,7 +219,7 @@ static void FN(inflow_cell)(orc_state *s, int j, K xj)
     A_(2, 0, j) = (S)((crho * P1) * (cte1 + cx05));
 }
 
-/* bcond.inflow.F90:190-285: outflow (x=l+1), inflow u=0.1 (x=0), periodic y */
+/* bcond.inflow.F90:59-154: outflow (x=l+1), inflow u=0.1 (x=0), periodic y */
 static void FN(bcond_inflow)(orc_state *s)
 {
     const int l = s->l, m = s->m, m1 = m + 1;
@@ -238,7 +238,7 @@ static void FN(bcond_inflow)(orc_state *s)
     }
 }
 
-/* bcond.couette.F90:193-253: periodic x (j=1..m), wall y=0, moving wall y=m+1 */
+/* bcond.couette.F90:41-104: periodic x (j=1..m), wall y=0, moving wall y=m+1 */
 static void FN(bcond_couette)(orc_state *s)
 {
     const int l = s->l, m = s->m, l1 = l + 1, m1 = m + 1;
@@ -498,7 +498,7 @@ static void FN(step)(orc_state *s, int nsteps, int nthreads)
     }
 }
 
-/* per-cell moments exactly as diagno.F90:285-307 */
+/* per-cell moments exactly as diagno.F90:82-93 */
 static inline void FN(moments)(const orc_state *s, int i, int j, K *rho_o, K *xj_o, K *yj_o)
 {
     const K cte1 = UNO;
@@ -512,7 +512,7 @@ static inline void FN(moments)(const orc_state *s, int i, int j, K *rho_o, K *xj
     *rho_o = rho;
 }
 
-/* diagno.F90:267-320 */
+/* diagno.F90:63-101 */
 static void FN(diagno)(const orc_state *s, int mode, double *out)
 {
     const int l = s->l, m = s->m;
@@ -551,7 +551,7 @@ static void FN(diagno)(const orc_state *s, int mode, double *out)
     }
 }
 
-/* draglift.F90:383-444 (box around the obstacle centre, border 3) */
+/* draglift.F90:41-100 (box around the obstacle centre, border 3) */
 static void FN(draglift)(const orc_state *s, int mode, double *out)
 {
     static const int icx[8] = {1, 1, 1, 0, -1, -1, -1, 0};
@@ -599,7 +599,7 @@ static void FN(prof_j)(const orc_state *s, int icoord, double *u, double *v, dou
     }
 }
 
-/* SRC/vtk_xy.binary.F90:75-140 and SRC/vtk_om.binary.F90:62-150: the VTK writers' fields in
+/* SRC/vtk_xy.binary.F90:75-140 and SRC/vtk_om.binary.F90:61-155: the VTK writers' fields in
  * real(sp).  Sums of stored values run in the storage kind S (mystorage, not mykind: float in
  * MIXED2) and are then rounded to sp; the
  * vorticity's quotients divide a storage-kind numerator by an sp denominator in the wider kind. */
