@@ -173,7 +173,7 @@ def run_profile(args):
     scheme, storage = args.profile.split("_")
     compute = "f64" if storage == "f64" else "f32"
     with bgk.Solver(args.size, args.size, tcase="LDC", svisc=SVISC * args.size / LX, u0=U0, storage=storage,
-                    compute=compute, scheme=scheme) as s:
+                    compute=compute, scheme=scheme, les=args.les) as s:
         if args.tile >= 0:
             s.set_tile(args.tile)
         s.set_prefetch(args.prefetch)
@@ -181,16 +181,16 @@ def run_profile(args):
         s.sync()
         ms = s.step_timed(args.steps)
     per = ms / args.steps
-    print(f"profile run {args.profile} {args.size}^2 tile={args.tile} prefetch={args.prefetch} "
+    print(f"profile run {args.profile}{'_les' if args.les else ''} {args.size}^2 tile={args.tile} prefetch={args.prefetch} "
           f"warmup={args.warmup} steps={args.steps} "
           f"ms/step={per:.4f} GLUPS={args.size * args.size / (per * 1e-3) / 1e9:.2f}")
     return 0
 
 
-def measure_variant(bgk, storage, scheme, steps, warmup, dev, tune=True):
+def measure_variant(bgk, storage, scheme, steps, warmup, dev, tune=True, les=False):
     compute = "f64" if storage == "f64" else "f32"
     with bgk.Solver(LX, LY, tcase="LDC", svisc=SVISC, u0=U0, storage=storage, compute=compute, scheme=scheme,
-                    device=dev) as s:
+                    device=dev, les=les) as s:
         cfg = s.tune(4 if storage == "f64" else 10)[0] if tune else None
         pf = s.prefetch()
         s.step(warmup)
@@ -356,6 +356,7 @@ def main():
     ap.add_argument("--size", type=int, default=2048)
     ap.add_argument("--tile", type=int, default=-1, help="tile configuration for --profile")
     ap.add_argument("--prefetch", type=int, default=0, help="L2 prefetch distance in blocks for --profile")
+    ap.add_argument("--les", action="store_true", help="Smagorinsky collision for --profile")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -426,12 +427,15 @@ def main():
     variants = {}
     if not args.no_variants and rank == 0:
         vsteps = max(20, args.steps // 10)
-        for name, st, sch in (("pingpong_f32", "f32", "pingpong"), ("aa_f32", "f32", "aa"),
-                              ("pingpong_f16", "f16", "pingpong"), ("aa_f16", "f16", "aa"),
-                              ("pingpong_bf16", "bf16", "pingpong"), ("pingpong_f64", "f64", "pingpong"),
-                              ("aa_f64", "f64", "aa"), ("original_f32", "f32", "original")):
+        # les_*: the Smagorinsky collision (SRC/col_MC.F90:178-248), cteS = 0.1
+        for name, st, sch, les in (("pingpong_f32", "f32", "pingpong", False), ("aa_f32", "f32", "aa", False),
+                                   ("pingpong_f16", "f16", "pingpong", False), ("aa_f16", "f16", "aa", False),
+                                   ("pingpong_bf16", "bf16", "pingpong", False),
+                                   ("pingpong_f64", "f64", "pingpong", False), ("aa_f64", "f64", "aa", False),
+                                   ("original_f32", "f32", "original", False),
+                                   ("les_f32", "f32", "pingpong", True), ("les_f16", "f16", "pingpong", True)):
             n = vsteps if st != "f64" else max(10, vsteps // 4)
-            g, msv, cfg, pf = measure_variant(bgk, st, sch, n, 5, local)
+            g, msv, cfg, pf = measure_variant(bgk, st, sch, n, 5, local, les=les)
             # the two-pass form moves every population twice per step (stream, then collide)
             bw = BYTES_PER_CELL[st] * (2 if sch == "original" else 1) * LX * LY / (msv * 1e-3) / 1e9
             variants[name] = {"GLUPS": round(g, 3), "ms_per_step": round(msv, 4), "algorithmic_GBps": round(bw, 1),

@@ -794,8 +794,11 @@ int bgk_tune(bgk_handle *h, int32_t trial_steps, int32_t *tile_cfg, int32_t *ste
     // the warp edges fall depends on the bytes per thread.  Only the 8-byte shapes (4, 5) are
     // tried, so the populations of a tuned run do not depend on which of them wins.
     const bool aa16 = h->L.scheme == BGK_SCHEME_AA && h->T.elem_bytes == 2;
-    for (int c = aa16 ? 4 : 0; c < ncfg; ++c) {
-        const int npf = (c < NUM_CFG && !h->L.les) ? 3 : 1;
+    // A handle with the Smagorinsky collision runs one kernel shape whatever the tile
+    // configuration: only the prefetch distance is tried.
+    const int c0 = h->L.les ? h->cfg : aa16 ? 4 : 0, c1 = h->L.les ? h->cfg + 1 : ncfg;
+    for (int c = c0; c < c1; ++c) {
+        const int npf = c < NUM_CFG ? 3 : 1;
         for (int p = 0; p < npf; ++p) {
             if ((rc = bgk_set_tile(h, c)) || (rc = bgk_set_prefetch(h, pfs[p]))) return rc;
             for (int s = 0; s < 2; ++s)

@@ -63,18 +63,16 @@ template <typename S, typename K, bool OBS>
 cudaError_t step_les(int kind, const Lattice &L, int parity, cudaStream_t st)
 {
     const dim3 block(128, 1);
-    if (kind == STEP_PP || kind == STEP_STREAM || kind == STEP_COLLIDE) {
-        constexpr int N = vec_of<S>();
-        const int nv = (L.lx + N - 1) / N;
-        const dim3 grid((unsigned)((nv + 127) / 128), (unsigned)L.ly);
-        if (kind == STEP_PP) pp_kernel<S, K, 128, 1, OBS, N, true><<<grid, block, 0, st>>>(L, parity);
-        else if (kind == STEP_STREAM) pp_kernel<S, K, 128, 1, OBS, N, false, false><<<grid, block, 0, st>>>(L, parity);
-        else col_kernel<S, K, 128, 1, N, true><<<grid, block, 0, st>>>(L, parity);
-    } else {
-        const dim3 grid((unsigned)((L.nvec + 127) / 128), (unsigned)L.ly);
-        if (kind == STEP_AA_P) aa_p_kernel<S, K, 128, 1, OBS, true><<<grid, block, 0, st>>>(L);
-        else aa_l_kernel<S, K, 128, 1, OBS, true><<<grid, block, 0, st>>>(L);
-    }
+    // 16-bit kinds: 8 bytes per thread and plane (64 registers, 8 blocks per SM), the fastest shape
+    // of their non-LES step; the 32/64-bit kinds: 16 bytes
+    constexpr int N = Is16<S>::value ? vec_of<S>() / 2 : vec_of<S>();
+    const int nv = (L.lx + N - 1) / N;
+    const dim3 grid((unsigned)((nv + 127) / 128), (unsigned)L.ly);
+    if (kind == STEP_PP) pp_kernel<S, K, 128, 1, OBS, N, true><<<grid, block, 0, st>>>(L, parity);
+    else if (kind == STEP_STREAM) pp_kernel<S, K, 128, 1, OBS, N, false, false><<<grid, block, 0, st>>>(L, parity);
+    else if (kind == STEP_COLLIDE) col_kernel<S, K, 128, 1, N, true><<<grid, block, 0, st>>>(L, parity);
+    else if (kind == STEP_AA_P) aa_p_kernel<S, K, 128, 1, OBS, true, N><<<grid, block, 0, st>>>(L);
+    else aa_l_kernel<S, K, 128, 1, OBS, true, N><<<grid, block, 0, st>>>(L);
     return cudaGetLastError();
 }
 

@@ -163,9 +163,12 @@ template <> __device__ __forceinline__ F2 splat<F2>(float a) { return f2_pack(a,
 // Same BGK relaxation as collide<K> rewritten for throughput: with j = rho u and
 // A = (rho - 1) - 1.5 j.u, the equilibrium deviation is w_q (A + 3 c.j + 4.5 (c.j)(c.u)); the
 // scales satisfy s_q w_q = 8/9 for every q, so D_q' = (1 - omega) D_q + (8/9) omega (...).
-// T = float: one cell; T = F2: two cells.
-template <typename T>
-__device__ __forceinline__ void collide_scaled(T (&D)[9], float omega, float fgrad, bool forced)
+// T = float: one cell; T = F2: two cells.  LES: the Smagorinsky rate of each cell replaces omega
+// (les_scaled below).
+template <typename T> __device__ __forceinline__ T les_rate(T p2, float omega, float cte_s);
+
+template <typename T, bool LES = false>
+__device__ __forceinline__ void collide_scaled(T (&D)[9], float omega, float fgrad, bool forced, float cte_s = 0.0f)
 {
     const T i32 = splat<T>(1.0f / 32.0f), i8 = splat<T>(1.0f / 8.0f);
     const T sd = op_add(op_add(D[D01], D[D03]), op_add(D[D10], D[D12]));
@@ -179,6 +182,43 @@ __device__ __forceinline__ void collide_scaled(T (&D)[9], float omega, float fgr
     const T rinv = op_rcp(rho);
     const T ux = op_mul(jx, rinv), uy = op_mul(jy, rinv);
     const T A = op_fma(splat<T>(-1.5f), op_fma(jx, ux, op_mul(jy, uy)), rho1);
+    if constexpr (LES) {
+        // Equilibrium deviations in scaled units, E = (8/9) (A + (c.j)(4.5 c.u) +- 3 c.j), and the
+        // non-equilibrium parts N = D - E (N_q / s_q is the reference's x_q - e_q).  The momentum
+        // flux P of the non-equilibrium parts sets the eddy viscosity (SRC/col_MC.F90:178-248):
+        // D' = D - omega_eff N.
+        const T c89 = splat<T>(8.0f / 9.0f);
+        const T ux45 = op_mul(splat<T>(4.5f), ux), uy45 = op_mul(splat<T>(4.5f), uy);
+        T E[9];
+        auto eq = [&](int qp, int qm, T cj, T cu45) {
+            const T t = op_fma(cj, cu45, A);
+            E[qp] = op_mul(c89, op_fma(splat<T>(3.0f), cj, t));
+            E[qm] = op_mul(c89, op_fma(splat<T>(-3.0f), cj, t));
+        };
+        eq(D05, D14, jx, ux45);
+        eq(D08, D17, jy, uy45);
+        eq(D03, D10, op_add(jx, jy), op_add(ux45, uy45));
+        eq(D01, D12, op_sub(jx, jy), op_sub(ux45, uy45));
+        E[D19] = op_mul(c89, A);
+        T N[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) N[q] = op_sub(D[q], E[q]);
+        const T nd = op_add(op_add(N[D01], N[D03]), op_add(N[D10], N[D12]));
+        const T pxx = op_fma(nd, i32, op_mul(op_add(N[D05], N[D14]), i8));
+        const T pyy = op_fma(nd, i32, op_mul(op_add(N[D08], N[D17]), i8));
+        const T pxy = op_mul(op_sub(op_add(N[D03], N[D10]), op_add(N[D01], N[D12])), i32);
+        const T p2 = op_fma(pxx, pxx, op_fma(op_add(pxy, pxy), pxy, op_mul(pyy, pyy)));
+        const T w = les_rate<T>(p2, omega, cte_s);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) D[q] = op_sub(D[q], op_mul(w, N[q]));
+        if (forced) {
+            const T F = op_mul(splat<T>(fgrad), rho);
+            const T F32 = op_mul(splat<T>(32.0f), F), F8 = op_mul(splat<T>(8.0f), F);
+            D[D01] = op_add(D[D01], F32); D[D03] = op_add(D[D03], F32); D[D05] = op_add(D[D05], F8);
+            D[D10] = op_sub(D[D10], F32); D[D12] = op_sub(D[D12], F32); D[D14] = op_sub(D[D14], F8);
+        }
+        return;
+    }
     const T omc = splat<T>(__fsub_rn(1.0f, omega)), k = splat<T>(__fmul_rn(omega, 8.0f / 9.0f));
     // k folded into A and j, 4.5 into u: per direction pair (q, opp q) with kcj = k c.j and
     // cu45 = 4.5 c.u,  D' = (1 - omega) D + kA + kcj cu45 +- 3 kcj
@@ -203,17 +243,35 @@ __device__ __forceinline__ void collide_scaled(T (&D)[9], float omega, float fgr
     }
 }
 
+// Smagorinsky rate of one cell from p2 = |P|^2 (SRC/col_MC.F90:178-248, as les_omega):
+// 1 / (1 / (2 omega) + sqrt(18 cte_s^2 |P| + 1 / omega^2) / 2)
+__device__ __forceinline__ float les_rate1(float p2, float omega, float cte_s)
+{
+    const float r = __fdividef(1.0f, omega);
+    const float a = __fmul_rn(__fmul_rn(18.0f, __fmul_rn(cte_s, cte_s)), __fsqrt_rn(p2));
+    const float ts = __fmaf_rn(0.5f, r, __fmul_rn(0.5f, __fsqrt_rn(__fmaf_rn(r, r, a))));
+    return __fdividef(1.0f, ts);
+}
+template <> __device__ __forceinline__ float les_rate<float>(float p2, float omega, float cte_s)
+{
+    return les_rate1(p2, omega, cte_s);
+}
+template <> __device__ __forceinline__ F2 les_rate<F2>(F2 p2, float omega, float cte_s)
+{
+    float lo, hi;
+    f2_unpack(p2, lo, hi);
+    return f2_pack(les_rate1(lo, omega, cte_s), les_rate1(hi, omega, cte_s));
+}
+
 // collision on unscaled deviations in compute kind K, for any storage kind
 template <typename S, typename K, bool LES = false>
 __device__ __forceinline__ void collide_stored(K (&v)[9], K omega, K fgrad, bool forced, K cte_s)
 {
-    if constexpr (Is16<S>::value && LES) {
-        collide<K, true>(v, omega, fgrad, forced, cte_s);
-    } else if constexpr (Is16<S>::value) {
+    if constexpr (Is16<S>::value) {
         float D[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) D[q] = (float)v[q] * scale_of(q);  // exact: powers of two
-        collide_scaled<float>(D, (float)omega, (float)fgrad, forced);
+        collide_scaled<float, LES>(D, (float)omega, (float)fgrad, forced, (float)cte_s);
 #pragma unroll
         for (int q = 0; q < 9; ++q) v[q] = (K)(D[q] * (1.0f / scale_of(q)));
     } else {
@@ -399,7 +457,7 @@ __device__ __forceinline__ K pull_rule(const Lattice &L, int q, int x, int y, Pl
 template <typename S, typename K, bool RAW, int N = vec_of<S>(), bool LES = false>
 __device__ __forceinline__ void relax_vec(K (&x)[9][N], K omega, K fgrad, bool forced, K cte_s)
 {
-    if constexpr (RAW && !LES) {
+    if constexpr (RAW) {
         // two cells per packed FP32 instruction
         static_assert(N % 2 == 0, "16-bit vectors hold an even number of cells");
 #pragma unroll
@@ -407,32 +465,20 @@ __device__ __forceinline__ void relax_vec(K (&x)[9][N], K omega, K fgrad, bool f
             F2 v[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) v[q] = f2_pack(x[q][c], x[q][c + 1]);
-            collide_scaled<F2>(v, (float)omega, (float)fgrad, forced);
+            collide_scaled<F2, LES>(v, (float)omega, (float)fgrad, forced, (float)cte_s);
 #pragma unroll
             for (int q = 0; q < 9; ++q) f2_unpack(v[q], x[q][c], x[q][c + 1]);
         }
-        return;
-    }
+    } else {
 #pragma unroll
-    for (int c = 0; c < N; ++c) {
-        K v[9];
+        for (int c = 0; c < N; ++c) {
+            K v[9];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) v[q] = x[q][c];
-        if constexpr (RAW) {
-            if constexpr (LES) {  // eddy viscosity on unscaled deviations, as the 32/64-bit kinds
-#pragma unroll
-                for (int q = 0; q < 9; ++q) v[q] *= (1.0f / scale_of(q));
-                collide<K, true>(v, omega, fgrad, forced, cte_s);
-#pragma unroll
-                for (int q = 0; q < 9; ++q) v[q] *= scale_of(q);
-            } else {
-                collide_scaled<float>(v, (float)omega, (float)fgrad, forced);
-            }
-        } else {
+            for (int q = 0; q < 9; ++q) v[q] = x[q][c];
             collide<K, LES>(v, omega, fgrad, forced, cte_s);
-        }
 #pragma unroll
-        for (int q = 0; q < 9; ++q) x[q][c] = v[q];
+            for (int q = 0; q < 9; ++q) x[q][c] = v[q];
+        }
     }
 }
 

@@ -116,7 +116,8 @@ typedef struct bgk_case_desc {
     int32_t device;           /* CUDA device ordinal */
     int32_t les;              /* 1: Smagorinsky eddy viscosity in the collision (-DLES,
                                  SRC/col_MC.F90:178-248); such a handle steps with its own
-                                 128x1 kernels and cannot join a batch */
+                                 128x1 kernels (bgk_tune picks only the prefetch distance) and
+                                 cannot join a batch */
     double cte_s;             /* Smagorinsky constant cteS (namelist, SRC/input.F90:55; default 0.1) */
     int32_t reserved[4];
 } bgk_case_desc;

@@ -79,3 +79,33 @@ def test_aa_16bit_tuned_run_is_reproducible(bgk, storage):
             s.step(50)
             out.append(s.download())
     assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("scheme", ["pingpong", "aa"])
+@pytest.mark.parametrize("storage", ["f16", "bf16"])
+def test_16bit_les_tracks_fp32_les(bgk, storage, scheme):
+    """The Smagorinsky collision in scaled 16-bit units (SRC/col_MC.F90:178-248 rewritten on
+    D_q = s_q (f_q - w_q)) against the FP32 LES step, which is bit-exact with the oracle.  The
+    16-bit LES error must stay within a small factor of the 16-bit error without LES, and well
+    below the change the eddy viscosity makes (FP32 LES against FP32 BGK): 10x for FP16, 2x for
+    BF16, whose 8-bit mantissa alone costs 1-2% here."""
+    kw = dict(tcase="LDC", svisc=0.01, u0=0.1, scheme=scheme)  # Re = 1280 on 128^2
+    out = {}
+    for st in (storage, "f32"):
+        for les in (True, False):
+            with bgk.Solver(128, 128, storage=st, les=les, cte_s=0.4, **kw) as s:
+                s.step(1500)
+                _, u, v = s.fields()
+                assert np.isfinite(u).all() and np.isfinite(v).all(), (st, les)
+                out[(st, les)] = (u, v)
+
+    def dist(a, b):
+        (u, v), (ur, vr) = out[a], out[b]
+        return float(np.sqrt(np.sum((u - ur) ** 2 + (v - vr) ** 2) / np.sum(ur ** 2 + vr ** 2)))
+
+    e_les = dist((storage, True), ("f32", True))
+    e_bgk = dist((storage, False), ("f32", False))
+    d_les = dist(("f32", True), ("f32", False))
+    print(storage, scheme, "L2 vs FP32: LES %.2e, BGK %.2e; LES vs BGK %.2e" % (e_les, e_bgk, d_les))
+    assert e_les < max(3 * e_bgk, TOL[storage] / 4), (e_les, e_bgk)
+    assert d_les > (10 if storage == "f16" else 2) * e_les, (d_les, e_les)
