@@ -43,8 +43,6 @@ struct bgk_batch {
 
 namespace {
 
-int bfail(bgk_handle *h, int code) { (void)h; return code; }
-
 int rebuild(bgk_batch *b)
 {
     if (!b->dirty) return BGK_OK;

@@ -83,9 +83,10 @@ static void FN(setup_scalars)(orc_state *s)
     s->u0 = (double)u0;
 }
 
-/* build.obs.F90:38-205 (circle by default, SQUARE, HALF_CIRCLE); d2 and R are mykind */
-static void FN(build_obs)(int l, int m, int shape, int radius, int icoord, int jcoord,
-                          int32_t *obs, int32_t *bbox)
+/* build.obs.F90:38-205 (circle by default, SQUARE, HALF_CIRCLE); d2 and R are mykind.  Inline:
+ * not every precision instance calls it. */
+static inline void FN(build_obs)(int l, int m, int shape, int radius, int icoord, int jcoord,
+                                 int32_t *obs, int32_t *bbox)
 {
     int imin = l, jmin = m, imax = 0, jmax = 0, nobs = 0;
     for (size_t k = 0; k < (size_t)l * (size_t)m; ++k) obs[k] = 0;
