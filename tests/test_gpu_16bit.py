@@ -109,3 +109,20 @@ def test_16bit_les_tracks_fp32_les(bgk, storage, scheme):
     print(storage, scheme, "L2 vs FP32: LES %.2e, BGK %.2e; LES vs BGK %.2e" % (e_les, e_bgk, d_les))
     assert e_les < max(3 * e_bgk, TOL[storage] / 4), (e_les, e_bgk)
     assert d_les > (10 if storage == "f16" else 2) * e_les, (d_les, e_les)
+
+
+def test_16bit_full_size_invariants(bgk):
+    """The 4096^2 cavity (Re = 10000) in FP16: the 16-byte (2) and 8-byte (5) register-vector
+    shapes and the staged kernel (8) give identical populations after 60 steps, and the mean
+    density stays 1 to within the stochastic rounding."""
+    pops = []
+    for tile in (2, 5, 8):
+        with bgk.Solver(4096, 4096, tcase="LDC", svisc=0.04096, u0=0.1, storage="f16") as s:
+            s.set_tile(tile)
+            s.step(60)
+            d = s.diagno()
+            assert abs(d[2] - 1.0) < 1e-5, d
+            assert np.isfinite(d).all()
+            pops.append(s.download())
+    assert np.array_equal(pops[0], pops[1])
+    assert np.array_equal(pops[0], pops[2])
