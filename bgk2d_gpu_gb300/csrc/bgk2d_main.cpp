@@ -3,7 +3,7 @@
 // Reads the reference's `bgk.input` namelist (SRC/input.F90:44-65), sets the case up like
 // SRC/initialize.F90, runs the time loop of SRC/bgk2d.F90:92-113 (boundaries, propagation and
 // collision are one fused step on the device) and writes the reference's text outputs at its
-// diagnostic cadence (SRC/diagnostic.F90): diagno.dat, probe.dat, prof_i.dat, prof_j.dat,
+// diagnostic cadence (SRC/diagnostic.F90): diagno.dat, probe.dat, u_med.dat, prof_i.dat, prof_j.dat,
 // drag.lift.dat, save.XXXXXXXX.bin checkpoints (Fortran unformatted sequential records, as
 // SRC/save_raw.F90), tec_xy/tec_om VTK files (SRC/vtk_xy.binary.F90, SRC/vtk_om.binary.F90, from
 // fields computed on the device) and bgk.perf.
@@ -146,6 +146,30 @@ void probe(const Pops &a, int i0, int j0, FILE *f, int itime)
                  fortran_e(rho).c_str());
 }
 
+// row means of u, w and rho over i = 1..lx (SRC/varm.F90:49-88, u_med.dat): sums over i in order
+// in the storage kind, times rvol = 1.0/float(l) (a default-real quotient)
+template <typename T>
+void varm(const Pops &a, FILE *f, int itime)
+{
+    const T rvol = (T)(1.0f / (float)a.lx);
+    std::fprintf(f, "# t=%7d\n", itime);
+    for (int j = 1; j <= a.ly; ++j) {
+        T u = 0, w = 0, den = 0;
+        for (int i = 1; i <= a.lx; ++i) {
+            T x[9];
+            for (int q = 0; q < 9; ++q) x[q] = (T)a.at(q, i, j);
+            const T rho = ((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8]) + (T)1;
+            const T rhoinv = (T)1 / rho;
+            den = den + rho;
+            u = u + (((((x[0] + x[1]) + x[2]) - x[4]) - x[5]) - x[6]) * rhoinv;
+            w = w + (((((x[1] + x[3]) + x[5]) - x[0]) - x[4]) - x[7]) * rhoinv;
+        }
+        std::fprintf(f, "%5d%s %s %s \n", j, fortran_e(u * rvol).c_str(), fortran_e(w * rvol).c_str(),
+                     fortran_e(den * rvol).c_str());
+    }
+    std::fprintf(f, "\n\n");
+}
+
 // Fortran unformatted sequential record: int32 length, payload, int32 length
 void write_record(FILE *f, const void *data, uint32_t bytes)
 {
@@ -184,7 +208,8 @@ std::string fa(const char *s, int w)
 
 // tec_xy.XXXXXXXX.vtk and tec_om.XXXXXXXX.vtk as SRC/vtk_xy.binary.F90 and SRC/vtk_om.binary.F90
 // write them (serial build: offsets 0), from the fields computed on the device
-int write_vtk(bgk_handle *h, const std::string &dir, int itime, int lx, int ly)
+// with_om = false: tec_xy only (the start-up call of SRC/initialize.F90:119-123)
+int write_vtk(bgk_handle *h, const std::string &dir, int itime, int lx, int ly, bool with_om = true)
 {
     const size_t n = (size_t)lx * ly, n2 = (size_t)(lx - 2) * (ly - 2);
     std::vector<float> u(n), w(n), rho(n), om(n2), st(n2);
@@ -213,6 +238,7 @@ int write_vtk(bgk_handle *h, const std::string &dir, int itime, int lx, int ly)
     std::fprintf(f, "%s\n%s\n", fa("SCALARS rho float", 21).c_str(), fa("LOOKUP_TABLE default", 20).c_str());
     write_be(f, rho.data(), n);
     std::fclose(f);
+    if (!with_om) return BGK_OK;
     std::snprintf(name, sizeof(name), "/tec_om.%08d.vtk", itime);
     f = std::fopen((dir + name).c_str(), "wb");
     if (!f) return BGK_E_INVALID;
@@ -299,9 +325,12 @@ int main(int argc, char **argv)
     FILE *fprobe = std::fopen((dir + "/probe.dat").c_str(), "w");
     FILE *fpi = std::fopen((dir + "/prof_i.dat").c_str(), "w");
     FILE *fpj = std::fopen((dir + "/prof_j.dat").c_str(), "w");
+    FILE *fumed = std::fopen((dir + "/u_med.dat").c_str(), "w");  // SRC/setup.F90:127-128
     FILE *fdrag = d.tcase == BGK_CASE_VKS ? std::fopen((dir + "/drag.lift.dat").c_str(), "w") : nullptr;
     const bool dbl = d.storage == BGK_STORE_F64;
-    auto diagnostic = [&](int itime) -> int {
+    // SRC/diagnostic.F90:70-82 at every icheck (diagno, probe, varm, prof_i, prof_j, draglift);
+    // SRC/bgk2d.F90:122-125 once after the loop (diagno, varm, prof_i, prof_j)
+    auto diagnostic = [&](int itime, bool final_call) -> int {
         double dg[4];
         int r = bgk_diagno(h, BGK_DIAGNO_REFERENCE, dg);  // the reference's own sums (diagno.dat)
         if (r && r != BGK_E_NUMERIC) return r;
@@ -309,19 +338,29 @@ int main(int argc, char **argv)
                      fortran_e(dg[2]).c_str(), fortran_e(dg[3]).c_str());
         std::fflush(fdiag);
         if ((r = bgk_download(h, pops.p, lx + 2))) return r;
-        if (dbl) { probe<double>(pops, lx / 2, ly / 2, fprobe, itime); prof_i<double>(pops, ly / 2, fpi, itime); prof_j<double>(pops, lx / 2, fpj, itime); }
-        else { probe<float>(pops, lx / 2, ly / 2, fprobe, itime); prof_i<float>(pops, ly / 2, fpi, itime); prof_j<float>(pops, lx / 2, fpj, itime); }
-        if (fdrag) {
+        if (dbl) {
+            if (!final_call) probe<double>(pops, lx / 2, ly / 2, fprobe, itime);
+            varm<double>(pops, fumed, itime);
+            prof_i<double>(pops, ly / 2, fpi, itime);
+            prof_j<double>(pops, lx / 2, fpj, itime);
+        } else {
+            if (!final_call) probe<float>(pops, lx / 2, ly / 2, fprobe, itime);
+            varm<float>(pops, fumed, itime);
+            prof_i<float>(pops, ly / 2, fpi, itime);
+            prof_j<float>(pops, lx / 2, fpj, itime);
+        }
+        if (fdrag && !final_call) {
             double fl[2];
             if ((r = bgk_draglift_reference(h, fl))) return r;  // the reference's own sums
             std::fprintf(fdrag, " %12d %24.16E %24.16E\n", itime, fl[0], fl[1]);
         }
         return BGK_OK;
     };
-    if (irestart != 1) {  // SRC/initialize.F90:118-124 writes the initial profiles
+    if (irestart != 1) {  // SRC/initialize.F90:116-123 writes the initial profiles and velocity field
         if ((rc = bgk_download(h, pops.p, lx + 2))) return die("bgk_download", rc);
-        if (dbl) { prof_i<double>(pops, ly / 2, fpi, 0); prof_j<double>(pops, lx / 2, fpj, 0); }
-        else { prof_i<float>(pops, ly / 2, fpi, 0); prof_j<float>(pops, lx / 2, fpj, 0); }
+        if (dbl) { varm<double>(pops, fumed, 0); prof_i<double>(pops, ly / 2, fpi, 0); prof_j<double>(pops, lx / 2, fpj, 0); }
+        else { varm<float>(pops, fumed, 0); prof_i<float>(pops, ly / 2, fpi, 0); prof_j<float>(pops, lx / 2, fpj, 0); }
+        if (lx > 2 && ly > 2 && (rc = write_vtk(h, dir, 0, lx, ly, false))) return die("vtk", rc);
     }
     const auto t1 = std::chrono::steady_clock::now();
     double t_last = 0;
@@ -335,7 +374,7 @@ int main(int argc, char **argv)
         itime = next;
         if (itime % ivtim == 0 && lx > 2 && ly > 2 && (rc = write_vtk(h, dir, itime, lx, ly)))  // SRC/diagnostic.F90:32-57
             return die("vtk", rc);
-        if (itime % icheck == 0 && (rc = diagnostic(itime))) return die("diagnostic", rc);
+        if (itime % icheck == 0 && (rc = diagnostic(itime, false))) return die("diagnostic", rc);
         if (itime % itsave == 0) {  // SRC/save_raw.F90
             if ((rc = bgk_download(h, pops.p, lx + 2))) return die("bgk_download", rc);
             char name[64];
@@ -356,7 +395,7 @@ int main(int argc, char **argv)
     bgk_sync(h);
     const auto t2 = std::chrono::steady_clock::now();
     const double loop = std::chrono::duration<double>(t2 - t1).count();
-    diagnostic(itime);  // SRC/bgk2d.F90:122-125
+    if ((rc = diagnostic(itime, true))) return die("diagnostic", rc);
     const double mlups = (double)lx * ly * (itfin - itstart) / loop / 1e6;
     FILE *fp = std::fopen((dir + "/bgk.perf").c_str(), "w");
     std::fprintf(fp, "# Run info\n %d %d\n# Time for section\n init %.6f\n loop %.6f\n", lx, ly,
@@ -364,7 +403,7 @@ int main(int argc, char **argv)
     std::fprintf(fp, "# Derived (global) metrics\n Mlups %.3f\n", mlups);
     std::fclose(fp);
     std::printf(" Mlups %.3f\n", mlups);
-    for (FILE *f : {fdiag, fprobe, fpi, fpj})
+    for (FILE *f : {fdiag, fprobe, fpi, fpj, fumed})
         if (f) std::fclose(f);
     if (fdrag) std::fclose(fdrag);
     bgk_destroy(h);

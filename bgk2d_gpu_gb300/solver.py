@@ -259,6 +259,10 @@ class Solver:
         v = ((c[1] - c[0]) + (c[3] - c[7]) + (c[5] - c[4])) / den
         return u, v, den
 
+    def varm(self, pops=None):
+        """Row means of u, w and rho (u_med.dat; SRC/varm.F90:49-88), see `varm`."""
+        return varm(self.download() if pops is None else pops, self.lx, self.ly)
+
     def probe(self, i0, j0, pops=None):
         """u, v, rho at one node (SRC/probe.F90:46-62)."""
         a = self.download() if pops is None else pops
@@ -268,6 +272,31 @@ class Solver:
         xj = x[0] + x[1] + x[2] - x[4] - x[5] - x[6]
         yj = x[1] + x[3] + x[5] - x[0] - x[4] - x[7]
         return xj / rho, yj / rho, rho
+
+
+def varm(pops, lx, ly):
+    """Row means over i = 1..lx of u, w and rho for j = 1..ly, as SRC/varm.F90:49-88 writes them to
+    u_med.dat: per cell rho = (a01 + ... + a19) + 1, rhoinv = 1/rho; the sums over i run in order
+    in the array's kind; the means are the sums times rvol = 1.0/float(lx), a default-real
+    quotient.  `pops` is the (9, ly+2, lx+2) array of `Solver.download`."""
+    k = pops.dtype.type
+    x = pops[:, 1:ly + 1, 1:lx + 1]
+    rho = x[0] + x[1]
+    for q in range(2, 9):
+        rho = rho + x[q]
+    rho = rho + k(1)
+    rinv = k(1) / rho
+    uu = (((((x[0] + x[1]) + x[2]) - x[4]) - x[5]) - x[6]) * rinv
+    ww = (((((x[1] + x[3]) + x[5]) - x[0]) - x[4]) - x[7]) * rinv
+    u = np.zeros(ly, dtype=k)
+    w = np.zeros(ly, dtype=k)
+    den = np.zeros(ly, dtype=k)
+    for i in range(lx):  # the reference's i loop: one addition per cell, in order
+        den = den + rho[:, i]
+        u = u + uu[:, i]
+        w = w + ww[:, i]
+    rvol = k(np.float32(1.0) / np.float32(lx))
+    return u * rvol, w * rvol, den * rvol
 
 
 class Batch:

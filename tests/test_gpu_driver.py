@@ -52,6 +52,20 @@ def test_driver_outputs_match_solver(bgk, tmp_path):
     vals = np.array([[float(x) for x in ln.split()] for ln in last])
     np.testing.assert_allclose(vals[:, 1], u, rtol=1e-5, atol=1e-11)
     assert (tmp_path / "save.00000150.bin").exists() and (tmp_path / "bgk.perf").exists()
+    # u_med.dat (SRC/varm.F90): at start-up, every icheck and once more at the end
+    text = (tmp_path / "u_med.dat").read_text()
+    assert [int(b.split()[0]) for b in text.split("# t=")[1:]] == [0, 100, 200, 300, 300]
+    with bgk.Solver(p["lx"], p["ly"], tcase="LDC", svisc=p["svisc"], u0=0.1) as s:
+        s.step(300)
+        um, wm, dm = s.varm()
+    last = text.split("# t=")[-1].strip().splitlines()[1:]
+    vals = np.array([[float(x) for x in ln.split()] for ln in last])
+    assert np.array_equal(vals[:, 0], np.arange(1, p["ly"] + 1))
+    np.testing.assert_allclose(vals[:, 1], um, rtol=1e-5, atol=1e-11)
+    np.testing.assert_allclose(vals[:, 2], wm, rtol=1e-5, atol=1e-11)
+    np.testing.assert_allclose(vals[:, 3], dm, rtol=1e-5)  # e14.6: 6 significant digits
+    # the final call writes no probe line (SRC/bgk2d.F90:122-125)
+    assert len((tmp_path / "probe.dat").read_text().splitlines()) == 3
 
 
 def test_checkpoint_restart_continues_exactly(bgk, tmp_path):
@@ -75,7 +89,8 @@ def test_checkpoint_restart_continues_exactly(bgk, tmp_path):
 def test_driver_vks_writes_drag_lift(bgk, tmp_path):
     run_driver(bgk, tmp_path, case="VKS", lx=160, ly=62, svisc=0.05, itfin=200, itsave=1000000)
     rows = [ln.split() for ln in (tmp_path / "drag.lift.dat").read_text().splitlines()]
-    assert len(rows) == 3 and all(np.isfinite(float(x)) for r in rows for x in r[1:])
+    # at every icheck; the end-of-run output has no drag/lift (SRC/bgk2d.F90:122-125)
+    assert len(rows) == 2 and all(np.isfinite(float(x)) for r in rows for x in r[1:])
 
 
 def _vtk_sections(path):
@@ -115,6 +130,8 @@ def test_driver_vtk_files(bgk, tmp_path):
     assert lines[4] == "DIMENSIONS %10d %10d %10d" % (lx, ly, 1) and npts == lx * ly
     _, npts2, om = _vtk_sections(tmp_path / "tec_om.00000200.vtk")
     assert npts2 == (lx - 2) * (ly - 2) and (tmp_path / "tec_xy.00000100.vtk").exists()
+    # the start-up field (SRC/initialize.F90:119-123): velocity only
+    assert (tmp_path / "tec_xy.00000000.vtk").exists() and not (tmp_path / "tec_om.00000000.vtk").exists()
     with bgk.Solver(lx, ly, tcase="LDC", svisc=p["svisc"], u0=0.1) as s:
         s.step(200)
         u, w, r, vort, st = s.vtk_fields()

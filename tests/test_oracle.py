@@ -157,3 +157,28 @@ def test_reference_profile_fixture(oracle_mod):
     u, v, d = o.prof_j(128)
     assert g20[-1, 3] > 1.15 and abs(d[-1] - 1.0) < 0.02
     assert np.abs(g20[:, 1]).max() < 0.01 and u.max() > 0.05
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_varm_host_reader_matches_reference_loop(dtype):
+    """solver.varm (u_med.dat) against a cell-by-cell restatement of SRC/varm.F90:49-88."""
+    from bgk2d_gpu_gb300.solver import varm
+    lx, ly = 9, 6
+    rng = np.random.default_rng(3)
+    a = (rng.standard_normal((9, ly + 2, lx + 2)) * 0.01).astype(dtype)
+    u, w, den = varm(a, lx, ly)
+    k = dtype
+    rvol = k(np.float32(1.0) / np.float32(lx))
+    for j in range(1, ly + 1):
+        su = sw = sd = k(0)
+        for i in range(1, lx + 1):
+            x = [a[q, j, i] for q in range(9)]
+            rho = x[0]
+            for q in range(1, 9):
+                rho = rho + x[q]
+            rho = rho + k(1)
+            rinv = k(1) / rho
+            sd = sd + rho
+            su = su + (x[0] + x[1] + x[2] - x[4] - x[5] - x[6]) * rinv
+            sw = sw + (x[1] + x[3] + x[5] - x[0] - x[4] - x[7]) * rinv
+        assert u[j - 1] == su * rvol and w[j - 1] == sw * rvol and den[j - 1] == sd * rvol
