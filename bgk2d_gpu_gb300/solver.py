@@ -259,6 +259,19 @@ class Solver:
         v = ((c[1] - c[0]) + (c[3] - c[7]) + (c[5] - c[4])) / den
         return u, v, den
 
+    def prof_i(self, jcoord, pops=None):
+        """u, v, rho along row jcoord, i = 1..lx (SRC/prof_i.F90:47-62)."""
+        a = self.download() if pops is None else pops
+        k = a.dtype.type
+        c = a[:, jcoord, 1:self.lx + 1]
+        den = c[0] + c[1]
+        for q in range(2, 9):
+            den = den + c[q]
+        den = den + k(1)
+        u = (((((c[0] + c[1]) + c[2]) - c[4]) - c[5]) - c[6]) / den
+        v = (((((c[1] + c[3]) + c[5]) - c[0]) - c[4]) - c[7]) / den
+        return u, v, den
+
     def varm(self, pops=None):
         """Row means of u, w and rho (u_med.dat; SRC/varm.F90:49-88), see `varm`."""
         return varm(self.download() if pops is None else pops, self.lx, self.ly)

@@ -182,3 +182,24 @@ def test_varm_host_reader_matches_reference_loop(dtype):
             su = su + (x[0] + x[1] + x[2] - x[4] - x[5] - x[6]) * rinv
             sw = sw + (x[1] + x[3] + x[5] - x[0] - x[4] - x[7]) * rinv
         assert u[j - 1] == su * rvol and w[j - 1] == sw * rvol and den[j - 1] == sd * rvol
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_prof_i_host_reader_matches_reference_loop(dtype):
+    """Solver.prof_i (prof_i.dat) against a cell-by-cell restatement of SRC/prof_i.F90:47-62."""
+    from types import SimpleNamespace
+    from bgk2d_gpu_gb300.solver import Solver
+    lx, ly, jc = 9, 6, 3
+    rng = np.random.default_rng(4)
+    a = (rng.standard_normal((9, ly + 2, lx + 2)) * 0.01).astype(dtype)
+    u, v, den = Solver.prof_i(SimpleNamespace(lx=lx, ly=ly), jc, a)
+    k = dtype
+    for i in range(1, lx + 1):
+        x = [a[q, jc, i] for q in range(9)]
+        d = x[0]
+        for q in range(1, 9):
+            d = d + x[q]
+        d = d + k(1)
+        assert den[i - 1] == d
+        assert u[i - 1] == (x[0] + x[1] + x[2] - x[4] - x[5] - x[6]) / d
+        assert v[i - 1] == (x[1] + x[3] + x[5] - x[0] - x[4] - x[7]) / d
