@@ -4,6 +4,7 @@
 // SRC/initialize.F90, runs the time loop of SRC/bgk2d.F90:92-113 (boundaries, propagation and
 // collision are one fused step on the device) and writes the reference's text outputs at its
 // diagnostic cadence (SRC/diagnostic.F90): diagno.dat, probe.dat, u_med.dat, prof_i.dat, prof_j.dat,
+// tec_ob.00000000.vtk and obstacle.dat for obstacle cases,
 // drag.lift.dat, save.XXXXXXXX.bin checkpoints (Fortran unformatted sequential records, as
 // SRC/save_raw.F90), tec_xy/tec_om VTK files (SRC/vtk_xy.binary.F90, SRC/vtk_om.binary.F90, from
 // fields computed on the device) and bgk.perf.
@@ -251,6 +252,40 @@ int write_vtk(bgk_handle *h, const std::string &dir, int itime, int lx, int ly, 
     return BGK_OK;
 }
 
+// The obstacle outputs of an obstacle build at start-up (SRC/initialize.F90:74-80):
+// tec_ob.00000000.vtk, the ASCII rectilinear-grid mask of SRC/vtk_obstacle.F90, and
+// obstacle.dat, the `i j obs` list of SRC/w.obs.F90.  Their numbers are list-directed output,
+// written with gfortran's widths: integers in 12 columns, the default-real mask values as
+// "   0.00000000    ".
+int write_obstacle_files(bgk_handle *h, const std::string &dir, int lx, int ly)
+{
+    std::vector<int32_t> obs((size_t)lx * ly);
+    int32_t bbox[5];
+    int rc = bgk_get_obs(h, obs.data(), bbox);
+    if (rc) return rc;
+    if (bbox[4] == 0) return BGK_OK;  // no obstacle cell: not an obstacle build
+    FILE *f = std::fopen((dir + "/tec_ob.00000000.vtk").c_str(), "w");
+    if (!f) return BGK_E_INVALID;
+    std::fprintf(f, "# vtk DataFile Version 2.0\nCampo\nASCII\nDATASET RECTILINEAR_GRID\n");
+    std::fprintf(f, "DIMENSIONS %10d %10d%s\n", lx, ly, fa(" 1", 3).c_str());
+    std::fprintf(f, "X_COORDINATES %10d double\n", lx);
+    for (int i = 1; i <= lx; ++i) std::fprintf(f, "%12d\n", i);
+    std::fprintf(f, "Y_COORDINATES %10d double\n", ly);
+    for (int j = 1; j <= ly; ++j) std::fprintf(f, "%12d\n", j);
+    std::fprintf(f, "Z_COORDINATES %10d double\n%12d\n", 1, 1);
+    std::fprintf(f, "%s%10d\n", fa("POINT_DATA ", 10).c_str(), lx * ly);
+    std::fprintf(f, "%s\n%s\n", fa("SCALARS obs float", 21).c_str(), fa("LOOKUP_TABLE default", 20).c_str());
+    for (int j = 0; j < ly; ++j)
+        for (int i = 0; i < lx; ++i) std::fprintf(f, "   %.8f    \n", (double)obs[(size_t)i + (size_t)j * lx]);
+    std::fclose(f);
+    f = std::fopen((dir + "/obstacle.dat").c_str(), "w");
+    if (!f) return BGK_E_INVALID;
+    for (int j = 1; j <= ly; ++j)
+        for (int i = 1; i <= lx; ++i) std::fprintf(f, "%12d%12d%12d\n", i, j, obs[(size_t)(i - 1) + (size_t)(j - 1) * lx]);
+    std::fclose(f);
+    return BGK_OK;
+}
+
 int die(const char *what, int rc)
 {
     std::fprintf(stderr, "bgk2d_gb300: %s failed (status %d)\n", what, rc);
@@ -321,6 +356,7 @@ int main(int argc, char **argv)
         if ((rc = bgk_upload(h, pops.p, lx + 2))) return die("bgk_upload", rc);
     }
     (void)ld;
+    if ((rc = write_obstacle_files(h, dir, lx, ly))) return die("obstacle files", rc);
     FILE *fdiag = std::fopen((dir + "/diagno.dat").c_str(), "w");
     FILE *fprobe = std::fopen((dir + "/probe.dat").c_str(), "w");
     FILE *fpi = std::fopen((dir + "/prof_i.dat").c_str(), "w");

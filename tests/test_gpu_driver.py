@@ -91,6 +91,17 @@ def test_driver_vks_writes_drag_lift(bgk, tmp_path):
     rows = [ln.split() for ln in (tmp_path / "drag.lift.dat").read_text().splitlines()]
     # at every icheck; the end-of-run output has no drag/lift (SRC/bgk2d.F90:122-125)
     assert len(rows) == 2 and all(np.isfinite(float(x)) for r in rows for x in r[1:])
+    # the obstacle outputs of SRC/initialize.F90:74-80 hold the mask of build_obs
+    with bgk.Solver(160, 62, tcase="VKS", svisc=0.05, u0=0.1) as s:
+        mask, bbox = s.obs()
+    rows = np.loadtxt(tmp_path / "obstacle.dat", dtype=np.int64)
+    assert rows.shape == (160 * 62, 3)
+    assert np.array_equal(rows[:, 2].reshape(62, 160), mask)
+    lines = (tmp_path / "tec_ob.00000000.vtk").read_text().splitlines()
+    assert lines[:4] == ["# vtk DataFile Version 2.0", "Campo", "ASCII", "DATASET RECTILINEAR_GRID"]
+    k = lines.index("LOOKUP_TABLE default")
+    vals = np.array([float(x) for x in lines[k + 1:]])
+    assert np.array_equal(vals.reshape(62, 160), mask.astype(float)) and vals.sum() == bbox[4]
 
 
 def _vtk_sections(path):
