@@ -24,6 +24,8 @@
 #include <string>
 #include <vector>
 
+#include <sys/resource.h>
+
 #include "../../include/bgk2d_gb300.h"
 
 namespace {
@@ -170,6 +172,30 @@ void varm(const Pops &a, FILE *f, int itime)
     }
     std::fprintf(f, "\n\n");
 }
+
+// peak resident set size in MB, as SRC/get_mem.c reports it
+double max_rss_mb()
+{
+    struct rusage u;
+    getrusage(RUSAGE_SELF, &u);
+    return (double)u.ru_maxrss / 1024.0;
+}
+
+// Fortran list-directed output of a default real, with gfortran's layout (9 significant digits)
+std::string list_real(double v)
+{
+    char b[64];
+    const double a = std::fabs(v);
+    if (v == 0.0) std::snprintf(b, sizeof(b), "   0.00000000    ");
+    else if (a >= 0.1 && a < 1e8) {
+        const int digits = std::max(1, (int)std::floor(std::log10(a)) + 1);
+        std::snprintf(b, sizeof(b), "   %.*f    ", 9 - digits, v);
+    } else std::snprintf(b, sizeof(b), "   %.8E", v);
+    return b;
+}
+
+// e14.6 of a value that may be infinite (a section that took no time)
+std::string fortran_e_inf(double v) { return std::isfinite(v) ? fortran_e(v) : std::string("      Infinity"); }
 
 // Fortran unformatted sequential record: int32 length, payload, int32 length
 void write_record(FILE *f, const void *data, uint32_t bytes)
@@ -344,6 +370,7 @@ int main(int argc, char **argv)
     const int hb = d.storage == BGK_STORE_F64 ? 8 : 4;
     const int64_t ld = lx + 2 + d.ipad;
     Pops pops(lx, ly, hb);
+    const double mem_start = max_rss_mb();  // after the allocations, as SRC/alloca.F90:168
     int itstart = 0;
     if (irestart == 1) {  // SRC/restore_raw.F90
         FILE *f = std::fopen((dir + "/restore.bin").c_str(), "rb");
@@ -399,18 +426,30 @@ int main(int argc, char **argv)
         if (lx > 2 && ly > 2 && (rc = write_vtk(h, dir, 0, lx, ly, false))) return die("vtk", rc);
     }
     const auto t1 = std::chrono::steady_clock::now();
-    double t_last = 0;
+    auto since = [](std::chrono::steady_clock::time_point a) {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+    };
+    // section times of SRC/finalize.F90: the fused step (boundaries, streaming and collision)
+    // counts as collision time; VTK files and checkpoints as I/O; diagnostics as diagno
+    double t_last = 0, t_coll = 0, t_dg = 0, t_io = 0, mem_stop = mem_start;
     int itime = itstart;
     while (itime < itfin) {
         // advance to the next diagnostic, save or signal step
         int next = itfin;
         for (int every : {icheck, itsave, isignal, ivtim})
             if (every > 0) next = std::min(next, (itime / every + 1) * every);
-        if ((rc = bgk_step(h, next - itime))) return die("bgk_step", rc);
+        auto ts = std::chrono::steady_clock::now();
+        if ((rc = bgk_step(h, next - itime)) || (rc = bgk_sync(h))) return die("bgk_step", rc);
+        t_coll += since(ts);
         itime = next;
+        ts = std::chrono::steady_clock::now();
         if (itime % ivtim == 0 && lx > 2 && ly > 2 && (rc = write_vtk(h, dir, itime, lx, ly)))  // SRC/diagnostic.F90:32-57
             return die("vtk", rc);
+        t_io += since(ts);
+        ts = std::chrono::steady_clock::now();
         if (itime % icheck == 0 && (rc = diagnostic(itime, false))) return die("diagnostic", rc);
+        t_dg += since(ts);
+        ts = std::chrono::steady_clock::now();
         if (itime % itsave == 0) {  // SRC/save_raw.F90
             if ((rc = bgk_download(h, pops.p, lx + 2))) return die("bgk_download", rc);
             char name[64];
@@ -421,24 +460,45 @@ int main(int argc, char **argv)
             for (int q = 0; q < 9; ++q) write_record(f, pops.p[q], (uint32_t)(pops.n * hb));
             std::fclose(f);
         }
+        t_io += since(ts);
         if (itime % isignal == 0) {  // SRC/profile.F90: mean time per step
-            bgk_sync(h);
-            const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
+            const double t = since(t1);
             std::printf(" Iteration %8d  time/step %12.5e s\n", itime, (t - t_last) / isignal);
             t_last = t;
+            mem_stop = max_rss_mb();
         }
     }
     bgk_sync(h);
-    const auto t2 = std::chrono::steady_clock::now();
-    const double loop = std::chrono::duration<double>(t2 - t1).count();
+    const double loop = since(t1), init = std::chrono::duration<double>(t1 - t0).count();
     if ((rc = diagnostic(itime, true))) return die("diagnostic", rc);
-    const double mlups = (double)lx * ly * (itfin - itstart) / loop / 1e6;
+    mem_stop = max_rss_mb();
+    // bgk.perf in the layout and formats of SRC/finalize.F90:34-75 (both clock columns hold the
+    // same wall time; move, boundary and obstacle work is inside the fused step)
+    const double steps = (double)(itfin - itstart), cells = (double)lx * ly;
+    const double mlups = cells * steps / loop / 1e6;
+    const char *bar = " #--------------------------------\n";
     FILE *fp = std::fopen((dir + "/bgk.perf").c_str(), "w");
-    std::fprintf(fp, "# Run info\n %d %d\n# Time for section\n init %.6f\n loop %.6f\n", lx, ly,
-                 std::chrono::duration<double>(t1 - t0).count(), loop);
-    std::fprintf(fp, "# Derived (global) metrics\n Mlups %.3f\n", mlups);
+    std::fprintf(fp, "%s # Run info \n%12d%12d\n%s # Time for section \n", bar, lx, ly, bar);
+    const struct { const char *name; double t; } sec[] = {
+        {"init   time", init}, {"loop   time", loop}, {"coll   time", t_coll}, {"move   time", 0.0},
+        {"bc     time", 0.0}, {"I/O    time", t_io}, {"diagno time", t_dg}, {"Obst   time", 0.0}};
+    for (const auto &x : sec) std::fprintf(fp, " # %s%s %s \n", x.name, fortran_e(x.t).c_str(), fortran_e(x.t).c_str());
+    std::fprintf(fp, " # Check      %s \n", fortran_e(loop - (t_coll + t_io + t_dg)).c_str());
+    std::fprintf(fp, "%s # Ratio per section (loop)\n", bar);
+    const struct { const char *name; double t; } rat[] = {{"I/O  ", t_io}, {"BC   ", 0.0}, {"Coll ", t_coll},
+                                                          {"Diag.", t_dg}, {"Move ", 0.0}, {"Obs  ", 0.0}};
+    for (const auto &x : rat) std::fprintf(fp, " # Ratio %s%7.3f %7.3f \n", x.name, x.t / loop, x.t / loop);
+    std::fprintf(fp, "%s # Derived (global) metrics \n", bar);
+    std::fprintf(fp, " # Mlups      %14.6f \n", mlups);
+    // the reference's own expressions (SRC/finalize.F90:61-68), units as it labels them
+    std::fprintf(fp, " # coll   Flop%s MFlops\n", fortran_e_inf(130.0 * cells * steps / t_coll / 1e6).c_str());
+    std::fprintf(fp, " # coll   BW  %s GB/s\n", fortran_e_inf(72.0 * cells * steps / t_coll / 1e6).c_str());
+    std::fprintf(fp, " # move   BW  %s GB/s\n", fortran_e_inf(64.0 * cells * steps / 0.0 / 1e6).c_str());
+    std::fprintf(fp, "%s # Memory (task 0) metrics \n", bar);
+    std::fprintf(fp, " # Memory (start,stop)%14.6f %14.6f MB\n", mem_start, mem_stop);
+    std::fprintf(fp, "%s\n%s", list_real((lx / 1024.0) * (ly / 1024.0) * 9 * 2 * 4).c_str(), bar);
     std::fclose(fp);
-    std::printf(" Mlups %.3f\n", mlups);
+    std::printf(" # Mlups      %14.6f \n", mlups);
     for (FILE *f : {fdiag, fprobe, fpi, fpj, fumed})
         if (f) std::fclose(f);
     if (fdrag) std::fclose(fdrag);

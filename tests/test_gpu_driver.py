@@ -52,6 +52,14 @@ def test_driver_outputs_match_solver(bgk, tmp_path):
     vals = np.array([[float(x) for x in ln.split()] for ln in last])
     np.testing.assert_allclose(vals[:, 1], u, rtol=1e-5, atol=1e-11)
     assert (tmp_path / "save.00000150.bin").exists() and (tmp_path / "bgk.perf").exists()
+    # bgk.perf in the reference's layout (SRC/finalize.F90:34-75)
+    perf = (tmp_path / "bgk.perf").read_text().splitlines()
+    assert perf[1] == " # Run info " and perf[2].split() == [str(p["lx"]), str(p["ly"])]
+    mlups = [ln for ln in perf if ln.startswith(" # Mlups      ")]
+    assert len(mlups) == 1 and float(mlups[0].split()[-1]) > 0
+    loop = float([ln for ln in perf if ln.startswith(" # loop   time")][0].split()[3])
+    coll = float([ln for ln in perf if ln.startswith(" # coll   time")][0].split()[3])
+    assert 0 < coll <= loop
     # u_med.dat (SRC/varm.F90): at start-up, every icheck and once more at the end
     text = (tmp_path / "u_med.dat").read_text()
     assert [int(b.split()[0]) for b in text.split("# t=")[1:]] == [0, 100, 200, 300, 300]
