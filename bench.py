@@ -187,11 +187,11 @@ def run_profile(args):
     return 0
 
 
-def measure_variant(bgk, storage, scheme, steps, warmup, dev, tune=True, les=False):
-    compute = "f64" if storage == "f64" else "f32"
+def measure_variant(bgk, storage, scheme, steps, warmup, dev, tune=True, les=False, compute=None):
+    compute = compute or ("f64" if storage == "f64" else "f32")
     with bgk.Solver(LX, LY, tcase="LDC", svisc=SVISC, u0=U0, storage=storage, compute=compute, scheme=scheme,
                     device=dev, les=les) as s:
-        cfg = s.tune(4 if storage == "f64" else 10)[0] if tune else None
+        cfg = s.tune(4 if compute == "f64" else 10)[0] if tune else None
         pf = s.prefetch()
         s.step(warmup)
         s.sync()
@@ -433,9 +433,12 @@ def main():
                                    ("pingpong_bf16", "bf16", "pingpong", False),
                                    ("pingpong_f64", "f64", "pingpong", False), ("aa_f64", "f64", "aa", False),
                                    ("original_f32", "f32", "original", False),
-                                   ("les_f32", "f32", "pingpong", True), ("les_f16", "f16", "pingpong", True)):
-            n = vsteps if st != "f64" else max(10, vsteps // 4)
-            g, msv, cfg, pf = measure_variant(bgk, st, sch, n, 5, local, les=les)
+                                   ("les_f32", "f32", "pingpong", True), ("les_f16", "f16", "pingpong", True),
+                                   ("mixed2_f32", "f32", "pingpong", False)):
+            # mixed2: FP32 storage with the FP64 collision of the reference's MIXED2 build
+            cp = "f64" if name.startswith("mixed2") else None
+            n = vsteps if st != "f64" and cp is None else max(10, vsteps // 4)
+            g, msv, cfg, pf = measure_variant(bgk, st, sch, n, 5, local, les=les, compute=cp)
             # the two-pass form moves every population twice per step (stream, then collide)
             bw = BYTES_PER_CELL[st] * (2 if sch == "original" else 1) * LX * LY / (msv * 1e-3) / 1e9
             variants[name] = {"GLUPS": round(g, 3), "ms_per_step": round(msv, 4), "algorithmic_GBps": round(bw, 1),
