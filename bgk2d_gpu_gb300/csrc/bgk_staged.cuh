@@ -9,7 +9,9 @@
 // on one mbarrier per stage), so the HBM latency is covered by copies in flight rather than by
 // registers held in loads.  The threads read their cells from shared memory, relax them with the
 // same code as pp_tile and store straight to HBM; the last warp to finish reading a row issues
-// the copies of the row STAGES further on into the same stage, so no warp waits for another.  The result is identical to pp_tile:
+// the copies of the row STAGES further on into the same stage, so no warp waits for another.
+// The launch gives each block a stripe of STAGES rows (step_staged), so all its copies go out
+// at once and the refill path serves only longer stripes.  The result is identical to pp_tile:
 // the same arithmetic per cell, the same hash words for the stochastic rounding, and the same
 // boundary-rule recomputation from the source buffer afterwards.
 //
