@@ -67,6 +67,7 @@ int fail(bgk_handle *h, int code, const char *fmt, ...)
         h->err = buf;  // the most recent failure (bgk_last_error)
         if (code == BGK_E_CUDA) h->sticky = code;
     }
+    if (code == BGK_E_CUDA || code == BGK_E_NOMEM) (void)cudaGetLastError();  // reported here
     return code;
 }
 
@@ -80,7 +81,7 @@ int fail(bgk_handle *h, int code, const char *fmt, ...)
     do {                                                    \
         if (!(h)) return BGK_E_INVALID;                     \
         if ((h)->sticky != BGK_OK) return (h)->sticky;      \
-        if (cudaSetDevice((h)->dev) != cudaSuccess) return fail(h, BGK_E_CUDA, "cudaSetDevice"); \
+        if (enter_device((h)->dev) != cudaSuccess) return fail(h, BGK_E_CUDA, "cudaSetDevice"); \
         if ((h)->wait_ev) CK(h, cudaStreamWaitEvent((h)->st, (h)->wait_ev, 0)); \
     } while (0)
 
@@ -324,7 +325,7 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
         delete h;
         return BGK_E_INVALID;
     }
-    if (cudaSetDevice(h->dev) != cudaSuccess) {
+    if (enter_device(h->dev) != cudaSuccess) {
         delete h;
         return BGK_E_CUDA;
     }
@@ -460,7 +461,7 @@ int bgk_destroy(bgk_handle *h)
 {
     if (!h) return BGK_E_INVALID;
     if (h->batch) bgk_batch_remove((bgk_batch *)h->batch, h);
-    cudaSetDevice(h->dev);
+    enter_device(h->dev);
     if (h->st) cudaStreamSynchronize(h->st);
     release(h);
     delete h;

@@ -202,7 +202,7 @@ int bgk_batch_create(int32_t storage, int32_t compute, int32_t device, bgk_batch
     d.device = device;
     // the kernel table comes from a probe handle of the same kind
     bgk_handle *probe = nullptr;
-    if (cudaSetDevice(device) != cudaSuccess) { delete b; return BGK_E_CUDA; }
+    if (enter_device(device) != cudaSuccess) { delete b; return BGK_E_CUDA; }
     int rc = bgk_create(&d, &probe);
     if (rc) { delete b; return rc; }
     b->T = probe->T;
@@ -221,7 +221,7 @@ int bgk_batch_create(int32_t storage, int32_t compute, int32_t device, bgk_batch
 int bgk_batch_destroy(bgk_batch *b)
 {
     if (!b) return BGK_E_INVALID;
-    cudaSetDevice(b->dev);
+    enter_device(b->dev);
     cudaStreamSynchronize(b->st);
     for (auto *h : b->members) { h->batch = nullptr; h->wait_ev = nullptr; }
     if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -247,7 +247,7 @@ int bgk_batch_add(bgk_batch *b, bgk_handle *h)
     // the batch kernels carry the plain BGK collision and the folded boundary rules only
     if (h->L.les || h->cs.bfs || h->two_pass) return BGK_E_UNSUPPORTED;
     if (h->sticky) return h->sticky;
-    cudaSetDevice(b->dev);
+    enter_device(b->dev);
     if (cudaStreamSynchronize(h->st) != cudaSuccess || cudaStreamSynchronize(b->st) != cudaSuccess) return BGK_E_CUDA;
     b->members.push_back(h);
     h->batch = b;
@@ -261,7 +261,7 @@ int bgk_batch_remove(bgk_batch *b, bgk_handle *h)
     if (!b || !h) return BGK_E_INVALID;
     auto it = std::find(b->members.begin(), b->members.end(), h);
     if (it == b->members.end()) return BGK_E_NOTFOUND;
-    cudaSetDevice(b->dev);
+    enter_device(b->dev);
     if (cudaStreamSynchronize(b->st) != cudaSuccess) return BGK_E_CUDA;
     b->members.erase(it);
     h->batch = nullptr;
@@ -283,14 +283,14 @@ int bgk_batch_size(bgk_batch *b, int32_t *members, int64_t *cells)
 int bgk_batch_step(bgk_batch *b, int32_t nsteps)
 {
     if (!b || nsteps < 0) return BGK_E_INVALID;
-    if (cudaSetDevice(b->dev) != cudaSuccess) return BGK_E_CUDA;
+    if (enter_device(b->dev) != cudaSuccess) return BGK_E_CUDA;
     return step_impl(b, nsteps, true);
 }
 
 int bgk_batch_step_timed(bgk_batch *b, int32_t nsteps, float *ms)
 {
     if (!b || !ms || nsteps < 0) return BGK_E_INVALID;
-    if (cudaSetDevice(b->dev) != cudaSuccess) return BGK_E_CUDA;
+    if (enter_device(b->dev) != cudaSuccess) return BGK_E_CUDA;
     int rc = rebuild(b);
     if (rc) return rc;
     if (cudaEventRecord(b->ev0, b->st) != cudaSuccess) return BGK_E_CUDA;
@@ -304,7 +304,7 @@ int bgk_batch_step_timed(bgk_batch *b, int32_t nsteps, float *ms)
 int bgk_batch_sync(bgk_batch *b)
 {
     if (!b) return BGK_E_INVALID;
-    cudaSetDevice(b->dev);
+    enter_device(b->dev);
     return cudaStreamSynchronize(b->st) == cudaSuccess ? BGK_OK : BGK_E_CUDA;
 }
 
@@ -341,7 +341,7 @@ int bgk_batch_get_config(bgk_batch *b, int32_t out[3])
 int bgk_batch_tune(bgk_batch *b, int32_t trial_steps, int32_t *steps_run)
 {
     if (!b || trial_steps < 2) return BGK_E_INVALID;
-    if (cudaSetDevice(b->dev) != cudaSuccess) return BGK_E_CUDA;
+    if (enter_device(b->dev) != cudaSuccess) return BGK_E_CUDA;
     int64_t run = 0;
     const int bps_opts[4] = {0, 4, 8, 16};
     float best = 1e30f;

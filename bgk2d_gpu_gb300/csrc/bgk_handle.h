@@ -14,6 +14,16 @@ using bgk::CaseSetup;
 using bgk::KernelTable;
 using bgk::Lattice;
 
+// Entry of every call that works on a device: select it and drop a runtime error that an
+// earlier failed call left pending (that call already reported it), so that the launch checks of
+// this call see only their own errors.  A sticky error still fails the next call.
+inline cudaError_t enter_device(int dev)
+{
+    const cudaError_t e = cudaSetDevice(dev);
+    (void)cudaGetLastError();
+    return e;
+}
+
 struct bgk_handle {
     bgk_case_desc desc;
     int dev = 0;

@@ -114,6 +114,7 @@ extern "C" int bgk_diagno_noalloc(const void *const pops[9], int64_t ld, int32_t
     if (chunks > NA_MAX_CHUNKS) return BGK_E_TOOLARGE;
     for (int q = 0; q < 9; ++q)
         if (!pops[q]) return BGK_E_INVALID;
+    (void)cudaGetLastError();  // an error left pending by an earlier failed call is not ours
     double *scratch = nullptr;
     int rc = scratch_for_current_device(&scratch);
     if (rc != BGK_OK) return rc;

@@ -314,9 +314,12 @@ int bgk_server_create(const bgk_server_config *cfg, bgk_server **out)
     *out = nullptr;
     bgk_server *S = new bgk_server();
     S->cfg = *cfg;
-    if (cudaSetDevice(cfg->device) != cudaSuccess) { delete S; return BGK_E_CUDA; }
     size_t fr = 0, tot = 0;
-    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { delete S; return BGK_E_CUDA; }
+    if (cudaSetDevice(cfg->device) != cudaSuccess || cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        (void)cudaGetLastError();  // reported here; later calls must not see it
+        delete S;
+        return BGK_E_CUDA;
+    }
     const int64_t avail = (int64_t)fr - ((int64_t)4 << 30);
     S->budget = cfg->hbm_budget > 0 ? std::min<int64_t>(cfg->hbm_budget, avail) : avail;
     if (S->budget <= 0) { delete S; return BGK_E_NOMEM; }
