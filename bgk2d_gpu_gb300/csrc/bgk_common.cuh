@@ -51,14 +51,59 @@ template <typename S> struct Is16 { static constexpr bool value = false; };
 template <> struct Is16<__half> { static constexpr bool value = true; };
 template <> struct Is16<__nv_bfloat16> { static constexpr bool value = true; };
 
+// float -> double without the FP64 pipe (GB300 has little FP64 throughput, and the conversion
+// instruction competes with the arithmetic for it).  Exact for every float: zeros and normal
+// numbers by moving the fields (exponent rebiased by 1023 - 127 = 896, mantissa into the top
+// of the 52-bit field); subnormals, infinities and NaN, which do not occur in a running
+// simulation, by the hardware conversion.
+__device__ __forceinline__ double widen(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t mag = b & 0x7fffffffu, e = mag >> 23;
+    uint64_t d = (uint64_t)(b & 0x80000000u) << 32;
+    if (mag != 0u) {
+        if (e == 0u || e == 0xffu) return (double)f;
+        d |= ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7fffffu) << 29);
+    }
+    return __longlong_as_double((long long)d);
+}
+template <typename K> __device__ __forceinline__ K widen_to(float v)
+{
+    if constexpr (sizeof(K) == 8) return widen(v);
+    else return (K)v;
+}
+
+// double -> float, rounded to nearest with ties to even, without the FP64 pipe.  Results in the
+// normal float range and zeros by integer operations on the fields; a result that would be
+// subnormal or overflow, and infinities and NaN, by the hardware conversion.
+__device__ __forceinline__ float narrow(double d)
+{
+    const uint64_t b = (uint64_t)__double_as_longlong(d);
+    const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    const int ed = (int)((b >> 52) & 0x7ffu);
+    const uint64_t m = b & 0xfffffffffffffull;
+    if (ed == 0 && m == 0) return __uint_as_float(sign);
+    const int ef = ed - 896;
+    if (ef <= 0 || ef >= 255) return (float)d;
+    uint32_t w = ((uint32_t)ef << 23) | (uint32_t)(m >> 29);
+    const uint32_t r = (uint32_t)m & 0x1fffffffu;  // the 29 bits dropped
+    w += (r > 0x10000000u || (r == 0x10000000u && (w & 1u))) ? 1u : 0u;  // a carry into the exponent is right
+    return __uint_as_float(sign | w);
+}
+template <typename K> __device__ __forceinline__ float narrow_from(K v)
+{
+    if constexpr (sizeof(K) == 8) return narrow(v);
+    else return (float)v;
+}
+
 template <> struct Store<float> {
     static constexpr int VEC = 4;
     __device__ __forceinline__ static float raw_get(float v) { return v; }
     __device__ __forceinline__ static float raw_put(float v) { return v; }
-    template <typename K, int q> __device__ __forceinline__ static K get(float v) { return (K)v; }
-    template <typename K, int q> __device__ __forceinline__ static float put(K v) { return (float)v; }
-    template <typename K> __device__ __forceinline__ static K getq(float v, int) { return (K)v; }
-    template <typename K> __device__ __forceinline__ static float putq(K v, int) { return (float)v; }
+    template <typename K, int q> __device__ __forceinline__ static K get(float v) { return widen_to<K>(v); }
+    template <typename K, int q> __device__ __forceinline__ static float put(K v) { return narrow_from<K>(v); }
+    template <typename K> __device__ __forceinline__ static K getq(float v, int) { return widen_to<K>(v); }
+    template <typename K> __device__ __forceinline__ static float putq(K v, int) { return narrow_from<K>(v); }
 };
 template <> struct Store<double> {
     static constexpr int VEC = 2;
