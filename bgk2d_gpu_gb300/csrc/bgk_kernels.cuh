@@ -50,10 +50,25 @@ __device__ __forceinline__ K les_omega(K n01, K n03, K n05, K n08, K n10, K n12,
     return uno / ts;
 }
 
+// +0 + y as the IEEE add gives it (y, except that -0 becomes +0).  The reference adds zeros:
+// cte0 = 1 - 1, and the force terms of an unforced case.  On GB300 an FP64 add costs scarce FP64
+// throughput, so the FP64 kind makes the same value by an integer select; the FP32 kind keeps
+// the add (its step is bound by memory, and the selects cost it registers).  y + (-0) is y.
+template <typename K>
+__device__ __forceinline__ K add_zero(K y)
+{
+    if constexpr (sizeof(K) == 8) {
+        const long long b = __double_as_longlong(y);
+        return __longlong_as_double(b == (long long)0x8000000000000000ull ? 0ll : b);
+    } else {
+        return (K)0 + y;
+    }
+}
+
 template <typename K, bool LES = false>
 __device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced, K cte_s = (K)0)
 {
-    const K uno = (K)1, cte1 = (K)1, cte0 = uno - cte1;
+    const K uno = (K)1, cte1 = (K)1;  // cte0 = uno - cte1 = +0: cte0 + z is add_zero(z)
     const K tre = (K)3, qf = (K)1.5, rf = (K)3;
     const K p0 = (K)(4.0 / 9.0), p1 = (K)(1.0 / 9.0), p2 = (K)(1.0 / 36.0);
     K x01 = x[0], x03 = x[1], x05 = x[2], x08 = x[3], x10 = x[4];
@@ -67,11 +82,11 @@ __device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced
     K vsq = vx2 + vy2;
     K vxpy = vx + vy;
     K vxmy = vx - vy;
-    K qxpy = cte0 + qf * ((tre * vxpy) * vxpy - vsq);
-    K qxmy = cte0 + qf * ((tre * vxmy) * vxmy - vsq);
-    K qx = cte0 + qf * (tre * vx2 - vsq);
-    K qy = cte0 + qf * (tre * vy2 - vsq);
-    K q0 = cte0 + qf * (-vsq);
+    K qxpy = add_zero(qf * ((tre * vxpy) * vxpy - vsq));
+    K qxmy = add_zero(qf * ((tre * vxmy) * vxmy - vsq));
+    K qx = add_zero(qf * (tre * vx2 - vsq));
+    K qy = add_zero(qf * (tre * vy2 - vsq));
+    K q0 = add_zero(qf * (-vsq));
     vx = rf * vx;
     vy = rf * vy;
     vxpy = rf * vxpy;
@@ -90,16 +105,27 @@ __device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced
     K e19 = rp0 * (q0) + cte1 * (rp0 - p0);
     if constexpr (LES) omega = les_omega<K>(x01 - e01, x03 - e03, x05 - e05, x08 - e08, x10 - e10, x12 - e12, x14 - e14,
                                   x17 - e17, omega, cte_s);
-    K fx = (K)0, fy = (K)0;
-    if (forced) fx = fgrad * rho;
-    x[0] = (x01 - omega * (x01 - e01)) + (fx - fy);
-    x[1] = (x03 - omega * (x03 - e03)) + (fx + fy);
-    x[2] = (x05 - omega * (x05 - e05)) + (fx);
-    x[3] = (x08 - omega * (x08 - e08)) + (fy);
-    x[4] = (x10 - omega * (x10 - e10)) + ((-fx) - fy);
-    x[5] = (x12 - omega * (x12 - e12)) + ((-fx) + fy);
-    x[6] = (x14 - omega * (x14 - e14)) + (-fx);
-    x[7] = (x17 - omega * (x17 - e17)) + (-fy);
+    if (forced || sizeof(K) == 4) {
+        const K fx = forced ? fgrad * rho : (K)0, fy = (K)0;
+        x[0] = (x01 - omega * (x01 - e01)) + (fx - fy);
+        x[1] = (x03 - omega * (x03 - e03)) + (fx + fy);
+        x[2] = (x05 - omega * (x05 - e05)) + (fx);
+        x[3] = (x08 - omega * (x08 - e08)) + (fy);
+        x[4] = (x10 - omega * (x10 - e10)) + ((-fx) - fy);
+        x[5] = (x12 - omega * (x12 - e12)) + ((-fx) + fy);
+        x[6] = (x14 - omega * (x14 - e14)) + (-fx);
+        x[7] = (x17 - omega * (x17 - e17)) + (-fy);
+    } else {
+        // fx = fy = +0: the force terms are +0 for 01, 03, 05, 08, 12 and -0 for 10, 14, 17
+        x[0] = add_zero(x01 - omega * (x01 - e01));
+        x[1] = add_zero(x03 - omega * (x03 - e03));
+        x[2] = add_zero(x05 - omega * (x05 - e05));
+        x[3] = add_zero(x08 - omega * (x08 - e08));
+        x[4] = x10 - omega * (x10 - e10);
+        x[5] = add_zero(x12 - omega * (x12 - e12));
+        x[6] = x14 - omega * (x14 - e14);
+        x[7] = x17 - omega * (x17 - e17);
+    }
     x[8] = x19 - omega * (x19 - e19);
 }
 
