@@ -409,19 +409,22 @@ def main():
     s.step(1)
     s.step(32)
     s.sync()
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    rc = L.bgk_upload(s._h, ptr_in, LX + 2)
-    rc |= L.bgk_step(s._h, args.steps)
-    rc |= L.bgk_download(s._h, ptr_out, LX + 2)
-    e2e_s = time.perf_counter() - t0
-    if rc:
-        raise RuntimeError("e2e path failed")
-    e2e_s = max_over_ranks(e2e_s, dist)
+    # three timed runs of upload + K steps + download; the median damps host-side jitter
+    runs = []
+    for _ in range(3):
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        rc = L.bgk_upload(s._h, ptr_in, LX + 2)
+        rc |= L.bgk_step(s._h, args.steps)
+        rc |= L.bgk_download(s._h, ptr_out, LX + 2)
+        runs.append(time.perf_counter() - t0)
+        if rc:
+            raise RuntimeError("e2e path failed")
+    e2e_s = max_over_ranks(sorted(runs)[1], dist)
     e2e = {"value": job_glups(LX * LY, args.steps, e2e_s, world), "unit": "GLUPS",
            "h2d_bytes_per_step": 9 * npl * 4 / args.steps, "d2h_bytes_per_step": 9 * npl * 4 / args.steps,
-           "timed": "bgk_upload (pinned host, 9 planes) + bgk_step(K) + bgk_download (9 planes)"}
+           "timed": "bgk_upload (pinned host, 9 planes) + bgk_step(K) + bgk_download (9 planes), median of 3 runs"}
     s.close()
 
     variants = {}
