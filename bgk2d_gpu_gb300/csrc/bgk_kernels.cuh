@@ -271,11 +271,14 @@ __device__ __forceinline__ void collide_scaled(T (&D)[9], float omega, float fgr
 
 // Smagorinsky rate of one cell from p2 = |P|^2 (SRC/col_MC.F90:178-248, as les_omega):
 // 1 / (1 / (2 omega) + sqrt(18 cte_s^2 |P| + 1 / omega^2) / 2)
+// The square roots come from the hardware reciprocal square root (about one ulp): the 16-bit
+// kinds store to three or four decimal digits.
+__device__ __forceinline__ float les_sqrt(float x) { return x > 0.0f ? __fmul_rn(x, rsqrtf(x)) : 0.0f; }
 __device__ __forceinline__ float les_rate1(float p2, float omega, float cte_s)
 {
     const float r = __fdividef(1.0f, omega);
-    const float a = __fmul_rn(__fmul_rn(18.0f, __fmul_rn(cte_s, cte_s)), __fsqrt_rn(p2));
-    const float ts = __fmaf_rn(0.5f, r, __fmul_rn(0.5f, __fsqrt_rn(__fmaf_rn(r, r, a))));
+    const float a = __fmul_rn(__fmul_rn(18.0f, __fmul_rn(cte_s, cte_s)), les_sqrt(p2));
+    const float ts = __fmaf_rn(0.5f, r, __fmul_rn(0.5f, les_sqrt(__fmaf_rn(r, r, a))));
     return __fdividef(1.0f, ts);
 }
 template <> __device__ __forceinline__ float les_rate<float>(float p2, float omega, float cte_s)
