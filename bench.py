@@ -424,7 +424,8 @@ def main():
     e2e_s = max_over_ranks(sorted(runs)[1], dist)
     e2e = {"value": job_glups(LX * LY, args.steps, e2e_s, world), "unit": "GLUPS",
            "h2d_bytes_per_step": 9 * npl * 4 / args.steps, "d2h_bytes_per_step": 9 * npl * 4 / args.steps,
-           "timed": "bgk_upload (pinned host, 9 planes) + bgk_step(K) + bgk_download (9 planes), median of 3 runs"}
+           "timed": "bgk_upload (pinned host, 9 planes) + bgk_step(K) + bgk_download (9 planes), median of 3 runs",
+           "runs_ms": [round(1e3 * t, 2) for t in runs]}
     s.close()
 
     variants = {}

@@ -32,7 +32,7 @@ __device__ __forceinline__ K post_value(const Lattice &L, int cur, int phase, in
 
 // host-kind staging plane (lx+2) x (ly+2), i fastest, -> device storage
 template <typename S, typename H>
-__global__ void scatter_plane_kernel(Lattice L, int cur, int q, const H *__restrict__ stage)
+__global__ void scatter_plane_kernel(Lattice L, int cur, int q, const H *__restrict__ stage, int64_t ld)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y;
@@ -42,7 +42,7 @@ __global__ void scatter_plane_kernel(Lattice L, int cur, int q, const H *__restr
     int p;
     if (L.scheme == 0) p = (cur ? 9 : 0) + q;
     else p = opp_of(q);
-    const H v = stage[(int64_t)y * (L.lx + 2) + x];
+    const H v = stage[(int64_t)y * ld + x];
     base[p * pe + cell_index<S>(L, x, y)] = Store<S>::template putq<double>((double)v, q);
 }
 
@@ -78,14 +78,14 @@ __global__ void init_tgv_kernel(Lattice L, double u0)
 
 // device storage -> host-kind staging plane; ghost entries are written as zero
 template <typename S, typename K, typename H, bool HAS_OBS>
-__global__ void gather_plane_kernel(Lattice L, int cur, int phase, int q, H *__restrict__ stage)
+__global__ void gather_plane_kernel(Lattice L, int cur, int phase, int q, H *__restrict__ stage, int64_t ld)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y;
     if (x > L.lx + 1) return;
     H v = (H)0;
     if (x >= 1 && x <= L.lx && y >= 1 && y <= L.ly) v = (H)post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
-    stage[(int64_t)y * (L.lx + 2) + x] = v;
+    stage[(int64_t)y * ld + x] = v;
 }
 
 // AA phase-0 outflow ghosts at x = lx+1, from cell (lx, y)'s stored post-collision values

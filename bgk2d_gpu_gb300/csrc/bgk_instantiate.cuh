@@ -100,19 +100,19 @@ cudaError_t step(int kind, const Lattice &L, int parity, bool obs, int cfg, cuda
 }
 
 template <typename S>
-cudaError_t scatter(const Lattice &L, int cur, int q, const void *stage, cudaStream_t st)
+cudaError_t scatter(const Lattice &L, int cur, int q, const void *stage, int64_t ld, cudaStream_t st)
 {
     const dim3 block(256), grid((unsigned)((L.lx + 2 + 255) / 256), (unsigned)(L.ly + 2));
-    scatter_plane_kernel<S, Host<S>><<<grid, block, 0, st>>>(L, cur, q, reinterpret_cast<const Host<S> *>(stage));
+    scatter_plane_kernel<S, Host<S>><<<grid, block, 0, st>>>(L, cur, q, reinterpret_cast<const Host<S> *>(stage), ld);
     return cudaGetLastError();
 }
 
 template <typename S, typename K>
-cudaError_t gather(const Lattice &L, int cur, int phase, int q, void *stage, bool obs, cudaStream_t st)
+cudaError_t gather(const Lattice &L, int cur, int phase, int q, void *stage, int64_t ld, bool obs, cudaStream_t st)
 {
     const dim3 block(256), grid((unsigned)((L.lx + 2 + 255) / 256), (unsigned)(L.ly + 2));
-    if (obs) gather_plane_kernel<S, K, Host<S>, true><<<grid, block, 0, st>>>(L, cur, phase, q, reinterpret_cast<Host<S> *>(stage));
-    else gather_plane_kernel<S, K, Host<S>, false><<<grid, block, 0, st>>>(L, cur, phase, q, reinterpret_cast<Host<S> *>(stage));
+    if (obs) gather_plane_kernel<S, K, Host<S>, true><<<grid, block, 0, st>>>(L, cur, phase, q, reinterpret_cast<Host<S> *>(stage), ld);
+    else gather_plane_kernel<S, K, Host<S>, false><<<grid, block, 0, st>>>(L, cur, phase, q, reinterpret_cast<Host<S> *>(stage), ld);
     return cudaGetLastError();
 }
 

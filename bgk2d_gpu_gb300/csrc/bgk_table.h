@@ -27,8 +27,8 @@ struct KernelTable {
     int vec;  // cells per 16-byte vector
     int elem_bytes;
     cudaError_t (*step)(int kind, const Lattice &L, int parity, bool obs, int cfg, cudaStream_t st);
-    cudaError_t (*scatter)(const Lattice &L, int cur, int q, const void *stage, cudaStream_t st);
-    cudaError_t (*gather)(const Lattice &L, int cur, int phase, int q, void *stage, bool obs, cudaStream_t st);
+    cudaError_t (*scatter)(const Lattice &L, int cur, int q, const void *src, int64_t ld, cudaStream_t st);
+    cudaError_t (*gather)(const Lattice &L, int cur, int phase, int q, void *dst, int64_t ld, bool obs, cudaStream_t st);
     cudaError_t (*fill_outflow)(const Lattice &L, cudaStream_t st);
     cudaError_t (*bcond_step)(const Lattice &L, int cur, int stepx, int stepy, cudaStream_t st);
     cudaError_t (*init_tgv)(const Lattice &L, double u0, cudaStream_t st);

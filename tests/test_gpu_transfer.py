@@ -1,8 +1,9 @@
 """Transfers through the C ABI (bgk_upload / bgk_download, the reference's host<->device updates).
 
-Page-locked (torch pinned) and pageable host arrays, contiguous planes (ld = lx+2, one linear
-copy per plane) and padded ones (ld = lx+2+ipad, a 2D copy): all must give the same populations,
-and a download never writes the padding.
+Page-locked host arrays (torch pinned) are read and written in place by the transfer kernels;
+pageable ones go through a device staging buffer (one linear copy per contiguous plane, a 2D
+copy for a padded one).  Both paths, with contiguous (ld = lx+2) and padded (ld = lx+2+ipad)
+planes, must give the same populations, and a download never writes the padding.
 """
 import ctypes
 
