@@ -44,3 +44,25 @@ def test_two_ranks_max_and_sum():
     for rank, t, g, r, w in out:
         assert t == 2.0 and r == rank and w == 2
         assert abs(g - 2 * 4096 * 4096 * 100 / 2.0 / 1e9) < 1e-9
+
+
+def test_reference_arm_prints_one_contract_line():
+    """`bench.py --impl reference` runs on the host cores alone (no GPU) and prints one JSON line
+    with the keys of the bench contract, on the same metric and workload as the GPU arm."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "3", "--warmup", "3"],
+                       cwd=root, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["metric"] == "GLUPS" and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    assert "4096x4096" in d["config"]["workload"]
