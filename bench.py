@@ -172,6 +172,26 @@ def run_profile(args):
     import bgk2d_gpu_gb300 as bgk
     scheme, storage = args.profile.split("_")
     compute = "f64" if storage == "f64" else "f32"
+    if scheme == "batch":  # the first --cases cavities of the 96-cavity batch, one launch per step
+        cases = cfg3_cases()[:args.cases]
+        cells = sum(n * n for n, _, _ in cases)
+        solvers = [bgk.Solver(n, n, tcase="LDC", svisc=u * n / re, u0=u, storage=storage, compute=compute)
+                   for n, re, u in cases]
+        with bgk.Batch(storage, compute) as b:
+            for sv in solvers:
+                b.add(sv)
+            b.set_config(args.tile if args.tile >= 0 else 2, 0, 32)
+            b.set_prefetch(args.prefetch)
+            b.step(args.warmup)
+            b.sync()
+            ms = b.step_timed(args.steps)
+        for sv in solvers:
+            sv.close()
+        per = ms / args.steps
+        print(f"profile run {args.profile} {len(cases)} cavities ({cells} cells) tile={args.tile} "
+              f"prefetch={args.prefetch} warmup={args.warmup} steps={args.steps} "
+              f"ms/step={per:.4f} GLUPS={cells / (per * 1e-3) / 1e9:.2f}")
+        return 0
     with bgk.Solver(args.size, args.size, tcase="LDC", svisc=SVISC * args.size / LX, u0=U0, storage=storage,
                     compute=compute, scheme=scheme, les=args.les) as s:
         if args.tile >= 0:
@@ -352,11 +372,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the precision, batched and serving forms")
     ap.add_argument("--profile", default=None,
-                    help="run only <scheme>_<storage> (e.g. pingpong_f32) on a --size^2 cavity, for ncu")
+                    help="run only <scheme>_<storage> (e.g. pingpong_f32) on a --size^2 cavity, or batch_<storage> "
+                         "on --cases cavities of the 96-cavity batch, for ncu")
     ap.add_argument("--size", type=int, default=2048)
     ap.add_argument("--tile", type=int, default=-1, help="tile configuration for --profile")
     ap.add_argument("--prefetch", type=int, default=0, help="L2 prefetch distance in blocks for --profile")
     ap.add_argument("--les", action="store_true", help="Smagorinsky collision for --profile")
+    ap.add_argument("--cases", type=int, default=24, help="cavities of the batch for --profile batch_<storage>")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
