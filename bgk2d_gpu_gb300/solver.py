@@ -97,12 +97,14 @@ class Solver:
 
     @classmethod
     def from_namelist(cls, path, tcase="LDC", **kw):
+        """A case from a `bgk.input` namelist (lx, ly, svisc, u0, radius, ipad, jpad; SRC/input.F90)."""
         p = read_namelist(path)
         return cls(p["lx"], p["ly"], tcase=tcase, svisc=p["svisc"], u0=p["u0"],
                    radius=p.get("radius", 16), ipad=p.get("ipad", 0), jpad=p.get("jpad", 0), **kw)
 
     # -- lifecycle ----------------------------------------------------------------------------
     def close(self):
+        """Release the device memory of the case (bgk_destroy; SRC/dealloca.F90)."""
         if getattr(self, "_h", None):
             self._L.bgk_destroy(self._h)
             self._h = None
@@ -127,23 +129,29 @@ class Solver:
 
     # -- the reference's step sequence (SRC/bgk2d.F90:100-102) ---------------------------------
     def boundaries(self):
+        """`call boundaries` (bgk_boundaries); the fused step applies the rules."""
         self._check(self._L.bgk_boundaries(self._h), "boundaries")
 
     def propagation(self):
+        """`call propagation` (bgk_propagation); the streaming pass of the two-pass scheme."""
         self._check(self._L.bgk_propagation(self._h), "propagation")
 
     def collision(self, itime=0):
+        """`call collision(itime)` (bgk_collision): completes one time step."""
         self._check(self._L.bgk_collision(self._h, int(itime)), "collision")
 
     def step(self, n=1):
+        """n full time steps, replayed from CUDA graphs (bgk_step); asynchronous."""
         self._check(self._L.bgk_step(self._h, int(n)), "step")
 
     def step_timed(self, n):
+        """n time steps bracketed by CUDA events; returns their device time in ms."""
         ms = ctypes.c_float()
         self._check(self._L.bgk_step_timed(self._h, int(n), ctypes.byref(ms)), "step_timed")
         return ms.value
 
     def sync(self):
+        """Wait for the case's stream; reports a failure of earlier asynchronous work."""
         self._check(self._L.bgk_sync(self._h), "sync")
 
     # -- populations ------------------------------------------------------------------------
@@ -157,6 +165,7 @@ class Solver:
         return out
 
     def upload(self, arr):
+        """Set the populations from a (9, ly+2, lx+2) host-kind array laid out as `download` returns."""
         a = np.ascontiguousarray(arr, dtype=self.hdtype)
         assert a.shape == (9, self.ly + 2, self.lx + 2)
         self._check(self._L.bgk_upload(self._h, self._ptrs(a), self.lx + 2), "upload")
@@ -180,11 +189,13 @@ class Solver:
         return out
 
     def residual(self):
+        """Steady-state residual ||u - u_prev|| / ||u|| since the previous call (1 on the first)."""
         out = ctypes.c_double()
         self._check(self._L.bgk_residual(self._h, ctypes.byref(out)), "residual")
         return out.value
 
     def fields(self):
+        """(rho, u, v) of the interior as (ly, lx) float64 arrays, in the diagno arithmetic."""
         n = self.lx * self.ly
         r, u, v = np.empty(n), np.empty(n), np.empty(n)
         P = ctypes.POINTER(ctypes.c_double)
@@ -194,6 +205,7 @@ class Solver:
         return r.reshape(sh), u.reshape(sh), v.reshape(sh)
 
     def obs(self):
+        """Obstacle mask (ly, lx) and (imin, imax, jmin, jmax, nobs) of build_obs."""
         mask = np.zeros(self.lx * self.ly, dtype=np.int32)
         bb = np.zeros(5, dtype=np.int32)
         P = ctypes.POINTER(ctypes.c_int32)
@@ -201,6 +213,7 @@ class Solver:
         return mask.reshape(self.ly, self.lx), bb
 
     def scalars(self):
+        """omega, fgrad, u00, u0 after build_bcond and hencol, and the step counter."""
         out = np.zeros(4)
         it = ctypes.c_int64()
         self._check(self._L.bgk_get_scalars(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
@@ -208,12 +221,14 @@ class Solver:
         return dict(omega=out[0], fgrad=out[1], u00=out[2], u0=out[3], itime=it.value)
 
     def footprint(self):
+        """(device bytes held, algorithmic bytes moved per lattice update)."""
         b = ctypes.c_int64()
         c = ctypes.c_int32()
         self._check(self._L.bgk_footprint(self._h, ctypes.byref(b), ctypes.byref(c)), "footprint")
         return b.value, c.value
 
     def set_tile(self, cfg):
+        """Tile configuration of the step kernels (0-5 register vectors, 6-8 staged rows)."""
         self._check(self._L.bgk_set_tile(self._h, int(cfg)), "set_tile")
 
     def vtk_fields(self):
@@ -227,9 +242,11 @@ class Solver:
         return u, w, r, om, st
 
     def set_prefetch(self, blocks_ahead):
+        """L2 prefetch distance of the step kernels, in blocks (0: off)."""
         self._check(self._L.bgk_set_prefetch(self._h, int(blocks_ahead)), "set_prefetch")
 
     def prefetch(self):
+        """The current L2 prefetch distance in blocks."""
         n = ctypes.c_int32()
         self._check(self._L.bgk_get_prefetch(self._h, ctypes.byref(n)), "get_prefetch")
         return n.value
@@ -241,6 +258,7 @@ class Solver:
         return c.value, n.value
 
     def launches(self):
+        """Kernels this library has launched for the case so far."""
         n = ctypes.c_int64()
         self._check(self._L.bgk_launch_count(self._h, ctypes.byref(n)), "launch_count")
         return n.value
@@ -332,52 +350,65 @@ class Batch:
             raise BgkError(rc, what)
 
     def add(self, solver):
+        """Attach a ping-pong case of the batch's kinds; it then steps only with the batch."""
         self._check(self._L.bgk_batch_add(self._b, solver._h), "batch_add")
         self.members.append(solver)
 
     def remove(self, solver):
+        """Detach a case; it keeps its state and can step alone again."""
         self._check(self._L.bgk_batch_remove(self._b, solver._h), "batch_remove")
         self.members.remove(solver)
 
     def size(self):
+        """(members, cells) of the batch."""
         n, c = ctypes.c_int32(), ctypes.c_int64()
         self._check(self._L.bgk_batch_size(self._b, ctypes.byref(n), ctypes.byref(c)), "batch_size")
         return n.value, c.value
 
     def step(self, n=1):
+        """n steps of every member, one launch per step."""
         self._check(self._L.bgk_batch_step(self._b, int(n)), "batch_step")
 
     def step_timed(self, n):
+        """n steps of every member; returns their device time in ms."""
         ms = ctypes.c_float()
         self._check(self._L.bgk_batch_step_timed(self._b, int(n), ctypes.byref(ms)), "batch_step_timed")
         return ms.value
 
     def sync(self):
+        """Wait for the batch's stream."""
         self._check(self._L.bgk_batch_sync(self._b), "batch_sync")
 
     def set_config(self, tile_cfg, blocks_per_sm, graph_steps):
+        """Tile shape, persistent blocks per SM (0: one block per tile) and steps per graph."""
         self._check(self._L.bgk_batch_set_config(self._b, int(tile_cfg), int(blocks_per_sm), int(graph_steps)),
                     "batch_set_config")
 
     def set_prefetch(self, tiles_ahead):
+        """L2 prefetch of the work-list entry this many tiles ahead (one block per tile)."""
         self._check(self._L.bgk_batch_set_prefetch(self._b, int(tiles_ahead)), "batch_set_prefetch")
 
     def config(self):
+        """(tile_cfg, blocks_per_sm, graph_steps) in use."""
         out = (ctypes.c_int32 * 3)()
         self._check(self._L.bgk_batch_get_config(self._b, out), "batch_get_config")
         return tuple(out)
 
     def tune(self, trial_steps=10):
+        """Time real steps over tile shapes, grid sizes and graph lengths and keep the fastest;
+        returns the steps run."""
         n = ctypes.c_int32()
         self._check(self._L.bgk_batch_tune(self._b, int(trial_steps), ctypes.byref(n)), "batch_tune")
         return n.value
 
     def launches(self):
+        """Kernels this batch has launched so far."""
         n = ctypes.c_int64()
         self._check(self._L.bgk_batch_launch_count(self._b, ctypes.byref(n)), "batch_launch_count")
         return n.value
 
     def close(self):
+        """Destroy the batch; its members can step alone again."""
         if getattr(self, "_b", None):
             self._L.bgk_batch_destroy(self._b)
             self._b = None
@@ -409,6 +440,7 @@ class Server:
         self.sizes = {}
 
     def submit(self, kind, n, re, u, storage="f32", max_steps=1000, tol=0.0, check_every=500, keep_fields=False):
+        """Queue a request; returns its id."""
         r = _lib.Request(_lib.REQ[kind], int(n), float(re), float(u), _lib.STORE[storage], int(max_steps),
                          float(tol), int(check_every), int(bool(keep_fields)))
         i = ctypes.c_int64()
@@ -418,6 +450,8 @@ class Server:
         return i.value
 
     def poll(self, max_results=1024):
+        """Finished results, oldest first, as dicts: id, status, steps, size, residual, diagno,
+        drag/lift and the submit, admit and done times."""
         buf = (_lib.Result * max_results)()
         n = ctypes.c_int32()
         rc = self._L.bgk_server_poll(self._s, buf, int(max_results), ctypes.byref(n))
@@ -432,11 +466,13 @@ class Server:
         return out
 
     def drain(self, timeout_s=600.0):
+        """Block until every submitted request finished, or the timeout passed."""
         rc = self._L.bgk_server_drain(self._s, float(timeout_s))
         if rc != 0:
             raise BgkError(rc, "bgk_server_drain")
 
     def fields(self, rid, lx, ly):
+        """(rho, u, v) of a finished request that kept its fields."""
         n = lx * ly
         r, u, v = np.empty(n), np.empty(n), np.empty(n)
         P = ctypes.POINTER(ctypes.c_double)
@@ -447,6 +483,7 @@ class Server:
         return r.reshape(ly, lx), u.reshape(ly, lx), v.reshape(ly, lx)
 
     def stats(self):
+        """Aggregate statistics: completed, GLUPS, p50/p99 latency, launches, rounds."""
         st = _lib.ServerStats()
         rc = self._L.bgk_server_get_stats(self._s, ctypes.byref(st))
         if rc != 0:
@@ -454,6 +491,7 @@ class Server:
         return {k: getattr(st, k) for k, _ in _lib.ServerStats._fields_}
 
     def close(self):
+        """Stop the serving thread and release the resident requests."""
         if getattr(self, "_s", None):
             self._L.bgk_server_destroy(self._s)
             self._s = None
