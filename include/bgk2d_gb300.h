@@ -134,7 +134,10 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out);
 int bgk_destroy(bgk_handle *h);
 
 /* Copy populations host -> device / device -> host (reference layout, see top).
- * pops[q] points at direction q's array; ld is its leading dimension in elements. */
+ * pops[q] points at direction q's array; ld is its leading dimension in elements.  Page-locked
+ * arrays (cudaHostAlloc, cudaHostRegister) are read or written in place by the transfer kernels,
+ * the fastest and steadiest path; pageable arrays go through a device staging buffer.  Both
+ * synchronise. */
 int bgk_upload(bgk_handle *h, void *const pops[9], int64_t ld);
 int bgk_download(bgk_handle *h, void *const pops[9], int64_t ld);
 
