@@ -191,6 +191,11 @@ __device__ __forceinline__ void block_sum4(double (&v)[4], double *out)
 constexpr int RED_NT = 256;
 
 // diagno: partial sums of rho, u, v, |u|^2 (FP64) per block
+// exact widening to FP64 for the FP64 sums; from FP32 by integer operations (widen), since the
+// FP64 pipe bounds these reductions on GB300
+__device__ __forceinline__ double to_f64(float v) { return widen(v); }
+__device__ __forceinline__ double to_f64(double v) { return v; }
+
 template <typename S, typename K, bool HAS_OBS>
 __global__ void __launch_bounds__(RED_NT) diagno_kernel(Lattice L, int cur, int phase, int fluid_only, double *partial)
 {
@@ -206,10 +211,10 @@ __global__ void __launch_bounds__(RED_NT) diagno_kernel(Lattice L, int cur, int 
         for (int q = 0; q < 9; ++q) a[q] = post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
         K rho, xj, yj;
         moments<K>(a, rho, xj, yj);
-        acc[0] += (double)xj;
-        acc[1] += (double)yj;
-        acc[2] += (double)rho;
-        acc[3] += (double)(xj * xj + yj * yj);
+        acc[0] += to_f64(xj);
+        acc[1] += to_f64(yj);
+        acc[2] += to_f64(rho);
+        acc[3] += to_f64(xj * xj + yj * yj);
     }
     block_sum4<RED_NT>(acc, partial + 4 * blockIdx.x);
 }
