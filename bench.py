@@ -10,6 +10,16 @@ A bench "step" is one lattice time step over the whole 4096^2 domain; the metric
 With N > 1 (torchrun) every rank advances its own cavity (independent domains, no exchange):
 weak scaling, value = sum over ranks.  `--impl reference` times the CPU restatement of the
 reference step (the oracle) on this machine's host cores for the same workload.
+
+The line also carries the end-to-end figure (host buffers through the C ABI), the roofline of
+the step kernel, the CPU baseline, the clocks seen while timing, `variants` (AA, FP16, BF16,
+FP64, MIXED2, the two-pass form, LES) and `forms` (the 16-bit precision case, the 96-cavity
+batch, the serving request stream).
+
+  python bench.py --profile <scheme>_<storage> [--size n] [--tile c] [--prefetch p] [--les]
+  python bench.py --profile batch_<storage> [--cases n]
+
+run one small case and print its device time per step (the commands of the ncu summaries).
 """
 from __future__ import annotations
 
