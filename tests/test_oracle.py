@@ -203,3 +203,28 @@ def test_prof_i_host_reader_matches_reference_loop(dtype):
         assert den[i - 1] == d
         assert u[i - 1] == (x[0] + x[1] + x[2] - x[4] - x[5] - x[6]) / d
         assert v[i - 1] == (x[1] + x[3] + x[5] - x[0] - x[4] - x[7]) / d
+
+
+def test_periodic_vortex_conserves_mass(oracle_mod):
+    """A fully periodic domain has no boundary sink: the total mass of the reference vortex stays
+    at its initial value to FP64 rounding (SRC/bcond.periodic.F90 with the BGK collision)."""
+    O = oracle_mod
+    o = O.Oracle(48, 40, prec=O.DOUBLE, tcase=O.TGV, svisc=0.05, u0=0.0)
+    m0 = o.diagno(1)[2]
+    o.step(200)
+    m1 = o.diagno(1)[2]
+    assert abs(m1 - m0) < 1e-13, (m0, m1)
+    o.close()
+
+
+def test_poiseuille_channel_is_mirror_symmetric(oracle_mod):
+    """The forced channel (SRC/bcond.channel.F90) is symmetric about its centre line: after any
+    number of steps u(y) = u(m+1-y) and v(y) = -v(m+1-y), to FP64 rounding."""
+    O = oracle_mod
+    o = O.Oracle(16, 24, prec=O.DOUBLE, tcase=O.POF, svisc=0.1, u0=0.1)
+    o.step(300)
+    _, u, v = o.fields()
+    assert np.abs(u).max() > 0
+    np.testing.assert_allclose(u, u[::-1, :], rtol=0, atol=1e-12 * np.abs(u).max())
+    np.testing.assert_allclose(v, -v[::-1, :], rtol=0, atol=1e-12 * np.abs(u).max())
+    o.close()
