@@ -33,6 +33,7 @@ struct Job {
     bgk_result res;
     bgk_handle *h = nullptr;
     int64_t bytes = 0;
+    int64_t charged = 0;  // bytes counted in the server's `used` while the job holds them
     int32_t steps = 0;
     int32_t lx = 0, ly = 0;
     bool res_started = false;
@@ -155,7 +156,9 @@ void finish(bgk_server *S, std::unique_ptr<Job> j, int status)
     j->res.ly = j->ly;
     if (j->h) {
         if (status == BGK_OK || status == BGK_E_NUMERIC) {
-            bgk_diagno(j->h, 0, j->res.diagno);
+            // a request without a residual check learns of a blow-up here: non-finite means
+            const int rc = bgk_diagno(j->h, 0, j->res.diagno);
+            if (status == BGK_OK && rc != BGK_OK) j->res.status = status = rc;
             if (j->req.kind == BGK_REQ_CYLINDER) bgk_draglift(j->h, j->res.draglift);
             if (j->req.keep_fields && status == BGK_OK) {
                 const size_t n = (size_t)j->lx * j->ly;
@@ -172,7 +175,7 @@ void finish(bgk_server *S, std::unique_ptr<Job> j, int status)
     }
     j->res.t_done = S->now();
     std::lock_guard<std::mutex> g(S->mu);
-    S->used -= j->bytes;
+    S->used -= j->charged;
     if (status == BGK_OK) S->completed++;
     else S->failed++;
     S->latencies.push_back(j->res.t_done - j->res.t_submit);
@@ -202,6 +205,7 @@ void prepare(bgk_server *S)
                 j = std::move(S->pending.front());
                 S->pending.pop_front();
                 S->used += j->bytes;
+                j->charged = j->bytes;
             }
         }
         if (j->bytes > S->budget) {
@@ -250,27 +254,37 @@ void round_once(bgk_server *S)
     int32_t n = std::max(1, S->cfg.chunk_steps);
     for (auto &j : S->active) n = std::min(n, next_event(*j));
     const auto t = clk::now();
+    int64_t launches = 0, cells = 0;
+    std::map<int, int> failed;  // storage kind -> status of a batch whose step or sync failed
     for (auto &kv : S->batches) {
         int32_t members = 0;
         bgk_batch_size(kv.second, &members, nullptr);
         if (members == 0) continue;
         int64_t l0 = 0, l1 = 0;
         bgk_batch_launch_count(kv.second, &l0);
-        bgk_batch_step(kv.second, n);  // asynchronous
+        if (int rc = bgk_batch_step(kv.second, n)) failed[kv.first] = rc;  // asynchronous
         bgk_batch_launch_count(kv.second, &l1);
-        S->launches += l1 - l0;
+        launches += l1 - l0;
     }
     prepare(S);  // new cases are created while the round runs
-    for (auto &kv : S->batches) bgk_batch_sync(kv.second);
-    S->busy_s += std::chrono::duration<double>(clk::now() - t).count();
-    S->rounds++;
-    S->round_steps += n;
+    for (auto &kv : S->batches)
+        if (int rc = bgk_batch_sync(kv.second)) failed.emplace(kv.first, rc);
+    for (auto &j : S->active) cells += (int64_t)n * j->lx * j->ly;
+    {
+        std::lock_guard<std::mutex> g(S->mu);  // the statistics are read by other threads
+        S->launches += launches;
+        S->busy_s += std::chrono::duration<double>(clk::now() - t).count();
+        S->rounds++;
+        S->round_steps += n;
+        S->cell_updates += cells;
+    }
     std::vector<std::unique_ptr<Job>> keep;
     for (auto &j : S->active) {
         j->steps += n;
-        S->cell_updates += (int64_t)n * j->lx * j->ly;
         int status = -1;
-        if (j->req.tol > 0 && j->req.check_every > 0 && j->steps % j->req.check_every == 0) {
+        auto f = failed.find(j->req.storage);
+        if (f != failed.end()) status = f->second;
+        if (status < 0 && j->req.tol > 0 && j->req.check_every > 0 && j->steps % j->req.check_every == 0) {
             double r = 0;
             int rc = bgk_residual(j->h, &r);
             if (!j->res_started) { j->res_started = true; r = 1.0; }  // first check sets the snapshot
