@@ -93,7 +93,9 @@ int fail(bgk_handle *h, int code, const char *fmt, ...)
 template <typename T>
 cudaError_t dalloc(bgk_handle *h, T **p, size_t bytes)
 {
-    return cudaMallocAsync(reinterpret_cast<void **>(p), bytes, h->st);
+    const cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(p), bytes, h->st);
+    if (e != cudaSuccess) *p = nullptr;  // release() frees only what was allocated
+    return e;
 }
 
 void dfree(bgk_handle *h, void *p)

@@ -64,22 +64,33 @@ int rebuild(bgk_batch *b)
             for (int bx = 0; bx < gx; ++bx) tiles.push_back(make_int4((int)i, bx, by, 0));
         }
     }
+    // a failed allocation leaves the pointers null and the capacity 0, so a later rebuild retries
+    // the allocation and never frees an array twice
     if (lats.size() > b->cap_lats) {
         if (b->d_lats) cudaFreeAsync(b->d_lats, b->st);
         if (b->d_cur) cudaFreeAsync(b->d_cur, b->st);
+        b->d_lats = nullptr;
+        b->d_cur = nullptr;
         b->cap_lats = std::max<size_t>(lats.size(), 2 * b->cap_lats);
-        if (cudaMallocAsync((void **)&b->d_lats, b->cap_lats * sizeof(Lattice), b->st) != cudaSuccess ||
-            cudaMallocAsync((void **)&b->d_cur, b->cap_lats * sizeof(int), b->st) != cudaSuccess) {
+        const cudaError_t e1 = cudaMallocAsync((void **)&b->d_lats, b->cap_lats * sizeof(Lattice), b->st);
+        const cudaError_t e2 =
+            e1 == cudaSuccess ? cudaMallocAsync((void **)&b->d_cur, b->cap_lats * sizeof(int), b->st) : e1;
+        if (e1 != cudaSuccess || e2 != cudaSuccess) {
             cudaGetLastError();
+            if (e1 == cudaSuccess) cudaFreeAsync(b->d_lats, b->st);
+            b->d_lats = nullptr;
+            b->d_cur = nullptr;
             b->cap_lats = 0;
             return BGK_E_NOMEM;
         }
     }
     if (tiles.size() > b->cap_tiles) {
         if (b->d_tiles) cudaFreeAsync(b->d_tiles, b->st);
+        b->d_tiles = nullptr;
         b->cap_tiles = std::max<size_t>(tiles.size(), 2 * b->cap_tiles);
         if (cudaMallocAsync((void **)&b->d_tiles, b->cap_tiles * sizeof(int4), b->st) != cudaSuccess) {
             cudaGetLastError();
+            b->d_tiles = nullptr;
             b->cap_tiles = 0;
             return BGK_E_NOMEM;
         }
