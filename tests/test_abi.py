@@ -54,6 +54,35 @@ int main(void){printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(bgk_case_desc), of
                     C.les.offset, C.cte_s.offset]
 
 
+STRUCTS = [("bgk_case_desc", "CaseDesc"), ("bgk_request", "Request"), ("bgk_result", "Result"),
+           ("bgk_server_config", "ServerConfig"), ("bgk_server_stats", "ServerStats")]
+
+
+def test_every_struct_layout_matches_c():
+    """Every struct that crosses the ABI: the C compiler's sizeof and the offset of every field
+    equal the ctypes mirror's, and the mirror names the same fields in the same order."""
+    from bgk2d_gpu_gb300 import _lib
+    lines = []
+    for cname, pyname in STRUCTS:
+        fields = [f[0] for f in getattr(_lib, pyname)._fields_]
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for f in fields:
+            lines.append(f'printf("{cname}.{f} %zu\\n", offsetof({cname}, {f}));')
+    src = ('#include <stdio.h>\n#include <stddef.h>\n#include "bgk2d_gb300.h"\nint main(void){'
+           + "\n".join(lines) + "return 0;}\n")
+    exe = os.path.join(ROOT, "bgk2d_gpu_gb300", "_build", "struct_layout")
+    os.makedirs(os.path.dirname(exe), exist_ok=True)
+    r = subprocess.run(["gcc", "-x", "c", "-", "-I", os.path.join(ROOT, "include"), "-o", exe], input=src,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr  # a field the mirror names but C lacks fails here
+    c = dict(ln.split() for ln in subprocess.run([exe], capture_output=True, text=True).stdout.splitlines())
+    for cname, pyname in STRUCTS:
+        P = getattr(_lib, pyname)
+        assert int(c[cname]) == ctypes.sizeof(P), cname
+        for f, *_ in P._fields_:
+            assert int(c[f"{cname}.{f}"]) == getattr(P, f).offset, (cname, f)
+
+
 def test_no_device_means_loud_error(bgk):
     """Without a usable GPU, creating a case fails with a CUDA status; there is no CPU path."""
     import bgk2d_gpu_gb300 as m
