@@ -360,6 +360,8 @@ int main(int argc, char **argv)
                                               {"VKS", BGK_CASE_VKS}, {"COU", BGK_CASE_COU}, {"BFS", BGK_CASE_BFS}};
     if (!cases.count(tcase)) { std::fprintf(stderr, "bgk2d_gb300: unknown case %s\n", tcase.c_str()); return 1; }
     d.tcase = cases.at(tcase);
+    // init_v is read but, as in SRC/init.F90 (whose argument is unused), the initial state depends
+    // on the case alone: the periodic vortex for TGV, rest flow otherwise
     if (d.tcase == BGK_CASE_TGV) d.init_v = BGK_INIT_TGV_REF;
     (void)init_v;
 
@@ -368,21 +370,24 @@ int main(int argc, char **argv)
     int rc = bgk_create(&d, &h);
     if (rc) return die("bgk_create", rc);
     const int hb = d.storage == BGK_STORE_F64 ? 8 : 4;
-    const int64_t ld = lx + 2 + d.ipad;
     Pops pops(lx, ly, hb);
+    // one plane per checkpoint record, behind a 4-byte length marker: below 2 GiB.  Longer records
+    // would need gfortran's subrecords, which this driver does not write.
+    const uint64_t rec_bytes = (uint64_t)pops.n * hb;
+    const bool rec_ok = rec_bytes < (1ull << 31);
     const double mem_start = max_rss_mb();  // after the allocations, as SRC/alloca.F90:168
     int itstart = 0;
     if (irestart == 1) {  // SRC/restore_raw.F90
+        if (!rec_ok) { std::fprintf(stderr, "bgk2d_gb300: restore.bin planes above 2 GiB are not supported\n"); return 1; }
         FILE *f = std::fopen((dir + "/restore.bin").c_str(), "rb");
         int32_t it = 0;
         bool ok = f && read_record(f, &it, 4);
-        for (int q = 0; ok && q < 9; ++q) ok = read_record(f, pops.p[q], (uint32_t)(pops.n * hb));
+        for (int q = 0; ok && q < 9; ++q) ok = read_record(f, pops.p[q], (uint32_t)rec_bytes);
         if (f) std::fclose(f);
         if (!ok) { std::fprintf(stderr, "bgk2d_gb300: cannot read restore.bin\n"); return 1; }
         itstart = it;
         if ((rc = bgk_upload(h, pops.p, lx + 2))) return die("bgk_upload", rc);
     }
-    (void)ld;
     if ((rc = write_obstacle_files(h, dir, lx, ly))) return die("obstacle files", rc);
     FILE *fdiag = std::fopen((dir + "/diagno.dat").c_str(), "w");
     FILE *fprobe = std::fopen((dir + "/probe.dat").c_str(), "w");
@@ -390,6 +395,10 @@ int main(int argc, char **argv)
     FILE *fpj = std::fopen((dir + "/prof_j.dat").c_str(), "w");
     FILE *fumed = std::fopen((dir + "/u_med.dat").c_str(), "w");  // SRC/setup.F90:127-128
     FILE *fdrag = d.tcase == BGK_CASE_VKS ? std::fopen((dir + "/drag.lift.dat").c_str(), "w") : nullptr;
+    if (!fdiag || !fprobe || !fpi || !fpj || !fumed || (d.tcase == BGK_CASE_VKS && !fdrag)) {
+        std::fprintf(stderr, "bgk2d_gb300: cannot write the output files in %s\n", dir.c_str());
+        return 1;
+    }
     const bool dbl = d.storage == BGK_STORE_F64;
     // SRC/diagnostic.F90:70-82 at every icheck (diagno, probe, varm, prof_i, prof_j, draglift);
     // SRC/bgk2d.F90:122-125 once after the loop (diagno, varm, prof_i, prof_j)
@@ -454,10 +463,12 @@ int main(int argc, char **argv)
             if ((rc = bgk_download(h, pops.p, lx + 2))) return die("bgk_download", rc);
             char name[64];
             std::snprintf(name, sizeof(name), "/save.%08d.bin", itime);
+            if (!rec_ok) { std::fprintf(stderr, "bgk2d_gb300: checkpoint planes above 2 GiB are not supported\n"); return 1; }
             FILE *f = std::fopen((dir + name).c_str(), "wb");
+            if (!f) { std::fprintf(stderr, "bgk2d_gb300: cannot write %s%s\n", dir.c_str(), name); return 1; }
             int32_t it = itime;
             write_record(f, &it, 4);
-            for (int q = 0; q < 9; ++q) write_record(f, pops.p[q], (uint32_t)(pops.n * hb));
+            for (int q = 0; q < 9; ++q) write_record(f, pops.p[q], (uint32_t)rec_bytes);
             std::fclose(f);
         }
         t_io += since(ts);
@@ -478,6 +489,7 @@ int main(int argc, char **argv)
     const double mlups = cells * steps / loop / 1e6;
     const char *bar = " #--------------------------------\n";
     FILE *fp = std::fopen((dir + "/bgk.perf").c_str(), "w");
+    if (!fp) { std::fprintf(stderr, "bgk2d_gb300: cannot write %s/bgk.perf\n", dir.c_str()); return 1; }
     std::fprintf(fp, "%s # Run info \n%12d%12d\n%s # Time for section \n", bar, lx, ly, bar);
     const struct { const char *name; double t; } sec[] = {
         {"init   time", init}, {"loop   time", loop}, {"coll   time", t_coll}, {"move   time", 0.0},
