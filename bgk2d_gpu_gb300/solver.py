@@ -67,7 +67,8 @@ class Solver:
         self._mask_keep = None
         if obs_mask is not None:
             mk = np.ascontiguousarray(obs_mask, dtype=np.int32)
-            assert mk.shape == (ly, lx)
+            if mk.shape != (ly, lx):
+                raise ValueError(f"obs_mask has shape {mk.shape}, expected (ly, lx) = {(ly, lx)}")
             self._mask_keep = mk
             d.obstacle = _lib.OBS["mask"]
             d.obs_mask = mk.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
@@ -167,7 +168,8 @@ class Solver:
     def upload(self, arr):
         """Set the populations from a (9, ly+2, lx+2) host-kind array laid out as `download` returns."""
         a = np.ascontiguousarray(arr, dtype=self.hdtype)
-        assert a.shape == (9, self.ly + 2, self.lx + 2)
+        if a.shape != (9, self.ly + 2, self.lx + 2):
+            raise ValueError(f"populations have shape {a.shape}, expected {(9, self.ly + 2, self.lx + 2)}")
         self._check(self._L.bgk_upload(self._h, self._ptrs(a), self.lx + 2), "upload")
 
     # -- reductions (FP64 on the device) ------------------------------------------------------
