@@ -330,6 +330,7 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
     *out = nullptr;
     const bgk_case_desc &d = *desc;
     if (d.lx < 2 || d.ly < 2 || d.ipad < 0 || d.jpad < 0) return BGK_E_INVALID;
+    if (d.ly > BGK_MAX_LY) return BGK_E_TOOLARGE;  // ly + 2 grid rows must fit gridDim.y (65535)
     if (d.scheme != BGK_SCHEME_PINGPONG && d.scheme != BGK_SCHEME_AA && d.scheme != BGK_SCHEME_ORIGINAL)
         return BGK_E_INVALID;
     KernelTable T;

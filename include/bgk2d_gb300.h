@@ -129,7 +129,9 @@ int bgk_default_desc(bgk_case_desc *desc);
 
 /* Allocate the device state for one case and set it up like alloca + initialize
  * (SRC/alloca.F90, SRC/initialize.F90:70-128: build_bcond, build_obs, init, hencol).
- * Returns BGK_E_NOMEM when the populations do not fit in free HBM. */
+ * Returns BGK_E_NOMEM when the populations do not fit in free HBM, and BGK_E_TOOLARGE when
+ * ly > BGK_MAX_LY (the kernels put one lattice row, ghost rows included, per grid row). */
+#define BGK_MAX_LY 65533
 int bgk_create(const bgk_case_desc *desc, bgk_handle **out);
 int bgk_destroy(bgk_handle *h);
 

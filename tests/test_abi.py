@@ -89,3 +89,13 @@ def test_mask_shape_is_checked_before_the_library():
     import bgk2d_gpu_gb300 as m
     with pytest.raises(ValueError):
         m.Solver(32, 16, obs_mask=np.zeros((32, 16), dtype=np.int32))
+
+
+@pytest.mark.parametrize("lx,ly,code", [(0, 16, 1), (16, 1, 1), (16, 65534, 9), (8, 1 << 20, 9)])
+def test_create_rejects_sizes_before_touching_a_device(lx, ly, code):
+    """Sizes outside the library's limits fail in bgk_create before any CUDA call:
+    BGK_E_INVALID below 2 cells, BGK_E_TOOLARGE above BGK_MAX_LY = 65533 rows."""
+    import bgk2d_gpu_gb300 as m
+    with pytest.raises(m.BgkError) as e:
+        m.Solver(lx, ly)
+    assert e.value.code == code
