@@ -278,7 +278,7 @@ typedef struct bgk_request {
     int32_t n;           /* cavity / vortex edge, or cylinder diameter */
     double re;           /* Reynolds number */
     double u;            /* lid speed, inflow peak or vortex amplitude */
-    int32_t storage;     /* BGK_STORE_F32 / F16 / BF16 */
+    int32_t storage;     /* BGK_STORE_F32 / F64 / F16 / BF16 */
     int32_t max_steps;   /* step budget */
     double tol;          /* residual tolerance; <= 0 runs max_steps */
     int32_t check_every; /* steps between residual checks (> 0) */
@@ -287,7 +287,9 @@ typedef struct bgk_request {
 
 typedef struct bgk_result {
     int64_t id;
-    int32_t status;       /* BGK_OK, BGK_E_NUMERIC, BGK_E_NOMEM (never admissible), ... */
+    int32_t status;       /* BGK_OK; BGK_E_NUMERIC when a residual or the final means are not
+                             finite; BGK_E_NOMEM when the request can never fit the budget; the
+                             status of a failed bgk_create, or of a failed step of its batch */
     int32_t steps;
     int32_t lx, ly;
     double residual;      /* last residual (0 when never checked) */
