@@ -8,10 +8,10 @@
 // deviations f - w) and a host array for the four means.
 //
 // The FP64 partial sums go to a fixed static device array instead of allocated scratch.  Every
-// GPU that loads the library holds that array until the process exits.  The array is shared
-// by all calls; each call overwrites the partials it reads, so nothing has to be cleared
-// between calls, but two calls that overlap on the GPU (different host threads, or different
-// devices' calls racing on one device) would race on it.
+// GPU that loads the library holds that array until the process exits.  Each call overwrites
+// the partials it reads, so nothing has to be cleared between calls.  Calls from different host
+// threads share the array: one process-wide mutex covers each call from its launches to the
+// synchronous read of the totals, so calls never overlap on the GPU.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -86,13 +86,12 @@ __global__ void noalloc_total_kernel(double *scratch, int nb)
 std::mutex g_mu;
 double *g_scratch_addr[NA_MAX_DEVICES] = {nullptr};
 
-// once per device, with that device current: the device address of the static array
+// once per device, with that device current and g_mu held: the device address of the static array
 int scratch_for_current_device(double **out)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return BGK_E_CUDA;
     if (dev < 0 || dev >= NA_MAX_DEVICES) return BGK_E_INVALID;
-    std::lock_guard<std::mutex> g(g_mu);
     if (!g_scratch_addr[dev]) {
         void *p = nullptr;
         if (cudaGetSymbolAddress(&p, g_diag_scratch) != cudaSuccess) return BGK_E_CUDA;
@@ -114,6 +113,7 @@ extern "C" int bgk_diagno_noalloc(const void *const pops[9], int64_t ld, int32_t
     if (chunks > NA_MAX_CHUNKS) return BGK_E_TOOLARGE;
     for (int q = 0; q < 9; ++q)
         if (!pops[q]) return BGK_E_INVALID;
+    std::lock_guard<std::mutex> g(g_mu);  // held until the totals are back on the host
     (void)cudaGetLastError();  // an error left pending by an earlier failed call is not ours
     double *scratch = nullptr;
     int rc = scratch_for_current_device(&scratch);

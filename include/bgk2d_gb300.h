@@ -229,7 +229,7 @@ const char *bgk_version(void);
  * a device looks up the array's device address (cudaGetSymbolAddress), so make that first
  * call before any stream capture.  Runs on the legacy default stream and returns when the
  * means are on the host; the caller makes sure the arrays are ready.  All calls share the
- * array: calls that overlap on the GPU (from several host threads) race on it. */
+ * array, so calls from several host threads are serialised by a process-wide lock. */
 int bgk_diagno_noalloc(const void *const pops[9], int64_t ld, int32_t lx, int32_t ly, int32_t storage,
                        double out[4]);
 
