@@ -10,8 +10,9 @@
 // fields computed on the device) and bgk.perf.
 //
 //   bgk2d_gb300 [--input bgk.input] [--case LDC|TGV|POF|VKS|COU|BFS] [--prec single|double|mixed2|f16|bf16]
-//               [--scheme pingpong|aa|original] [--les 0|1] [--dir OUTDIR]
+//               [--scheme pingpong|aa|original] [--les 0|1] [--dir OUTDIR] [--check-input 0|1]
 // `--les 1` stands for the reference's -DLES build (Smagorinsky constant from the namelist key cteS).
+// `--check-input 1` parses the input, prints the case it describes and exits, without a GPU.
 #include <cctype>
 #include <chrono>
 #include <cmath>
@@ -60,6 +61,9 @@ std::map<std::string, std::string> read_namelist(const std::string &path)
     std::stringstream ss;
     ss << f.rdbuf();
     std::string t = ss.str();
+    for (char &c : t) c = (char)std::tolower((unsigned char)c);  // namelist names ignore case
+    for (size_t c = t.find('!'); c != std::string::npos; c = t.find('!', c))  // comments run to end of line
+        t.erase(c, t.find('\n', c) == std::string::npos ? std::string::npos : t.find('\n', c) - c);
     std::map<std::string, std::string> kv;
     size_t a = t.find("&parameters");
     if (a == std::string::npos) return kv;
@@ -79,8 +83,7 @@ std::map<std::string, std::string> read_namelist(const std::string &path)
         if (k.empty() && i > 0) k = toks[i - 1];
         if (v.empty() && i + 1 < toks.size()) v = toks[++i];
         for (char &c : v)
-            if (c == 'd' || c == 'D') c = 'e';
-        for (char &c : k) c = (char)std::tolower((unsigned char)c);  // namelist names ignore case
+            if (c == 'd') c = 'e';
         kv[k] = v;
     }
     return kv;
@@ -323,6 +326,12 @@ int die(const char *what, int rc)
 int main(int argc, char **argv)
 {
     std::string input = "bgk.input", tcase = "LDC", prec = "single", scheme = "pingpong", dir = ".", les = "0";
+    std::string check = "0";
+    const auto bad = [](const char *what, const std::string &v) {
+        std::fprintf(stderr, "bgk2d_gb300: bad %s '%s'\n", what, v.c_str());
+        return 2;
+    };
+    if (argc % 2 == 0) return bad("option (no value)", argv[argc - 1]);
     for (int i = 1; i + 1 < argc; i += 2) {
         std::string k = argv[i], v = argv[i + 1];
         if (k == "--input") input = v;
@@ -331,7 +340,14 @@ int main(int argc, char **argv)
         else if (k == "--scheme") scheme = v;
         else if (k == "--dir") dir = v;
         else if (k == "--les") les = v;
+        else if (k == "--check-input") check = v;
+        else return bad("option", k);
     }
+    if (prec != "single" && prec != "double" && prec != "mixed2" && prec != "f16" && prec != "bf16")
+        return bad("--prec", prec);
+    if (scheme != "pingpong" && scheme != "aa" && scheme != "original") return bad("--scheme", scheme);
+    if (les != "0" && les != "1") return bad("--les", les);
+    if (check != "0" && check != "1") return bad("--check-input", check);
     auto kv = read_namelist(input);
     if (kv.empty()) { std::fprintf(stderr, "bgk2d_gb300: no &parameters namelist in %s\n", input.c_str()); return 1; }
     auto geti = [&](const char *k, int d) { return kv.count(k) ? std::atoi(kv[k].c_str()) : d; };
@@ -364,6 +380,13 @@ int main(int argc, char **argv)
     // on the case alone: the periodic vortex for TGV, rest flow otherwise
     if (d.tcase == BGK_CASE_TGV) d.init_v = BGK_INIT_TGV_REF;
     (void)init_v;
+    if (check == "1") {
+        std::printf("case=%s prec=%s scheme=%s les=%d lx=%d ly=%d ipad=%d jpad=%d svisc=%.17g u0=%.17g "
+                    "ctes=%.17g radius=%d itfin=%d ivtim=%d isignal=%d itsave=%d icheck=%d irestart=%d\n",
+                    tcase.c_str(), prec.c_str(), scheme.c_str(), d.les, d.lx, d.ly, d.ipad, d.jpad, d.svisc, d.u0,
+                    d.cte_s, d.radius, itfin, ivtim, isignal, itsave, icheck, irestart);
+        return 0;
+    }
 
     const auto t0 = std::chrono::steady_clock::now();
     bgk_handle *h = nullptr;

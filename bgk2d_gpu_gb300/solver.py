@@ -24,19 +24,21 @@ WEIGHTS = np.array([1 / 36, 1 / 36, 1 / 9, 1 / 9, 1 / 36, 1 / 36, 1 / 9, 1 / 9, 
 
 def read_namelist(path: str) -> dict:
     """Parse the `&parameters` namelist of bgk.input (SRC/input.F90:44-65) into a dict,
-    with the reference defaults (SRC/input.F90:51-61) for absent keys."""
-    text = open(path).read()
+    with the reference defaults (SRC/input.F90:51-61) for absent keys.  As in Fortran list-
+    directed namelist input, names ignore case (keys are returned in lower case, e.g. `ctes`),
+    `!` starts a comment, and `d`/`D` exponents are accepted."""
+    text = re.sub(r"!.*", "", open(path).read())
     m = re.search(r"&parameters(.*?)/", text, flags=re.S | re.I)
     if not m:
         raise ValueError(f"{path}: no &parameters namelist")
-    vals = dict(flag1=0, flag2=0, flag3=0, init_v=0, cteS=0.1, ipad=0, jpad=0, radius=16)
+    vals = dict(flag1=0, flag2=0, flag3=0, init_v=0, ctes=0.1, ipad=0, jpad=0, radius=16)
     for key, val in re.findall(r"(\w+)\s*=\s*([^,\s/]+)", m.group(1)):
         v = val.strip().rstrip(",").replace("d", "e").replace("D", "e")
         try:
             num = int(v)
         except ValueError:
             num = float(v)
-        vals[key.strip()] = num
+        vals[key.strip().lower()] = num
     return vals
 
 
@@ -98,8 +100,10 @@ class Solver:
 
     @classmethod
     def from_namelist(cls, path, tcase="LDC", **kw):
-        """A case from a `bgk.input` namelist (lx, ly, svisc, u0, radius, ipad, jpad; SRC/input.F90)."""
+        """A case from a `bgk.input` namelist (lx, ly, svisc, u0, radius, ipad, jpad, cteS;
+        SRC/input.F90)."""
         p = read_namelist(path)
+        kw.setdefault("cte_s", p["ctes"])
         return cls(p["lx"], p["ly"], tcase=tcase, svisc=p["svisc"], u0=p["u0"],
                    radius=p.get("radius", 16), ipad=p.get("ipad", 0), jpad=p.get("jpad", 0), **kw)
 

@@ -99,3 +99,33 @@ def test_create_rejects_sizes_before_touching_a_device(lx, ly, code):
     with pytest.raises(m.BgkError) as e:
         m.Solver(lx, ly)
     assert e.value.code == code
+
+
+def test_namelist_fortran_forms(tmp_path):
+    """Fortran namelist input as SRC/input.F90 reads it: names in any case, `!` comments,
+    commas between items, d/D exponents; absent keys take the reference defaults."""
+    from bgk2d_gpu_gb300 import read_namelist
+    p = tmp_path / "bgk.input"
+    p.write_text("! a run\n&PARAMETERS\nLX = 512, Ly=256  ! domain\nsvisc=4.d-2\nU0=1.0D-1\n"
+                 "CTES=0.2 /\n")
+    v = read_namelist(str(p))
+    assert (v["lx"], v["ly"], v["svisc"], v["u0"], v["ctes"]) == (512, 256, 0.04, 0.1, 0.2)
+    assert v["radius"] == 16 and v["ipad"] == 0
+
+
+def test_driver_reads_fortran_namelist_and_rejects_bad_options(bgk, tmp_path):
+    """The C++ driver's own namelist reader (case-blind names, `!` comments, d exponents), seen
+    through --check-input, which stops before any device call; bad options exit with status 2."""
+    from bgk2d_gpu_gb300 import build
+    p = tmp_path / "bgk.input"
+    p.write_text("! a run\n&PARAMETERS\nLX = 512, Ly=256  ! domain\nsvisc=4.d-2\nU0=1.0D-1\nitfin=10\n"
+                 "CTES=0.2 /\n")
+    r = subprocess.run([build.EXE_PATH, "--input", str(p), "--check-input", "1", "--prec", "f16"],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    v = dict(kv.split("=") for kv in r.stdout.split())
+    assert (v["lx"], v["ly"], v["itfin"], v["radius"], v["prec"]) == ("512", "256", "10", "16", "f16")
+    assert (float(v["svisc"]), float(v["u0"]), float(v["ctes"])) == (0.04, 0.1, 0.2)
+    for args in (["--prec", "dobule"], ["--scheme", "ab"], ["--bogus", "1"], ["--input"]):
+        r = subprocess.run([build.EXE_PATH, *args], capture_output=True, text=True, timeout=60)
+        assert r.returncode == 2, (args, r.stderr)
