@@ -140,7 +140,7 @@ def load(build_if_missing: bool = True):
         "bgk_server_submit": (I32, [VP, P(Request), P(I64)]),
         "bgk_server_poll": (I32, [VP, P(Result), I32, P(I32)]),
         "bgk_server_drain": (I32, [VP, F64]),
-        "bgk_server_fields": (I32, [VP, I64, P(F64), P(F64), P(F64)]),
+        "bgk_server_fields": (I32, [VP, I64, P(F64), P(F64), P(F64), I64]),
         "bgk_server_get_stats": (I32, [VP, P(ServerStats)]),
         "bgk_diagno_noalloc": (I32, [P(VP), I64, I32, I32, I32, P(F64)]),
     }

@@ -405,13 +405,14 @@ int bgk_server_drain(bgk_server *S, double timeout_s)
     return ok ? BGK_OK : BGK_E_TIMEOUT;
 }
 
-int bgk_server_fields(bgk_server *S, int64_t id, double *rho, double *u, double *v)
+int bgk_server_fields(bgk_server *S, int64_t id, double *rho, double *u, double *v, int64_t capacity)
 {
     if (!S || !rho || !u || !v) return BGK_E_INVALID;
     std::lock_guard<std::mutex> g(S->mu);
     auto it = S->kept.find(id);
     if (it == S->kept.end()) return BGK_E_NOTFOUND;
     Job &j = *it->second;
+    if (capacity < (int64_t)j.rho.size()) return BGK_E_INVALID;  // kept for a call with room
     std::memcpy(rho, j.rho.data(), j.rho.size() * sizeof(double));
     std::memcpy(u, j.u.data(), j.u.size() * sizeof(double));
     std::memcpy(v, j.v.data(), j.v.size() * sizeof(double));

@@ -483,7 +483,7 @@ class Server:
         r, u, v = np.empty(n), np.empty(n), np.empty(n)
         P = ctypes.POINTER(ctypes.c_double)
         rc = self._L.bgk_server_fields(self._s, int(rid), r.ctypes.data_as(P), u.ctypes.data_as(P),
-                                       v.ctypes.data_as(P))
+                                       v.ctypes.data_as(P), n)
         if rc != 0:
             raise BgkError(rc, "bgk_server_fields")
         return r.reshape(ly, lx), u.reshape(ly, lx), v.reshape(ly, lx)

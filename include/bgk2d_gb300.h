@@ -329,8 +329,10 @@ int bgk_server_submit(bgk_server *s, const bgk_request *req, int64_t *id);
 int bgk_server_poll(bgk_server *s, bgk_result *out, int32_t max, int32_t *n);
 /* block until every submitted request finished or timeout_s elapsed (BGK_E_TIMEOUT) */
 int bgk_server_drain(bgk_server *s, double timeout_s);
-/* fields of a finished request that asked for them (lx*ly doubles each, i fastest) */
-int bgk_server_fields(bgk_server *s, int64_t id, double *rho, double *u, double *v);
+/* fields of a finished request that asked for them: lx*ly doubles each, i fastest, into arrays
+ * of `capacity` doubles each.  BGK_E_INVALID when capacity < lx*ly (the fields stay kept);
+ * BGK_E_NOTFOUND when the request kept none or they were already taken. */
+int bgk_server_fields(bgk_server *s, int64_t id, double *rho, double *u, double *v, int64_t capacity);
 int bgk_server_get_stats(bgk_server *s, bgk_server_stats *out);
 
 #ifdef __cplusplus
