@@ -11,6 +11,7 @@ import os
 import numpy as np
 import pytest
 
+GHIA = "/root/reference/TEST/DrivenCavity/ghia.y.dat"
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
 
@@ -117,11 +118,11 @@ def test_poiseuille_profile_and_energy(oracle_mod):
     assert abs(e / (8 * u0 ** 2 / 15) - 1) < 5e-3
 
 
+@pytest.mark.skipif(not os.path.exists(GHIA), reason="reference tree not mounted")
 def test_ldc_re100_against_ghia(oracle_mod):
-    """TEST/DrivenCavity/plot.R00100.gnu: u(y)/U at x = l/2 against TEST/DrivenCavity/ghia.y.dat
-    (committed unchanged as tests/golden/ghia_y_ref.txt)."""
+    """TEST/DrivenCavity/plot.R00100.gnu: u(y)/U at x = l/2 against ghia.y.dat (read in place)."""
     O = oracle_mod
-    g = np.loadtxt(os.path.join(GOLDEN, "ghia_y_ref.txt"))
+    g = np.loadtxt(GHIA)
     o = O.Oracle(128, 128, prec=O.DOUBLE, tcase=O.LDC, svisc=0.128, u0=0.1)
     o.step(50000, threads=8)
     u, v, d = o.prof_j(64)
