@@ -273,12 +273,14 @@ int bgk_batch_remove(bgk_batch *b, bgk_handle *h)
     auto it = std::find(b->members.begin(), b->members.end(), h);
     if (it == b->members.end()) return BGK_E_NOTFOUND;
     enter_device(b->dev);
-    if (cudaStreamSynchronize(b->st) != cudaSuccess) return BGK_E_CUDA;
+    // detached even when the batch's stream reports a failure: bgk_destroy frees the handle next,
+    // and the batch must not keep a pointer to it
+    const bool ok = cudaStreamSynchronize(b->st) == cudaSuccess;
     b->members.erase(it);
     h->batch = nullptr;
     h->wait_ev = nullptr;
     b->dirty = true;
-    return BGK_OK;
+    return ok ? BGK_OK : BGK_E_CUDA;
 }
 
 int bgk_batch_size(bgk_batch *b, int32_t *members, int64_t *cells)
