@@ -4,7 +4,8 @@ csrc/bgk_serve.cpp is compiled unchanged against tests/serve_fake/ (a fake of th
 entry points, and of the few CUDA runtime calls it makes), where a step only counts steps. The
 tests check what the scheduler itself decides: admission against the HBM budget and the slot
 limit, FIFO order, residual checks at multiples of check_every, per-request statuses when a
-batch fails or a result is not finite, and the fields hand-over."""
+batch fails or a result is not finite, the fields hand-over, and (under ThreadSanitizer) that
+client threads and the scheduler thread share no state without a lock."""
 import ctypes
 import os
 import subprocess
@@ -174,3 +175,20 @@ def test_fields_capacity(srvlib):
     assert s.L.bgk_server_fields(s.s, i, rho.ctypes.data_as(p), u.ctypes.data_as(p), v.ctypes.data_as(p),
                                  rho.size) == E_NOTFOUND  # handed over once
     s.close()
+
+
+def test_scheduler_has_no_data_races(tmp_path):
+    """tests/serve_fake/race_main.cpp under ThreadSanitizer: client threads submit, poll and read
+    statistics while the scheduler thread runs rounds; no unsynchronised access is reported."""
+    exe = str(tmp_path / "race")
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-g", "-fsanitize=thread", "-I", FAKE,
+                        os.path.join(FAKE, "race_main.cpp"),
+                        os.path.join(ROOT, "bgk2d_gpu_gb300", "csrc", "bgk_serve.cpp"),
+                        os.path.join(FAKE, "fake_abi.cpp"), "-o", exe, "-lpthread"], capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip("no ThreadSanitizer in this toolchain: " + r.stderr.strip().splitlines()[-1][:120])
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    if "unexpected memory mapping" in r.stderr or "FATAL: ThreadSanitizer" in r.stderr:
+        pytest.skip("ThreadSanitizer cannot run on this kernel's memory layout")
+    assert "WARNING: ThreadSanitizer" not in r.stderr, r.stderr[:4000]
+    assert r.returncode == 0, (r.stdout, r.stderr[:2000])
