@@ -64,20 +64,23 @@ def traffic_from_profiles(kernel_key):
 
 
 class ClockSampler:
-    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    """nvidia-smi samples (every 50 ms) of SM clock and throttle reasons while the GPU works:
+    started before the autotuner and stopped after the end-to-end runs, so that the record covers
+    the timed region even when that region is a few milliseconds long."""
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, dev):
+    def __init__(self, dev, period_ms=50):
         self.dev = dev
+        self.period_ms = period_ms
         self.proc = None
         self.lines = []
 
-    def __enter__(self):
+    def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -85,11 +88,7 @@ class ClockSampler:
             self.proc = None
         return self
 
-    def _read(self):
-        for ln in self.proc.stdout:
-            self.lines.append(ln.strip())
-
-    def __exit__(self, *a):
+    def stop(self):
         if self.proc:
             self.proc.terminate()
             try:
@@ -97,8 +96,18 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
+    def __enter__(self):
+        return self.start()
+
+    def __exit__(self, *a):
+        self.stop()
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
     def summary(self):
-        sm, mx, reasons = [], [], set()
+        sm, mx, pw, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             p = [x.strip() for x in ln.split(",")]
@@ -107,6 +116,7 @@ class ClockSampler:
             try:
                 sm.append(float(p[0]))
                 mx.append(float(p[1]))
+                pw.append(float(p[2]))
             except ValueError:
                 continue
             for n, v in zip(names, p[3:7]):
@@ -115,7 +125,34 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "power_w_max": max(pw), "period_ms": self.period_ms,
+                "window": "autotune, warm-up, timed steps and end-to-end runs of the headline case"}
+
+
+def free_port():
+    import socket
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        return so.getsockname()[1]
+
+
+def spawn_ranks(n, argv, script=None, timeout=3600):
+    """One process per GPU when bench.py is started without torchrun: rank r runs `script argv`
+    with RANK, LOCAL_RANK, WORLD_SIZE and MASTER_ADDR/PORT set (gloo carries the timing barrier
+    and the max over ranks).  Rank 0's stdout is forwarded; returns the worst exit code."""
+    script = script or os.path.abspath(__file__)
+    port = free_port()
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(n), LOCAL_WORLD_SIZE=str(n),
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, script] + list(argv), env=env,
+                                      stdout=subprocess.PIPE if r == 0 else subprocess.DEVNULL, text=True))
+    out, _ = procs[0].communicate(timeout=timeout)
+    sys.stdout.write(out)
+    sys.stdout.flush()
+    rcs = [procs[0].returncode] + [p.wait(timeout=timeout) for p in procs[1:]]
+    return next((rc for rc in rcs if rc != 0), 0)
 
 
 def dist_env():
@@ -138,6 +175,13 @@ def max_over_ranks(value, dist=None):
 def job_glups(cells_per_rank, steps, seconds, world):
     """Whole-job throughput: every rank advances its own domain (weak scaling)."""
     return world * cells_per_rank * steps / seconds / 1e9
+
+
+def bench_config(world):
+    """`config` of the JSON line, the same for both arms (tuning choices go elsewhere)."""
+    return {"workload": WORKLOAD, "lx": LX, "ly": LY, "scheme": "pingpong", "storage": "f32",
+            "l2": "inputs larger than L2: 1.21 GB of populations per step",
+            "parallelism": f"{world} independent cavities, one per GPU" if world > 1 else "single domain"}
 
 
 def cpu_reference(steps_budget_s=15.0, max_steps=None):
@@ -167,10 +211,10 @@ def run_reference(args):
         return 0
     # a bounded sample: 5 s per 1000 requested steps, between 5 s and 60 s of host time
     cb = cpu_reference(steps_budget_s=min(60.0, max(5.0, 5.0 * args.steps / 1000)), max_steps=max(args.steps, 3))
-    line = {"metric": "GLUPS", "value": cb["value"], "unit": "GLUPS", "n_gpus": args.gpus, "steps": args.steps,
+    line = {"metric": "GLUPS", "value": cb["value"], "unit": "GLUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": LX * LY / (cb["value"] * 1e9) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "lx": LX, "ly": LY}, "impl": "reference", "cpu_baseline": cb,
+            "config": bench_config(world), "impl": "reference", "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -276,6 +320,88 @@ def bench_precision(bgk, dev, n=2048, steps=10000):
     return out
 
 
+def bench_precision_ldc(bgk, dev, steps=2000):
+    """The headline cavity (4096^2, Re = 10000, 2000 steps) in FP64, FP32, FP16 and BF16 storage:
+    GLUPS of each, device-timed over the same run, and the velocity-field L2 error of each
+    against the FP64 run, ||u - u64||_2 / ||u64||_2 over the interior."""
+    import numpy as np
+
+    def run(st):
+        kw = dict(tcase="LDC", svisc=SVISC, u0=U0, storage=st, device=dev)
+        with bgk.Solver(LX, LY, **kw) as t:  # tuned on a separate copy: the measured run keeps its step count
+            cfg, _ = t.tune(4 if st == "f64" else 10)
+            pf = t.prefetch()
+        with bgk.Solver(LX, LY, **kw) as s:
+            s.set_tile(cfg)
+            s.set_prefetch(pf)
+            ms = s.step_timed(steps)
+            _, u, v = s.fields()
+        return u, v, LX * LY * steps / (ms * 1e-3) / 1e9
+
+    u64, v64, g64 = run("f64")
+    den = float(np.sqrt(np.sum(u64 ** 2 + v64 ** 2)))
+    out = {"workload": f"lid-driven cavity {LX}x{LY}, Re=10000, U=0.1, {steps} steps", "f64": {"GLUPS": round(g64, 3)}}
+    for st in ("f32", "f16", "bf16"):
+        u, v, g = run(st)
+        out[st] = {"GLUPS": round(g, 3),
+                   "velocity_L2_vs_fp64": float(np.sqrt(np.sum((u - u64) ** 2 + (v - v64) ** 2)) / den)}
+    for st in ("f16", "bf16"):
+        out[st]["over_f32"] = round(out[st]["GLUPS"] / out["f32"]["GLUPS"], 3)
+    return out
+
+
+def host_link(torch, host, out, dev):
+    """Page-locked host <-> device copy rates of one 604 MB buffer by the copy engines
+    (cudaMemcpyAsync through torch), each direction alone and both at once: the ceiling of the
+    end-to-end transfers."""
+    d = torch.empty(host.shape, dtype=host.dtype, device=f"cuda:{dev}")
+    nbytes = host.numel() * host.element_size()
+    s1, s2 = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+
+    def timed(fn, reps=4):
+        best = 1e30
+        for r in range(reps):
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s1)
+            fn()
+            e1.record(s1)
+            e1.synchronize()
+            if r:
+                best = min(best, e0.elapsed_time(e1))
+        return best
+
+    def h2d():
+        with torch.cuda.stream(s1):
+            d.copy_(host, non_blocking=True)
+
+    def d2h():
+        with torch.cuda.stream(s1):
+            out.copy_(d, non_blocking=True)
+
+    def both():
+        half = host.shape[0] // 2
+        ev = torch.cuda.Event()
+        ev.record(s1)
+        s2.wait_event(ev)
+        with torch.cuda.stream(s1):
+            d[:half].copy_(host[:half], non_blocking=True)
+        with torch.cuda.stream(s2):
+            out[half:].copy_(d[half:], non_blocking=True)
+        ev2 = torch.cuda.Event()
+        ev2.record(s2)
+        s1.wait_event(ev2)
+
+    t_up, t_dn = timed(h2d), timed(d2h)
+    half_bytes = (host.shape[0] // 2) * host[0].numel() * host.element_size()
+    rest_bytes = nbytes - half_bytes
+    t_bi = timed(both)
+    del d
+    return {"h2d_GBps": round(nbytes / t_up / 1e6, 1), "d2h_GBps": round(nbytes / t_dn / 1e6, 1),
+            "both_GBps": round((half_bytes + rest_bytes) / t_bi / 1e6, 1),
+            "how": "pinned 604 MB buffer, cudaMemcpyAsync (torch copy_), best of 3, CUDA events"}
+
+
 def cfg3_cases(seed=0, count=96):
     """96 lid-driven cavities: edge in {128, 192, ..., 1536}, Re log-uniform [100, 5000],
     lid speed uniform [0.05, 0.1], tau = 3 U N / Re + 1/2."""
@@ -323,8 +449,9 @@ def bench_batched(bgk, dev, steps=5000, seq_steps=1000):
             "hbm_frac": round(72 * batched / peaks()[0], 4)}
 
 
-def cfg4_stream(rate, count, seed=1):
-    """Poisson arrivals of three case types (cavity, cylinder channel, Taylor-Green)."""
+def cfg4_stream(rate, count, seed=1, storages=("f32", "f16")):
+    """Poisson arrivals of three case types (cavity, cylinder channel, Taylor-Green); each request
+    stores its populations in one of `storages` (equally likely)."""
     import numpy as np
     rng = np.random.default_rng(seed)
     t = 0.0
@@ -332,7 +459,7 @@ def cfg4_stream(rate, count, seed=1):
     for _ in range(count):
         t += rng.exponential(1.0 / rate)
         kind = rng.choice(["ldc", "cylinder", "tgv"])
-        storage = "f32" if rng.uniform() < 0.5 else "f16"
+        storage = storages[min(int(rng.uniform() * len(storages)), len(storages) - 1)]
         if kind == "ldc":
             n = int(rng.choice(np.arange(128, 2049, 64)))
             re = float(np.exp(rng.uniform(np.log(100), np.log(min(10000, 5 * n)))))
@@ -348,10 +475,10 @@ def cfg4_stream(rate, count, seed=1):
     return reqs
 
 
-def bench_serving(bgk, dev, rates=(10.0, 30.0, 100.0), count=120):
+def bench_serving(bgk, dev, rates=(10.0, 30.0, 100.0), count=120, storages=("f32", "f16")):
     out = []
     for rate in rates:
-        stream = cfg4_stream(rate, count)
+        stream = cfg4_stream(rate, count, storages=storages)
         with bgk.Server(max_slots=64, chunk_steps=200, device=dev) as srv:
             t0 = time.perf_counter()
             for t, r in stream:
@@ -362,7 +489,8 @@ def bench_serving(bgk, dev, rates=(10.0, 30.0, 100.0), count=120):
             srv.drain(600)
             res = srv.poll()
             st = srv.stats()
-        out.append({"rate_per_s": rate, "requests": count, "completed": st["completed"], "failed": st["failed"],
+        out.append({"rate_per_s": rate, "storages": list(storages), "requests": count, "completed": st["completed"],
+                    "failed": st["failed"],
                     "GLUPS": round(st["glups"], 3), "p50_s": round(st["p50_s"], 4), "p99_s": round(st["p99_s"], 4),
                     "mean_queue_s": round(st["mean_queue_s"], 4), "peak_resident": st["peak_resident"],
                     "launches": st["launches"], "rounds": st["rounds"],
@@ -392,6 +520,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ and not args.profile:
+        # started without torchrun: one process per GPU, launched here
+        return spawn_ranks(args.gpus, sys.argv[1:])
     if args.impl == "reference":
         return run_reference(args)
     if args.profile:
@@ -403,10 +534,13 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
+        if torch.cuda.device_count() < world:
+            raise RuntimeError(f"{world} ranks but {torch.cuda.device_count()} visible GPUs")
     torch.cuda.set_device(local)
     import bgk2d_gpu_gb300 as bgk
-    bgk.load()
+    L = bgk.load()
     peak, peak_kind = peaks()
+    clk = ClockSampler(local).start()
 
     # ---- device-timed value: K steps from HBM-resident state --------------------------------
     s = bgk.Solver(LX, LY, tcase="LDC", svisc=SVISC, u0=U0, storage="f32", scheme="pingpong", device=local)
@@ -418,8 +552,7 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     n0 = s.launches()
-    with ClockSampler(local) as clk:
-        ms = s.step_timed(args.steps)
+    ms = s.step_timed(args.steps)
     torch.cuda.synchronize()
     launches = s.launches() - n0
     ms = max_over_ranks(ms, dist)
@@ -429,36 +562,53 @@ def main():
     diag = s.diagno()
 
     # ---- end-to-end through the C ABI with host buffers --------------------------------------
+    # bgk_advance_host: 9 page-locked host planes up, K steps, 9 planes down, one call
     npl = (LX + 2) * (LY + 2)
-    host = torch.zeros((9, LY + 2, LX + 2), dtype=torch.float32, pin_memory=True)
+    host = torch.zeros((9, LY + 2, LX + 2), dtype=torch.float32, pin_memory=True)  # rest state f = w
     out = torch.empty_like(host).pin_memory()
-    import ctypes
-    L = bgk.load()
-    ptr_in = (ctypes.c_void_p * 9)(*[host[q].data_ptr() for q in range(9)])
-    ptr_out = (ctypes.c_void_p * 9)(*[out[q].data_ptr() for q in range(9)])
+    ptr_in = s._host_ptrs(host)
+    ptr_out = s._host_ptrs(out)
     # one-time setup outside the timed region: the step graphs of both buffer parities
     s.step(32)
     s.step(1)
     s.step(32)
     s.sync()
-    # three timed runs of upload + K steps + download; the median damps host-side jitter
-    runs = []
-    for _ in range(3):
-        if dist:
-            dist.barrier()
-        t0 = time.perf_counter()
-        rc = L.bgk_upload(s._h, ptr_in, LX + 2)
-        rc |= L.bgk_step(s._h, args.steps)
-        rc |= L.bgk_download(s._h, ptr_out, LX + 2)
-        runs.append(time.perf_counter() - t0)
-        if rc:
-            raise RuntimeError("e2e path failed")
+    if L.bgk_advance_host(s._h, ptr_in, ptr_out, LX + 2, args.steps):
+        raise RuntimeError("advance_host failed")  # warm-up of the call itself
+
+    def timed_runs(fn, n=3):
+        runs = []
+        for _ in range(n):
+            if dist:
+                dist.barrier()
+            n1 = s.launches()
+            t0 = time.perf_counter()
+            rc = fn()
+            runs.append(time.perf_counter() - t0)
+            if rc:
+                raise RuntimeError("end-to-end call failed")
+        return runs, s.launches() - n1
+
+    runs, e2e_launches = timed_runs(lambda: L.bgk_advance_host(s._h, ptr_in, ptr_out, LX + 2, args.steps))
     e2e_s = max_over_ranks(sorted(runs)[1], dist)
+    # the same through the three separate calls, for comparison
+    seq, _ = timed_runs(lambda: L.bgk_upload(s._h, ptr_in, LX + 2) | L.bgk_step(s._h, args.steps) |
+                        L.bgk_download(s._h, ptr_out, LX + 2))
+    seq_s = max_over_ranks(sorted(seq)[1], dist)
+    link = host_link(torch, host, out, local) if rank == 0 else None
+    xfer_bytes = 2 * 9 * npl * 4
     e2e = {"value": job_glups(LX * LY, args.steps, e2e_s, world), "unit": "GLUPS",
            "h2d_bytes_per_step": 9 * npl * 4 / args.steps, "d2h_bytes_per_step": 9 * npl * 4 / args.steps,
-           "timed": "bgk_upload (pinned host, 9 planes) + bgk_step(K) + bgk_download (9 planes), median of 3 runs",
-           "runs_ms": [round(1e3 * t, 2) for t in runs]}
+           "timed": "bgk_advance_host: 9 pinned host planes up, K steps, 9 planes down (pipelined), median of 3 runs",
+           "runs_ms": [round(1e3 * t, 2) for t in runs], "launches": e2e_launches,
+           "sequential": {"value": round(job_glups(LX * LY, args.steps, seq_s, world), 3),
+                          "timed": "bgk_upload + bgk_step(K) + bgk_download, median of 3 runs",
+                          "runs_ms": [round(1e3 * t, 2) for t in seq]}}
+    if link:
+        e2e["host_link"] = link
+        e2e["link_frac"] = round(xfer_bytes / e2e_s / 1e9 / link["both_GBps"], 3)
     s.close()
+    clk.stop()
 
     variants = {}
     if not args.no_variants and rank == 0:
@@ -483,9 +633,11 @@ def main():
 
     forms = {}
     if rank == 0 and not args.no_forms:
+        forms["precision_ldc4096"] = bench_precision_ldc(bgk, local)
         forms["precision_tgv2048"] = bench_precision(bgk, local)
         forms["batched_96_cavities"] = bench_batched(bgk, local)
         forms["serving_poisson"] = bench_serving(bgk, local)
+        forms["serving_poisson_f32"] = bench_serving(bgk, local, rates=(100.0,), storages=("f32",))
 
     cpu = None
     if rank == 0 and not args.no_cpu and world == 1:
@@ -497,10 +649,17 @@ def main():
             "metric": "GLUPS", "value": round(glups, 3), "unit": "GLUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 5), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (rest-state start, no dataset)",
-            "config": {"workload": WORKLOAD, "lx": LX, "ly": LY, "scheme": "pingpong", "storage": "f32",
-                       "l2": "inputs larger than L2: 1.21 GB of populations per step",
-                       "parallelism": f"{world} independent cavities" if world > 1 else "single domain",
-                       "tile_cfg": tile_cfg, "prefetch_blocks": prefetch},
+            "config": bench_config(world),
+        }
+        p16 = forms.get("precision_ldc4096")
+        if p16:  # the 16-bit storage form on the same cavity, up front so that a tail of the line keeps it
+            line["f16_GLUPS"] = p16["f16"]["GLUPS"]
+            line["f16_over_f32"] = p16["f16"]["over_f32"]
+            line["f16_L2_vs_fp64"] = p16["f16"]["velocity_L2_vs_fp64"]
+            line["bf16_over_f32"] = p16["bf16"]["over_f32"]
+            line["bf16_L2_vs_fp64"] = p16["bf16"]["velocity_L2_vs_fp64"]
+        line.update({
+            "tuning": {"tile_cfg": tile_cfg, "prefetch_blocks": prefetch},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": kt, "peak_kind": peak_kind,
                          "traffic_source": "profiles/dram_traffic.txt, same tile configuration and prefetch"
@@ -514,7 +673,7 @@ def main():
             "diagno": [float(x) for x in diag],
             "variants": variants,
             "forms": forms,
-        }
+        })
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)

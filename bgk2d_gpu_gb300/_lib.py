@@ -100,6 +100,7 @@ def load(build_if_missing: bool = True):
         "bgk_destroy": (I32, [H]),
         "bgk_upload": (I32, [H, P(VP), I64]),
         "bgk_download": (I32, [H, P(VP), I64]),
+        "bgk_advance_host": (I32, [H, P(VP), P(VP), I64, I32]),
         "bgk_boundaries": (I32, [H]),
         "bgk_propagation": (I32, [H]),
         "bgk_collision": (I32, [H, I32]),

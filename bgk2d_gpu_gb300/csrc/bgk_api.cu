@@ -151,17 +151,34 @@ const void *mapped_host(const void *p)
     return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
-// host population arrays (reference layout) -> device state
-int upload_impl(bgk_handle *h, const void *const pops[9], int64_t ld)
+// Mapped device addresses of nine page-locked host planes, or false when one of them is
+// pageable (or not aligned to its element size).
+bool all_mapped(const bgk_handle *h, void *const pops[9], int64_t ld, HostPlanes &hp)
+{
+    hp.ld = ld;
+    for (int q = 0; q < 9; ++q) {
+        const void *dp = mapped_host(pops[q]);
+        if (!dp || ((uintptr_t)dp % (uintptr_t)h->host_bytes) != 0) return false;
+        hp.p[q] = const_cast<void *>(dp);
+    }
+    return true;
+}
+
+// host population arrays (reference layout) -> device state.  Page-locked arrays are read in
+// place by one transfer launch for all nine planes; pageable ones go through the staging plane.
+int upload_impl(bgk_handle *h, const void *const pops[9], int64_t ld, bool sync = true)
 {
     const int l = h->desc.lx, m = h->desc.ly;
     if (ld < l + 2) return fail(h, BGK_E_INVALID, "leading dimension %lld < lx+2", (long long)ld);
     const size_t hb = (size_t)h->host_bytes;
-    for (int q = 0; q < 9; ++q) {
+    for (int q = 0; q < 9; ++q)
         if (!pops[q]) return fail(h, BGK_E_INVALID, "population %d is NULL", q);
-        if (const void *dp = mapped_host(pops[q])) {
-            CK(h, h->T.scatter(h->L, h->cur, q, dp, ld, h->st));
-        } else {
+    HostPlanes hp;
+    if (all_mapped(h, const_cast<void *const *>(pops), ld, hp)) {
+        CK(h, h->T.xfer(h->L, h->cur, h->phase, true, hp, h->cs.has_obs, h->st));
+        h->launches++;
+    } else {
+        for (int q = 0; q < 9; ++q) {
             int rc = ensure_stage(h);
             if (rc) return rc;
             if (ld == l + 2)  // contiguous host plane: one linear copy (3x faster than the 2D form)
@@ -170,14 +187,43 @@ int upload_impl(bgk_handle *h, const void *const pops[9], int64_t ld)
                 CK(h, cudaMemcpy2DAsync(h->d_stage, (l + 2) * hb, pops[q], (size_t)ld * hb, (l + 2) * hb, m + 2,
                                         cudaMemcpyHostToDevice, h->st));
             CK(h, h->T.scatter(h->L, h->cur, q, h->d_stage, l + 2, h->st));
+            h->launches++;
         }
-        h->launches++;
     }
     if (h->L.scheme == BGK_SCHEME_AA) {
         h->phase = 0;
         if (h->cs.faces[XHI] == FK_OUTFLOW_EQ || h->cs.faces[XHI] == FK_OUTFLOW_ZG) {
             CK(h, h->T.fill_outflow(h->L, h->st));
             h->launches++;
+        }
+    }
+    if (sync) CK(h, cudaStreamSynchronize(h->st));
+    return BGK_OK;
+}
+
+// device state -> host population arrays (synchronises)
+int download_impl(bgk_handle *h, void *const pops[9], int64_t ld)
+{
+    const int l = h->desc.lx, m = h->desc.ly;
+    if (!pops || ld < l + 2) return fail(h, BGK_E_INVALID, "bad download arguments");
+    const size_t hb = (size_t)h->host_bytes;
+    for (int q = 0; q < 9; ++q)
+        if (!pops[q]) return fail(h, BGK_E_INVALID, "population %d is NULL", q);
+    HostPlanes hp;
+    if (all_mapped(h, pops, ld, hp)) {
+        CK(h, h->T.xfer(h->L, h->cur, h->phase, false, hp, h->cs.has_obs, h->st));
+        h->launches++;
+    } else {
+        for (int q = 0; q < 9; ++q) {
+            h->launches++;
+            int rc = ensure_stage(h);
+            if (rc) return rc;
+            CK(h, h->T.gather(h->L, h->cur, h->phase, q, h->d_stage, l + 2, h->cs.has_obs, h->st));
+            if (ld == l + 2)
+                CK(h, cudaMemcpyAsync(pops[q], h->d_stage, (size_t)(l + 2) * (m + 2) * hb, cudaMemcpyDeviceToHost, h->st));
+            else
+                CK(h, cudaMemcpy2DAsync(pops[q], (size_t)ld * hb, h->d_stage, (l + 2) * hb, (l + 2) * hb, m + 2,
+                                        cudaMemcpyDeviceToHost, h->st));
         }
     }
     CK(h, cudaStreamSynchronize(h->st));
@@ -277,6 +323,98 @@ int reduce4(bgk_handle *h, double out[4])
     CK(h, launch_finalize4(h->d_partial, h->nb_red, h->d_out, h->st));
     h->launches++;
     CK(h, cudaMemcpyAsync(out, h->d_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    return check_status(h);
+}
+
+// ---- pipelined host -> steps -> host (bgk_advance_host) ----------------------------------
+// The state moves over the host link while the steps run: the rows are cut into bands, and
+// wave w uploads band w, applies step k to band w - 2k and downloads band w - 2K - 1 in one
+// launch (WaveArgs).  Up and down traffic share the link and the steps hide under both, so a
+// short run costs about one transfer time instead of upload + steps + download.
+
+// Steps pipelined with each transfer when a run is long: the rest run from the step graphs.
+constexpr int PIPE_STEPS = 16;
+
+bool pipeline_ok(const bgk_handle *h)
+{
+    // pulls reach one row up and one row down, nothing else: no periodic y faces (row 1 pulls
+    // from row ly), no whole-lattice boundary kernel (BFS), no two-pass form, no LES tiles
+    return h->L.scheme == BGK_SCHEME_PINGPONG && !h->two_pass && !h->cs.bfs && !h->L.les &&
+           h->cs.faces[YLO] != FK_PERIODIC && h->cs.faces[YHI] != FK_PERIODIC && h->desc.ly >= 8;
+}
+
+int env_int(const char *name, int dflt)
+{
+    const char *v = std::getenv(name);
+    return (v && *v) ? std::atoi(v) : dflt;
+}
+
+// one pipelined run of K steps: with the upload of `in` (or from the state in buffer h->cur)
+// and with the download into `out` (or leaving the state on the device)
+int run_waves(bgk_handle *h, const HostPlanes *in, const HostPlanes *out, int K)
+{
+    const int lx = h->desc.lx, ly = h->desc.ly;
+    // bands of about ly/256 rows (16 at 4096^2): a band's transfer takes about as long as the
+    // steps of one wave; BGK_PIPE_ROWS / BGK_PIPE_XFER override the band height and the grid
+    // rows per transfer
+    const int R = std::max(1, std::min(ly, env_int("BGK_PIPE_ROWS", std::max(4, (ly + 255) / 256))));
+    const int cdiv = (h->cfg < NUM_CFG && TILE_CFGS[h->cfg].cdiv == 2) || h->T.elem_bytes == 2 ? 2 : 1;
+    const int nvec = (lx + h->T.vec / cdiv - 1) / (h->T.vec / cdiv);
+    const int gx = (nvec + 127) / 128;
+    // about 64 blocks of 128 threads per transfer keep the link busy
+    const int xrows = std::max(1, env_int("BGK_PIPE_XFER", 64) / gx);
+    WaveArgs a{};
+    if (in) a.in = *in;
+    if (out) a.out = *out;
+    a.band_rows = R;
+    a.nbands = (ly + R - 1) / R;
+    a.nsteps = K;
+    a.cur0 = h->cur;
+    a.xfer_rows = xrows;
+    const int nb = a.nbands;
+    const int last = (nb - 1) + 2 * K + (out ? 1 : 0);
+    for (int w = 0; w <= last; ++w) {
+        a.wave = w;
+        a.up_band = (in && w < nb) ? w : -1;
+        const int d = w - 2 * K - 1;
+        a.down_band = (out && d >= 0 && d < nb) ? d : -1;
+        a.k_lo = std::max(1, w - nb + 1 > 0 ? (w - nb + 2) / 2 : 1);
+        a.k_hi = std::min(K, w / 2);
+        const int nk = std::max(0, a.k_hi - a.k_lo + 1);
+        const int gy = (a.up_band >= 0 ? xrows : 0) + (a.down_band >= 0 ? xrows : 0) + nk * R;
+        if (gy == 0) continue;
+        CK(h, h->T.wave(h->L, a, h->cs.has_obs, cdiv, gy, h->st));
+        h->launches++;
+    }
+    h->cur = (h->cur + K) & 1;
+    h->itime += K;
+    return BGK_OK;
+}
+
+int advance_impl(bgk_handle *h, void *const in[9], void *const out[9], int64_t ld, int32_t nsteps)
+{
+    const int l = h->desc.lx;
+    if (!in || !out || ld < l + 2 || nsteps < 0) return fail(h, BGK_E_INVALID, "bad advance arguments");
+    for (int q = 0; q < 9; ++q)
+        if (!in[q] || !out[q]) return fail(h, BGK_E_INVALID, "population %d is NULL", q);
+    if (h->streamed) return fail(h, BGK_E_INVALID, "two-pass step half done: call bgk_collision first");
+    HostPlanes hin, hout;
+    int rc;
+    if (nsteps == 0 || !pipeline_ok(h) || !all_mapped(h, in, ld, hin) || !all_mapped(h, out, ld, hout)) {
+        // the same three calls in sequence
+        if ((rc = upload_impl(h, in, ld, false))) return rc;
+        if ((rc = steps_impl(h, nsteps))) return rc;
+        if ((rc = download_impl(h, out, ld))) return rc;
+        return check_status(h);
+    }
+    if (nsteps <= 2 * PIPE_STEPS) {
+        if ((rc = run_waves(h, &hin, &hout, nsteps))) return rc;
+    } else {
+        if ((rc = run_waves(h, &hin, nullptr, PIPE_STEPS))) return rc;
+        if ((rc = steps_impl(h, nsteps - 2 * PIPE_STEPS))) return rc;
+        if ((rc = run_waves(h, nullptr, &hout, PIPE_STEPS))) return rc;
+    }
     CK(h, cudaStreamSynchronize(h->st));
     return check_status(h);
 }
@@ -500,27 +638,7 @@ int bgk_upload(bgk_handle *h, void *const pops[9], int64_t ld)
 int bgk_download(bgk_handle *h, void *const pops[9], int64_t ld)
 {
     CHECK_HANDLE(h);
-    const int l = h->desc.lx, m = h->desc.ly;
-    if (!pops || ld < l + 2) return fail(h, BGK_E_INVALID, "bad download arguments");
-    const size_t hb = (size_t)h->host_bytes;
-    for (int q = 0; q < 9; ++q) {
-        if (!pops[q]) return fail(h, BGK_E_INVALID, "population %d is NULL", q);
-        h->launches++;
-        if (void *dp = const_cast<void *>(mapped_host(pops[q]))) {
-            CK(h, h->T.gather(h->L, h->cur, h->phase, q, dp, ld, h->cs.has_obs, h->st));
-            continue;
-        }
-        int rc = ensure_stage(h);
-        if (rc) return rc;
-        CK(h, h->T.gather(h->L, h->cur, h->phase, q, h->d_stage, l + 2, h->cs.has_obs, h->st));
-        if (ld == l + 2)
-            CK(h, cudaMemcpyAsync(pops[q], h->d_stage, (size_t)(l + 2) * (m + 2) * hb, cudaMemcpyDeviceToHost, h->st));
-        else
-            CK(h, cudaMemcpy2DAsync(pops[q], (size_t)ld * hb, h->d_stage, (l + 2) * hb, (l + 2) * hb, m + 2,
-                                    cudaMemcpyDeviceToHost, h->st));
-    }
-    CK(h, cudaStreamSynchronize(h->st));
-    return BGK_OK;
+    return download_impl(h, pops, ld);
 }
 
 int bgk_boundaries(bgk_handle *h)
@@ -581,6 +699,13 @@ int bgk_step_timed(bgk_handle *h, int32_t nsteps, float *ms)
     CK(h, cudaEventSynchronize(h->ev1));
     CK(h, cudaEventElapsedTime(ms, h->ev0, h->ev1));
     return check_status(h);
+}
+
+int bgk_advance_host(bgk_handle *h, void *const in[9], void *const out[9], int64_t ld, int32_t nsteps)
+{
+    CHECK_HANDLE(h);
+    NOT_IN_BATCH(h);
+    return advance_impl(h, in, out, ld, nsteps);
 }
 
 int bgk_sync(bgk_handle *h)

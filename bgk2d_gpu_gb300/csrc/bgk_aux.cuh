@@ -2,6 +2,7 @@
 #pragma once
 
 #include "bgk_kernels.cuh"
+#include "bgk_table.h"
 
 namespace bgk {
 
@@ -86,6 +87,132 @@ __global__ void gather_plane_kernel(Lattice L, int cur, int phase, int q, H *__r
     H v = (H)0;
     if (x >= 1 && x <= L.lx && y >= 1 && y <= L.ly) v = (H)post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
     stage[(int64_t)y * ld + x] = v;
+}
+
+// Rows ya..yb of the nine mapped host planes <-> state buffer cur, moved by warp wid of nw.
+// Work unit: 32 consecutive host elements of one plane, the first of them on a 128-byte boundary
+// of the host address space (units run across row ends when ld = lx + 2), so that each warp
+// access covers whole lines of the host link.  A warp keeps XFER_UNROLL units in flight.
+// Callers keep (yb - ya + 1) * ld below 2^26, so the unit arithmetic fits 32 bits.
+// UP: host -> device, the conversion of scatter_plane_kernel; !UP: device -> host, the values of
+// gather_plane_kernel (ghost entries written as zero).
+constexpr int XFER_UNROLL = 4;
+
+template <typename S, typename K, typename H, bool HAS_OBS, bool UP>
+__device__ __forceinline__ void xfer_rows(const Lattice &L, const int cur, const int phase, const HostPlanes &hp,
+                                          const int ya, const int yb, const int wid, const int nw)
+{
+    const int64_t ld = hp.ld;
+    const uint32_t n = (uint32_t)((int64_t)(yb - ya + 1) * ld);
+    const uint32_t ld32 = (uint32_t)ld;
+    const uint32_t umax = (n + 63u) / 32u;  // units of any plane: its first unit starts < 32 elements early
+    const uint32_t total = 9u * umax;
+    const int lane = threadIdx.x & 31;
+    S *base = reinterpret_cast<S *>(L.planes);
+    const int64_t pe = L.plane_elems;
+    for (uint32_t u0 = (uint32_t)wid; u0 < total; u0 += (uint32_t)nw * XFER_UNROLL) {
+        H v[XFER_UNROLL];
+        H *hptr[XFER_UNROLL];
+        int qs[XFER_UNROLL], xs[XFER_UNROLL], ys[XFER_UNROLL];
+        bool ok[XFER_UNROLL];
+#pragma unroll
+        for (int i = 0; i < XFER_UNROLL; ++i) {
+            const uint32_t uu = u0 + (uint32_t)i * (uint32_t)nw;
+            ok[i] = false;
+            qs[i] = 0; xs[i] = 0; ys[i] = 0;
+            hptr[i] = nullptr;
+            if (uu < total) {
+                const int q = (int)(uu / umax);
+                const uint32_t u = uu - (uint32_t)q * umax;
+                H *row = reinterpret_cast<H *>(hp.p[q]) + (int64_t)ya * ld;
+                const uint32_t sh = (uint32_t)(((uintptr_t)row & 127u) / sizeof(H));
+                const int64_t e = (int64_t)u * 32 + lane - (int64_t)sh;
+                if (e >= 0 && e < (int64_t)n) {
+                    const uint32_t r = (uint32_t)e / ld32;
+                    const int x = (int)((uint32_t)e - r * ld32);
+                    if (x <= L.lx + 1) {
+                        ok[i] = true;
+                        qs[i] = q; xs[i] = x; ys[i] = ya + (int)r;
+                        hptr[i] = row + e;
+                    }
+                }
+            }
+        }
+        if constexpr (UP) {
+#pragma unroll
+            for (int i = 0; i < XFER_UNROLL; ++i)
+                if (ok[i]) v[i] = *hptr[i];
+#pragma unroll
+            for (int i = 0; i < XFER_UNROLL; ++i)
+                if (ok[i]) {
+                    const int p = L.scheme == 0 ? (cur ? 9 : 0) + qs[i] : opp_of(qs[i]);
+                    base[p * pe + cell_index<S>(L, xs[i], ys[i])] = Store<S>::template putq<double>((double)v[i], qs[i]);
+                }
+        } else {
+#pragma unroll
+            for (int i = 0; i < XFER_UNROLL; ++i) {
+                v[i] = (H)0;
+                if (ok[i] && xs[i] >= 1 && xs[i] <= L.lx && ys[i] >= 1 && ys[i] <= L.ly)
+                    v[i] = (H)post_value<S, K, HAS_OBS>(L, cur, phase, qs[i], xs[i], ys[i]);
+            }
+#pragma unroll
+            for (int i = 0; i < XFER_UNROLL; ++i)
+                if (ok[i]) *hptr[i] = v[i];
+        }
+    }
+}
+
+// whole-lattice transfer of rows ya..yb (one launch per chunk of rows), 8 warps per block
+template <typename S, typename K, typename H, bool HAS_OBS, bool UP>
+__global__ void __launch_bounds__(256) xfer_kernel(const Lattice L, const int cur, const int phase, const HostPlanes hp,
+                                                   const int ya, const int yb)
+{
+    xfer_rows<S, K, H, HAS_OBS, UP>(L, cur, phase, hp, ya, yb, (int)(blockIdx.x * 8 + (threadIdx.x >> 5)),
+                                    (int)(gridDim.x * 8));
+}
+
+// host rows of band b (interior rows b*R+1 .. (b+1)*R, and the ghost row beside the first and
+// the last band)
+__device__ __forceinline__ void band_rows(const Lattice &L, const WaveArgs &a, int b, int &ya, int &yb)
+{
+    ya = b == 0 ? 0 : 1 + b * a.band_rows;
+    yb = b == a.nbands - 1 ? L.ly + 1 : (b + 1) * a.band_rows;
+}
+
+// One wave of bgk_advance_host (WaveArgs): grid rows 0.. carry the upload of band up_band, then
+// the download of band down_band (xfer_rows grid rows each, scheduled first so that the host
+// link is busy from the start of the wave), then band_rows grid rows per step item.  The step
+// items are pp_kernel's tiles (128 x 1 threads, N cells per thread) of one row each.
+template <typename S, typename K, typename H, bool HAS_OBS, int N>
+__global__ void __launch_bounds__(128, (N * sizeof(S) <= 8 || (sizeof(S) == 4 && N == 4)) ? 8 : (sizeof(S) == 2 ? 4 : 1))
+    wave_kernel(const Lattice L, const WaveArgs a)
+{
+    int by = blockIdx.y;
+    const int nw = a.xfer_rows * (int)gridDim.x * 4;
+    if (a.up_band >= 0) {
+        if (by < a.xfer_rows) {
+            int ya, yb;
+            band_rows(L, a, a.up_band, ya, yb);
+            xfer_rows<S, K, H, HAS_OBS, true>(L, a.cur0, 0, a.in, ya, yb,
+                                              (by * (int)gridDim.x + (int)blockIdx.x) * 4 + (int)(threadIdx.x >> 5), nw);
+            return;
+        }
+        by -= a.xfer_rows;
+    }
+    if (a.down_band >= 0) {
+        if (by < a.xfer_rows) {
+            int ya, yb;
+            band_rows(L, a, a.down_band, ya, yb);
+            xfer_rows<S, K, H, HAS_OBS, false>(L, (a.cur0 + a.nsteps) & 1, 0, a.out, ya, yb,
+                                               (by * (int)gridDim.x + (int)blockIdx.x) * 4 + (int)(threadIdx.x >> 5), nw);
+            return;
+        }
+        by -= a.xfer_rows;
+    }
+    const int k = a.k_lo + by / a.band_rows;
+    const int y = (a.wave - 2 * k) * a.band_rows + by % a.band_rows + 1;
+    if (y > L.ly) return;
+    pp_tile<S, K, 128, 1, HAS_OBS, N>(L, (int)blockIdx.x, y - 1, (a.cur0 + k - 1) & 1);
 }
 
 // AA phase-0 outflow ghosts at x = lx+1, from cell (lx, y)'s stored post-collision values

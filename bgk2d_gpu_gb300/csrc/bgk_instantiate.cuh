@@ -116,6 +116,45 @@ cudaError_t gather(const Lattice &L, int cur, int phase, int q, void *stage, int
     return cudaGetLastError();
 }
 
+// All nine mapped host planes <-> buffer cur in chunks of rows of fewer than 2^26 host elements
+// (the 32-bit unit arithmetic of xfer_rows), 4 blocks of 256 threads per SM at most.
+template <typename S, typename K, bool OBS, bool UP>
+cudaError_t xfer_launch(const Lattice &L, int cur, int phase, const HostPlanes &hp, cudaStream_t st)
+{
+    const int64_t rows_per_chunk = std::max<int64_t>(1, ((int64_t)1 << 26) / hp.ld - 1);
+    for (int64_t ya = 0; ya <= L.ly + 1; ya += rows_per_chunk) {
+        const int64_t yb = std::min<int64_t>(ya + rows_per_chunk - 1, L.ly + 1);
+        const int64_t units = 9 * (((yb - ya + 1) * hp.ld + 63) / 32);
+        const int64_t warps = (units + XFER_UNROLL - 1) / XFER_UNROLL;
+        const unsigned grid = (unsigned)std::min<int64_t>(4 * 152, (warps + 7) / 8);
+        xfer_kernel<S, K, Host<S>, OBS, UP><<<grid, 256, 0, st>>>(L, cur, phase, hp, (int)ya, (int)yb);
+    }
+    return cudaGetLastError();
+}
+
+template <typename S, typename K>
+cudaError_t xfer(const Lattice &L, int cur, int phase, bool up, const HostPlanes &hp, bool obs, cudaStream_t st)
+{
+    if (up) return obs ? xfer_launch<S, K, true, true>(L, cur, phase, hp, st) : xfer_launch<S, K, false, true>(L, cur, phase, hp, st);
+    return obs ? xfer_launch<S, K, true, false>(L, cur, phase, hp, st) : xfer_launch<S, K, false, false>(L, cur, phase, hp, st);
+}
+
+template <typename S, typename K, bool OBS, int N>
+cudaError_t wave_launch(const Lattice &L, const WaveArgs &a, int grid_y, cudaStream_t st)
+{
+    const int nv = (L.lx + N - 1) / N;
+    wave_kernel<S, K, Host<S>, OBS, N><<<dim3((unsigned)((nv + 127) / 128), (unsigned)grid_y), 128, 0, st>>>(L, a);
+    return cudaGetLastError();
+}
+
+template <typename S, typename K>
+cudaError_t wave(const Lattice &L, const WaveArgs &a, bool obs, int cdiv, int grid_y, cudaStream_t st)
+{
+    constexpr int V = vec_of<S>();
+    if (cdiv == 2) return obs ? wave_launch<S, K, true, V / 2>(L, a, grid_y, st) : wave_launch<S, K, false, V / 2>(L, a, grid_y, st);
+    return obs ? wave_launch<S, K, true, V>(L, a, grid_y, st) : wave_launch<S, K, false, V>(L, a, grid_y, st);
+}
+
 template <typename S, typename K>
 cudaError_t fill_outflow(const Lattice &L, cudaStream_t st)
 {
@@ -252,6 +291,8 @@ KernelTable make_table()
     t.fields = &fields<S, K>;
     t.vtk = &vtk<S, K>;
     t.batch_step = &batch_step<S, K>;
+    t.xfer = &xfer<S, K>;
+    t.wave = &wave<S, K>;
     return t;
 }
 

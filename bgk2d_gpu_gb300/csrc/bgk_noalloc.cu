@@ -26,7 +26,6 @@ namespace {
 constexpr int NA_THREADS = 256;
 constexpr int NA_CHUNK = 4096;                      // cells reduced by one block
 constexpr int NA_MAX_CHUNKS = 4096;                 // at most 4096 * 4096 = 16,777,216 cells
-constexpr int NA_MAX_DEVICES = 64;
 
 struct Planes {
     const void *p[9];
@@ -84,20 +83,16 @@ __global__ void noalloc_total_kernel(double *scratch, int nb)
 }
 
 std::mutex g_mu;
-double *g_scratch_addr[NA_MAX_DEVICES] = {nullptr};
 
-// once per device, with that device current and g_mu held: the device address of the static array
+// with g_mu held and the caller's device current: the device address of the static array in
+// the current context.  Looked up on every call (a cheap runtime query next to the synchronous
+// copy of the totals), so a context created after a cudaDeviceReset, or another context made
+// current by the caller's runtime, gets its own module's address rather than a stale one.
 int scratch_for_current_device(double **out)
 {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return BGK_E_CUDA;
-    if (dev < 0 || dev >= NA_MAX_DEVICES) return BGK_E_INVALID;
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_diag_scratch) != cudaSuccess) return BGK_E_CUDA;
-        g_scratch_addr[dev] = static_cast<double *>(p);
-    }
-    *out = g_scratch_addr[dev];
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_diag_scratch) != cudaSuccess) return BGK_E_CUDA;
+    *out = static_cast<double *>(p);
     return BGK_OK;
 }
 

@@ -185,10 +185,26 @@ void finish(bgk_server *S, std::unique_ptr<Job> j, int status)
     S->done_cv.notify_all();
 }
 
+// HBM left free on the device, less the headroom kept for the runtime and other users
+constexpr int64_t HEADROOM = (int64_t)4 << 30;
+
+int64_t free_hbm()
+{
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return INT64_MAX;  // unknown: the budget alone decides
+    }
+    return (int64_t)fr - HEADROOM;
+}
+
 // Create device state for queued requests (FIFO) while slots and HBM allow.  Each new case
-// lives on its own stream, so this overlaps with the batches' kernels.
+// lives on its own stream, so this overlaps with the batches' kernels.  A request is admitted
+// when it fits in the server's budget (fixed at creation) and in the HBM free right now: memory
+// that other processes took, or gave back, since the server started counts at every admission.
 void prepare(bgk_server *S)
 {
+    int64_t avail = -1;  // free HBM, read once per call and reduced by what this call admits
     for (;;) {
         std::unique_ptr<Job> j;
         {
@@ -196,12 +212,14 @@ void prepare(bgk_server *S)
             if (S->pending.empty()) return;
             if ((int)(S->active.size() + S->prepared.size()) >= S->cfg.max_slots) return;
             Job &head = *S->pending.front();
+            if (head.bytes <= S->budget && avail < 0) avail = std::max<int64_t>(free_hbm(), 0);
             if (head.bytes > S->budget) {  // can never fit: reject now
                 j = std::move(S->pending.front());
                 S->pending.pop_front();
-            } else if (S->used + head.bytes > S->budget) {
+            } else if (S->used + head.bytes > S->budget || head.bytes > avail) {
                 return;  // wait for memory to free up (FIFO)
             } else {
+                avail -= head.bytes;
                 j = std::move(S->pending.front());
                 S->pending.pop_front();
                 S->used += j->bytes;
@@ -334,7 +352,7 @@ int bgk_server_create(const bgk_server_config *cfg, bgk_server **out)
         delete S;
         return BGK_E_CUDA;
     }
-    const int64_t avail = (int64_t)fr - ((int64_t)4 << 30);
+    const int64_t avail = (int64_t)fr - HEADROOM;
     S->budget = cfg->hbm_budget > 0 ? std::min<int64_t>(cfg->hbm_budget, avail) : avail;
     if (S->budget <= 0) { delete S; return BGK_E_NOMEM; }
     S->t0 = clk::now();

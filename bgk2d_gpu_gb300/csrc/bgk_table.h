@@ -23,6 +23,28 @@ constexpr TileCfg TILE_CFGS[NUM_CFG] = {{32, 4, 1}, {64, 2, 1}, {128, 1, 1}, {12
 // 6 = 128 threads, 3 rows in flight; 7 = 128 threads, 4 rows; 8 = 256 threads, 3 rows.
 constexpr int NUM_STEP_CFG = 9;
 
+// Nine host planes in the reference layout: element (x, y) of direction q at p[q] + y * ld + x.
+// Page-locked and mapped into the device address space: the transfer code reads and writes them
+// in place over the host link.
+struct HostPlanes {
+    void *p[9];
+    int64_t ld;
+};
+
+// One launch (a "wave") of the pipelined upload -> steps -> download of bgk_advance_host.  The
+// interior rows are cut into bands of band_rows rows.  Wave w uploads band w, runs local step k
+// (1..nsteps) on band w - 2k for k in [k_lo, k_hi], and downloads band w - 2 nsteps - 1.  Step k
+// reads buffer (cur0 + k - 1) & 1.  Band b's step k thus runs after step k-1 on bands b-1, b and
+// b+1 (the rows it pulls from, and the rows whose pulls read the rows it overwrites), and the
+// bands of one wave are two apart, so no two items of a wave touch the same rows of a buffer.
+struct WaveArgs {
+    HostPlanes in, out;
+    int32_t band_rows, nbands, nsteps, cur0;
+    int32_t wave, k_lo, k_hi;
+    int32_t up_band, down_band;  // -1: none in this wave
+    int32_t xfer_rows;           // grid rows (blockIdx.y) given to each transfer of the wave
+};
+
 struct KernelTable {
     int vec;  // cells per 16-byte vector
     int elem_bytes;
@@ -47,6 +69,10 @@ struct KernelTable {
                           cudaStream_t st);
     cudaError_t (*vtk)(const Lattice &L, int cur, int phase, bool obs, float *u, float *w, float *rho, float *vort,
                        float *stream, float *phi, cudaStream_t st);
+    // all nine mapped host planes <-> state buffer cur, one launch per chunk of rows
+    cudaError_t (*xfer)(const Lattice &L, int cur, int phase, bool up, const HostPlanes &hp, bool obs, cudaStream_t st);
+    // one wave of bgk_advance_host: cdiv as in TileCfg (128 x 1 threads), grid_y grid rows
+    cudaError_t (*wave)(const Lattice &L, const WaveArgs &a, bool obs, int cdiv, int grid_y, cudaStream_t st);
 };
 
 KernelTable table_f32_f32();

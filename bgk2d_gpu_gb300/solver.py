@@ -176,6 +176,24 @@ class Solver:
             raise ValueError(f"populations have shape {a.shape}, expected {(9, self.ly + 2, self.lx + 2)}")
         self._check(self._L.bgk_upload(self._h, self._ptrs(a), self.lx + 2), "upload")
 
+    @staticmethod
+    def _host_ptrs(arr):
+        if hasattr(arr, "data_ptr"):  # torch tensor (page-locked when pinned)
+            return (ctypes.c_void_p * 9)(*[arr[q].data_ptr() for q in range(9)])
+        return (ctypes.c_void_p * 9)(*[arr[q].ctypes.data for q in range(9)])
+
+    def advance_host(self, src, dst, nsteps):
+        """bgk_advance_host: upload `src`, run nsteps steps, download into `dst`.  Both are host
+        arrays of shape (9, ly+2, ld), ld >= lx+2, numpy or torch (`dst` may be `src`); with
+        page-locked (torch pinned) arrays the transfers and the steps are pipelined."""
+        for a in (src, dst):
+            if tuple(a.shape[:2]) != (9, self.ly + 2) or a.shape[2] < self.lx + 2:
+                raise ValueError(f"host populations have shape {tuple(a.shape)}, expected (9, {self.ly + 2}, >= {self.lx + 2})")
+        if src.shape[2] != dst.shape[2]:
+            raise ValueError("src and dst must have the same leading dimension")
+        rc = self._L.bgk_advance_host(self._h, self._host_ptrs(src), self._host_ptrs(dst), int(src.shape[2]), int(nsteps))
+        self._check(rc, "advance_host")
+
     # -- reductions (FP64 on the device) ------------------------------------------------------
     def diagno(self, mode=0):
         """(<u>, <v>, <rho>, <|u|^2>) (SRC/diagno.F90:63-101).  mode 0: FP64 sums over all cells;

@@ -143,6 +143,16 @@ int bgk_destroy(bgk_handle *h);
 int bgk_upload(bgk_handle *h, void *const pops[9], int64_t ld);
 int bgk_download(bgk_handle *h, void *const pops[9], int64_t ld);
 
+/* Upload `in`, run nsteps time steps, download into `out`: the same result, bit for bit, as
+ * bgk_upload(in) + bgk_step(nsteps) + bgk_download(out), for a driver that keeps its populations
+ * on the host between chunks of steps (the SRC/bgk2d.F90:92-113 loop with host arrays updated
+ * at every diagnostic step).  `out` may be `in`.  With page-locked arrays, a ping-pong handle
+ * and no periodic y face, backward-facing step, LES or two-pass form, the transfers and the
+ * steps are pipelined: row bands go up, through the steps and back down in overlapping waves,
+ * so a run of up to 32 steps costs about one round trip over the host link (longer runs pipeline
+ * their first and last 16 steps).  Other cases run the three calls in sequence.  Synchronises. */
+int bgk_advance_host(bgk_handle *h, void *const in[9], void *const out[9], int64_t ld, int32_t nsteps);
+
 /* The reference's per-step call sequence.  bgk_boundaries and bgk_propagation record the
  * call order; the boundary rules and the streaming run inside the fused kernel launched by
  * bgk_collision (SRC/collision.F90:37-41 with FUSED).  Asynchronous. */
@@ -225,11 +235,13 @@ const char *bgk_version(void);
  * host array for out = <u>, <v>, <rho>, <|u|^2> (SRC/diagno.F90 per-cell arithmetic, FP64
  * sums).  The partial sums go to one static device array of 128 KiB that every GPU loading the
  * library holds until exit; lx*ly may be at most 16,777,216 (4096^2), larger domains return
- * BGK_E_TOOLARGE.  Nothing is allocated: no cudaMalloc/cudaFree, no pools.  The first call on
- * a device looks up the array's device address (cudaGetSymbolAddress), so make that first
- * call before any stream capture.  Runs on the legacy default stream and returns when the
- * means are on the host; the caller makes sure the arrays are ready.  All calls share the
- * array, so calls from several host threads are serialised by a process-wide lock. */
+ * BGK_E_TOOLARGE.  Nothing is allocated: no cudaMalloc/cudaFree, no pools.  Every call looks
+ * up the array's device address in the current context (cudaGetSymbolAddress); the first call
+ * on a device also loads the library's device code there, so make that first call before any
+ * stream capture.  Runs on the legacy default stream and returns when the means are on the
+ * host; the caller orders its own writes to the arrays before the call.  All calls share the
+ * array, so calls from several host threads are serialised by a process-wide lock.  When a
+ * sum is not finite the call returns BGK_E_NUMERIC and out holds the non-finite means. */
 int bgk_diagno_noalloc(const void *const pops[9], int64_t ld, int32_t lx, int32_t ly, int32_t storage,
                        double out[4]);
 

@@ -26,6 +26,8 @@ struct bgk_batch {
     int64_t launches = 0;
 };
 
+size_t g_fake_free_bytes = (size_t)64 << 30;  // what the fake cudaMemGetInfo reports as free
+
 namespace {
 std::mutex mu;
 int fail_storage = -1;
@@ -41,6 +43,13 @@ void fake_configure(int32_t storage_that_fails, double u0_that_blows_up)
     fail_storage = storage_that_fails;
     nan_u0 = u0_that_blows_up;
     live = max_live = created = 0;
+}
+
+// free device memory as the next cudaMemGetInfo sees it (another process taking or giving back HBM)
+void fake_set_free_bytes(int64_t bytes)
+{
+    std::lock_guard<std::mutex> g(mu);
+    g_fake_free_bytes = (size_t)bytes;
 }
 
 void fake_counts(int64_t out[3])

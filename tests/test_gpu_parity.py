@@ -230,6 +230,30 @@ def test_bfs_bit_exact(oracle_mod, bgk, prec, tile):
             assert bad.size == 0, f"{bad.size} populations differ after {n}"
 
 
+@pytest.mark.parametrize("tile", [2, 6])
+@pytest.mark.parametrize("prec", ["single", "double"])
+def test_bfs_fluid_cells_never_read_the_solid_block(oracle_mod, bgk, prec, tile):
+    """The poison check of the reference's allocation (SRC/alloca.F90:133-151 fills the second
+    buffer with huge()): here the whole solid block x < lx/20, y < ly/2 of the starting state
+    holds the largest finite value of the storage kind.  The fluid cells stay bit-identical to
+    the oracle's, which starts with zeros there, so no fluid update reads a block value."""
+    oprec, st, cp = PRECS[prec]
+    lx, ly = 200, 64
+    sx, sy = lx // 20, ly // 2
+    o = oracle_mod.Oracle(lx, ly, prec=oprec, tcase=oracle_mod.BFS, svisc=0.02, u0=0.1)
+    with bgk.Solver(lx, ly, tcase="BFS", svisc=0.02, u0=0.1, storage=st, compute=cp) as s:
+        s.set_tile(tile)
+        a = s.download()
+        a[:, 1:sy, 1:sx] = np.finfo(a.dtype).max
+        s.upload(a)
+        for n in (1, 2, 40):
+            s.step(n)
+            o.step(n)
+            got = s.download()
+            assert np.array_equal(_bfs_fluid(got, lx, ly), _bfs_fluid(o.raw(), lx, ly)), f"after {n} more steps"
+            assert not np.isfinite(got[:, 1:sy - 1, 1:sx - 1]).any()  # the block itself stays poisoned
+
+
 def test_bfs_rejects_aa_and_batches(bgk):
     from bgk2d_gpu_gb300 import _lib
     with pytest.raises(bgk.BgkError):

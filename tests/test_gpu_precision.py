@@ -67,3 +67,23 @@ def test_residual_decreases_to_steady_state(bgk):
     r2 = s.residual()
     assert 0 < r2 < r1 * 1e-2 and r2 < 1e-5
     s.close()
+
+
+@pytest.mark.parametrize("storage,bound", [("f16", 2e-3), ("bf16", 2e-2)])
+def test_tgv_decay_rate_16bit(bgk, storage, bound):
+    """The vortex mode of a 16-bit-storage run decays at the analytic rate nu (kx^2 + ky^2), with the
+    same projection and window as the FP64/FP32 test above.  The 0.1% bar of that test is not met
+    in 16 bits: FP16 measured 1.46e-3 (its velocity L2 error against FP64 is 5.7e-4 here, and the
+    amplitude decays by 15% over the window); BF16 keeps 8 significant bits."""
+    s = tgv(bgk, storage)
+    _, ui, vi = s.fields()
+    t = int(round(18 * N * np.sqrt(3) / 2))
+    s.step(t)
+    _, u, v = s.fields()
+    amp = np.sum(u * ui + v * vi) / np.sum(ui * ui + vi * vi)
+    rate = -np.log(amp) / t
+    k2 = 2 * (2 * np.pi / N) ** 2
+    err = abs(rate / (NU * k2) - 1)
+    print(f"{storage}: decay rate {rate:.6e}, analytic {NU * k2:.6e}, relative error {err:.2e}")
+    assert err < bound
+    s.close()

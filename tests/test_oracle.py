@@ -11,7 +11,12 @@ import os
 import numpy as np
 import pytest
 
-GHIA = "/root/reference/TEST/DrivenCavity/ghia.y.dat"
+# The reference tree (for its third-party Ghia tables, read in place and never copied): the
+# directory named by BGK2D_REFERENCE_ROOT.  The checks that need it are skipped without it.
+REF_ROOT = os.environ.get("BGK2D_REFERENCE_ROOT", "")
+GHIA_Y = os.path.join(REF_ROOT, "TEST", "DrivenCavity", "ghia.y.dat")
+GHIA_X = os.path.join(REF_ROOT, "TEST", "DrivenCavity", "ghia.x.dat")
+HAVE_GHIA = bool(REF_ROOT) and os.path.exists(GHIA_Y) and os.path.exists(GHIA_X)
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
 
@@ -118,17 +123,41 @@ def test_poiseuille_profile_and_energy(oracle_mod):
     assert abs(e / (8 * u0 ** 2 / 15) - 1) < 5e-3
 
 
-@pytest.mark.skipif(not os.path.exists(GHIA), reason="reference tree not mounted")
+def _ghia_errors(o, n, col):
+    """Largest |u/U - Ghia| on the vertical centre line (prof_j at x = n/2, SRC/prof_j.F90) and
+    |v/U - Ghia| on the horizontal one (row y = n/2, SRC/prof_i.F90), at the table's stations
+    (walls excluded), for the Reynolds-number column `col` of ghia.{y,x}.dat."""
+    gy, gx = np.loadtxt(GHIA_Y), np.loadtxt(GHIA_X)
+    u, _, _ = o.prof_j(n // 2)
+    _, _, v = o.fields()
+    pos = (np.arange(1, n + 1) - 0.5) / n
+    eu = np.max(np.abs(np.interp(gy[1:-1, 0], pos, u / 0.1) - gy[1:-1, col]))
+    ev = np.max(np.abs(np.interp(gx[1:-1, 0], pos, v[n // 2 - 1, :] / 0.1) - gx[1:-1, col]))
+    return eu, ev
+
+
+@pytest.mark.skipif(not HAVE_GHIA, reason="BGK2D_REFERENCE_ROOT does not name the reference tree")
 def test_ldc_re100_against_ghia(oracle_mod):
-    """TEST/DrivenCavity/plot.R00100.gnu: u(y)/U at x = l/2 against ghia.y.dat (read in place)."""
+    """TEST/DrivenCavity/plot.R00100.gnu: u(y)/U on x = l/2 against ghia.y.dat and v(x)/U on
+    y = m/2 against ghia.x.dat (read in place), Re = 100 on 128^2 (measured 0.0029 and 0.0018)."""
     O = oracle_mod
-    g = np.loadtxt(GHIA)
     o = O.Oracle(128, 128, prec=O.DOUBLE, tcase=O.LDC, svisc=0.128, u0=0.1)
     o.step(50000, threads=8)
-    u, v, d = o.prof_j(64)
-    y = (np.arange(1, 129) - 0.5) / 128
-    ui = np.interp(g[1:-1, 0], y, u / 0.1)
-    assert np.max(np.abs(ui - g[1:-1, 1])) < 5e-3
+    eu, ev = _ghia_errors(o, 128, 1)
+    assert eu < 5e-3 and ev < 5e-3, (eu, ev)
+
+
+@pytest.mark.skipif(not HAVE_GHIA, reason="BGK2D_REFERENCE_ROOT does not name the reference tree")
+def test_ldc_re1000_against_ghia(oracle_mod):
+    """TEST/DrivenCavity/plot.R01000.gnu: the Re = 1000 cavity (SINGLE, as the reference's
+    multicore run of UTIL/bgk.512.R1000.input) against the Re = 1000 columns of ghia.{y,x}.dat.
+    On 256^2 rather than the reference's 512^2 so that the oracle reaches the steady state in
+    seconds (120000 steps); measured 0.0056 (u) and 0.0052 (v) of the lid speed."""
+    O = oracle_mod
+    o = O.Oracle(256, 256, prec=O.SINGLE, tcase=O.LDC, svisc=0.0256, u0=0.1)
+    o.step(120000, threads=8)
+    eu, ev = _ghia_errors(o, 256, 2)
+    assert eu < 1e-2 and ev < 1e-2, (eu, ev)
 
 
 def test_reference_profile_fixture(oracle_mod):

@@ -40,6 +40,7 @@ def srvlib(tmp_path_factory):
         "bgk_server_get_stats": [VP, P(_lib.ServerStats)],
         "fake_configure": [I32, F64],
         "fake_counts": [P(I64)],
+        "fake_set_free_bytes": [I64],
     }.items():
         getattr(L, name).argtypes = args
         getattr(L, name).restype = I32 if name.startswith("bgk_") else None
@@ -192,3 +193,24 @@ def test_scheduler_has_no_data_races(tmp_path):
         pytest.skip("ThreadSanitizer cannot run on this kernel's memory layout")
     assert "WARNING: ThreadSanitizer" not in r.stderr, r.stderr[:4000]
     assert r.returncode == 0, (r.stdout, r.stderr[:2000])
+
+
+def test_admission_sees_memory_taken_after_creation(srvlib):
+    """Free HBM is read again at every admission: while another process holds the memory (the
+    fake's cudaMemGetInfo reports less than a request needs beyond the 4 GiB headroom), a request
+    that fits the budget waits in the queue; once the memory is back it is admitted and runs."""
+    import time
+    L, _ = srvlib
+    s = Srv(srvlib, max_slots=64)
+    need = request_bytes(256)
+    try:
+        L.fake_set_free_bytes((4 << 30) + need // 2)
+        a = s.submit(n=256, max_steps=300)
+        time.sleep(0.2)
+        assert s.counts()[2] == 0  # nothing created: it does not fit in what is free now
+        L.fake_set_free_bytes(64 << 30)
+        res, st = s.finish()
+        assert res[a].status == OK and res[a].steps == 300 and st.completed == 1
+    finally:
+        L.fake_set_free_bytes(64 << 30)
+        s.close()

@@ -95,3 +95,46 @@ def test_initial_state(hostlib, oracle_mod, prec, tcase, vortex):
     assert np.array_equal(got.view(itype), want.view(itype))  # bit for bit, signs of zero included
     if vortex:
         assert np.abs(want).max() > 0
+
+
+MASK_CASES = [  # l, m, shape (1 circle, 2 square, 3 half circle), radius, centre (-1: 2l/5, m/2)
+    (160, 62, 1, 6, (-1, -1)), (200, 90, 1, 16, (-1, -1)), (97, 61, 1, 11, (40, 30)), (64, 64, 1, 1, (5, 60)),
+    (64, 48, 1, 9, (11, 38)), (120, 80, 2, 7, (-1, -1)), (50, 40, 2, 4, (45, 6)), (128, 96, 3, 13, (-1, -1)),
+    (80, 64, 3, 20, (30, 20)),
+]
+
+
+@pytest.mark.parametrize("case", MASK_CASES)
+def test_obstacle_mask_against_direct_formula(hostlib, case):
+    """The obstacle builder against the shape written directly as array expressions over the grid
+    (SRC/build.obs.F90:49-80 square |i - ic|, |j - jc| <= r; 81-116 half circle from row m/2;
+    174-205 circle (ic - i)^2 + (jc - j)^2 <= r^2 with integer i, j, ic, jc and R = radius),
+    sharing no code with either builder; the bounding box and count follow from the mask.  Boxes
+    one cell from the walls are the closest the product accepts (a mask touching row or column 1
+    or the last one is rejected)."""
+    l, m, shape, r, (ic, jc) = case
+    _, mask, bb = product_setup(hostlib, l, m, LDC, 0.05, 0.1, SINGLE, shape, r, (ic, jc))
+    ic = 2 * l // 5 if ic < 0 else ic
+    jc = m // 2 if jc < 0 else jc
+    J, I = np.mgrid[1:m + 1, 1:l + 1]
+    if shape == 2:
+        want = (np.abs(I - ic) <= r) & (np.abs(J - jc) <= r)
+    else:
+        want = (ic - I) ** 2 + (jc - J) ** 2 <= r * r
+        if shape == 3:
+            want &= J >= m // 2
+    assert np.array_equal(mask.astype(bool), want)
+    jj, ii = np.nonzero(want)
+    assert bb.tolist() == [ii.min() + 1, ii.max() + 1, jj.min() + 1, jj.max() + 1, int(want.sum())]
+
+
+@pytest.mark.parametrize("r", [1, 2, 3, 6, 10, 16, 25])
+def test_circle_count_is_the_lattice_point_count(hostlib, r):
+    """A circle away from the walls covers exactly the lattice points with dx^2 + dy^2 <= r^2:
+    sum over dy of 2 isqrt(r^2 - dy^2) + 1 (5, 13, 29, 113, 317, 797, 1961 for the radii here)."""
+    import math
+    n = 2 * r + 9
+    _, mask, bb = product_setup(hostlib, n, n, LDC, 0.05, 0.1, DOUBLE, 1, r, (n // 2, n // 2))
+    count = sum(2 * math.isqrt(r * r - dy * dy) + 1 for dy in range(-r, r + 1))
+    assert int(mask.sum()) == count == bb[4]
+    assert bb.tolist()[:4] == [n // 2 - r, n // 2 + r, n // 2 - r, n // 2 + r]

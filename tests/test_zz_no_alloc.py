@@ -52,3 +52,26 @@ def test_noalloc_diagno_rejects_too_large_and_bad_arguments(bgk):
     assert rc == _lib.E_INVALID
     rc = L.bgk_diagno_noalloc(fake, 66, 64, 64, 2, out.ctypes.data_as(P))  # 16-bit storage not accepted
     assert rc == _lib.E_INVALID
+
+
+@pytest.mark.parametrize("lx,ly,pad", [(130, 67, 9), (1024, 1024, 0), (1000, 1000, 37)])
+def test_noalloc_diagno_padded_rows_and_many_chunks(bgk, lx, ly, pad):
+    """Rows longer than lx + 2 (a padded leading dimension, as ipad gives) and domains of a few
+    hundred chunks, against bgk_diagno, on two calls in a row."""
+    torch = pytest.importorskip("torch")
+    from bgk2d_gpu_gb300 import _lib
+    L = _lib.load()
+    ld = lx + 2 + pad
+    with bgk.Solver(lx, ly, tcase="LDC", svisc=0.05, u0=0.1) as s:
+        s.step(60)
+        want = s.diagno()
+        pops = s.download()
+    dev = torch.full((9, ly + 2, ld), 1e30, dtype=torch.float32, device="cuda")  # padding never read
+    dev[:, :, :lx + 2] = torch.from_numpy(pops).cuda()
+    torch.cuda.synchronize()
+    ptrs = (ctypes.c_void_p * 9)(*[dev[q].data_ptr() for q in range(9)])
+    for call in range(2):
+        out = np.zeros(4)
+        rc = L.bgk_diagno_noalloc(ptrs, ld, lx, ly, 0, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        assert rc == 0, (call, rc)
+        np.testing.assert_allclose(out, want, rtol=1e-12, atol=1e-15)
