@@ -225,7 +225,7 @@ def run_profile(args):
     `--steps` device-timed steps; prints one tag line with the time per step."""
     import bgk2d_gpu_gb300 as bgk
     scheme, storage = args.profile.split("_")
-    compute = "f64" if storage == "f64" else "f32"
+    compute = args.compute or ("f64" if storage == "f64" else "f32")
     if scheme == "batch":  # the first --cases cavities of the 96-cavity batch, one launch per step
         cases = cfg3_cases()[:args.cases]
         cells = sum(n * n for n, _, _ in cases)
@@ -255,7 +255,7 @@ def run_profile(args):
         s.sync()
         ms = s.step_timed(args.steps)
     per = ms / args.steps
-    print(f"profile run {args.profile}{'_les' if args.les else ''} {args.size}^2 tile={args.tile} prefetch={args.prefetch} "
+    print(f"profile run {args.profile}{'_les' if args.les else ''} compute={compute} {args.size}^2 tile={args.tile} prefetch={args.prefetch} "
           f"warmup={args.warmup} steps={args.steps} "
           f"ms/step={per:.4f} GLUPS={args.size * args.size / (per * 1e-3) / 1e9:.2f}")
     return 0
@@ -516,6 +516,7 @@ def main():
     ap.add_argument("--tile", type=int, default=-1, help="tile configuration for --profile")
     ap.add_argument("--prefetch", type=int, default=0, help="L2 prefetch distance in blocks for --profile")
     ap.add_argument("--les", action="store_true", help="Smagorinsky collision for --profile")
+    ap.add_argument("--compute", default=None, help="collision kind for --profile (f64 with f32 storage: MIXED2)")
     ap.add_argument("--cases", type=int, default=24, help="cavities of the batch for --profile batch_<storage>")
     args = ap.parse_args()
     if args.warmup < 3:

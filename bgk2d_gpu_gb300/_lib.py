@@ -144,6 +144,7 @@ def load(build_if_missing: bool = True):
         "bgk_server_fields": (I32, [VP, I64, P(F64), P(F64), P(F64), I64]),
         "bgk_server_get_stats": (I32, [VP, P(ServerStats)]),
         "bgk_diagno_noalloc": (I32, [P(VP), I64, I32, I32, I32, P(F64)]),
+        "bgk_peak_fp64": (I32, [I32, P(F64)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

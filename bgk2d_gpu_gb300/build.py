@@ -23,6 +23,7 @@ SOURCES = {
     "bgk_api.cu": ["-fmad=false"],
     "bgk_batch.cu": ["-fmad=false"],
     "bgk_noalloc.cu": ["-fmad=false"],
+    "bgk_peaks.cu": ["-fmad=false"],
     "bgk_inst_f32_f32.cu": ["-fmad=false"],
     "bgk_inst_f32_f64.cu": ["-fmad=false"],
     "bgk_inst_f64_f64.cu": ["-fmad=false"],

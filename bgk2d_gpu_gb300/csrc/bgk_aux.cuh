@@ -209,6 +209,34 @@ __global__ void __launch_bounds__(128, (N * sizeof(S) <= 8 || (sizeof(S) == 4 &&
         }
         by -= a.xfer_rows;
     }
+    if (a.zero_band >= 0) {
+        if (by == 0) {
+            // ghost cells of the band in the final buffer: columns 0 and lx+1 of its rows, and
+            // the whole ghost row beside the first and the last band (the values a download
+            // writes for them)
+            int ya, yb;
+            band_rows(L, a, a.zero_band, ya, yb);
+            S *base = reinterpret_cast<S *>(L.planes) + (((a.cur0 + a.nsteps) & 1) ? 9 : 0) * L.plane_elems;
+            const int w = L.lx + 2, rows = yb - ya + 1;
+            const int per_plane = 2 * rows + (ya == 0 ? w : 0) + (yb == L.ly + 1 ? w : 0);
+            for (int t = (int)(blockIdx.x * blockDim.x + threadIdx.x); t < 9 * per_plane; t += (int)(gridDim.x * blockDim.x)) {
+                const int q = t / per_plane;
+                int r = t - q * per_plane, x, y;
+                if (r < 2 * rows) {
+                    y = ya + r / 2;
+                    x = (r & 1) ? L.lx + 1 : 0;
+                } else {
+                    r -= 2 * rows;
+                    const bool first = ya == 0 && r < w;
+                    y = first ? 0 : L.ly + 1;
+                    x = first ? r : r - (ya == 0 ? w : 0);
+                }
+                base[q * L.plane_elems + cell_index<S>(L, x, y)] = S(0.0f);
+            }
+            return;
+        }
+        by -= 1;
+    }
     const int k = a.k_lo + by / a.band_rows;
     const int y = (a.wave - 2 * k) * a.band_rows + by % a.band_rows + 1;
     if (y > L.ly) return;
@@ -238,7 +266,7 @@ __global__ void aa_fill_outflow_kernel(Lattice L)
 // sequential loops do, so one block runs the four loops in order.  The step kernel then pulls
 // these stored values (faces of kind FK_STORED).  Inflow values come from L.inflow.
 template <typename S, typename K>
-__global__ void bfs_bcond_kernel(const Lattice L, const int cur, const int stepx, const int stepy)
+__device__ __forceinline__ void bfs_bcond_block(const Lattice &L, const int cur, const int stepx, const int stepy)
 {
     const int64_t pe = L.plane_elems;
     S *a = reinterpret_cast<S *>(L.planes) + (cur ? 9 : 0) * pe;
@@ -277,6 +305,22 @@ __global__ void bfs_bcond_kernel(const Lattice L, const int cur, const int stepx
         at(D01, stepx - 1, j + 1) = at(D12, stepx, j);
         at(D05, stepx - 1, j) = at(D14, stepx, j);
     }
+}
+
+template <typename S, typename K>
+__global__ void bfs_bcond_kernel(const Lattice L, const int cur, const int stepx, const int stepy)
+{
+    bfs_bcond_block<S, K>(L, cur, stepx, stepy);
+}
+
+// the same boundary routine for the backward-facing-step members of a batch, one block each:
+// entry = (member, stepx, stepy, -), source buffer cur[member] ^ parity
+template <typename S, typename K>
+__global__ void batch_bfs_kernel(const Lattice *__restrict__ lats, const int *__restrict__ cur,
+                                 const int4 *__restrict__ members, const int parity)
+{
+    const int4 e = members[blockIdx.x];
+    bfs_bcond_block<S, K>(lats[e.x], cur[e.x] ^ parity, e.y, e.z);
 }
 
 // moments with the reference's per-cell arithmetic (SRC/diagno.F90:82-93)

@@ -169,6 +169,13 @@ cudaError_t bcond_step(const Lattice &L, int cur, int stepx, int stepy, cudaStre
     return cudaGetLastError();
 }
 
+template <typename S, typename K>
+cudaError_t batch_bfs(const Lattice *lats, const int *cur, const int4 *members, int n, int parity, cudaStream_t st)
+{
+    batch_bfs_kernel<S, K><<<n, 1024, 0, st>>>(lats, cur, members, parity);
+    return cudaGetLastError();
+}
+
 template <typename S>
 cudaError_t init_tgv(const Lattice &L, double u0, cudaStream_t st)
 {
@@ -282,6 +289,7 @@ KernelTable make_table()
     t.gather = &gather<S, K>;
     t.fill_outflow = &fill_outflow<S, K>;
     t.bcond_step = &bcond_step<S, K>;
+    t.batch_bfs = &batch_bfs<S, K>;
     t.init_tgv = &init_tgv<S>;
     t.diagno = &diagno<S, K>;
     t.diagno_seq = &diagno_seq<S, K>;

@@ -41,8 +41,11 @@ struct WaveArgs {
     HostPlanes in, out;
     int32_t band_rows, nbands, nsteps, cur0;
     int32_t wave, k_lo, k_hi;
-    int32_t up_band, down_band;  // -1: none in this wave
+    int32_t up_band, down_band;  // -1: none in this wave (transfers by the wave's own blocks)
     int32_t xfer_rows;           // grid rows (blockIdx.y) given to each transfer of the wave
+    int32_t zero_band;           // -1 or the band whose ghost cells in buffer (cur0 + nsteps) & 1
+                                 // this wave sets to zero (after step nsteps on it, before a copy
+                                 // engine downloads it)
 };
 
 struct KernelTable {
@@ -53,6 +56,9 @@ struct KernelTable {
     cudaError_t (*gather)(const Lattice &L, int cur, int phase, int q, void *dst, int64_t ld, bool obs, cudaStream_t st);
     cudaError_t (*fill_outflow)(const Lattice &L, cudaStream_t st);
     cudaError_t (*bcond_step)(const Lattice &L, int cur, int stepx, int stepy, cudaStream_t st);
+    // the backward-facing-step boundary routine of n batch members (entries member, stepx, stepy)
+    cudaError_t (*batch_bfs)(const Lattice *lats, const int *cur, const int4 *members, int n, int parity,
+                             cudaStream_t st);
     cudaError_t (*init_tgv)(const Lattice &L, double u0, cudaStream_t st);
     cudaError_t (*diagno)(const Lattice &L, int cur, int phase, int fluid_only, bool obs, double *partial, int nb,
                           cudaStream_t st);

@@ -223,6 +223,12 @@ int bgk_tune(bgk_handle *h, int32_t trial_steps, int32_t *tile_cfg, int32_t *ste
 int bgk_footprint(bgk_handle *h, int64_t *device_bytes, int32_t *bytes_per_cell);
 /* number of kernels this library launched on the handle so far */
 int bgk_launch_count(bgk_handle *h, int64_t *launches);
+
+/* Measured FP64 instruction rates of a device: out = DFMA, DADD and DMUL thread operations per
+ * second, from independent chains of each on every SM (CUDA events, best of five).  GB300 runs
+ * FP64 at a small fraction of its FP32 rate, so this, not HBM, bounds the DOUBLE and MIXED2
+ * steps.  No counterpart in the reference (a measurement helper).  Synchronises. */
+int bgk_peak_fp64(int32_t device, double out[3]);
 int bgk_last_error(bgk_handle *h, char *buf, size_t len);
 const char *bgk_version(void);
 

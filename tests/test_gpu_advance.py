@@ -75,13 +75,39 @@ def test_advance_aa_takes_the_sequential_path(bgk):
     _run(bgk, torch, "ldc", "f32", 64, 40, 9, scheme="aa")
 
 
+@pytest.mark.parametrize("ce", ["0", "1", "2", "3"])
 @pytest.mark.parametrize("rows", ["1", "3", "16"])
-def test_advance_band_heights_padding_and_alias(bgk, rows, monkeypatch):
+def test_advance_band_heights_padding_and_alias(bgk, rows, ce, monkeypatch):
+    """Bands moved by the waves' own blocks (ce=0, and always for 16-bit storage) or by the copy
+    engines (bit 0 uploads, bit 1 downloads; FP32/FP64 storage with evenly spaced host planes)."""
     torch = pytest.importorskip("torch")
     monkeypatch.setenv("BGK_PIPE_ROWS", rows)
     monkeypatch.setenv("BGK_PIPE_XFER", "3")
+    monkeypatch.setenv("BGK_PIPE_CE", ce)
     _run(bgk, torch, "ldc", "f32", 130, 67, 12, pad=5)
+    _run(bgk, torch, "vks", "f64", 150, 45, 7, alias=True)
     _run(bgk, torch, "vks", "f16", 200, 61, 40, alias=True)
+
+
+def test_advance_unevenly_spaced_planes(bgk):
+    """Nine separate page-locked planes (not one allocation): the in-kernel transfers take them."""
+    torch = pytest.importorskip("torch")
+    lx, ly, K = 90, 52, 9
+    kw = dict(tcase="LDC", svisc=0.05, u0=0.1)
+    with bgk.Solver(lx, ly, **kw) as a, bgk.Solver(lx, ly, **kw) as b:
+        a.step(5)
+        start = a.download()
+        b.upload(start)
+        b.step(K)
+        want = b.download()
+        src = [torch.from_numpy(start[q].copy()).pin_memory() for q in range(9)]
+        dst = [torch.zeros((ly + 2, lx + 2), dtype=torch.float32).pin_memory() for _ in range(9)]
+        import ctypes
+        pin = (ctypes.c_void_p * 9)(*[t.data_ptr() for t in src])
+        pout = (ctypes.c_void_p * 9)(*[t.data_ptr() for t in dst])
+        assert a._L.bgk_advance_host(a._h, pin, pout, lx + 2, K) == 0
+        got = np.stack([t.numpy() for t in dst])
+        assert np.array_equal(got, want)
 
 
 def test_advance_pageable_arrays(bgk):
