@@ -1051,8 +1051,11 @@ int bgk_tune(bgk_handle *h, int32_t trial_steps, int32_t *tile_cfg, int32_t *ste
     // tried, so the populations of a tuned run do not depend on which of them wins.
     const bool aa16 = h->L.scheme == BGK_SCHEME_AA && h->T.elem_bytes == 2;
     // A handle with the Smagorinsky collision runs one kernel shape whatever the tile
-    // configuration: only the prefetch distance is tried.
-    const int c0 = h->L.les ? h->cfg : aa16 ? 4 : 0, c1 = h->L.les ? h->cfg + 1 : ncfg;
+    // configuration, except 16-bit ping-pong, whose configurations 0-3 are register budgets of
+    // its LES kernel; otherwise only the prefetch distance is tried.
+    const bool les16 = h->L.les && h->T.elem_bytes == 2 && h->L.scheme == BGK_SCHEME_PINGPONG && !h->two_pass;
+    const int c0 = les16 ? 0 : h->L.les ? h->cfg : aa16 ? 4 : 0;
+    const int c1 = les16 ? 4 : h->L.les ? h->cfg + 1 : ncfg;
     for (int c = c0; c < c1; ++c) {
         const int npf = c < NUM_CFG ? 3 : 1;
         for (int p = 0; p < npf; ++p) {

@@ -57,10 +57,27 @@ cudaError_t step_staged(const Lattice &L, int parity, cudaStream_t st)
 
 // steps with the Smagorinsky collision: their own instantiation (128 x 1 threads, a whole vector
 // per thread), so that the eddy-viscosity code takes no registers from the plain kernels
+template <typename S, typename K, bool OBS, int N, int MINB>
+cudaError_t les16_launch(const Lattice &L, int parity, cudaStream_t st)
+{
+    const int nv = (L.lx + N - 1) / N;
+    pp_les_kernel<S, K, OBS, N, MINB><<<dim3((unsigned)((nv + 127) / 128), (unsigned)L.ly), 128, 0, st>>>(L, parity);
+    return cudaGetLastError();
+}
+
 template <typename S, typename K, bool OBS>
-cudaError_t step_les(int kind, const Lattice &L, int parity, cudaStream_t st)
+cudaError_t step_les(int kind, const Lattice &L, int parity, int cfg, cudaStream_t st)
 {
     const dim3 block(128, 1);
+    // 16-bit ping-pong: register budgets tried by the autotuner (tile configuration 0-3): 4 cells
+    // per thread at 8 blocks per SM (64 registers) or 6 (80); 8 cells at 4 (128) or 3 (168)
+    if constexpr (Is16<S>::value) {
+        if (kind == STEP_PP && cfg >= 1 && cfg <= 3) {
+            if (cfg == 1) return les16_launch<S, K, OBS, vec_of<S>() / 2, 6>(L, parity, st);
+            if (cfg == 2) return les16_launch<S, K, OBS, vec_of<S>(), 4>(L, parity, st);
+            return les16_launch<S, K, OBS, vec_of<S>(), 3>(L, parity, st);
+        }
+    }
     // 16-bit kinds: 8 bytes per thread and plane (64 registers, 8 blocks per SM), the fastest shape
     // of their non-LES step; the 32/64-bit kinds: 16 bytes
     constexpr int N = Is16<S>::value ? vec_of<S>() / 2 : vec_of<S>();
@@ -77,7 +94,7 @@ cudaError_t step_les(int kind, const Lattice &L, int parity, cudaStream_t st)
 template <typename S, typename K, bool OBS>
 cudaError_t step_obs(int kind, const Lattice &L, int parity, int cfg, cudaStream_t st)
 {
-    if (L.les) return step_les<S, K, OBS>(kind, L, parity, st);
+    if (L.les) return step_les<S, K, OBS>(kind, L, parity, cfg, st);
     if (kind == STEP_PP && cfg >= NUM_CFG) {
         if (cfg == 6) return step_staged<S, K, 128, 3, OBS>(L, parity, st);
         if (cfg == 7) return step_staged<S, K, 128, 4, OBS>(L, parity, st);

@@ -28,7 +28,6 @@
 #pragma once
 
 #include "bgk_common.cuh"
-#include "bgk_softfp64.h"
 
 namespace bgk {
 
@@ -66,52 +65,7 @@ __device__ __forceinline__ K add_zero(K y)
     }
 }
 
-// FP64 addition, subtraction and multiplication on the integer pipes (SOFT) or on the FP64 pipe.
-// The integer form gives the IEEE result for normal operands and results and for zeros (see
-// bgk_softfp64.h); a lane with another case (subnormal, infinite, NaN, overflow) takes the
-// hardware instruction, behind a warp vote so that warps without such a lane skip it.
-template <bool SOFT>
-__device__ __forceinline__ double d_add(double a, double b)
-{
-    if constexpr (!SOFT) {
-        return a + b;
-    } else {
-        uint64_t r;
-        const bool ok = sfp::add((uint64_t)__double_as_longlong(a), (uint64_t)__double_as_longlong(b), &r);
-        double v = __longlong_as_double((long long)r);
-        if (__any_sync(__activemask(), !ok)) {
-            if (!ok) v = __dadd_rn(a, b);
-        }
-        return v;
-    }
-}
-template <bool SOFT> __device__ __forceinline__ double d_sub(double a, double b) { return d_add<SOFT>(a, -b); }  // a - b = a + (-b), zeros included
-template <bool SOFT>
-__device__ __forceinline__ double d_mul(double a, double b)
-{
-    if constexpr (!SOFT) {
-        return a * b;
-    } else {
-        uint64_t r;
-        const bool ok = sfp::mul((uint64_t)__double_as_longlong(a), (uint64_t)__double_as_longlong(b), &r);
-        double v = __longlong_as_double((long long)r);
-        if (__any_sync(__activemask(), !ok)) {
-            if (!ok) v = __dmul_rn(a, b);
-        }
-        return v;
-    }
-}
-
-// Groups of the FP64 collision's operations that run on the integer pipes (bit g set: group g),
-// chosen by timing the collision alone with each split: the FP64 pipe and the integer pipes then
-// share the work.  0: rho, 1: velocities, 2: squares and sums of velocities, 3: the quadratic
-// equilibrium terms, 4: scaled velocities and rho * weights, 5: equilibria, 6: relaxation.
-#ifndef BGK_F64_SOFT
-#define BGK_F64_SOFT 0u
-#endif
-constexpr unsigned F64_SOFT = BGK_F64_SOFT;
-
-template <typename K, bool LES = false, unsigned SOFT = F64_SOFT>
+template <typename K, bool LES = false>
 __device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced, K cte_s = (K)0)
 {
     const K uno = (K)1, cte1 = (K)1;  // cte0 = uno - cte1 = +0: cte0 + z is add_zero(z)
@@ -119,64 +73,6 @@ __device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced
     const K p0 = (K)(4.0 / 9.0), p1 = (K)(1.0 / 9.0), p2 = (K)(1.0 / 36.0);
     K x01 = x[0], x03 = x[1], x05 = x[2], x08 = x[3], x10 = x[4];
     K x12 = x[5], x14 = x[6], x17 = x[7], x19 = x[8];
-    if constexpr (sizeof(K) == 8 && !LES && SOFT != 0u) {
-        // the same expression tree, each operation on the pipe its group is given to
-        constexpr bool G0 = SOFT & 1u, G1 = SOFT & 2u, G2 = SOFT & 4u, G3 = SOFT & 8u, G4 = SOFT & 16u,
-                       G5 = SOFT & 32u, G6 = SOFT & 64u;
-        const K rho = d_add<G0>(d_add<G0>(d_add<G0>(d_add<G0>(d_add<G0>(x01, x03), x10), x12),
-                                          d_add<G0>(d_add<G0>(d_add<G0>(x05, x08), x14), x17)), x19);
-        const K rho1 = d_add<G0>(rho, cte1);
-        const K rhoinv = uno / rho1;
-        K vx = d_mul<G1>(d_add<G1>(d_add<G1>(d_sub<G1>(x03, x12), d_sub<G1>(x01, x10)), d_sub<G1>(x05, x14)), rhoinv);
-        K vy = d_mul<G1>(d_add<G1>(d_add<G1>(d_sub<G1>(x03, x01), d_sub<G1>(x12, x10)), d_sub<G1>(x08, x17)), rhoinv);
-        const K vx2 = d_mul<G2>(vx, vx), vy2 = d_mul<G2>(vy, vy);
-        const K vsq = d_add<G2>(vx2, vy2);
-        K vxpy = d_add<G2>(vx, vy), vxmy = d_sub<G2>(vx, vy);
-        const K qxpy = add_zero(d_mul<G3>(qf, d_sub<G3>(d_mul<G3>(d_mul<G3>(tre, vxpy), vxpy), vsq)));
-        const K qxmy = add_zero(d_mul<G3>(qf, d_sub<G3>(d_mul<G3>(d_mul<G3>(tre, vxmy), vxmy), vsq)));
-        const K qx = add_zero(d_mul<G3>(qf, d_sub<G3>(d_mul<G3>(tre, vx2), vsq)));
-        const K qy = add_zero(d_mul<G3>(qf, d_sub<G3>(d_mul<G3>(tre, vy2), vsq)));
-        const K q0 = add_zero(d_mul<G3>(qf, -vsq));
-        vx = d_mul<G4>(rf, vx);
-        vy = d_mul<G4>(rf, vy);
-        vxpy = d_mul<G4>(rf, vxpy);
-        vxmy = d_mul<G4>(rf, vxmy);
-        const K rp0 = d_mul<G4>(rho1, p0), rp1 = d_mul<G4>(rho1, p1), rp2 = d_mul<G4>(rho1, p2);
-        // cte1 * z is z (a product by one is exact)
-        const K c0 = d_sub<G5>(rp0, p0), c1 = d_sub<G5>(rp1, p1), c2 = d_sub<G5>(rp2, p2);
-        const K e01 = d_add<G5>(d_mul<G5>(rp2, d_add<G5>(vxmy, qxmy)), c2);
-        const K e03 = d_add<G5>(d_mul<G5>(rp2, d_add<G5>(vxpy, qxpy)), c2);
-        const K e05 = d_add<G5>(d_mul<G5>(rp1, d_add<G5>(vx, qx)), c1);
-        const K e08 = d_add<G5>(d_mul<G5>(rp1, d_add<G5>(vy, qy)), c1);
-        const K e10 = d_add<G5>(d_mul<G5>(rp2, d_add<G5>(-vxpy, qxpy)), c2);
-        const K e12 = d_add<G5>(d_mul<G5>(rp2, d_add<G5>(-vxmy, qxmy)), c2);
-        const K e14 = d_add<G5>(d_mul<G5>(rp1, d_add<G5>(-vx, qx)), c1);
-        const K e17 = d_add<G5>(d_mul<G5>(rp1, d_add<G5>(-vy, qy)), c1);
-        const K e19 = d_add<G5>(d_mul<G5>(rp0, q0), c0);
-        if (forced) {
-            const K fx = fgrad * rho1, fy = (K)0;
-            x[0] = (x01 - omega * (x01 - e01)) + (fx - fy);
-            x[1] = (x03 - omega * (x03 - e03)) + (fx + fy);
-            x[2] = (x05 - omega * (x05 - e05)) + (fx);
-            x[3] = (x08 - omega * (x08 - e08)) + (fy);
-            x[4] = (x10 - omega * (x10 - e10)) + ((-fx) - fy);
-            x[5] = (x12 - omega * (x12 - e12)) + ((-fx) + fy);
-            x[6] = (x14 - omega * (x14 - e14)) + (-fx);
-            x[7] = (x17 - omega * (x17 - e17)) + (-fy);
-        } else {
-            // fx = fy = +0: the force terms are +0 for 01, 03, 05, 08, 12 and -0 for 10, 14, 17
-            x[0] = add_zero(d_sub<G6>(x01, d_mul<G6>(omega, d_sub<G6>(x01, e01))));
-            x[1] = add_zero(d_sub<G6>(x03, d_mul<G6>(omega, d_sub<G6>(x03, e03))));
-            x[2] = add_zero(d_sub<G6>(x05, d_mul<G6>(omega, d_sub<G6>(x05, e05))));
-            x[3] = add_zero(d_sub<G6>(x08, d_mul<G6>(omega, d_sub<G6>(x08, e08))));
-            x[4] = d_sub<G6>(x10, d_mul<G6>(omega, d_sub<G6>(x10, e10)));
-            x[5] = add_zero(d_sub<G6>(x12, d_mul<G6>(omega, d_sub<G6>(x12, e12))));
-            x[6] = d_sub<G6>(x14, d_mul<G6>(omega, d_sub<G6>(x14, e14)));
-            x[7] = d_sub<G6>(x17, d_mul<G6>(omega, d_sub<G6>(x17, e17)));
-        }
-        x[8] = d_sub<G6>(x19, d_mul<G6>(omega, d_sub<G6>(x19, e19)));
-        return;
-    }
     K rho = ((((x01 + x03) + x10) + x12) + (((x05 + x08) + x14) + x17) + x19) + cte1;
     K rhoinv = uno / rho;
     K vx = (((x03 - x12) + (x01 - x10)) + (x05 - x14)) * rhoinv;
@@ -832,6 +728,16 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
 {
     if (L.pf_ahead > 0) prefetch_tile<S, TXV, TY, N, PF_PP>(L, parity);
     pp_tile<S, K, TXV, TY, HAS_OBS, N, LES, COLLIDE>(L, blockIdx.x, tile_row(blockIdx.y, gridDim.y), parity);
+}
+
+// The Smagorinsky ping-pong step of the 16-bit kinds with an explicit register budget (MINB
+// resident blocks of 128 threads per SM): its collision holds more live values than the plain
+// one, and the best split between registers and occupancy is chosen by timing.
+template <typename S, typename K, bool HAS_OBS, int N, int MINB>
+__global__ void __launch_bounds__(128, MINB) pp_les_kernel(const Lattice L, const int parity)
+{
+    if (L.pf_ahead > 0) prefetch_tile<S, 128, 1, N, PF_PP>(L, parity);
+    pp_tile<S, K, 128, 1, HAS_OBS, N, true>(L, blockIdx.x, tile_row(blockIdx.y, gridDim.y), parity);
 }
 
 // Persistent ping-pong step over many lattices.  The work list holds (lattice, tile x, tile y)
