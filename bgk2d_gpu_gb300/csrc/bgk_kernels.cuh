@@ -213,30 +213,30 @@ __device__ __forceinline__ void collide_scaled(T (&D)[9], float omega, float fgr
         // non-equilibrium parts N = D - E (N_q / s_q is the reference's x_q - e_q).  The momentum
         // flux P of the non-equilibrium parts sets the eddy viscosity (SRC/col_MC.F90:178-248):
         // D' = D - omega_eff N.
-        // With (8/9) folded into A and c.j: N_q = (D_q - (8/9)(A + c.j 4.5 c.u)) -+ 3 (8/9) c.j.
         const T c89 = splat<T>(8.0f / 9.0f);
-        const T A89 = op_mul(c89, A);
         const T ux45 = op_mul(splat<T>(4.5f), ux), uy45 = op_mul(splat<T>(4.5f), uy);
-        T N[9];
-        auto neq = [&](int qp, int qm, T cj, T cu45) {
-            const T cj89 = op_mul(c89, cj);
-            const T t = op_fma(cj89, cu45, A89);
-            N[qp] = op_fma(splat<T>(-3.0f), cj89, op_sub(D[qp], t));
-            N[qm] = op_fma(splat<T>(3.0f), cj89, op_sub(D[qm], t));
+        T E[9];
+        auto eq = [&](int qp, int qm, T cj, T cu45) {
+            const T t = op_fma(cj, cu45, A);
+            E[qp] = op_mul(c89, op_fma(splat<T>(3.0f), cj, t));
+            E[qm] = op_mul(c89, op_fma(splat<T>(-3.0f), cj, t));
         };
-        neq(D05, D14, jx, ux45);
-        neq(D08, D17, jy, uy45);
-        neq(D03, D10, op_add(jx, jy), op_add(ux45, uy45));
-        neq(D01, D12, op_sub(jx, jy), op_sub(ux45, uy45));
-        N[D19] = op_sub(D[D19], A89);
+        eq(D05, D14, jx, ux45);
+        eq(D08, D17, jy, uy45);
+        eq(D03, D10, op_add(jx, jy), op_add(ux45, uy45));
+        eq(D01, D12, op_sub(jx, jy), op_sub(ux45, uy45));
+        E[D19] = op_mul(c89, A);
+        T N[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) N[q] = op_sub(D[q], E[q]);
         const T nd = op_add(op_add(N[D01], N[D03]), op_add(N[D10], N[D12]));
         const T pxx = op_fma(nd, i32, op_mul(op_add(N[D05], N[D14]), i8));
         const T pyy = op_fma(nd, i32, op_mul(op_add(N[D08], N[D17]), i8));
         const T pxy = op_mul(op_sub(op_add(N[D03], N[D10]), op_add(N[D01], N[D12])), i32);
         const T p2 = op_fma(pxx, pxx, op_fma(op_add(pxy, pxy), pxy, op_mul(pyy, pyy)));
-        const T nw = op_sub(splat<T>(0.0f), les_rate<T>(p2, omega, cte_s));
+        const T w = les_rate<T>(p2, omega, cte_s);
 #pragma unroll
-        for (int q = 0; q < 9; ++q) D[q] = op_fma(nw, N[q], D[q]);  // D - omega_eff N
+        for (int q = 0; q < 9; ++q) D[q] = op_sub(D[q], op_mul(w, N[q]));
         if (forced) {
             const T F = op_mul(splat<T>(fgrad), rho);
             const T F32 = op_mul(splat<T>(32.0f), F), F8 = op_mul(splat<T>(8.0f), F);
