@@ -26,6 +26,7 @@ struct bgk_batch {
     int4 *d_tiles = nullptr;
     int ntiles = 0;
     size_t cap_lats = 0, cap_tiles = 0;
+    int nles = 0;                   // LES members' tiles, stored after the ntiles others
     int4 *d_bfs = nullptr;          // backward-facing-step members: (member, stepx, stepy, -)
     int nbfs = 0;
     size_t cap_bfs = 0;
@@ -52,22 +53,28 @@ int rebuild(bgk_batch *b)
     const TileCfg tc = TILE_CFGS[b->cfg];
     std::vector<Lattice> lats;
     std::vector<int> cur;
-    std::vector<int4> tiles, bfs;
+    std::vector<int4> tiles, les_tiles, bfs;
     for (size_t i = 0; i < b->members.size(); ++i) {
         bgk_handle *h = b->members[i];
         lats.push_back(h->L);
         cur.push_back(h->cur);
         if (h->cs.bfs) bfs.push_back(make_int4((int)i, h->cs.stepx, h->cs.stepy, 0));
-        const int n = b->T.vec / tc.cdiv;
+        // LES members: the Smagorinsky kernel's own shape (128 x 1 threads, the cells per
+        // thread of the single-domain LES step), in a list of their own
+        const bool les = h->L.les != 0;
+        const int txv = les ? 128 : tc.txv, ty = les ? 1 : tc.ty;
+        const int n = les ? (b->T.elem_bytes == 2 ? b->T.vec / 2 : b->T.vec) : b->T.vec / tc.cdiv;
         const int nv = (h->L.lx + n - 1) / n;
-        const int gx = (nv + tc.txv - 1) / tc.txv, gy = (h->L.ly + tc.ty - 1) / tc.ty;
+        const int gx = (nv + txv - 1) / txv, gy = (h->L.ly + ty - 1) / ty;
         // the lattice's last tile row (boundary-rule cells) second, as tile_row() orders single
         // domains, so that it does not trail its lattice's work
         for (int b = 0; b < gy; ++b) {
             const int by = (gy < 2 || b == 0) ? b : (b == 1 ? gy - 1 : b - 1);
-            for (int bx = 0; bx < gx; ++bx) tiles.push_back(make_int4((int)i, bx, by, 0));
+            for (int bx = 0; bx < gx; ++bx) (les ? les_tiles : tiles).push_back(make_int4((int)i, bx, by, 0));
         }
     }
+    const size_t nplain = tiles.size();
+    tiles.insert(tiles.end(), les_tiles.begin(), les_tiles.end());  // LES entries after the others
     // a failed allocation leaves the pointers null and the capacity 0, so a later rebuild retries
     // the allocation and never frees an array twice
     if (lats.size() > b->cap_lats) {
@@ -120,7 +127,8 @@ int rebuild(bgk_batch *b)
             return BGK_E_CUDA;
     }
     if (cudaStreamSynchronize(b->st) != cudaSuccess) return BGK_E_CUDA;
-    b->ntiles = (int)tiles.size();
+    b->ntiles = (int)nplain;
+    b->nles = (int)les_tiles.size();
     b->nbfs = (int)bfs.size();
     b->dirty = false;
     b->generation++;
@@ -146,17 +154,24 @@ int grid_of(const bgk_batch *b)
 
 int launch_one(bgk_batch *b, int parity)
 {
-    if (b->ntiles == 0) return BGK_OK;
+    if (b->ntiles == 0 && b->nles == 0) return BGK_OK;
     // backward-facing-step members: their boundary routine writes the source buffers' ghost and
     // step-face values first (the step kernel pulls them as stored faces)
     if (b->nbfs > 0) {
         if (b->T.batch_bfs(b->d_lats, b->d_cur, b->d_bfs, b->nbfs, parity, b->st) != cudaSuccess) return BGK_E_CUDA;
         b->launches++;
     }
-    if (b->T.batch_step(b->d_lats, b->d_cur, b->d_tiles, b->ntiles, parity, b->cfg, grid_of(b), b->pf, b->st) !=
-        cudaSuccess)
-        return BGK_E_CUDA;
-    b->launches++;
+    if (b->ntiles > 0) {
+        if (b->T.batch_step(b->d_lats, b->d_cur, b->d_tiles, b->ntiles, parity, b->cfg, grid_of(b), b->pf, b->st) !=
+            cudaSuccess)
+            return BGK_E_CUDA;
+        b->launches++;
+    }
+    if (b->nles > 0) {  // members with the Smagorinsky collision: their own launch of the same step
+        if (b->T.batch_les(b->d_lats, b->d_cur, b->d_tiles + b->ntiles, b->nles, parity, b->st) != cudaSuccess)
+            return BGK_E_CUDA;
+        b->launches++;
+    }
     return BGK_OK;
 }
 
@@ -201,7 +216,7 @@ int step_impl(bgk_batch *b, int n, bool use_graph)
         while (n >= b->graph_steps) {
             if (b->graph_built_for != b->generation && (rc = capture(b))) return rc;
             if (cudaGraphLaunch(b->graph, b->st) != cudaSuccess) return BGK_E_CUDA;
-            b->launches += (int64_t)b->graph_steps * (b->nbfs > 0 ? 2 : 1);
+            b->launches += (int64_t)b->graph_steps * ((b->nbfs > 0) + (b->ntiles > 0) + (b->nles > 0));
             advance_members(b, b->graph_steps);  // graph_steps is even: buffers unchanged
             n -= b->graph_steps;
         }
@@ -281,9 +296,9 @@ int bgk_batch_add(bgk_batch *b, bgk_handle *h)
     if (h->desc.storage != b->storage || h->desc.compute != b->compute || h->dev != b->dev ||
         h->L.scheme != BGK_SCHEME_PINGPONG)
         return BGK_E_INVALID;
-    // the batch kernels carry the plain BGK collision (no LES) and the fused one-pass step; a
-    // backward-facing step's boundary routine runs as its own batched launch before each step
-    if (h->L.les || h->two_pass) return BGK_E_UNSUPPORTED;
+    // the batch kernels carry the fused one-pass step; a backward-facing step's boundary routine
+    // and the Smagorinsky members' step run as batched launches of their own
+    if (h->two_pass) return BGK_E_UNSUPPORTED;
     if (h->sticky) return h->sticky;
     enter_device(b->dev);
     if (cudaStreamSynchronize(h->st) != cudaSuccess || cudaStreamSynchronize(b->st) != cudaSuccess) return BGK_E_CUDA;

@@ -187,6 +187,14 @@ cudaError_t bcond_step(const Lattice &L, int cur, int stepx, int stepy, cudaStre
 }
 
 template <typename S, typename K>
+cudaError_t batch_les(const Lattice *lats, const int *cur, const int4 *tiles, int n, int parity, cudaStream_t st)
+{
+    constexpr int N = Is16<S>::value ? vec_of<S>() / 2 : vec_of<S>();
+    batch_les_kernel<S, K, N><<<n, 128, 0, st>>>(lats, cur, tiles, parity);
+    return cudaGetLastError();
+}
+
+template <typename S, typename K>
 cudaError_t batch_bfs(const Lattice *lats, const int *cur, const int4 *members, int n, int parity, cudaStream_t st)
 {
     batch_bfs_kernel<S, K><<<n, 1024, 0, st>>>(lats, cur, members, parity);
@@ -307,6 +315,7 @@ KernelTable make_table()
     t.fill_outflow = &fill_outflow<S, K>;
     t.bcond_step = &bcond_step<S, K>;
     t.batch_bfs = &batch_bfs<S, K>;
+    t.batch_les = &batch_les<S, K>;
     t.init_tgv = &init_tgv<S>;
     t.diagno = &diagno<S, K>;
     t.diagno_seq = &diagno_seq<S, K>;

@@ -1210,6 +1210,17 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
     pp_tile<S, K, TXV, TY, true, N>(L, tile.y, tile.z, __ldg(cur + tile.x) ^ parity);
 }
 
+// Batch members with the Smagorinsky collision: one block of 128 x 1 threads per work-list entry,
+// the tile of the single-domain LES step (N cells per thread).
+template <typename S, typename K, int N>
+__global__ void __launch_bounds__(128, (N * sizeof(S) <= 8 || (sizeof(S) == 4 && N == 4)) ? 8 : (sizeof(S) == 2 ? 4 : 1))
+    batch_les_kernel(const Lattice *__restrict__ lats, const int *__restrict__ cur, const int4 *__restrict__ tiles,
+                     const int parity)
+{
+    const int4 tile = __ldg(tiles + blockIdx.x);
+    pp_tile<S, K, 128, 1, true, N, true>(lats[tile.x], tile.y, tile.z, __ldg(cur + tile.x) ^ parity);
+}
+
 // Collision half of the two-pass form (SRC/col.F90): every interior cell of buffer `parity`
 // relaxes in place, obstacle cells included, as the reference's col loop does.
 template <typename S, typename K, int TXV, int TY, int N, bool LES = false>

@@ -59,6 +59,8 @@ struct KernelTable {
     // the backward-facing-step boundary routine of n batch members (entries member, stepx, stepy)
     cudaError_t (*batch_bfs)(const Lattice *lats, const int *cur, const int4 *members, int n, int parity,
                              cudaStream_t st);
+    // the Smagorinsky step of a batch's LES members over their n work-list entries
+    cudaError_t (*batch_les)(const Lattice *lats, const int *cur, const int4 *tiles, int n, int parity, cudaStream_t st);
     cudaError_t (*init_tgv)(const Lattice &L, double u0, cudaStream_t st);
     cudaError_t (*diagno)(const Lattice &L, int cur, int phase, int fluid_only, bool obs, double *partial, int nb,
                           cudaStream_t st);

@@ -21,6 +21,9 @@ def make_cases(bgk, storage):
         # backward-facing steps: their boundary routine runs as one batched launch before each step
         dict(lx=200, ly=64, tcase="BFS", svisc=0.02, u0=0.1),
         dict(lx=120, ly=50, tcase="BFS", svisc=0.03, u0=0.1),
+        # Smagorinsky members: their step runs as a batched launch of its own
+        dict(lx=144, ly=96, tcase="LDC", svisc=0.005, u0=0.1, les=True, cte_s=0.2),
+        dict(lx=128, ly=64, tcase="TGV", svisc=0.01, u0=0.0, init="tgv", tgv_u0=0.02, les=True, cte_s=0.3),
     ]
     return [bgk.Solver(storage=storage, **c) for c in cases], cases
 
@@ -107,10 +110,10 @@ def test_batch_prefetch_does_not_change_results(bgk, tile, pf):
 
 
 def test_unsupported_members_are_rejected(bgk):
-    """LES and two-pass handles carry steps the batch kernel does not (backward-facing-step
-    members are taken: their boundary routine runs as a batched launch)."""
+    """Two-pass handles carry a second pass the batch kernels do not (backward-facing-step and
+    LES members are taken: their boundary routine and their step run as batched launches)."""
     from bgk2d_gpu_gb300 import _lib
-    for kw in (dict(tcase="LDC", les=True), dict(tcase="LDC", scheme="original")):
+    for kw in (dict(tcase="LDC", scheme="original"),):
         lx = kw.pop("lx", 64)
         with bgk.Solver(lx, 64, **kw) as s, bgk.Batch("f32") as b:
             with pytest.raises(bgk.BgkError) as e:

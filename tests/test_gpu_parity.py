@@ -254,17 +254,11 @@ def test_bfs_fluid_cells_never_read_the_solid_block(oracle_mod, bgk, prec, tile)
             assert not np.isfinite(got[:, 1:sy - 1, 1:sx - 1]).any()  # the block itself stays poisoned
 
 
-def test_bfs_rejects_aa_and_batches_reject_les(bgk):
+def test_bfs_rejects_aa(bgk):
     """The backward-facing step has no AA form (AA keeps no ghost frame for its boundary routine
-    to write before the step); batches take BFS members (tests/test_gpu_batch.py) but not LES
-    ones, whose collision the batch kernels do not carry."""
-    from bgk2d_gpu_gb300 import _lib
+    to write before the step); batches take BFS members (tests/test_gpu_batch.py)."""
     with pytest.raises(bgk.BgkError):
         bgk.Solver(200, 64, tcase="BFS", scheme="aa")
-    with bgk.Solver(64, 64, les=True) as s, bgk.Batch("f32") as b:
-        with pytest.raises(bgk.BgkError) as e:
-            b.add(s)
-        assert e.value.code == _lib.E_UNSUPPORTED
 
 
 @pytest.mark.parametrize("scheme", ["pingpong", "aa"])
