@@ -278,8 +278,8 @@ def run_profile(args):
 def run_profile_advance(args, storage, compute):
     """--profile advance_<storage> --size n --steps K: the end-to-end call on page-locked host
     planes (rest state), median of five runs each: bgk_advance_host (pipelined), the three calls in
-    sequence, and the upload and the download alone.  BGK_PIPE_ROWS / BGK_PIPE_CE set the band
-    height and the copy-engine option of the pipelined call."""
+    sequence, and the upload and the download alone.  BGK_PIPE_ROWS sets the band height of the
+    pipelined call."""
     import torch
     import bgk2d_gpu_gb300 as bgk
     L = bgk.load()

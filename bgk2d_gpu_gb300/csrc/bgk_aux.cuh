@@ -209,34 +209,6 @@ __global__ void __launch_bounds__(128, (N * sizeof(S) <= 8 || (sizeof(S) == 4 &&
         }
         by -= a.xfer_rows;
     }
-    if (a.zero_band >= 0) {
-        if (by == 0) {
-            // ghost cells of the band in the final buffer: columns 0 and lx+1 of its rows, and
-            // the whole ghost row beside the first and the last band (the values a download
-            // writes for them)
-            int ya, yb;
-            band_rows(L, a, a.zero_band, ya, yb);
-            S *base = reinterpret_cast<S *>(L.planes) + (((a.cur0 + a.nsteps) & 1) ? 9 : 0) * L.plane_elems;
-            const int w = L.lx + 2, rows = yb - ya + 1;
-            const int per_plane = 2 * rows + (ya == 0 ? w : 0) + (yb == L.ly + 1 ? w : 0);
-            for (int t = (int)(blockIdx.x * blockDim.x + threadIdx.x); t < 9 * per_plane; t += (int)(gridDim.x * blockDim.x)) {
-                const int q = t / per_plane;
-                int r = t - q * per_plane, x, y;
-                if (r < 2 * rows) {
-                    y = ya + r / 2;
-                    x = (r & 1) ? L.lx + 1 : 0;
-                } else {
-                    r -= 2 * rows;
-                    const bool first = ya == 0 && r < w;
-                    y = first ? 0 : L.ly + 1;
-                    x = first ? r : r - (ya == 0 ? w : 0);
-                }
-                base[q * L.plane_elems + cell_index<S>(L, x, y)] = S(0.0f);
-            }
-            return;
-        }
-        by -= 1;
-    }
     const int k = a.k_lo + by / a.band_rows;
     const int y = (a.wave - 2 * k) * a.band_rows + by % a.band_rows + 1;
     if (y > L.ly) return;

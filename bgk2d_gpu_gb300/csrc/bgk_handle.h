@@ -4,7 +4,6 @@
 #include <cuda_runtime.h>
 
 #include <string>
-#include <vector>
 
 #include "../../include/bgk2d_gb300.h"
 #include "bgk_common.cuh"
@@ -59,7 +58,5 @@ struct bgk_handle {
     int sticky = BGK_OK;
     void *batch = nullptr;   // owning batch while attached (steps go through the batch)
     cudaEvent_t wait_ev = nullptr;  // batch event the handle's stream waits on before touching the state
-    cudaStream_t st_up = nullptr, st_dn = nullptr;  // copy-engine streams of bgk_advance_host
-    std::vector<cudaEvent_t> pipe_ev;               // its per-band events (kept between calls)
     std::string err;
 };

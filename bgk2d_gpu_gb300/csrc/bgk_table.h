@@ -41,11 +41,8 @@ struct WaveArgs {
     HostPlanes in, out;
     int32_t band_rows, nbands, nsteps, cur0;
     int32_t wave, k_lo, k_hi;
-    int32_t up_band, down_band;  // -1: none in this wave (transfers by the wave's own blocks)
+    int32_t up_band, down_band;  // -1: none in this wave
     int32_t xfer_rows;           // grid rows (blockIdx.y) given to each transfer of the wave
-    int32_t zero_band;           // -1 or the band whose ghost cells in buffer (cur0 + nsteps) & 1
-                                 // this wave sets to zero (after step nsteps on it, before a copy
-                                 // engine downloads it)
 };
 
 struct KernelTable {

@@ -75,22 +75,18 @@ def test_advance_aa_takes_the_sequential_path(bgk):
     _run(bgk, torch, "ldc", "f32", 64, 40, 9, scheme="aa")
 
 
-@pytest.mark.parametrize("ce", ["0", "1", "2", "3"])
 @pytest.mark.parametrize("rows", ["1", "3", "16"])
-def test_advance_band_heights_padding_and_alias(bgk, rows, ce, monkeypatch):
-    """Bands moved by the waves' own blocks (ce=0, and always for 16-bit storage) or by the copy
-    engines (bit 0 uploads, bit 1 downloads; FP32/FP64 storage with evenly spaced host planes)."""
+def test_advance_band_heights_padding_and_alias(bgk, rows, monkeypatch):
     torch = pytest.importorskip("torch")
     monkeypatch.setenv("BGK_PIPE_ROWS", rows)
     monkeypatch.setenv("BGK_PIPE_XFER", "3")
-    monkeypatch.setenv("BGK_PIPE_CE", ce)
     _run(bgk, torch, "ldc", "f32", 130, 67, 12, pad=5)
     _run(bgk, torch, "vks", "f64", 150, 45, 7, alias=True)
     _run(bgk, torch, "vks", "f16", 200, 61, 40, alias=True)
 
 
 def test_advance_unevenly_spaced_planes(bgk):
-    """Nine separate page-locked planes (not one allocation): the in-kernel transfers take them."""
+    """Nine separate page-locked planes (not one allocation), as a driver may pass them."""
     torch = pytest.importorskip("torch")
     lx, ly, K = 90, 52, 9
     kw = dict(tcase="LDC", svisc=0.05, u0=0.1)
