@@ -40,7 +40,8 @@ class CaseDesc(ctypes.Structure):
         ("inflow_profile", I32), ("obstacle", I32), ("radius", I32),
         ("obs_icoord", I32), ("obs_jcoord", I32),
         ("obs_mask", ctypes.POINTER(I32)),
-        ("init_v", I32), ("tgv_u0", F64), ("device", I32), ("les", I32), ("cte_s", F64), ("reserved", I32 * 4),
+        ("init_v", I32), ("tgv_u0", F64), ("device", I32), ("les", I32), ("cte_s", F64), ("trick1", I32),
+        ("reserved", I32 * 3),
     ]
 
 

@@ -10,8 +10,9 @@
 // fields computed on the device) and bgk.perf.
 //
 //   bgk2d_gb300 [--input bgk.input] [--case LDC|TGV|POF|VKS|COU|BFS] [--prec single|double|mixed2|f16|bf16]
-//               [--scheme pingpong|aa|original] [--les 0|1] [--dir OUTDIR] [--check-input 0|1]
-// `--les 1` stands for the reference's -DLES build (Smagorinsky constant from the namelist key cteS).
+//               [--scheme pingpong|aa|original] [--les 0|1] [--trick1 0|1] [--dir OUTDIR] [--check-input 0|1]
+// `--les 1` stands for the reference's -DLES build (Smagorinsky constant from the namelist key cteS),
+// `--trick1 1` for its -DTRICK1 build (lid-cavity boundaries in one merged loop; square LDC only).
 // `--check-input 1` parses the input, prints the case it describes and exits, without a GPU.
 #include <cctype>
 #include <chrono>
@@ -326,7 +327,7 @@ int die(const char *what, int rc)
 int main(int argc, char **argv)
 {
     std::string input = "bgk.input", tcase = "LDC", prec = "single", scheme = "pingpong", dir = ".", les = "0";
-    std::string check = "0";
+    std::string check = "0", trick1 = "0";
     const auto bad = [](const char *what, const std::string &v) {
         std::fprintf(stderr, "bgk2d_gb300: bad %s '%s'\n", what, v.c_str());
         return 2;
@@ -340,6 +341,7 @@ int main(int argc, char **argv)
         else if (k == "--scheme") scheme = v;
         else if (k == "--dir") dir = v;
         else if (k == "--les") les = v;
+        else if (k == "--trick1") trick1 = v;
         else if (k == "--check-input") check = v;
         else return bad("option", k);
     }
@@ -347,6 +349,7 @@ int main(int argc, char **argv)
         return bad("--prec", prec);
     if (scheme != "pingpong" && scheme != "aa" && scheme != "original") return bad("--scheme", scheme);
     if (les != "0" && les != "1") return bad("--les", les);
+    if (trick1 != "0" && trick1 != "1") return bad("--trick1", trick1);
     if (check != "0" && check != "1") return bad("--check-input", check);
     auto kv = read_namelist(input);
     if (kv.empty()) { std::fprintf(stderr, "bgk2d_gb300: no &parameters namelist in %s\n", input.c_str()); return 1; }
@@ -366,6 +369,7 @@ int main(int argc, char **argv)
     d.u0 = getd("u0", 0.1);
     d.radius = geti("radius", 16);
     d.les = les == "1";
+    d.trick1 = trick1 == "1";
     d.cte_s = getd("ctes", 0.1);
     d.scheme = scheme == "aa" ? BGK_SCHEME_AA : scheme == "original" ? BGK_SCHEME_ORIGINAL : BGK_SCHEME_PINGPONG;
     if (prec == "double") { d.storage = BGK_STORE_F64; d.compute = BGK_COMPUTE_F64; }
@@ -381,9 +385,9 @@ int main(int argc, char **argv)
     if (d.tcase == BGK_CASE_TGV) d.init_v = BGK_INIT_TGV_REF;
     (void)init_v;
     if (check == "1") {
-        std::printf("case=%s prec=%s scheme=%s les=%d lx=%d ly=%d ipad=%d jpad=%d svisc=%.17g u0=%.17g "
+        std::printf("case=%s prec=%s scheme=%s les=%d trick1=%d lx=%d ly=%d ipad=%d jpad=%d svisc=%.17g u0=%.17g "
                     "ctes=%.17g radius=%d itfin=%d ivtim=%d isignal=%d itsave=%d icheck=%d irestart=%d\n",
-                    tcase.c_str(), prec.c_str(), scheme.c_str(), d.les, d.lx, d.ly, d.ipad, d.jpad, d.svisc, d.u0,
+                    tcase.c_str(), prec.c_str(), scheme.c_str(), d.les, d.trick1, d.lx, d.ly, d.ipad, d.jpad, d.svisc, d.u0,
                     d.cte_s, d.radius, itfin, ivtim, isignal, itsave, icheck, irestart);
         return 0;
     }

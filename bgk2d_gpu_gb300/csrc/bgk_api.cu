@@ -536,6 +536,7 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
         L.faces[f] = h->cs.faces[f];
         for (int q = 0; q < 9; ++q) L.wt[f][q] = h->cs.wt[f][q];
     }
+    L.corner_x = h->cs.corner_x;
     L.omega = h->cs.omega;
     L.fgrad = h->cs.fgrad;
     L.forced = h->cs.forced;

@@ -434,7 +434,9 @@ __device__ __forceinline__ void pull_vec(const Lattice &L, const S *plane, int x
 // ---------------------------------------------------------------------------------------------
 // Boundary rules for one pulled value.  (sx, sy) is the source of direction q for cell (x, y).
 // The y-face rule is applied first and wins at corners, as the reference's y-loop runs after
-// its x-loop (e.g. SRC/bcond.driven.F90:100-108 then :136-143).
+// its x-loop (e.g. SRC/bcond.driven.F90:100-108 then :136-143).  With L.corner_x (the merged
+// loop of SRC/bcond.driven.F90:43-81, whose x-wall statements of j = m come last at the two
+// upper corners) the x-face rule wins instead; both faces are walls there.
 //   plane_of(q, cx, cy): element holding the value of direction q "at" (cx, cy) in the
 //   current state; own(q): the pulling cell's own post-collision value of direction q.
 // ---------------------------------------------------------------------------------------------
@@ -445,7 +447,7 @@ __device__ __forceinline__ K pull_rule(const Lattice &L, int q, int x, int y, Pl
     int sx = x - cx_of(q), sy = y - cy_of(q);
     const int l = L.lx, m = L.ly;
     const int oq = opp_of(q);
-    if (sy < 1 || sy > m) {
+    if ((sy < 1 || sy > m) && !(L.corner_x && (sx < 1 || sx > l))) {
         const int f = sy < 1 ? YLO : YHI;
         if (L.faces[f] == FK_STORED) {
             return plane_at(q, sx, sy);
@@ -786,7 +788,7 @@ __device__ __forceinline__ void aa_push_rule(const Lattice &L, S *base, int q, i
     const S gs = Store<S>::template putq<K>(g, q);
     // the reference adds the wall term to the stored value (SRC/bcond.driven.F90:141-143)
     const K gr = Store<S>::template getq<K>(gs, q);
-    if (ty < 1 || ty > m) {
+    if ((ty < 1 || ty > m) && !(L.corner_x && (tx < 1 || tx > l))) {
         const int f = ty < 1 ? YLO : YHI;
         if (L.faces[f] == FK_PERIODIC) {
             ty = (ty < 1) ? m : 1;

@@ -21,6 +21,7 @@ struct CaseSetup {
     int forced;
     int bfs = 0;                    // backward-facing step: boundary kernel before each step
     int stepx = 0, stepy = 0;       // step corner (SRC/input.F90:74-75)
+    int corner_x = 0;               // the x-wall rule sets the corner ghosts (-DTRICK1)
     int les;                        // Smagorinsky eddy viscosity on
     double cte_s;                   // Smagorinsky constant (compute kind)
     double u_inflow;                // compute-kind inflow speed (peak for the parabolic profile)
@@ -192,6 +193,12 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
         break;
     default:
         return "unknown test case";
+    }
+    if (d.trick1) {
+        // the merged loop of SRC/bcond.driven.F90:43-81 indexes the lid by the wall index j = 1..m
+        if (d.tcase != BGK_CASE_LDC) return "trick1: lid-driven cavity only";
+        if (l != m) return "trick1: square box mandatory (SRC/check_case.F90:173-178)";
+        cs.corner_x = 1;
     }
     for (int f = 0; f < 4; ++f)
         if ((cs.faces[f] < FK_WALL || cs.faces[f] > FK_OUTFLOW_ZG) && !cs.bfs) return "unknown face kind";

@@ -48,7 +48,8 @@ class Solver:
     def __init__(self, lx, ly, tcase="LDC", svisc=0.1, u0=0.1, storage="f32", compute=None,
                  scheme="pingpong", radius=16, obstacle=None, obs_center=(-1, -1), obs_mask=None,
                  init="rest", omega=None, u_inflow=None, inflow_profile=0, faces=None,
-                 wall_u=None, tgv_u0=0.02, ipad=0, jpad=0, device=0, les=False, cte_s=0.1):
+                 wall_u=None, tgv_u0=0.02, ipad=0, jpad=0, device=0, les=False, cte_s=0.1,
+                 trick1=False):
         L = _lib.load()
         d = CaseDesc()
         L.bgk_default_desc(ctypes.byref(d))
@@ -81,6 +82,7 @@ class Solver:
         d.device = int(device)
         d.les = int(bool(les))
         d.cte_s = float(cte_s)
+        d.trick1 = int(bool(trick1))
         if faces is not None:
             for i, f in enumerate(faces):
                 d.faces[i] = _lib.FACE[f]

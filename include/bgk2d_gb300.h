@@ -119,7 +119,11 @@ typedef struct bgk_case_desc {
                                  128x1 kernels (bgk_tune picks only the prefetch distance) and
                                  cannot join a batch */
     double cte_s;             /* Smagorinsky constant cteS (namelist, SRC/input.F90:55; default 0.1) */
-    int32_t reserved[4];
+    int32_t trick1;           /* 1: the lid-cavity boundaries of the reference's -DTRICK1 build
+                                 (SRC/bcond.driven.F90:43-81): its merged loop lets the side walls
+                                 set the two upper corner ghosts, which then carry no lid term.
+                                 BGK_CASE_LDC on a square box only (SRC/check_case.F90:173-178) */
+    int32_t reserved[3];
 } bgk_case_desc;
 
 typedef struct bgk_handle bgk_handle;

@@ -42,7 +42,8 @@ module bgk_gpu
      integer(c_int)  :: device
      integer(c_int)  :: les
      real(c_double)  :: cte_s
-     integer(c_int)  :: reserved(4)
+     integer(c_int)  :: trick1
+     integer(c_int)  :: reserved(3)
   end type bgk_case_desc
 
   interface

@@ -89,6 +89,7 @@ struct orc_state {
 orc_state *orc_create(const orc_params *p)
 {
     if (p->l < 2 || p->m < 2) return NULL;
+    if (p->trick1 && (p->tcase != ORC_LDC || p->l != p->m)) return NULL;
     orc_state *s = (orc_state *)calloc(1, sizeof(orc_state));
     s->p = *p;
     s->l = p->l; s->m = p->m; s->ld = p->l + 2;

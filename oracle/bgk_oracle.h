@@ -55,6 +55,8 @@ typedef struct {
     double u0;         /* namelist u0, rounded to mykind */
     int les;           /* 1: Smagorinsky eddy viscosity (-DLES, SRC/col_MC.F90:178-264) */
     double cte_s;      /* namelist cteS (SRC/input.F90:55), rounded to mykind */
+    int trick1;        /* 1: the merged lid-cavity boundary loop of -DTRICK1 (SRC/bcond.driven.F90:43-81);
+                        * LDC on a square box only (SRC/check_case.F90:173-178) */
 } orc_params;
 
 orc_state *orc_create(const orc_params *p);

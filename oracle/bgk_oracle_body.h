@@ -145,6 +145,30 @@ static void FN(bcond_driven)(orc_state *s)
     }
 }
 
+/* bcond.driven.F90:43-81 (-DTRICK1, square box): one loop over j = 1..m that writes, in this
+ * order, the lid (y = m), the x = l wall, the x = 0 wall and the y = 0 wall of index j.  In the
+ * serial order the x-wall statements of j = m overwrite the lid's two upper corner ghosts, so
+ * a01(0,m1) and a10(l1,m1) carry no lid term; every other ghost equals the default order's. */
+static void FN(bcond_driven_trick1)(orc_state *s)
+{
+    const int l = s->l, m = s->m, l1 = l + 1, m1 = m + 1;
+    const K force = (K)s->u00 / (K)6.0;
+    for (int j = 1; j <= m; ++j) {
+        A_(0, j - 1, m1) = (S)(RA(5, j, m) + force);     /* a01(j-1,m1) = a12(j,m) + force */
+        A_(7, j, m1) = A_(3, j, m);                      /* a17(j,m1)   = a08(j,m) */
+        A_(4, j + 1, m1) = (S)(RA(1, j, m) - force);     /* a10(j+1,m1) = a03(j,m) - force */
+        A_(5, l1, j - 1) = A_(0, l, j);                  /* a12(l1,j-1) = a01(l,j) */
+        A_(4, l1, j + 1) = A_(1, l, j);                  /* a10(l1,j+1) = a03(l,j) */
+        A_(6, l1, j) = A_(2, l, j);                      /* a14(l1,j)   = a05(l,j) */
+        A_(1, 0, j - 1) = A_(4, 1, j);                   /* a03(0,j-1)  = a10(1,j) */
+        A_(0, 0, j + 1) = A_(5, 1, j);                   /* a01(0,j+1)  = a12(1,j) */
+        A_(2, 0, j) = A_(6, 1, j);                       /* a05(0,j)    = a14(1,j) */
+        A_(1, j - 1, 0) = A_(4, j, 1);                   /* a03(j-1,0)  = a10(j,1) */
+        A_(3, j, 0) = A_(7, j, 1);                       /* a08(j,0)    = a17(j,1) */
+        A_(5, j + 1, 0) = A_(0, j, 1);                   /* a12(j+1,0)  = a01(j,1) */
+    }
+}
+
 /* bcond.periodic.F90:45-114 */
 static void FN(bcond_periodic)(orc_state *s)
 {
@@ -349,7 +373,7 @@ static void FN(boundaries)(orc_state *s)
     case ORC_VKS: FN(bcond_inflow)(s); break;
     case ORC_COU: FN(bcond_couette)(s); break;
     case ORC_BFS: FN(bcond_step)(s); break;
-    default: FN(bcond_driven)(s); break;
+    default: if (s->p.trick1) FN(bcond_driven_trick1)(s); else FN(bcond_driven)(s); break;
     }
     if (s->p.obstacle) FN(bcond_obs)(s);
 }

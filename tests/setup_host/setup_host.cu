@@ -43,6 +43,26 @@ extern "C" int host_setup(int lx, int ly, int tcase, double svisc, double u0, in
     return 0;
 }
 
+// -DTRICK1 setup (SRC/check_case.F90:173-178): 1 when accepted with the x-wall corner rule on,
+// -1 when refused
+extern "C" int host_trick1(int lx, int ly, int tcase)
+{
+    bgk_case_desc d;
+    std::memset(&d, 0, sizeof(d));
+    d.lx = lx;
+    d.ly = ly;
+    d.tcase = tcase;
+    d.svisc = 0.05;
+    d.u0 = 0.1;
+    d.storage = BGK_STORE_F32;
+    d.compute = BGK_COMPUTE_F32;
+    d.scheme = BGK_SCHEME_PINGPONG;
+    d.trick1 = 1;
+    CaseSetup cs;
+    const std::string msg = setup_case<float>(d, cs);
+    return msg.empty() ? cs.corner_x : -1;
+}
+
 // the nine (0:l+1, 0:m+1) population planes of the reference initial state, in the storage kind
 extern "C" void host_init(int l, int m, int vortex, int prec, void *out)
 {

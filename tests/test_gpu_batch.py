@@ -13,6 +13,7 @@ def make_cases(bgk, storage):
     cases = [
         dict(lx=128, ly=128, tcase="LDC", svisc=0.0256, u0=0.1),
         dict(lx=192, ly=192, tcase="LDC", svisc=0.05, u0=0.07),
+        dict(lx=96, ly=96, tcase="LDC", svisc=0.02, u0=0.1, trick1=True),  # -DTRICK1 corners
         dict(lx=100, ly=60, tcase="LDC", svisc=0.02, u0=0.05),
         dict(lx=256, ly=64, tcase="TGV", svisc=0.04, u0=0.0, init="tgv", tgv_u0=0.02),
         dict(lx=512, ly=128, tcase="CUSTOM", svisc=0.02, u0=0.0, faces=("inflow", "outflow_zg", "wall", "wall"),

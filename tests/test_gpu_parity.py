@@ -201,6 +201,48 @@ def test_les_bit_exact(oracle_mod, bgk, case, prec, scheme):
             assert_same(o, s, scheme)
 
 
+@pytest.mark.parametrize("scheme", ["pingpong", "aa", "original"])
+@pytest.mark.parametrize("prec", ["single", "double", "mixed2"])
+def test_trick1_bit_exact(oracle_mod, bgk, prec, scheme):
+    """-DTRICK1 lid-cavity boundaries (SRC/bcond.driven.F90:43-81) on a square box: the x-wall rule
+    sets the two upper corner ghosts.  Bit-identical to the oracle's merged loop, and different
+    from the default order."""
+    n = 56
+    oprec, st, cp = PRECS[prec]
+    kw = dict(prec=oprec, tcase=0, svisc=0.02, u0=0.1, fused=scheme != "original")
+    o = oracle_mod.Oracle(n, n, trick1=True, **kw)
+    d = oracle_mod.Oracle(n, n, **kw)
+    with bgk.Solver(n, n, tcase="LDC", svisc=0.02, u0=0.1, storage=st, compute=cp, scheme=scheme,
+                    trick1=True) as s:
+        for k in (1, 2, 40, 75):
+            s.step(k)
+            o.step(k)
+            d.step(k)
+            assert_same(o, s, scheme)
+    assert not np.array_equal(interior(o.raw(), n, n), interior(d.raw(), n, n))
+
+
+@pytest.mark.parametrize("tile", range(9))
+def test_trick1_every_tile_and_les(oracle_mod, bgk, tile):
+    """The corner rule in every ping-pong kernel shape (register tiles and the staged copies),
+    alone and with the Smagorinsky collision."""
+    n = 72
+    for les in ((False, True) if tile == 0 else (False,)):
+        o = oracle_mod.Oracle(n, n, prec=0, tcase=0, svisc=0.01, u0=0.1, trick1=True, les=les, cte_s=0.2)
+        with bgk.Solver(n, n, tcase="LDC", svisc=0.01, u0=0.1, trick1=True, les=les, cte_s=0.2) as s:
+            if not les:
+                s.set_tile(tile)
+            s.step(33)
+            o.step(33)
+            assert_same(o, s, "pingpong")
+
+
+def test_trick1_refused_off_the_square_cavity(bgk):
+    for kw in (dict(lx=64, ly=48, tcase="LDC"), dict(lx=64, ly=64, tcase="COU")):
+        with pytest.raises(bgk.BgkError):
+            bgk.Solver(trick1=True, **kw)
+
+
 def _bfs_fluid(a, lx, ly):
     """Interior populations outside the step block x < lx/20, y < ly/2 (SRC/input.F90:74-75)."""
     sx, sy = lx // 20, ly // 2

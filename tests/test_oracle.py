@@ -71,6 +71,34 @@ def test_les_fused_equals_original_and_adds_viscosity(oracle_mod, prec):
     assert e_les < e_bgk * 0.999, (e_les, e_bgk)
 
 
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_trick1_changes_only_the_upper_lid_corners(oracle_mod, prec):
+    """-DTRICK1 (SRC/bcond.driven.F90:43-81) writes the same ghosts as the default order except
+    a01(0,m1) and a10(l1,m1), which the x-wall statements of j = m set without the lid term: after
+    one step from rest only the cells (1,m) and (l,m) that pull them differ.  The two-pass form
+    agrees with the fused one, and a non-square or non-cavity case is refused
+    (SRC/check_case.F90:173-178)."""
+    O = oracle_mod
+    n = 24
+    kw = dict(prec=prec, tcase=O.LDC, svisc=0.05, u0=0.1)
+    a = O.Oracle(n, n, **kw)
+    b = O.Oracle(n, n, trick1=True, **kw)
+    c = O.Oracle(n, n, trick1=True, fused=False, **kw)
+    for o in (a, b, c):
+        o.step(1)
+    ia, ib, ic = (o.raw()[:, 1:n + 1, 1:n + 1] for o in (a, b, c))
+    rows, cols = np.nonzero((ia != ib).any(axis=0))
+    assert sorted(zip((rows + 1).tolist(), (cols + 1).tolist())) == [(n, 1), (n, n)]
+    assert np.array_equal(ib, ic)
+    for o in (a, b, c):
+        o.step(30)
+    assert np.array_equal(b.raw()[:, 1:n + 1, 1:n + 1], c.raw()[:, 1:n + 1, 1:n + 1])
+    with pytest.raises(ValueError):
+        O.Oracle(n, n + 2, trick1=True, **kw)
+    with pytest.raises(ValueError):
+        O.Oracle(n, n, prec=prec, tcase=O.COU, svisc=0.05, u0=0.1, trick1=True)
+
+
 def test_obstacle_loop_order_only_affects_obstacle_cells(oracle_mod):
     O = oracle_mod
     a = O.Oracle(160, 62, tcase=O.VKS, svisc=0.05, u0=0.1, obstacle=O.OBS_CIRCLE, radius=6, obs_order=O.OBS_SERIAL)

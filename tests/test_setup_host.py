@@ -35,6 +35,8 @@ def hostlib(tmp_path_factory):
     L.host_setup.restype = ctypes.c_int
     L.host_init.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p]
     L.host_init.restype = None
+    L.host_trick1.argtypes = [ctypes.c_int] * 3
+    L.host_trick1.restype = ctypes.c_int
     return L
 
 
@@ -138,3 +140,13 @@ def test_circle_count_is_the_lattice_point_count(hostlib, r):
     count = sum(2 * math.isqrt(r * r - dy * dy) + 1 for dy in range(-r, r + 1))
     assert int(mask.sum()) == count == bb[4]
     assert bb.tolist()[:4] == [n // 2 - r, n // 2 + r, n // 2 - r, n // 2 + r]
+
+
+def test_trick1_accepts_only_the_square_cavity(hostlib, oracle_mod):
+    """bgk_case_desc.trick1 turns on the corner rule for a square lid-driven cavity and is refused
+    elsewhere, as the oracle (and SRC/check_case.F90:173-178) refuses it."""
+    assert hostlib.host_trick1(64, 64, LDC) == 1
+    for l, m, tc in ((64, 48, LDC), (64, 64, COU), (64, 64, TGV), (64, 64, POF)):
+        assert hostlib.host_trick1(l, m, tc) == -1
+        with pytest.raises(ValueError):
+            oracle_mod.Oracle(l, m, tcase=tc, trick1=True)
