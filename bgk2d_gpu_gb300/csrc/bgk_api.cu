@@ -953,12 +953,13 @@ int bgk_tune(bgk_handle *h, int32_t trial_steps, int32_t *tile_cfg, int32_t *ste
     const bool aa16 = h->L.scheme == BGK_SCHEME_AA && h->T.elem_bytes == 2;
     // A handle with the Smagorinsky collision runs one kernel shape whatever the tile
     // configuration, except 16-bit ping-pong, whose configurations 0-3 are register budgets of
-    // its LES kernel; otherwise only the prefetch distance is tried.
+    // its LES kernel and 4-5 its staged forms; otherwise only the prefetch distance is tried.
     const bool les16 = h->L.les && h->T.elem_bytes == 2 && h->L.scheme == BGK_SCHEME_PINGPONG && !h->two_pass;
     const int c0 = les16 ? 0 : h->L.les ? h->cfg : aa16 ? 4 : 0;
-    const int c1 = les16 ? 4 : h->L.les ? h->cfg + 1 : ncfg;
+    const int c1 = les16 ? 6 : h->L.les ? h->cfg + 1 : ncfg;
     for (int c = c0; c < c1; ++c) {
-        const int npf = c < NUM_CFG ? 3 : 1;
+        const bool staged = c >= NUM_CFG || (les16 && c >= 4);
+        const int npf = staged ? 1 : 3;
         for (int p = 0; p < npf; ++p) {
             if ((rc = bgk_set_tile(h, c)) || (rc = bgk_set_prefetch(h, pfs[p]))) return rc;
             for (int s = 0; s < 2; ++s)

@@ -36,12 +36,12 @@ cudaError_t step_cfg(int kind, const Lattice &L, int parity, cudaStream_t st)
 
 // ping-pong step through shared-memory staging: one wave of blocks, each a band of T*N columns
 // and a stripe of rows
-template <typename S, typename K, int T, int STAGES, bool OBS>
+template <typename S, typename K, int T, int STAGES, bool OBS, bool LES = false, int MINB = 0>
 cudaError_t step_staged(const Lattice &L, int parity, cudaStream_t st)
 {
     constexpr int N = vec_of<S>() / 2;
     constexpr size_t smem = staged_smem_bytes<S, T, N, STAGES>();
-    auto kern = pp_staged_kernel<S, K, T, N, STAGES, OBS>;
+    auto kern = pp_staged_kernel<S, K, T, N, STAGES, OBS, LES, MINB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     // A stripe of STAGES rows per block: every copy of the block is issued at once, and the
@@ -70,14 +70,21 @@ cudaError_t step_les(int kind, const Lattice &L, int parity, int cfg, cudaStream
 {
     const dim3 block(128, 1);
     // 16-bit ping-pong: register budgets tried by the autotuner (tile configuration 0-3): 4 cells
-    // per thread at 8 blocks per SM (64 registers) or 6 (80); 8 cells at 4 (128) or 3 (168)
+    // per thread at 8 blocks per SM (64 registers) or 6 (80); 8 cells at 4 (128) or 3 (168).
+    // Configurations 4 and 5: the source rows staged in shared memory by bulk async copies (4 cells
+    // per thread, stripes of 4 rows at 5 blocks per SM or of 3 rows at 6), so that no register
+    // holds a load in flight.
     if constexpr (Is16<S>::value) {
-        if (kind == STEP_PP && cfg >= 1 && cfg <= 3) {
+        if (kind == STEP_PP && cfg >= 1 && cfg <= 5) {
             if (cfg == 1) return les16_launch<S, K, OBS, vec_of<S>() / 2, 6>(L, parity, st);
             if (cfg == 2) return les16_launch<S, K, OBS, vec_of<S>(), 4>(L, parity, st);
-            return les16_launch<S, K, OBS, vec_of<S>(), 3>(L, parity, st);
+            if (cfg == 3) return les16_launch<S, K, OBS, vec_of<S>(), 3>(L, parity, st);
+            if (cfg == 4) return step_staged<S, K, 128, 4, OBS, true, 5>(L, parity, st);
+            return step_staged<S, K, 128, 3, OBS, true, 6>(L, parity, st);
         }
     }
+    // staged configurations of a single-domain ping-pong step (6-8): one staged LES shape
+    if (kind == STEP_PP && cfg >= NUM_CFG) return step_staged<S, K, 128, 4, OBS, true>(L, parity, st);
     // 16-bit kinds: 8 bytes per thread and plane (64 registers, 8 blocks per SM), the fastest shape
     // of their non-LES step; the 32/64-bit kinds: 16 bytes
     constexpr int N = Is16<S>::value ? vec_of<S>() / 2 : vec_of<S>();

@@ -589,8 +589,8 @@ __device__ void pp_cell_slow(const Lattice &L, const S *src, S *dst, int x, int 
 // First (x = 1, LOW) or last (x = lx) cell of a row in rows 2..ly-1 away from obstacles: only the
 // three inputs that come from the x ghost column need the boundary rules; they replace the
 // vector-loaded values in place (position C of the thread's N cells, scaled when RAW).
-template <typename S, typename K, bool HAS_OBS, bool RAW, int C, bool LOW, int N>
-__device__ __forceinline__ void pp_edge_pull(const Lattice &L, const S *src, int x, int y, K (&v)[9][N])
+template <typename S, typename K, bool HAS_OBS, bool RAW, bool LOW, int N>
+__device__ __forceinline__ void pp_edge_pull(const Lattice &L, const S *src, int x, int y, int C, K (&v)[9][N])
 {
     const int64_t pe = L.plane_elems;
     const int64_t me = cell_index<S>(L, x, y);
@@ -609,9 +609,28 @@ __device__ __forceinline__ void pp_edge_pull(const Lattice &L, const S *src, int
     const K a = pull_rule<S, K, HAS_OBS>(L, q0, x, y, plane_at, own, ghost_xhi);
     const K b = pull_rule<S, K, HAS_OBS>(L, q1, x, y, plane_at, own, ghost_xhi);
     const K c = pull_rule<S, K, HAS_OBS>(L, q2, x, y, plane_at, own, ghost_xhi);
-    v[q0][C] = RAW ? (K)((float)a * scale_of(q0)) : a;
-    v[q1][C] = RAW ? (K)((float)b * scale_of(q1)) : b;
-    v[q2][C] = RAW ? (K)((float)c * scale_of(q2)) : c;
+    const K as = RAW ? (K)((float)a * scale_of(q0)) : a;
+    const K bs = RAW ? (K)((float)b * scale_of(q1)) : b;
+    const K cs = RAW ? (K)((float)c * scale_of(q2)) : c;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {  // a select per position, so v stays in registers
+        if (i == C) {
+            v[q0][i] = as;
+            v[q1][i] = bs;
+            v[q2][i] = cs;
+        }
+    }
+}
+
+// Edge cells of a row that take the in-place rules of pp_edge_pull: x = 1 and x = lx of rows
+// 2..ly-1 outside the obstacle zone, whatever the vector width, so that every tile shape
+// computes and rounds them alike.  Returns whether cell x qualifies.
+template <bool HAS_OBS>
+__device__ __forceinline__ bool edge_cell(const Lattice &L, int x, int y)
+{
+    if (y == 1 || y == L.ly) return false;
+    if (HAS_OBS && y >= L.ob_y0 && y <= L.ob_y1 && x >= L.ob_x0 && x <= L.ob_x1) return false;
+    return true;
 }
 
 // one tile of TXV*VEC x TY cells at tile coordinates (bx, by) of lattice L.  Every lane takes the
@@ -656,10 +675,15 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
     const bool rowb = (y == 1) || (y == L.ly);
     bool obsz = false;
     if (HAS_OBS) obsz = y >= L.ob_y0 && y <= L.ob_y1 && xv + N - 1 >= L.ob_x0 && xv <= L.ob_x1;
-    const bool left_cell = !rowb && !obsz && k == 0 && nv > 1;
-    const bool right_cell = !rowb && !obsz && k == nv - 1 && nv > 1 && (L.lx % N) == 0;
-    if (left_cell) pp_edge_pull<S, K, HAS_OBS, RAW, 0, true, N>(L, src, xv, y, x);
-    if (right_cell) pp_edge_pull<S, K, HAS_OBS, RAW, N - 1, false, N>(L, src, xv + N - 1, y, x);
+    // 16-bit kinds: the row's end cell at any position of the last vector (edge_cell), so that
+    // every tile shape rounds it alike; the exact kinds give the same result either way and keep
+    // the in-place rules to a last vector that ends at lx.
+    const bool left_cell = RAW ? k == 0 && edge_cell<HAS_OBS>(L, 1, y) : !rowb && !obsz && k == 0 && nv > 1;
+    const bool right_cell = RAW ? k == nv - 1 && edge_cell<HAS_OBS>(L, L.lx, y)
+                                : !rowb && !obsz && k == nv - 1 && nv > 1 && (L.lx % N) == 0;
+    if (left_cell) pp_edge_pull<S, K, HAS_OBS, RAW, true, N>(L, src, xv, y, 0, x);
+    if (right_cell)
+        pp_edge_pull<S, K, HAS_OBS, RAW, false, N>(L, src, RAW ? L.lx : xv + N - 1, y, RAW ? L.lx - xv : N - 1, x);
 
     if constexpr (COLLIDE) relax_vec<S, K, RAW, N, LES>(x, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
     const int64_t me = cell_index<S>(L, xv, y);
@@ -682,7 +706,8 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
         const int xe = min(xv + N - 1, L.lx);
 #pragma unroll 1
         for (int xc = xv; xc <= xe; ++xc)
-            if (needs_rule<HAS_OBS>(L, xc, y)) pp_cell_slow<S, K, HAS_OBS, LES, COLLIDE>(L, src, dst, xc, y);
+            if (needs_rule<HAS_OBS>(L, xc, y) && !(RAW && ((xc == 1 && left_cell) || (xc == L.lx && right_cell))))
+                pp_cell_slow<S, K, HAS_OBS, LES, COLLIDE>(L, src, dst, xc, y);
     }
 }
 

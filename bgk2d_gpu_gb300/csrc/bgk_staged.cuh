@@ -122,9 +122,11 @@ __device__ __forceinline__ void pull_staged(const S *seg, int i0, K (&out)[N])
 }
 
 // Grid: (bands, stripes); block b.x covers columns 1 + b.x * BW .., block b.y rows
-// 1 + b.y * rows .. min(ly, (b.y + 1) * rows).
-template <typename S, typename K, int T, int N, int STAGES, bool HAS_OBS>
-__global__ void __launch_bounds__(T, ((N * sizeof(S) <= 8) ? 1024 : 512) / T)
+// 1 + b.y * rows .. min(ly, (b.y + 1) * rows).  LES: the Smagorinsky collision.  MINB > 0 sets
+// the blocks per SM that the register budget is sized for (the shared-memory stages bound the
+// residency anyway, so the eddy-viscosity collision can take the registers it needs).
+template <typename S, typename K, int T, int N, int STAGES, bool HAS_OBS, bool LES = false, int MINB = 0>
+__global__ void __launch_bounds__(T, MINB > 0 ? MINB : ((N * sizeof(S) <= 8) ? 1024 : 512) / T)
     pp_staged_kernel(const Lattice L, const int parity, const int rows)
 {
     constexpr int VEC = vec_of<S>();
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(T, ((N * sizeof(S) <= 8) ? 1024 : 512) / T)
     const bool active = k < nv;
     const int xv = 1 + k * N;
     const int i0 = VEC + t * N;  // staged index of the thread's first cell
-    const K omega = lat_omega<K>(L), fgrad = lat_fgrad<K>(L);
+    const K omega = lat_omega<K>(L), fgrad = lat_fgrad<K>(L), cte_s = lat_cte_s<K>(L);
     const bool forced = L.forced != 0;
     constexpr int NW = T / 32;
 
@@ -227,12 +229,17 @@ __global__ void __launch_bounds__(T, ((N * sizeof(S) <= 8) ? 1024 : 512) / T)
             const bool rowb = (y == 1) || (y == L.ly);
             bool obsz = false;
             if (HAS_OBS) obsz = y >= L.ob_y0 && y <= L.ob_y1 && xv + N - 1 >= L.ob_x0 && xv <= L.ob_x1;
-            const bool left_cell = !rowb && !obsz && k == 0 && nv > 1;
-            const bool right_cell = !rowb && !obsz && k == nv - 1 && nv > 1 && (L.lx % N) == 0;
-            if (left_cell) pp_edge_pull<S, K, HAS_OBS, RAW, 0, true, N>(L, src, xv, y, x);
-            if (right_cell) pp_edge_pull<S, K, HAS_OBS, RAW, N - 1, false, N>(L, src, xv + N - 1, y, x);
+            // 16-bit kinds: the row's end cell at any position of the last vector (edge_cell), so that
+            // every tile shape rounds it alike; the exact kinds give the same result either way and keep
+            // the in-place rules to a last vector that ends at lx.
+            const bool left_cell = RAW ? k == 0 && edge_cell<HAS_OBS>(L, 1, y) : !rowb && !obsz && k == 0 && nv > 1;
+            const bool right_cell = RAW ? k == nv - 1 && edge_cell<HAS_OBS>(L, L.lx, y)
+                                        : !rowb && !obsz && k == nv - 1 && nv > 1 && (L.lx % N) == 0;
+            if (left_cell) pp_edge_pull<S, K, HAS_OBS, RAW, true, N>(L, src, xv, y, 0, x);
+            if (right_cell)
+                pp_edge_pull<S, K, HAS_OBS, RAW, false, N>(L, src, RAW ? L.lx : xv + N - 1, y, RAW ? L.lx - xv : N - 1, x);
 
-            relax_vec<S, K, RAW, N>(x, omega, fgrad, forced, (K)0);
+            relax_vec<S, K, RAW, N, LES>(x, omega, fgrad, forced, cte_s);
             const int64_t me = cell_index<S>(L, xv, y);
             uint32_t rh[npair<N>()] = {};
 #pragma unroll
@@ -252,7 +259,8 @@ __global__ void __launch_bounds__(T, ((N * sizeof(S) <= 8) ? 1024 : 512) / T)
                 const int xe = min(xv + N - 1, L.lx);
 #pragma unroll 1
                 for (int xc = xv; xc <= xe; ++xc)
-                    if (needs_rule<HAS_OBS>(L, xc, y)) pp_cell_slow<S, K, HAS_OBS>(L, src, dst, xc, y);
+                    if (needs_rule<HAS_OBS>(L, xc, y) && !(RAW && ((xc == 1 && left_cell) || (xc == L.lx && right_cell))))
+                        pp_cell_slow<S, K, HAS_OBS, LES>(L, src, dst, xc, y);
             }
         }
     }

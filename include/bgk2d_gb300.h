@@ -115,9 +115,9 @@ typedef struct bgk_case_desc {
     double tgv_u0;            /* amplitude for BGK_INIT_TGV */
     int32_t device;           /* CUDA device ordinal */
     int32_t les;              /* 1: Smagorinsky eddy viscosity in the collision (-DLES,
-                                 SRC/col_MC.F90:178-248); such a handle steps with its own
-                                 128x1 kernels (bgk_tune picks only the prefetch distance) and
-                                 cannot join a batch */
+                                 SRC/col_MC.F90:178-248); such a handle steps with kernels of its
+                                 own: bgk_tune picks the prefetch distance, and for 16-bit
+                                 ping-pong also the kernel shape */
     double cte_s;             /* Smagorinsky constant cteS (namelist, SRC/input.F90:55; default 0.1) */
     int32_t trick1;           /* 1: the lid-cavity boundaries of the reference's -DTRICK1 build
                                  (SRC/bcond.driven.F90:43-81): its merged loop lets the side walls

@@ -70,16 +70,21 @@ def test_staged_tuner_may_pick_it(bgk):
         s.sync()
 
 
-@pytest.mark.parametrize("prec", ["single", "double"])
+@pytest.mark.parametrize("prec", ["single", "double", "mixed2"])
 def test_staged_les_bit_exact(oracle_mod, bgk, prec):
-    """The eddy-viscosity collision through the staged kernel."""
-    oprec, st = (0, "f32") if prec == "single" else (1, "f64")
-    o = oracle_mod.Oracle(200, 90, prec=oprec, tcase=0, svisc=0.01, u0=0.1, les=True, cte_s=0.2)
-    with bgk.Solver(200, 90, tcase="LDC", svisc=0.01, u0=0.1, storage=st, compute=st, les=True, cte_s=0.2) as s:
-        s.set_tile(6)
-        s.step(50)
-        o.step(50)
-        assert_same(o, s, "pingpong")
+    """The eddy-viscosity collision through the staged kernel (a staged configuration of an LES
+    handle), on a cavity and on a channel with a cylinder."""
+    oprec, st, cp = {"single": (0, "f32", "f32"), "double": (1, "f64", "f64"), "mixed2": (2, "f32", "f64")}[prec]
+    for tc, otc, lx, ly, kw, okw in (("LDC", 0, 200, 90, {}, {}),
+                                     ("VKS", 3, 160, 62, {"radius": 6}, {"obstacle": 1, "radius": 6})):
+        o = oracle_mod.Oracle(lx, ly, prec=oprec, tcase=otc, svisc=0.01, u0=0.1, les=True, cte_s=0.2,
+                              obs_order=oracle_mod.OBS_SNAPSHOT, **okw)
+        with bgk.Solver(lx, ly, tcase=tc, svisc=0.01, u0=0.1, storage=st, compute=cp, les=True, cte_s=0.2,
+                        **kw) as s:
+            s.set_tile(7)
+            s.step(50)
+            o.step(50)
+            assert_same(o, s, "pingpong")
 
 
 def test_staged_wait_timeout_reports_status(oracle_mod, bgk, monkeypatch):
