@@ -41,7 +41,7 @@ class CaseDesc(ctypes.Structure):
         ("obs_icoord", I32), ("obs_jcoord", I32),
         ("obs_mask", ctypes.POINTER(I32)),
         ("init_v", I32), ("tgv_u0", F64), ("device", I32), ("les", I32), ("cte_s", F64), ("trick1", I32),
-        ("reserved", I32 * 3),
+        ("noshift", I32), ("reserved", I32 * 2),
     ]
 
 

@@ -10,9 +10,11 @@
 // fields computed on the device) and bgk.perf.
 //
 //   bgk2d_gb300 [--input bgk.input] [--case LDC|TGV|POF|VKS|COU|BFS] [--prec single|double|mixed2|f16|bf16]
-//               [--scheme pingpong|aa|original] [--les 0|1] [--trick1 0|1] [--dir OUTDIR] [--check-input 0|1]
+//               [--scheme pingpong|aa|original] [--les 0|1] [--trick1 0|1] [--noshift 0|1] [--dir OUTDIR]
+//               [--check-input 0|1]
 // `--les 1` stands for the reference's -DLES build (Smagorinsky constant from the namelist key cteS),
-// `--trick1 1` for its -DTRICK1 build (lid-cavity boundaries in one merged loop; square LDC only).
+// `--trick1 1` for its -DTRICK1 build (lid-cavity boundaries in one merged loop; square LDC only),
+// `--noshift 1` for its -DNOSHIFT build (whole populations, not deviations; FP32/FP64 only).
 // `--check-input 1` parses the input, prints the case it describes and exits, without a GPU.
 #include <cctype>
 #include <chrono>
@@ -108,45 +110,49 @@ struct Pops {
     }
 };
 
-// host readers with the reference's per-cell arithmetic in the storage kind
-template <typename T>
-void prof_j(const Pops &a, int icoord, FILE *f, int itime)
+// host readers with the reference's per-cell arithmetic.  prof_i, prof_j and varm add the stored
+// values as they lie in the arrays, in the storage kind S (real(sp) under MIXED2), then add cte1
+// and divide in the compute kind K; probe copies the values into K temporaries first
+// (SRC/probe.F90:46-54).  cte1 = 1, or 0 for populations stored whole (SRC/prof_j.F90:40-44,
+// prof_i.F90:40-44, probe.F90:40-44, varm.F90:42-46).
+template <typename S, typename K>
+void prof_j(const Pops &a, int icoord, FILE *f, int itime, K cte1)
 {
     std::fprintf(f, "# t=%7d\n", itime);
     for (int j = 1; j <= a.ly; ++j) {
-        T x[9];
-        for (int q = 0; q < 9; ++q) x[q] = (T)a.at(q, icoord, j);
-        T den = ((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8]) + (T)1;
-        T u = (((x[0] - x[4]) + (x[1] - x[5])) + (x[2] - x[6])) / den;
-        T v = (((x[1] - x[0]) + (x[3] - x[7])) + (x[5] - x[4])) / den;
+        S x[9];
+        for (int q = 0; q < 9; ++q) x[q] = (S)a.at(q, icoord, j);
+        K den = (K)((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8]) + cte1;
+        K u = (K)(((x[0] - x[4]) + (x[1] - x[5])) + (x[2] - x[6])) / den;
+        K v = (K)(((x[1] - x[0]) + (x[3] - x[7])) + (x[5] - x[4])) / den;
         std::fprintf(f, "%s %s %s %s \n", fortran_e(j - 0.5).c_str(), fortran_e(u).c_str(), fortran_e(v).c_str(),
                      fortran_e(den).c_str());
     }
     std::fprintf(f, "\n\n");
 }
 
-template <typename T>
-void prof_i(const Pops &a, int jcoord, FILE *f, int itime)
+template <typename S, typename K>
+void prof_i(const Pops &a, int jcoord, FILE *f, int itime, K cte1)
 {
     std::fprintf(f, "# t=%7d\n", itime);
     for (int i = 1; i <= a.lx; ++i) {
-        T x[9];
-        for (int q = 0; q < 9; ++q) x[q] = (T)a.at(q, i, jcoord);
-        T den = ((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8]) + (T)1;
-        T u = (((((x[0] + x[1]) + x[2]) - x[4]) - x[5]) - x[6]) / den;
-        T v = (((((x[1] + x[3]) + x[5]) - x[0]) - x[4]) - x[7]) / den;
+        S x[9];
+        for (int q = 0; q < 9; ++q) x[q] = (S)a.at(q, i, jcoord);
+        K den = (K)((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8]) + cte1;
+        K u = (K)(((((x[0] + x[1]) + x[2]) - x[4]) - x[5]) - x[6]) / den;
+        K v = (K)(((((x[1] + x[3]) + x[5]) - x[0]) - x[4]) - x[7]) / den;
         std::fprintf(f, "%s %s %s %s \n", fortran_e(i - 0.5).c_str(), fortran_e(u).c_str(), fortran_e(v).c_str(),
                      fortran_e(den).c_str());
     }
     std::fprintf(f, "\n\n");
 }
 
-template <typename T>
-void probe(const Pops &a, int i0, int j0, FILE *f, int itime)
+template <typename S, typename T>
+void probe(const Pops &a, int i0, int j0, FILE *f, int itime, T cte1)
 {
     T x[9];
-    for (int q = 0; q < 9; ++q) x[q] = (T)a.at(q, i0, j0);
-    T rho = (((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8])) + (T)1;
+    for (int q = 0; q < 9; ++q) x[q] = (T)(S)a.at(q, i0, j0);
+    T rho = (((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8])) + cte1;
     T xj = ((((x[0] + x[1]) + x[2]) - x[4]) - x[5]) - x[6];
     T yj = ((((x[1] + x[3]) + x[5]) - x[0]) - x[4]) - x[7];
     std::fprintf(f, "%8d%s %s %s \n", itime, fortran_e(xj / rho).c_str(), fortran_e(yj / rho).c_str(),
@@ -155,21 +161,21 @@ void probe(const Pops &a, int i0, int j0, FILE *f, int itime)
 
 // row means of u, w and rho over i = 1..lx (SRC/varm.F90:49-88, u_med.dat): sums over i in order
 // in the storage kind, times rvol = 1.0/float(l) (a default-real quotient)
-template <typename T>
-void varm(const Pops &a, FILE *f, int itime)
+template <typename S, typename T>
+void varm(const Pops &a, FILE *f, int itime, T cte1)
 {
     const T rvol = (T)(1.0f / (float)a.lx);
     std::fprintf(f, "# t=%7d\n", itime);
     for (int j = 1; j <= a.ly; ++j) {
         T u = 0, w = 0, den = 0;
         for (int i = 1; i <= a.lx; ++i) {
-            T x[9];
-            for (int q = 0; q < 9; ++q) x[q] = (T)a.at(q, i, j);
-            const T rho = ((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8]) + (T)1;
+            S x[9];
+            for (int q = 0; q < 9; ++q) x[q] = (S)a.at(q, i, j);
+            const T rho = (T)((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8]) + cte1;
             const T rhoinv = (T)1 / rho;
             den = den + rho;
-            u = u + (((((x[0] + x[1]) + x[2]) - x[4]) - x[5]) - x[6]) * rhoinv;
-            w = w + (((((x[1] + x[3]) + x[5]) - x[0]) - x[4]) - x[7]) * rhoinv;
+            u = u + (T)(((((x[0] + x[1]) + x[2]) - x[4]) - x[5]) - x[6]) * rhoinv;
+            w = w + (T)(((((x[1] + x[3]) + x[5]) - x[0]) - x[4]) - x[7]) * rhoinv;
         }
         std::fprintf(f, "%5d%s %s %s \n", j, fortran_e(u * rvol).c_str(), fortran_e(w * rvol).c_str(),
                      fortran_e(den * rvol).c_str());
@@ -327,7 +333,7 @@ int die(const char *what, int rc)
 int main(int argc, char **argv)
 {
     std::string input = "bgk.input", tcase = "LDC", prec = "single", scheme = "pingpong", dir = ".", les = "0";
-    std::string check = "0", trick1 = "0";
+    std::string check = "0", trick1 = "0", noshift = "0";
     const auto bad = [](const char *what, const std::string &v) {
         std::fprintf(stderr, "bgk2d_gb300: bad %s '%s'\n", what, v.c_str());
         return 2;
@@ -342,6 +348,7 @@ int main(int argc, char **argv)
         else if (k == "--dir") dir = v;
         else if (k == "--les") les = v;
         else if (k == "--trick1") trick1 = v;
+        else if (k == "--noshift") noshift = v;
         else if (k == "--check-input") check = v;
         else return bad("option", k);
     }
@@ -350,6 +357,7 @@ int main(int argc, char **argv)
     if (scheme != "pingpong" && scheme != "aa" && scheme != "original") return bad("--scheme", scheme);
     if (les != "0" && les != "1") return bad("--les", les);
     if (trick1 != "0" && trick1 != "1") return bad("--trick1", trick1);
+    if (noshift != "0" && noshift != "1") return bad("--noshift", noshift);
     if (check != "0" && check != "1") return bad("--check-input", check);
     auto kv = read_namelist(input);
     if (kv.empty()) { std::fprintf(stderr, "bgk2d_gb300: no &parameters namelist in %s\n", input.c_str()); return 1; }
@@ -370,6 +378,7 @@ int main(int argc, char **argv)
     d.radius = geti("radius", 16);
     d.les = les == "1";
     d.trick1 = trick1 == "1";
+    d.noshift = noshift == "1";
     d.cte_s = getd("ctes", 0.1);
     d.scheme = scheme == "aa" ? BGK_SCHEME_AA : scheme == "original" ? BGK_SCHEME_ORIGINAL : BGK_SCHEME_PINGPONG;
     if (prec == "double") { d.storage = BGK_STORE_F64; d.compute = BGK_COMPUTE_F64; }
@@ -385,9 +394,9 @@ int main(int argc, char **argv)
     if (d.tcase == BGK_CASE_TGV) d.init_v = BGK_INIT_TGV_REF;
     (void)init_v;
     if (check == "1") {
-        std::printf("case=%s prec=%s scheme=%s les=%d trick1=%d lx=%d ly=%d ipad=%d jpad=%d svisc=%.17g u0=%.17g "
+        std::printf("case=%s prec=%s scheme=%s les=%d trick1=%d noshift=%d lx=%d ly=%d ipad=%d jpad=%d svisc=%.17g u0=%.17g "
                     "ctes=%.17g radius=%d itfin=%d ivtim=%d isignal=%d itsave=%d icheck=%d irestart=%d\n",
-                    tcase.c_str(), prec.c_str(), scheme.c_str(), d.les, d.trick1, d.lx, d.ly, d.ipad, d.jpad, d.svisc, d.u0,
+                    tcase.c_str(), prec.c_str(), scheme.c_str(), d.les, d.trick1, d.noshift, d.lx, d.ly, d.ipad, d.jpad, d.svisc, d.u0,
                     d.cte_s, d.radius, itfin, ivtim, isignal, itsave, icheck, irestart);
         return 0;
     }
@@ -427,6 +436,22 @@ int main(int argc, char **argv)
         return 1;
     }
     const bool dbl = d.storage == BGK_STORE_F64;
+    const double c1 = d.noshift ? 0.0 : 1.0;  // cte1 of the host readers
+    // the readers in (storage, compute) kinds: FP64/FP64, FP32/FP64 (MIXED2), FP32/FP32 otherwise
+    // (the 16-bit kinds download FP32 values)
+    auto readers_in = [&](auto s_tag, auto k_tag, int itime, bool with_probe) {
+        using S = decltype(s_tag);
+        using K = decltype(k_tag);
+        if (with_probe) probe<S, K>(pops, lx / 2, ly / 2, fprobe, itime, (K)c1);
+        varm<S, K>(pops, fumed, itime, (K)c1);
+        prof_i<S, K>(pops, ly / 2, fpi, itime, (K)c1);
+        prof_j<S, K>(pops, lx / 2, fpj, itime, (K)c1);
+    };
+    auto readers = [&](int itime, bool with_probe) {
+        if (dbl) readers_in(0.0, 0.0, itime, with_probe);
+        else if (d.compute == BGK_COMPUTE_F64) readers_in(0.0f, 0.0, itime, with_probe);
+        else readers_in(0.0f, 0.0f, itime, with_probe);
+    };
     // SRC/diagnostic.F90:70-82 at every icheck (diagno, probe, varm, prof_i, prof_j, draglift);
     // SRC/bgk2d.F90:122-125 once after the loop (diagno, varm, prof_i, prof_j)
     auto diagnostic = [&](int itime, bool final_call) -> int {
@@ -437,17 +462,7 @@ int main(int argc, char **argv)
                      fortran_e(dg[2]).c_str(), fortran_e(dg[3]).c_str());
         std::fflush(fdiag);
         if ((r = bgk_download(h, pops.p, lx + 2))) return r;
-        if (dbl) {
-            if (!final_call) probe<double>(pops, lx / 2, ly / 2, fprobe, itime);
-            varm<double>(pops, fumed, itime);
-            prof_i<double>(pops, ly / 2, fpi, itime);
-            prof_j<double>(pops, lx / 2, fpj, itime);
-        } else {
-            if (!final_call) probe<float>(pops, lx / 2, ly / 2, fprobe, itime);
-            varm<float>(pops, fumed, itime);
-            prof_i<float>(pops, ly / 2, fpi, itime);
-            prof_j<float>(pops, lx / 2, fpj, itime);
-        }
+        readers(itime, !final_call);
         if (fdrag && !final_call) {
             double fl[2];
             if ((r = bgk_draglift_reference(h, fl))) return r;  // the reference's own sums
@@ -457,8 +472,7 @@ int main(int argc, char **argv)
     };
     if (irestart != 1) {  // SRC/initialize.F90:116-123 writes the initial profiles and velocity field
         if ((rc = bgk_download(h, pops.p, lx + 2))) return die("bgk_download", rc);
-        if (dbl) { varm<double>(pops, fumed, 0); prof_i<double>(pops, ly / 2, fpi, 0); prof_j<double>(pops, lx / 2, fpj, 0); }
-        else { varm<float>(pops, fumed, 0); prof_i<float>(pops, ly / 2, fpi, 0); prof_j<float>(pops, lx / 2, fpj, 0); }
+        readers(0, false);
         if (lx > 2 && ly > 2 && (rc = write_vtk(h, dir, 0, lx, ly, false))) return die("vtk", rc);
     }
     const auto t1 = std::chrono::steady_clock::now();

@@ -339,8 +339,9 @@ constexpr int PIPE_STEPS = 16;
 bool pipeline_ok(const bgk_handle *h)
 {
     // pulls reach one row up and one row down, nothing else: no periodic y faces (row 1 pulls
-    // from row ly), no whole-lattice boundary kernel (BFS), no two-pass form, no LES tiles
-    return h->L.scheme == BGK_SCHEME_PINGPONG && !h->two_pass && !h->cs.bfs && !h->L.les &&
+    // from row ly), no whole-lattice boundary kernel (BFS), no two-pass form, no collision
+    // variant (LES, NOSHIFT: the waves run the plain collision)
+    return h->L.scheme == BGK_SCHEME_PINGPONG && !h->two_pass && !h->cs.bfs && !h->L.les && !h->L.noshift &&
            h->cs.faces[YLO] != FK_PERIODIC && h->cs.faces[YHI] != FK_PERIODIC && h->desc.ly >= 8;
 }
 
@@ -537,6 +538,7 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
         for (int q = 0; q < 9; ++q) L.wt[f][q] = h->cs.wt[f][q];
     }
     L.corner_x = h->cs.corner_x;
+    L.noshift = h->cs.noshift;
     L.omega = h->cs.omega;
     L.fgrad = h->cs.fgrad;
     L.forced = h->cs.forced;
@@ -598,18 +600,21 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
             (h->cs.faces[XHI] == FK_OUTFLOW_EQ || h->cs.faces[XHI] == FK_OUTFLOW_ZG)) {
             if (h->T.fill_outflow(h->L, h->st) != cudaSuccess) rc = BGK_E_CUDA;
         }
-    } else if (d.init_v == BGK_INIT_TGV_REF) {
+    } else if (d.init_v == BGK_INIT_TGV_REF || (d.init_v == BGK_INIT_REST && h->cs.noshift)) {
+        // the reference's init (SRC/init.F90:83-137) on the host; the rest state of whole
+        // populations is f = w, which the zeroed planes do not hold
+        const bool vortex = d.init_v == BGK_INIT_TGV_REF, ns = h->cs.noshift != 0;
         const size_t n = (size_t)(l + 2) * (m + 2);
         void *ptrs[9];
         if (h->host_bytes == 8) {
             std::vector<double> a;
-            init_reference<double, double>(l, m, true, a);
+            init_reference<double, double>(l, m, vortex, a, ns);
             for (int q = 0; q < 9; ++q) ptrs[q] = a.data() + q * n;
             rc = upload_impl(h, ptrs, l + 2);
         } else {
             std::vector<float> a;
-            if (d.compute == BGK_COMPUTE_F64) init_reference<double, float>(l, m, true, a);
-            else init_reference<float, float>(l, m, true, a);
+            if (d.compute == BGK_COMPUTE_F64) init_reference<double, float>(l, m, vortex, a, ns);
+            else init_reference<float, float>(l, m, vortex, a, ns);
             for (int q = 0; q < 9; ++q) ptrs[q] = a.data() + q * n;
             rc = upload_impl(h, ptrs, l + 2);
         }

@@ -49,7 +49,8 @@ __global__ void scatter_plane_kernel(Lattice L, int cur, int q, const H *__restr
 
 // Pressure-corrected Taylor-Green start (BGK_INIT_TGV), computed on the device in FP64:
 // u = U0 sin(kx x) cos(ky y), v = -U0 cos(kx x) sin(ky y),
-// rho = 1 - 3 U0^2/4 (cos 2kx x + cos 2ky y), x = i - 1/2, y = j - 1/2, f - w = feq - w.
+// rho = 1 - 3 U0^2/4 (cos 2kx x + cos 2ky y), x = i - 1/2, y = j - 1/2, f - w = feq - w
+// (f = feq when the populations are stored whole, L.noshift).
 template <typename S>
 __global__ void init_tgv_kernel(Lattice L, double u0)
 {
@@ -71,7 +72,7 @@ __global__ void init_tgv_kernel(Lattice L, double u0)
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         const double cu = cx_of(q) * u + cy_of(q) * v;
-        const double f = w[q] * rho * (1.0 + 3.0 * cu + 4.5 * cu * cu - 1.5 * usq) - w[q];
+        const double f = w[q] * rho * (1.0 + 3.0 * cu + 4.5 * cu * cu - 1.5 * usq) - (L.noshift ? 0.0 : w[q]);
         const int p = L.scheme == 0 ? q : opp_of(q);
         base[p * pe + i] = Store<S>::template putq<double>(f, q);
     }
@@ -250,7 +251,7 @@ __device__ __forceinline__ void bfs_bcond_block(const Lattice &L, const int cur,
         for (int q = 0; q < 8; ++q) v[q] = Store<S>::template getq<K>(at(q, l, j), q);
 #pragma unroll
         for (int q = D10; q <= D14; ++q)
-            at(q, l + 1, j) = Store<S>::template putq<K>(outflow_eq<K>(q, v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7]), q);
+            at(q, l + 1, j) = Store<S>::template putq<K>(outflow_eq<K>(q, v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], L.noshift != 0), q);
         if (j >= stepy) {
 #pragma unroll
             for (int t = 0; t < 3; ++t) at(t, 0, j) = Store<S>::template putq<K>((K)L.inflow[(int64_t)t * (m + 2) + j], t);
@@ -295,11 +296,12 @@ __global__ void batch_bfs_kernel(const Lattice *__restrict__ lats, const int *__
     bfs_bcond_block<S, K>(lats[e.x], cur[e.x] ^ parity, e.y, e.z);
 }
 
-// moments with the reference's per-cell arithmetic (SRC/diagno.F90:82-93)
+// moments with the reference's per-cell arithmetic (SRC/diagno.F90:82-93); cte1 = 1, or 0 for
+// populations stored whole (SRC/diagno.F90:42-46)
 template <typename K>
-__device__ __forceinline__ void moments(const K (&a)[9], K &rho, K &xj, K &yj)
+__device__ __forceinline__ void moments(const K (&a)[9], K &rho, K &xj, K &yj, bool noshift)
 {
-    const K cte1 = (K)1, uno = (K)1;
+    const K cte1 = noshift ? (K)0 : (K)1, uno = (K)1;
     rho = ((((a[0] + a[1]) + a[4]) + a[5]) + (((a[2] + a[3]) + a[6]) + a[7]) + a[8]) + cte1;
     K rhoinv = uno / rho;
     xj = (((a[1] - a[5]) + (a[0] - a[4])) + (a[2] - a[6])) * rhoinv;
@@ -353,7 +355,7 @@ __global__ void __launch_bounds__(RED_NT) diagno_kernel(Lattice L, int cur, int 
 #pragma unroll
         for (int q = 0; q < 9; ++q) a[q] = post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
         K rho, xj, yj;
-        moments<K>(a, rho, xj, yj);
+        moments<K>(a, rho, xj, yj, L.noshift != 0);
         acc[0] += to_f64(xj);
         acc[1] += to_f64(yj);
         acc[2] += to_f64(rho);
@@ -379,7 +381,7 @@ __global__ void __launch_bounds__(1024) diagno_seq_kernel(Lattice L, int cur, in
 #pragma unroll
             for (int q = 0; q < 9; ++q) a[q] = post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
             K rho, xj, yj;
-            moments<K>(a, rho, xj, yj);
+            moments<K>(a, rho, xj, yj, L.noshift != 0);
             sh[0][threadIdx.x] = rho;
             sh[1][threadIdx.x] = xj;
             sh[2][threadIdx.x] = yj;
@@ -422,7 +424,7 @@ __global__ void __launch_bounds__(RED_NT) residual_kernel(Lattice L, int cur, in
 #pragma unroll
         for (int q = 0; q < 9; ++q) a[q] = post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
         K rho, xj, yj;
-        moments<K>(a, rho, xj, yj);
+        moments<K>(a, rho, xj, yj, L.noshift != 0);
         const double u = (double)xj, v = (double)yj;
         const double du = u - uprev[c], dv = v - vprev[c];
         acc[0] += du * du + dv * dv;
@@ -503,7 +505,7 @@ __global__ void fields_kernel(Lattice L, int cur, int phase, double *rho, double
 #pragma unroll
         for (int q = 0; q < 9; ++q) a[q] = post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
         K r, xj, yj;
-        moments<K>(a, r, xj, yj);
+        moments<K>(a, r, xj, yj, L.noshift != 0);
         rho[c] = (double)r;
         u[c] = (double)xj;
         v[c] = (double)yj;
@@ -528,7 +530,7 @@ __device__ __forceinline__ void vtk_sums(const Lattice &L, int cur, int phase, i
 #pragma unroll
     for (int q = 0; q < 9; ++q) a[q] = (T)post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
     const T t = ((((((((a[0] + a[1]) + a[2]) + a[3]) + a[4]) + a[5]) + a[6]) + a[7]) + a[8]);
-    den = (float)(t + (T)1.0f);
+    den = (float)(t + (T)(L.noshift ? 0.0f : 1.0f));  // + cte1 (SRC/vtk_xy.binary.F90:46-50)
     u = ((((a[D01] + a[D03]) + a[D05]) - a[D10]) - a[D12]) - a[D14];
     v = ((((a[D03] + a[D08]) + a[D12]) - a[D01]) - a[D10]) - a[D17];
 }

@@ -296,9 +296,9 @@ int bgk_batch_add(bgk_batch *b, bgk_handle *h)
     if (h->desc.storage != b->storage || h->desc.compute != b->compute || h->dev != b->dev ||
         h->L.scheme != BGK_SCHEME_PINGPONG)
         return BGK_E_INVALID;
-    // the batch kernels carry the fused one-pass step; a backward-facing step's boundary routine
-    // and the Smagorinsky members' step run as batched launches of their own
-    if (h->two_pass) return BGK_E_UNSUPPORTED;
+    // the batch kernels carry the fused one-pass step of deviations; a backward-facing step's
+    // boundary routine and the Smagorinsky members' step run as batched launches of their own
+    if (h->two_pass || h->L.noshift) return BGK_E_UNSUPPORTED;
     if (h->sticky) return h->sticky;
     enter_device(b->dev);
     if (cudaStreamSynchronize(h->st) != cudaSuccess || cudaStreamSynchronize(b->st) != cudaSuccess) return BGK_E_CUDA;

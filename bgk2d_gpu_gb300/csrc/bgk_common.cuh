@@ -198,6 +198,7 @@ struct Lattice {
     int32_t scheme;          // 0 ping-pong, 1 AA
     int32_t faces[4];        // FaceKind per face
     int32_t corner_x;        // 1: at a corner the x-face rule wins over the y-face rule (-DTRICK1)
+    int32_t noshift;         // 1: planes hold the populations f, not the deviations f - w (-DNOSHIFT)
     double wt[4][9];         // wall term added to the bounced population, per face and direction
     double omega, fgrad;     // relaxation rate and body-force gradient (compute kind)
     int32_t forced;          // 1 when the x body force fgrad*rho is applied (CHANNEL)

@@ -36,12 +36,12 @@ cudaError_t step_cfg(int kind, const Lattice &L, int parity, cudaStream_t st)
 
 // ping-pong step through shared-memory staging: one wave of blocks, each a band of T*N columns
 // and a stripe of rows
-template <typename S, typename K, int T, int STAGES, bool OBS, bool LES = false, int MINB = 0>
+template <typename S, typename K, int T, int STAGES, bool OBS, int CV = 0, int MINB = 0>
 cudaError_t step_staged(const Lattice &L, int parity, cudaStream_t st)
 {
     constexpr int N = vec_of<S>() / 2;
     constexpr size_t smem = staged_smem_bytes<S, T, N, STAGES>();
-    auto kern = pp_staged_kernel<S, K, T, N, STAGES, OBS, LES, MINB>;
+    auto kern = pp_staged_kernel<S, K, T, N, STAGES, OBS, CV, MINB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     // A stripe of STAGES rows per block: every copy of the block is issued at once, and the
@@ -55,8 +55,9 @@ cudaError_t step_staged(const Lattice &L, int parity, cudaStream_t st)
     return cudaGetLastError();
 }
 
-// steps with the Smagorinsky collision: their own instantiation (128 x 1 threads, a whole vector
-// per thread), so that the eddy-viscosity code takes no registers from the plain kernels
+// steps with a collision variant (CV_LES, CV_NOSHIFT or both): their own instantiation (128 x 1
+// threads, a whole vector per thread), so that the variant's code takes no registers from the
+// plain kernels
 template <typename S, typename K, bool OBS, int N, int MINB>
 cudaError_t les16_launch(const Lattice &L, int parity, cudaStream_t st)
 {
@@ -65,8 +66,8 @@ cudaError_t les16_launch(const Lattice &L, int parity, cudaStream_t st)
     return cudaGetLastError();
 }
 
-template <typename S, typename K, bool OBS>
-cudaError_t step_les(int kind, const Lattice &L, int parity, int cfg, cudaStream_t st)
+template <typename S, typename K, bool OBS, int CV>
+cudaError_t step_cv(int kind, const Lattice &L, int parity, int cfg, cudaStream_t st)
 {
     const dim3 block(128, 1);
     // 16-bit ping-pong: register budgets tried by the autotuner (tile configuration 0-3): 4 cells
@@ -79,29 +80,38 @@ cudaError_t step_les(int kind, const Lattice &L, int parity, int cfg, cudaStream
             if (cfg == 1) return les16_launch<S, K, OBS, vec_of<S>() / 2, 6>(L, parity, st);
             if (cfg == 2) return les16_launch<S, K, OBS, vec_of<S>(), 4>(L, parity, st);
             if (cfg == 3) return les16_launch<S, K, OBS, vec_of<S>(), 3>(L, parity, st);
-            if (cfg == 4) return step_staged<S, K, 128, 4, OBS, true, 5>(L, parity, st);
-            return step_staged<S, K, 128, 3, OBS, true, 6>(L, parity, st);
+            if (cfg == 4) return step_staged<S, K, 128, 4, OBS, CV_LES, 5>(L, parity, st);
+            return step_staged<S, K, 128, 3, OBS, CV_LES, 6>(L, parity, st);
         }
     }
     // staged configurations of a single-domain ping-pong step (6-8): one staged LES shape
-    if (kind == STEP_PP && cfg >= NUM_CFG) return step_staged<S, K, 128, 4, OBS, true>(L, parity, st);
+    if constexpr (CV == CV_LES)
+        if (kind == STEP_PP && cfg >= NUM_CFG) return step_staged<S, K, 128, 4, OBS, CV_LES>(L, parity, st);
     // 16-bit kinds: 8 bytes per thread and plane (64 registers, 8 blocks per SM), the fastest shape
     // of their non-LES step; the 32/64-bit kinds: 16 bytes
     constexpr int N = Is16<S>::value ? vec_of<S>() / 2 : vec_of<S>();
     const int nv = (L.lx + N - 1) / N;
     const dim3 grid((unsigned)((nv + 127) / 128), (unsigned)L.ly);
-    if (kind == STEP_PP) pp_kernel<S, K, 128, 1, OBS, N, true><<<grid, block, 0, st>>>(L, parity);
-    else if (kind == STEP_STREAM) pp_kernel<S, K, 128, 1, OBS, N, false, false><<<grid, block, 0, st>>>(L, parity);
-    else if (kind == STEP_COLLIDE) col_kernel<S, K, 128, 1, N, true><<<grid, block, 0, st>>>(L, parity);
-    else if (kind == STEP_AA_P) aa_p_kernel<S, K, 128, 1, OBS, true, N><<<grid, block, 0, st>>>(L);
-    else aa_l_kernel<S, K, 128, 1, OBS, true, N><<<grid, block, 0, st>>>(L);
+    if (kind == STEP_PP) pp_kernel<S, K, 128, 1, OBS, N, CV><<<grid, block, 0, st>>>(L, parity);
+    else if (kind == STEP_STREAM) pp_kernel<S, K, 128, 1, OBS, N, 0, false><<<grid, block, 0, st>>>(L, parity);
+    else if (kind == STEP_COLLIDE) col_kernel<S, K, 128, 1, N, CV><<<grid, block, 0, st>>>(L, parity);
+    else if (kind == STEP_AA_P) aa_p_kernel<S, K, 128, 1, OBS, CV, N><<<grid, block, 0, st>>>(L);
+    else aa_l_kernel<S, K, 128, 1, OBS, CV, N><<<grid, block, 0, st>>>(L);
     return cudaGetLastError();
 }
 
 template <typename S, typename K, bool OBS>
 cudaError_t step_obs(int kind, const Lattice &L, int parity, int cfg, cudaStream_t st)
 {
-    if (L.les) return step_les<S, K, OBS>(kind, L, parity, cfg, st);
+    if (L.les || L.noshift) {
+        // whole-population storage exists for the exact kinds only (bgk_create refuses the rest)
+        if constexpr (!Is16<S>::value) {
+            if (L.noshift)
+                return L.les ? step_cv<S, K, OBS, CV_LES | CV_NOSHIFT>(kind, L, parity, cfg, st)
+                             : step_cv<S, K, OBS, CV_NOSHIFT>(kind, L, parity, cfg, st);
+        }
+        return step_cv<S, K, OBS, CV_LES>(kind, L, parity, cfg, st);
+    }
     if (kind == STEP_PP && cfg >= NUM_CFG) {
         if (cfg == 6) return step_staged<S, K, 128, 3, OBS>(L, parity, st);
         if (cfg == 7) return step_staged<S, K, 128, 4, OBS>(L, parity, st);

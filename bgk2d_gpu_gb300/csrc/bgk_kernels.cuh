@@ -20,7 +20,8 @@
 // Each thread updates N consecutive cells of a row with 8- or 16-byte vector accesses; the +-x
 // neighbours come from adjacent lanes.  A block may first ask for an L2 prefetch of the rows of
 // the block a set distance ahead in launch order (prefetch_tile).  The collision with the
-// Smagorinsky eddy viscosity is a template parameter (LES), instantiated separately.
+// Smagorinsky eddy viscosity and whole-population storage are template parameters (the
+// collision variant CV: CV_LES, CV_NOSHIFT), instantiated separately.
 //
 // All arithmetic is one IEEE operation per reference operation: this file is compiled with
 // -fmad=false for the FP32/FP64 kinds so that results are bit-identical to the reference's
@@ -30,6 +31,12 @@
 #include "bgk_common.cuh"
 
 namespace bgk {
+
+// Collision variants (bits of the template parameter CV of the step kernels):
+// CV_LES      the Smagorinsky eddy viscosity of -DLES (SRC/col_MC.F90:178-248);
+// CV_NOSHIFT  the planes hold the populations f themselves, not f - w (-DNOSHIFT,
+//             SRC/col_MC.F90:70-75): cte1 = 0 and cte0 = 1 in the collision.  FP32/FP64 kinds only.
+constexpr int CV_LES = 1, CV_NOSHIFT = 2;
 
 // ---------------------------------------------------------------------------------------------
 // collision: SRC/col_MC.F90:128-176 (equilibrium) and :285-293 (relaxation + body force)
@@ -65,15 +72,26 @@ __device__ __forceinline__ K add_zero(K y)
     }
 }
 
-template <typename K, bool LES = false>
+// x + 0 * d as the IEEE operations give it: 0 * d is +0 for d >= +0 and -0 for d <= -0, and adding
+// -0 changes nothing.  The FP64 kind selects on the sign bits, the FP32 kind keeps the operations.
+template <typename K>
+__device__ __forceinline__ K add_zero_times(K x, K d)
+{
+    if constexpr (sizeof(K) == 8) return (__double_as_longlong(d) < 0) ? x : add_zero(x);
+    else return x + (K)0 * d;
+}
+
+template <typename K, int CV = 0>
 __device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced, K cte_s = (K)0)
 {
+    constexpr bool NS = (CV & CV_NOSHIFT) != 0;
     const K uno = (K)1, cte1 = (K)1;  // cte0 = uno - cte1 = +0: cte0 + z is add_zero(z)
     const K tre = (K)3, qf = (K)1.5, rf = (K)3;
     const K p0 = (K)(4.0 / 9.0), p1 = (K)(1.0 / 9.0), p2 = (K)(1.0 / 36.0);
     K x01 = x[0], x03 = x[1], x05 = x[2], x08 = x[3], x10 = x[4];
     K x12 = x[5], x14 = x[6], x17 = x[7], x19 = x[8];
-    K rho = ((((x01 + x03) + x10) + x12) + (((x05 + x08) + x14) + x17) + x19) + cte1;
+    const K sum = (((x01 + x03) + x10) + x12) + (((x05 + x08) + x14) + x17) + x19;
+    K rho = NS ? add_zero(sum) : sum + cte1;  // NOSHIFT: cte1 = 0
     K rhoinv = uno / rho;
     K vx = (((x03 - x12) + (x01 - x10)) + (x05 - x14)) * rhoinv;
     K vy = (((x03 - x01) + (x12 - x10)) + (x08 - x17)) * rhoinv;
@@ -82,11 +100,13 @@ __device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced
     K vsq = vx2 + vy2;
     K vxpy = vx + vy;
     K vxmy = vx - vy;
-    K qxpy = add_zero(qf * ((tre * vxpy) * vxpy - vsq));
-    K qxmy = add_zero(qf * ((tre * vxmy) * vxmy - vsq));
-    K qx = add_zero(qf * (tre * vx2 - vsq));
-    K qy = add_zero(qf * (tre * vy2 - vsq));
-    K q0 = add_zero(qf * (-vsq));
+    // cte0 + z: cte0 = +0 (add_zero), or 1 under NOSHIFT
+    auto cte0_plus = [&](K z) -> K { return NS ? uno + z : add_zero(z); };
+    K qxpy = cte0_plus(qf * ((tre * vxpy) * vxpy - vsq));
+    K qxmy = cte0_plus(qf * ((tre * vxmy) * vxmy - vsq));
+    K qx = cte0_plus(qf * (tre * vx2 - vsq));
+    K qy = cte0_plus(qf * (tre * vy2 - vsq));
+    K q0 = cte0_plus(qf * (-vsq));
     vx = rf * vx;
     vy = rf * vy;
     vxpy = rf * vxpy;
@@ -94,16 +114,18 @@ __device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced
     K rp0 = rho * p0;
     K rp1 = rho * p1;
     K rp2 = rho * p2;
-    K e01 = rp2 * (vxmy + qxmy) + cte1 * (rp2 - p2);
-    K e03 = rp2 * (vxpy + qxpy) + cte1 * (rp2 - p2);
-    K e05 = rp1 * (vx + qx) + cte1 * (rp1 - p1);
-    K e08 = rp1 * (vy + qy) + cte1 * (rp1 - p1);
-    K e10 = rp2 * (-vxpy + qxpy) + cte1 * (rp2 - p2);
-    K e12 = rp2 * (-vxmy + qxmy) + cte1 * (rp2 - p2);
-    K e14 = rp1 * (-vx + qx) + cte1 * (rp1 - p1);
-    K e17 = rp1 * (-vy + qy) + cte1 * (rp1 - p1);
-    K e19 = rp0 * (q0) + cte1 * (rp0 - p0);
-    if constexpr (LES) omega = les_omega<K>(x01 - e01, x03 - e03, x05 - e05, x08 - e08, x10 - e10, x12 - e12, x14 - e14,
+    // + cte1 * (rp - p): cte1 = 1, or 0 under NOSHIFT
+    auto eq = [&](K z, K d) -> K { return NS ? add_zero_times(z, d) : z + cte1 * d; };
+    K e01 = eq(rp2 * (vxmy + qxmy), rp2 - p2);
+    K e03 = eq(rp2 * (vxpy + qxpy), rp2 - p2);
+    K e05 = eq(rp1 * (vx + qx), rp1 - p1);
+    K e08 = eq(rp1 * (vy + qy), rp1 - p1);
+    K e10 = eq(rp2 * (-vxpy + qxpy), rp2 - p2);
+    K e12 = eq(rp2 * (-vxmy + qxmy), rp2 - p2);
+    K e14 = eq(rp1 * (-vx + qx), rp1 - p1);
+    K e17 = eq(rp1 * (-vy + qy), rp1 - p1);
+    K e19 = eq(rp0 * (q0), rp0 - p0);
+    if constexpr ((CV & CV_LES) != 0) omega = les_omega<K>(x01 - e01, x03 - e03, x05 - e05, x08 - e08, x10 - e10, x12 - e12, x14 - e14,
                                   x17 - e17, omega, cte_s);
     if (forced || sizeof(K) == 4) {
         const K fx = forced ? fgrad * rho : (K)0, fy = (K)0;
@@ -293,26 +315,28 @@ template <> __device__ __forceinline__ F2 les_rate<F2>(F2 p2, float omega, float
 }
 
 // collision on unscaled deviations in compute kind K, for any storage kind
-template <typename S, typename K, bool LES = false>
+template <typename S, typename K, int CV = 0>
 __device__ __forceinline__ void collide_stored(K (&v)[9], K omega, K fgrad, bool forced, K cte_s)
 {
     if constexpr (Is16<S>::value) {
+        static_assert((CV & CV_NOSHIFT) == 0, "the 16-bit kinds store scaled deviations only");
         float D[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) D[q] = (float)v[q] * scale_of(q);  // exact: powers of two
-        collide_scaled<float, LES>(D, (float)omega, (float)fgrad, forced, (float)cte_s);
+        collide_scaled<float, (CV & CV_LES) != 0>(D, (float)omega, (float)fgrad, forced, (float)cte_s);
 #pragma unroll
         for (int q = 0; q < 9; ++q) v[q] = (K)(D[q] * (1.0f / scale_of(q)));
     } else {
-        collide<K, LES>(v, omega, fgrad, forced, cte_s);
+        collide<K, CV>(v, omega, fgrad, forced, cte_s);
     }
 }
 
-// equilibrium deviation of the outflow ghost (rho = 1, local u): bcond.inflow.F90:80-99
+// equilibrium deviation of the outflow ghost (rho = 1, local u): bcond.inflow.F90:80-99; the
+// equilibrium itself (cte1 = 1, bcond.inflow.F90:48-52) for populations stored whole
 template <typename K>
-__device__ __forceinline__ K outflow_eq(int q, K a01, K a03, K a05, K a08, K a10, K a12, K a14, K a17)
+__device__ __forceinline__ K outflow_eq(int q, K a01, K a03, K a05, K a08, K a10, K a12, K a14, K a17, bool noshift)
 {
-    const K rhoinv = (K)1, crho = (K)1, cte1 = (K)0, rf = (K)3, qf = (K)1.5;
+    const K rhoinv = (K)1, crho = (K)1, cte1 = noshift ? (K)1 : (K)0, rf = (K)3, qf = (K)1.5;
     const K p1 = (K)(1.0 / 9.0), p2 = (K)(1.0 / 36.0);
     K xj = (((a03 - a12) + (a01 - a10)) + (a05 - a14)) * rhoinv;
     K yj = (((a03 - a01) + (a12 - a10)) + (a08 - a17)) * rhoinv;
@@ -485,18 +509,19 @@ __device__ __forceinline__ K pull_rule(const Lattice &L, int q, int x, int y, Pl
 }
 
 // relax N cells in place: x[q][c] holds direction q of cell c (scaled 16-bit units when RAW)
-template <typename S, typename K, bool RAW, int N = vec_of<S>(), bool LES = false>
+template <typename S, typename K, bool RAW, int N = vec_of<S>(), int CV = 0>
 __device__ __forceinline__ void relax_vec(K (&x)[9][N], K omega, K fgrad, bool forced, K cte_s)
 {
     if constexpr (RAW) {
         // two cells per packed FP32 instruction
         static_assert(N % 2 == 0, "16-bit vectors hold an even number of cells");
+        static_assert((CV & CV_NOSHIFT) == 0, "the 16-bit kinds store scaled deviations only");
 #pragma unroll
         for (int c = 0; c < N; c += 2) {
             F2 v[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) v[q] = f2_pack(x[q][c], x[q][c + 1]);
-            collide_scaled<F2, LES>(v, (float)omega, (float)fgrad, forced, (float)cte_s);
+            collide_scaled<F2, (CV & CV_LES) != 0>(v, (float)omega, (float)fgrad, forced, (float)cte_s);
 #pragma unroll
             for (int q = 0; q < 9; ++q) f2_unpack(v[q], x[q][c], x[q][c + 1]);
         }
@@ -506,7 +531,7 @@ __device__ __forceinline__ void relax_vec(K (&x)[9][N], K omega, K fgrad, bool f
             K v[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) v[q] = x[q][c];
-            collide<K, LES>(v, omega, fgrad, forced, cte_s);
+            collide<K, CV>(v, omega, fgrad, forced, cte_s);
 #pragma unroll
             for (int q = 0; q < 9; ++q) x[q][c] = v[q];
         }
@@ -561,7 +586,7 @@ __device__ __forceinline__ bool needs_rule(const Lattice &L, int x, int y)
 }
 
 // one cell with the boundary rules: reads the source buffer only, writes the destination
-template <typename S, typename K, bool HAS_OBS, bool LES = false, bool COLLIDE = true>
+template <typename S, typename K, bool HAS_OBS, int CV = 0, bool COLLIDE = true>
 __device__ void pp_cell_slow(const Lattice &L, const S *src, S *dst, int x, int y)
 {
     const int64_t pe = L.plane_elems;
@@ -575,13 +600,13 @@ __device__ void pp_cell_slow(const Lattice &L, const S *src, S *dst, int x, int 
         K a[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) a[k] = ldq<S, K>(src + k * pe, i, k);
-        return rnd<S, K>(q, outflow_eq<K>(q, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7]));
+        return rnd<S, K>(q, outflow_eq<K>(q, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], L.noshift != 0));
     };
     K v[9];
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) v[q] = pull_rule<S, K, HAS_OBS>(L, q, x, y, plane_at, own, ghost_xhi);
     v[8] = ldq<S, K>(src + D19 * pe, me, D19);
-    if constexpr (COLLIDE) collide_stored<S, K, LES>(v, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
+    if constexpr (COLLIDE) collide_stored<S, K, CV>(v, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
 #pragma unroll
     for (int q = 0; q < 9; ++q) dst[q * pe + me] = Store<S>::template putq<K>(v[q], q);
 }
@@ -603,7 +628,7 @@ __device__ __forceinline__ void pp_edge_pull(const Lattice &L, const S *src, int
         K a[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) a[k] = ldq<S, K>(src + k * pe, i, k);
-        return rnd<S, K>(q, outflow_eq<K>(q, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7]));
+        return rnd<S, K>(q, outflow_eq<K>(q, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], L.noshift != 0));
     };
     constexpr int q0 = LOW ? D01 : D10, q1 = LOW ? D03 : D12, q2 = LOW ? D05 : D14;
     const K a = pull_rule<S, K, HAS_OBS>(L, q0, x, y, plane_at, own, ghost_xhi);
@@ -637,7 +662,7 @@ __device__ __forceinline__ bool edge_cell(const Lattice &L, int x, int y)
 // vector path; cells whose inputs come from the boundary rules are then recomputed one by one
 // and overwritten (the source buffer is read-only during the step, so the recompute sees the
 // same inputs).
-template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N = vec_of<S>(), bool LES = false,
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N = vec_of<S>(), int CV = 0,
           bool COLLIDE = true>
 __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const int by, const int parity)
 {
@@ -685,7 +710,7 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
     if (right_cell)
         pp_edge_pull<S, K, HAS_OBS, RAW, false, N>(L, src, RAW ? L.lx : xv + N - 1, y, RAW ? L.lx - xv : N - 1, x);
 
-    if constexpr (COLLIDE) relax_vec<S, K, RAW, N, LES>(x, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
+    if constexpr (COLLIDE) relax_vec<S, K, RAW, N, CV>(x, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
     const int64_t me = cell_index<S>(L, xv, y);
     uint32_t rh[npair<N>()] = {};
 #pragma unroll
@@ -707,7 +732,7 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
 #pragma unroll 1
         for (int xc = xv; xc <= xe; ++xc)
             if (needs_rule<HAS_OBS>(L, xc, y) && !(RAW && ((xc == 1 && left_cell) || (xc == L.lx && right_cell))))
-                pp_cell_slow<S, K, HAS_OBS, LES, COLLIDE>(L, src, dst, xc, y);
+                pp_cell_slow<S, K, HAS_OBS, CV, COLLIDE>(L, src, dst, xc, y);
     }
 }
 
@@ -750,11 +775,11 @@ __device__ __forceinline__ void prefetch_tile(const Lattice &L, const int parity
 
 // COLLIDE = false: the streaming half of the two-pass form (SRC/movef.F90 with the boundary
 // rules folded in, the rest population copied); the collision then runs in col_kernel.
-template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N, bool LES = false, bool COLLIDE = true>
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int N, int CV = 0, bool COLLIDE = true>
 __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 || (sizeof(S) == 4 && N == 4)) ? 8 : (sizeof(S) == 2 ? 4 : 1)) pp_kernel(const Lattice L, const int parity)
 {
     if (L.pf_ahead > 0) prefetch_tile<S, TXV, TY, N, PF_PP>(L, parity);
-    pp_tile<S, K, TXV, TY, HAS_OBS, N, LES, COLLIDE>(L, blockIdx.x, tile_row(blockIdx.y, gridDim.y), parity);
+    pp_tile<S, K, TXV, TY, HAS_OBS, N, CV, COLLIDE>(L, blockIdx.x, tile_row(blockIdx.y, gridDim.y), parity);
 }
 
 // The Smagorinsky ping-pong step of the 16-bit kinds with an explicit register budget (MINB
@@ -764,7 +789,7 @@ template <typename S, typename K, bool HAS_OBS, int N, int MINB>
 __global__ void __launch_bounds__(128, MINB) pp_les_kernel(const Lattice L, const int parity)
 {
     if (L.pf_ahead > 0) prefetch_tile<S, 128, 1, N, PF_PP>(L, parity);
-    pp_tile<S, K, 128, 1, HAS_OBS, N, true>(L, blockIdx.x, tile_row(blockIdx.y, gridDim.y), parity);
+    pp_tile<S, K, 128, 1, HAS_OBS, N, CV_LES>(L, blockIdx.x, tile_row(blockIdx.y, gridDim.y), parity);
 }
 
 // Persistent ping-pong step over many lattices.  The work list holds (lattice, tile x, tile y)
@@ -882,7 +907,7 @@ __device__ __forceinline__ void aa_incoming(const Lattice &L, S *base, int x, in
             }
             K v = (L.faces[XHI] == FK_OUTFLOW_ZG)
                       ? g[q]
-                      : outflow_eq<K>(q, g[0], g[1], g[2], g[3], g[4], g[5], g[6], g[7]);
+                      : outflow_eq<K>(q, g[0], g[1], g[2], g[3], g[4], g[5], g[6], g[7], L.noshift != 0);
             base[q * pe + cell_index<S>(L, l, ty)] = Store<S>::template putq<K>(v, q);
         }
     }
@@ -899,12 +924,12 @@ __device__ __forceinline__ void aa_outflow_ghost(const Lattice &L, S *base, int 
     for (int t = 0; t < 3; ++t) {
         const int q = t == 0 ? D10 : t == 1 ? D12 : D14;
         K v = (L.faces[XHI] == FK_OUTFLOW_ZG) ? g[q]
-                                              : outflow_eq<K>(q, g[0], g[1], g[2], g[3], g[4], g[5], g[6], g[7]);
+                                              : outflow_eq<K>(q, g[0], g[1], g[2], g[3], g[4], g[5], g[6], g[7], L.noshift != 0);
         base[opp_of(q) * pe + cell_index<S>(L, l + 1, y)] = Store<S>::template putq<K>(v, q);
     }
 }
 
-template <typename S, typename K, bool HAS_OBS, bool LES = false>
+template <typename S, typename K, bool HAS_OBS, int CV = 0>
 __device__ void aa_p_cell_slow(const Lattice &L, S *base, int x, int y)
 {
     const int64_t pe = L.plane_elems;
@@ -923,7 +948,7 @@ __device__ void aa_p_cell_slow(const Lattice &L, S *base, int x, int y)
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) v[q] = pull_rule<S, K, HAS_OBS>(L, q, x, y, plane_at, own, ghost_xhi);
     v[8] = ldq<S, K>(base + D19 * pe, me, D19);
-    collide_stored<S, K, LES>(v, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
+    collide_stored<S, K, CV>(v, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) aa_push_rule<S, K, HAS_OBS>(L, base, q, x, y, v[q]);
     base[D19 * pe + me] = Store<S>::template putq<K>(v[8], D19);
@@ -1074,7 +1099,7 @@ __device__ __forceinline__ void push_vec(const Lattice &L, S *plane, int xv, int
     }
 }
 
-template <typename S, typename K, int TXV, int TY, bool HAS_OBS, bool LES = false, int N = vec_of<S>()>
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int CV = 0, int N = vec_of<S>()>
 __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 ? 8 : (sizeof(S) == 2 ? 4 : 1)))
     aa_p_kernel(const Lattice L)
 {
@@ -1122,7 +1147,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
     const bool left_edge = (tx % W) == 0 || left_slow;
     const bool right_edge = (tx % W) == W - 1 || right_slow;
 
-    relax_vec<S, K, RAW, VEC, LES>(x, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
+    relax_vec<S, K, RAW, VEC, CV>(x, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
     K (&g)[9][VEC] = x;
     const bool store = !slow;
     uint32_t rh[npair<VEC>()] = {};
@@ -1143,11 +1168,11 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
     if (!active || !slow) return;
     const int xe = min(xv + VEC - 1, L.lx);
 #pragma unroll 1
-    for (int xc = xv; xc <= xe; ++xc) aa_p_cell_slow<S, K, HAS_OBS, LES>(L, base, xc, y);
+    for (int xc = xv; xc <= xe; ++xc) aa_p_cell_slow<S, K, HAS_OBS, CV>(L, base, xc, y);
 }
 
 // L step: local collision, phase 1 -> 0
-template <typename S, typename K, int TXV, int TY, bool HAS_OBS, bool LES = false, int N = vec_of<S>()>
+template <typename S, typename K, int TXV, int TY, bool HAS_OBS, int CV = 0, int N = vec_of<S>()>
 __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 ? 8 : (sizeof(S) == 2 ? 4 : 1)))
     aa_l_kernel(const Lattice L)
 {
@@ -1177,7 +1202,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
             K v[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) v[q] = ldq<S, K>(base + q * pe, i, q);
-            collide_stored<S, K, LES>(v, omega, fgrad, forced, lat_cte_s<K>(L));
+            collide_stored<S, K, CV>(v, omega, fgrad, forced, lat_cte_s<K>(L));
             K g[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) {
@@ -1201,7 +1226,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
             else x[q][c] = Store<S>::template getq<K>(v[c], q);
         }
     }
-    relax_vec<S, K, RAW, VEC, LES>(x, omega, fgrad, forced, lat_cte_s<K>(L));
+    relax_vec<S, K, RAW, VEC, CV>(x, omega, fgrad, forced, lat_cte_s<K>(L));
     uint32_t rh[npair<VEC>()] = {};
 #pragma unroll
     for (int j = 0; j < VEC / 2; ++j)
@@ -1245,12 +1270,12 @@ __global__ void __launch_bounds__(128, (N * sizeof(S) <= 8 || (sizeof(S) == 4 &&
                      const int parity)
 {
     const int4 tile = __ldg(tiles + blockIdx.x);
-    pp_tile<S, K, 128, 1, true, N, true>(lats[tile.x], tile.y, tile.z, __ldg(cur + tile.x) ^ parity);
+    pp_tile<S, K, 128, 1, true, N, CV_LES>(lats[tile.x], tile.y, tile.z, __ldg(cur + tile.x) ^ parity);
 }
 
 // Collision half of the two-pass form (SRC/col.F90): every interior cell of buffer `parity`
 // relaxes in place, obstacle cells included, as the reference's col loop does.
-template <typename S, typename K, int TXV, int TY, int N, bool LES = false>
+template <typename S, typename K, int TXV, int TY, int N, int CV = 0>
 __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) <= 8 || (sizeof(S) == 4 && N == 4)) ? 8 : (sizeof(S) == 2 ? 4 : 1))
     col_kernel(const Lattice L, const int parity)
 {
@@ -1272,7 +1297,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
             K v[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) v[q] = ldq<S, K>(base + q * pe, i, q);
-            collide_stored<S, K, LES>(v, omega, fgrad, forced, lat_cte_s<K>(L));
+            collide_stored<S, K, CV>(v, omega, fgrad, forced, lat_cte_s<K>(L));
 #pragma unroll
             for (int q = 0; q < 9; ++q) base[q * pe + i] = Store<S>::template putq<K>(v[q], q);
         }
@@ -1290,7 +1315,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
             else x[q][c] = Store<S>::template getq<K>(v[c], q);
         }
     }
-    relax_vec<S, K, RAW, N, LES>(x, omega, fgrad, forced, lat_cte_s<K>(L));
+    relax_vec<S, K, RAW, N, CV>(x, omega, fgrad, forced, lat_cte_s<K>(L));
     uint32_t rh[npair<N>()] = {};
 #pragma unroll
     for (int j = 0; j < N / 2; ++j) rh[j] = RAW ? cell_hash((uint32_t)me + 2 * j, (float)x[D19][2 * j]) : 0u;

@@ -22,6 +22,7 @@ struct CaseSetup {
     int bfs = 0;                    // backward-facing step: boundary kernel before each step
     int stepx = 0, stepy = 0;       // step corner (SRC/input.F90:74-75)
     int corner_x = 0;               // the x-wall rule sets the corner ghosts (-DTRICK1)
+    int noshift = 0;                // populations stored whole, not as deviations (-DNOSHIFT)
     int les;                        // Smagorinsky eddy viscosity on
     double cte_s;                   // Smagorinsky constant (compute kind)
     double u_inflow;                // compute-kind inflow speed (peak for the parabolic profile)
@@ -33,12 +34,13 @@ struct CaseSetup {
 };
 
 // equilibrium deviation of an inflow ghost at velocity (xj, 0) with rho = 1
-// (SRC/bcond.inflow.F90:101-113).  The `3.d0` literal promotes that sub-expression to double
-// even in a single-precision build, which is kept here.
+// (SRC/bcond.inflow.F90:101-113), or the equilibrium itself for populations stored whole
+// (cte1 = 1, SRC/bcond.inflow.F90:48-52).  The `3.d0` literal promotes that sub-expression to
+// double even in a single-precision build, which is kept here.
 template <typename K>
-inline void inflow_eq(K xj, K out[3])
+inline void inflow_eq(K xj, K out[3], bool noshift = false)
 {
-    const K rf = (K)3, qf = (K)1.5, crho = (K)1, cte1 = (K)0;
+    const K rf = (K)3, qf = (K)1.5, crho = (K)1, cte1 = noshift ? (K)1 : (K)0;
     const K p1 = (K)(1.0 / 9.0), p2 = (K)(1.0 / 36.0);
     const K yj = (K)0;
     const K cvsq = xj * xj + yj * yj;
@@ -83,14 +85,15 @@ inline void build_obs(int l, int m, int shape, int radius, int icoord, int jcoor
 }
 
 // initial populations (host kind H, reference layout (0:l+1, 0:m+1) per direction)
-// BGK_INIT_REST / BGK_INIT_TGV_REF: SRC/init.F90:83-137 in kind K.
+// BGK_INIT_REST / BGK_INIT_TGV_REF: SRC/init.F90:83-137 in kind K; cte1 = 1 for populations
+// stored whole (SRC/init.F90:73-77).
 template <typename K, typename H>
-inline void init_reference(int l, int m, bool vortex, std::vector<H> &out)
+inline void init_reference(int l, int m, bool vortex, std::vector<H> &out, bool noshift = false)
 {
     const size_t n = (size_t)(l + 2) * (size_t)(m + 2);
     out.assign(9 * n, (H)0);
     const K pi = (K)3.14159265358979323846f;  // default-real literal in init.F90:63
-    const K rf = (K)3, qf = (K)1.5, crho = (K)1, cte1 = (K)0;
+    const K rf = (K)3, qf = (K)1.5, crho = (K)1, cte1 = noshift ? (K)1 : (K)0;
     const K p0 = (K)(4.0 / 9.0), p1 = (K)(1.0 / 9.0), p2 = (K)(1.0 / 36.0);
     for (int j = 0; j <= m + 1; ++j) {
         const K y = (K)(((double)(K)j - 0.5) / (double)(K)m);
@@ -194,6 +197,11 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
     default:
         return "unknown test case";
     }
+    if (d.noshift) {
+        // SRC/precision.F90: the reference stores half-precision populations as deviations only
+        if (d.storage != BGK_STORE_F32 && d.storage != BGK_STORE_F64) return "noshift: FP32 or FP64 storage only";
+        cs.noshift = 1;
+    }
     if (d.trick1) {
         // the merged loop of SRC/bcond.driven.F90:43-81 indexes the lid by the wall index j = 1..m
         if (d.tcase != BGK_CASE_LDC) return "trick1: lid-driven cavity only";
@@ -220,7 +228,7 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
         for (int j = sy; j <= m + 1; ++j) {
             const K xj = ((uin * (K)(float)(j - sy)) * (K)(float)(m - j)) / (K)(float)(((m - sy) * (m - sy)) / 4);
             K e[3];
-            inflow_eq<K>(xj, e);
+            inflow_eq<K>(xj, e, d.noshift != 0);
             for (int t = 0; t < 3; ++t) cs.inflow[(size_t)t * (m + 2) + j] = (double)e[t];
         }
     }
@@ -232,7 +240,7 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
                 u = (K)(4.0 * (double)uin * yy * ((double)m - yy) / ((double)m * (double)m));
             }
             K e[3];
-            inflow_eq<K>(u, e);
+            inflow_eq<K>(u, e, d.noshift != 0);
             for (int t = 0; t < 3; ++t) cs.inflow[(size_t)t * (m + 2) + j] = (double)e[t];
         }
     }

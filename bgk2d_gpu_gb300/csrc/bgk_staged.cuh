@@ -122,10 +122,10 @@ __device__ __forceinline__ void pull_staged(const S *seg, int i0, K (&out)[N])
 }
 
 // Grid: (bands, stripes); block b.x covers columns 1 + b.x * BW .., block b.y rows
-// 1 + b.y * rows .. min(ly, (b.y + 1) * rows).  LES: the Smagorinsky collision.  MINB > 0 sets
+// 1 + b.y * rows .. min(ly, (b.y + 1) * rows).  CV: the collision variant.  MINB > 0 sets
 // the blocks per SM that the register budget is sized for (the shared-memory stages bound the
 // residency anyway, so the eddy-viscosity collision can take the registers it needs).
-template <typename S, typename K, int T, int N, int STAGES, bool HAS_OBS, bool LES = false, int MINB = 0>
+template <typename S, typename K, int T, int N, int STAGES, bool HAS_OBS, int CV = 0, int MINB = 0>
 __global__ void __launch_bounds__(T, MINB > 0 ? MINB : ((N * sizeof(S) <= 8) ? 1024 : 512) / T)
     pp_staged_kernel(const Lattice L, const int parity, const int rows)
 {
@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(T, MINB > 0 ? MINB : ((N * sizeof(S) <= 8) ? 1
             if (right_cell)
                 pp_edge_pull<S, K, HAS_OBS, RAW, false, N>(L, src, RAW ? L.lx : xv + N - 1, y, RAW ? L.lx - xv : N - 1, x);
 
-            relax_vec<S, K, RAW, N, LES>(x, omega, fgrad, forced, cte_s);
+            relax_vec<S, K, RAW, N, CV>(x, omega, fgrad, forced, cte_s);
             const int64_t me = cell_index<S>(L, xv, y);
             uint32_t rh[npair<N>()] = {};
 #pragma unroll
@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(T, MINB > 0 ? MINB : ((N * sizeof(S) <= 8) ? 1
 #pragma unroll 1
                 for (int xc = xv; xc <= xe; ++xc)
                     if (needs_rule<HAS_OBS>(L, xc, y) && !(RAW && ((xc == 1 && left_cell) || (xc == L.lx && right_cell))))
-                        pp_cell_slow<S, K, HAS_OBS, LES>(L, src, dst, xc, y);
+                        pp_cell_slow<S, K, HAS_OBS, CV>(L, src, dst, xc, y);
             }
         }
     }

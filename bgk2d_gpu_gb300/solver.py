@@ -49,7 +49,7 @@ class Solver:
                  scheme="pingpong", radius=16, obstacle=None, obs_center=(-1, -1), obs_mask=None,
                  init="rest", omega=None, u_inflow=None, inflow_profile=0, faces=None,
                  wall_u=None, tgv_u0=0.02, ipad=0, jpad=0, device=0, les=False, cte_s=0.1,
-                 trick1=False):
+                 trick1=False, noshift=False):
         L = _lib.load()
         d = CaseDesc()
         L.bgk_default_desc(ctypes.byref(d))
@@ -83,6 +83,7 @@ class Solver:
         d.les = int(bool(les))
         d.cte_s = float(cte_s)
         d.trick1 = int(bool(trick1))
+        d.noshift = int(bool(noshift))
         if faces is not None:
             for i, f in enumerate(faces):
                 d.faces[i] = _lib.FACE[f]
@@ -93,6 +94,8 @@ class Solver:
         self.lx, self.ly = int(lx), int(ly)
         self.storage, self.compute, self.scheme, self.tcase = storage, compute, scheme, tcase
         self.hdtype = np.float64 if storage == "f64" else np.float32
+        self.noshift = bool(noshift)
+        self._cte1 = 0 if noshift else 1  # the host readers' cte1 (SRC/probe.F90:40-44)
         self._L = L
         h = ctypes.c_void_p()
         rc = L.bgk_create(ctypes.byref(d), ctypes.byref(h))
@@ -289,62 +292,72 @@ class Solver:
         self._check(self._L.bgk_launch_count(self._h, ctypes.byref(n)), "launch_count")
         return n.value
 
-    # -- host-side readers of downloaded populations (reference arithmetic, storage kind) ----
+    # -- host-side readers of downloaded populations (reference arithmetic) ------------------
+    # prof_i, prof_j and varm add the stored values as they lie in the arrays, in the storage
+    # kind (real(sp) under MIXED2); cte1 and everything after it are in the compute kind.
+    # probe copies the values into compute-kind temporaries first (SRC/probe.F90:46-54).
+    def _kind(self, a):
+        """The compute kind of the reference readers for arrays `a`."""
+        return np.float64 if getattr(self, "compute", None) == "f64" else a.dtype.type
+
     def prof_j(self, icoord, pops=None):
         """u, v, rho along column icoord, j = 1..ly (SRC/prof_j.F90:47-67)."""
         a = self.download() if pops is None else pops
-        k = a.dtype.type
+        k = self._kind(a)
         c = a[:, 1:self.ly + 1, icoord]
         den = c[0] + c[1]
         for q in range(2, 8):
             den = den + c[q]
-        den = (den + c[8]) + k(1)
-        u = ((c[0] - c[4]) + (c[1] - c[5]) + (c[2] - c[6])) / den
-        v = ((c[1] - c[0]) + (c[3] - c[7]) + (c[5] - c[4])) / den
+        den = (den + c[8]).astype(k) + k(self._cte1)
+        u = ((c[0] - c[4]) + (c[1] - c[5]) + (c[2] - c[6])).astype(k) / den
+        v = ((c[1] - c[0]) + (c[3] - c[7]) + (c[5] - c[4])).astype(k) / den
         return u, v, den
 
     def prof_i(self, jcoord, pops=None):
         """u, v, rho along row jcoord, i = 1..lx (SRC/prof_i.F90:47-62)."""
         a = self.download() if pops is None else pops
-        k = a.dtype.type
+        k = self._kind(a)
         c = a[:, jcoord, 1:self.lx + 1]
         den = c[0] + c[1]
         for q in range(2, 9):
             den = den + c[q]
-        den = den + k(1)
-        u = (((((c[0] + c[1]) + c[2]) - c[4]) - c[5]) - c[6]) / den
-        v = (((((c[1] + c[3]) + c[5]) - c[0]) - c[4]) - c[7]) / den
+        den = den.astype(k) + k(self._cte1)
+        u = (((((c[0] + c[1]) + c[2]) - c[4]) - c[5]) - c[6]).astype(k) / den
+        v = (((((c[1] + c[3]) + c[5]) - c[0]) - c[4]) - c[7]).astype(k) / den
         return u, v, den
 
     def varm(self, pops=None):
         """Row means of u, w and rho (u_med.dat; SRC/varm.F90:49-88), see `varm`."""
-        return varm(self.download() if pops is None else pops, self.lx, self.ly)
+        a = self.download() if pops is None else pops
+        return varm(a, self.lx, self.ly, noshift=self.noshift, kind=self._kind(a))
 
     def probe(self, i0, j0, pops=None):
         """u, v, rho at one node (SRC/probe.F90:46-62)."""
         a = self.download() if pops is None else pops
-        x = a[:, j0, i0]
-        k = a.dtype.type
-        rho = x[0] + x[1] + x[2] + x[3] + x[4] + x[5] + x[6] + x[7] + x[8] + k(1)
+        k = self._kind(a)
+        x = a[:, j0, i0].astype(k)
+        rho = x[0] + x[1] + x[2] + x[3] + x[4] + x[5] + x[6] + x[7] + x[8] + k(self._cte1)
         xj = x[0] + x[1] + x[2] - x[4] - x[5] - x[6]
         yj = x[1] + x[3] + x[5] - x[0] - x[4] - x[7]
         return xj / rho, yj / rho, rho
 
 
-def varm(pops, lx, ly):
+def varm(pops, lx, ly, noshift=False, kind=None):
     """Row means over i = 1..lx of u, w and rho for j = 1..ly, as SRC/varm.F90:49-88 writes them to
-    u_med.dat: per cell rho = (a01 + ... + a19) + 1, rhoinv = 1/rho; the sums over i run in order
-    in the array's kind; the means are the sums times rvol = 1.0/float(lx), a default-real
-    quotient.  `pops` is the (9, ly+2, lx+2) array of `Solver.download`."""
-    k = pops.dtype.type
+    u_med.dat: per cell rho = (a01 + ... + a19) + cte1 (1, or 0 for populations stored whole,
+    SRC/varm.F90:42-46), the sum in the arrays' kind and the rest in the compute kind `kind`
+    (default: the arrays' kind), rhoinv = 1/rho; the sums over i run in order in the compute
+    kind; the means are the sums times rvol = 1.0/float(lx), a default-real quotient.  `pops` is
+    the (9, ly+2, lx+2) array of `Solver.download`."""
+    k = kind or pops.dtype.type
     x = pops[:, 1:ly + 1, 1:lx + 1]
     rho = x[0] + x[1]
     for q in range(2, 9):
         rho = rho + x[q]
-    rho = rho + k(1)
+    rho = rho.astype(k) + k(0 if noshift else 1)
     rinv = k(1) / rho
-    uu = (((((x[0] + x[1]) + x[2]) - x[4]) - x[5]) - x[6]) * rinv
-    ww = (((((x[1] + x[3]) + x[5]) - x[0]) - x[4]) - x[7]) * rinv
+    uu = (((((x[0] + x[1]) + x[2]) - x[4]) - x[5]) - x[6]).astype(k) * rinv
+    ww = (((((x[1] + x[3]) + x[5]) - x[0]) - x[4]) - x[7]).astype(k) * rinv
     u = np.zeros(ly, dtype=k)
     w = np.zeros(ly, dtype=k)
     den = np.zeros(ly, dtype=k)

@@ -123,7 +123,11 @@ typedef struct bgk_case_desc {
                                  (SRC/bcond.driven.F90:43-81): its merged loop lets the side walls
                                  set the two upper corner ghosts, which then carry no lid term.
                                  BGK_CASE_LDC on a square box only (SRC/check_case.F90:173-178) */
-    int32_t reserved[3];
+    int32_t noshift;          /* 1: the reference's -DNOSHIFT build: the arrays hold the populations
+                                 f themselves instead of the deviations f - w (SRC/col_MC.F90:70-75,
+                                 SRC/init.F90:73-77, SRC/diagno.F90:42-46, ...).  FP32 and FP64
+                                 storage only; ping-pong, AA and two-pass; not in batches */
+    int32_t reserved[2];
 } bgk_case_desc;
 
 typedef struct bgk_handle bgk_handle;

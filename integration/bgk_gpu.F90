@@ -43,7 +43,8 @@ module bgk_gpu
      integer(c_int)  :: les
      real(c_double)  :: cte_s
      integer(c_int)  :: trick1
-     integer(c_int)  :: reserved(3)
+     integer(c_int)  :: noshift
+     integer(c_int)  :: reserved(2)
   end type bgk_case_desc
 
   interface

@@ -57,6 +57,8 @@ typedef struct {
     double cte_s;      /* namelist cteS (SRC/input.F90:55), rounded to mykind */
     int trick1;        /* 1: the merged lid-cavity boundary loop of -DTRICK1 (SRC/bcond.driven.F90:43-81);
                         * LDC on a square box only (SRC/check_case.F90:173-178) */
+    int noshift;       /* 1: -DNOSHIFT, the populations f themselves are stored instead of f - w
+                        * (cte1/cte0 of SRC/col_MC.F90:70-75, SRC/init.F90:73-77, ...) */
 } orc_params;
 
 orc_state *orc_create(const orc_params *p);

@@ -26,14 +26,15 @@
 #define P1 ((K)(1.0 / 9.0))
 #define P2 ((K)(1.0 / 36.0))
 
-/* init.F90:33-137 (NOSHIFT off: cte1 = 0; rest flow, or the periodic vortex under PERIODIC) */
+/* init.F90:33-137 (cte1 = 0, or 1 under NOSHIFT: init.F90:73-77; rest flow, or the periodic
+ * vortex under PERIODIC) */
 static void FN(init)(orc_state *s)
 {
     const int l = s->l, m = s->m;
     /* parameter(pi=3.1415...) is a default-real literal: it is rounded to REAL(4) */
     const K pi = (K)3.14159265358979323846f;
     const K crho = (K)1;
-    const K cte1 = ZERO;
+    const K cte1 = s->p.noshift ? UNO : ZERO;
     K xj = (K)0, yj = (K)0;
     for (int j = 0; j <= m + 1; ++j) {
         K y = (K)(((double)(K)j - 0.5) / (double)(K)m);
@@ -217,7 +218,7 @@ static void FN(bcond_channel)(orc_state *s)
 static void FN(outflow_col)(orc_state *s, int j)
 {
     const int l = s->l, l1 = l + 1;
-    const K crho = UNO, rhoinv = UNO, cte1 = ZERO;
+    const K crho = UNO, rhoinv = UNO, cte1 = s->p.noshift ? UNO : ZERO;  /* bcond.inflow.F90:48-52 */
     K xj = (((RA(1, l, j) - RA(5, l, j)) + (RA(0, l, j) - RA(4, l, j))) + (RA(2, l, j) - RA(6, l, j))) * rhoinv;
     K yj = (((RA(1, l, j) - RA(0, l, j)) + (RA(5, l, j) - RA(4, l, j))) + (RA(3, l, j) - RA(7, l, j))) * rhoinv;
     K cvsq = xj * xj + yj * yj;
@@ -232,7 +233,7 @@ static void FN(outflow_col)(orc_state *s, int j)
 /* inflow equilibrium at velocity (xj, 0): bcond.inflow.F90:101-113, bcond.step.F90:135-150 */
 static void FN(inflow_cell)(orc_state *s, int j, K xj)
 {
-    const K crho = UNO, cte1 = ZERO;
+    const K crho = UNO, cte1 = s->p.noshift ? UNO : ZERO;
     K yj = ZERO;
     K cvsq = xj * xj + yj * yj;
     double dc = (double)cvsq;
@@ -379,10 +380,11 @@ static void FN(boundaries)(orc_state *s)
 }
 
 /* col_MC.F90:114-176 / col.F90:90-152 (equilibrium) and :285-293 / :229-237 (relaxation);
- * x[] holds x01..x19, out[] receives the nine post-collision values in mykind */
-static inline void FN(collide)(const K *x, K omega, K fgrad, int forced, int les, K cte_s, K *out)
+ * x[] holds x01..x19, out[] receives the nine post-collision values in mykind.  cte1 = 1, or 0
+ * under NOSHIFT (col_MC.F90:70-75, col.F90:61-66), and cte0 = 1 - cte1 */
+static inline void FN(collide)(const K *x, K omega, K fgrad, int forced, int les, K cte_s, int noshift, K *out)
 {
-    const K cte1 = UNO, cte0 = UNO - cte1;
+    const K cte1 = noshift ? ZERO : UNO, cte0 = UNO - cte1;
     K x01 = x[0], x03 = x[1], x05 = x[2], x08 = x[3], x10 = x[4];
     K x12 = x[5], x14 = x[6], x17 = x[7], x19 = x[8];
     K rho = ((((x01 + x03) + x10) + x12) + (((x05 + x08) + x14) + x17) + x19) + cte1;
@@ -449,7 +451,7 @@ static inline void FN(collide)(const K *x, K omega, K fgrad, int forced, int les
  * runs several cells per SIMD instruction (each cell's IEEE operations are unchanged) */
 static void FN(col_MC_rows_plain)(orc_state *s, int j0, int j1)
 {
-    const int l = s->l;
+    const int l = s->l, noshift = s->p.noshift;
     const size_t ld = (size_t)s->ld;
     const K omega = (K)s->omega;
     for (int j = j0; j <= j1; ++j) {
@@ -474,7 +476,7 @@ static void FN(col_MC_rows_plain)(orc_state *s, int j0, int j1)
             K x[9], o[9];
             x[0] = (K)p01[i]; x[1] = (K)p03[i]; x[2] = (K)p05[i]; x[3] = (K)p08[i]; x[4] = (K)p10[i];
             x[5] = (K)p12[i]; x[6] = (K)p14[i]; x[7] = (K)p17[i]; x[8] = (K)p19[i];
-            FN(collide)(x, omega, ZERO, 0, 0, ZERO, o);
+            FN(collide)(x, omega, ZERO, 0, 0, ZERO, noshift, o);
             b01[i] = (S)o[0]; b03[i] = (S)o[1]; b05[i] = (S)o[2]; b08[i] = (S)o[3];
             b10[i] = (S)o[4]; b12[i] = (S)o[5]; b14[i] = (S)o[6]; b17[i] = (S)o[7];
             p19[i] = (S)o[8];
@@ -504,7 +506,7 @@ static void FN(col_MC_rows)(orc_state *s, int j0, int j1)
             x[6] = RA(6, i + 1, j);
             x[7] = RA(7, i, j + 1);
             x[8] = RA(8, i, j);
-            FN(collide)(x, omega, fgrad, forced, les, cte_s, o);
+            FN(collide)(x, omega, fgrad, forced, les, cte_s, s->p.noshift, o);
             for (int q = 0; q < 8; ++q) B_(q, i, j) = (S)o[q];
             A_(8, i, j) = (S)o[8];
         }
@@ -539,7 +541,7 @@ static void FN(movef_col)(orc_state *s)
         for (int i = 1; i <= l; ++i) {
             for (int q = 0; q < 8; ++q) x[q] = RB(q, i, j);
             x[8] = RA(8, i, j);
-            FN(collide)(x, omega, fgrad, forced, les, cte_s, o);
+            FN(collide)(x, omega, fgrad, forced, les, cte_s, s->p.noshift, o);
             for (int q = 0; q < 9; ++q) A_(q, i, j) = (S)o[q];
         }
     }
@@ -568,7 +570,7 @@ static void FN(step)(orc_state *s, int nsteps, int nthreads)
 /* per-cell moments exactly as diagno.F90:82-93 */
 static inline void FN(moments)(const orc_state *s, int i, int j, K *rho_o, K *xj_o, K *yj_o)
 {
-    const K cte1 = UNO;
+    const K cte1 = s->p.noshift ? ZERO : UNO;  /* diagno.F90:42-46 */
     K x01 = RA(0, i, j), x03 = RA(1, i, j), x05 = RA(2, i, j), x08 = RA(3, i, j);
     K x10 = RA(4, i, j), x12 = RA(5, i, j), x14 = RA(6, i, j), x17 = RA(7, i, j);
     K x19 = RA(8, i, j);
@@ -653,15 +655,19 @@ static void FN(draglift)(const orc_state *s, int mode, double *out)
     else { out[0] = fD[0] * (double)norm; out[1] = fD[1] * (double)norm; }
 }
 
-/* prof_j.F90:47-67 */
+/* prof_j.F90:47-67.  The a?? arrays are read directly, so their sums run in the storage kind S
+ * (real(sp) in MIXED2); adding cte1 (mykind) and the divisions by den (mykind) run in K. */
 static void FN(prof_j)(const orc_state *s, int icoord, double *u, double *v, double *den)
 {
-    const K cte1 = UNO;
+    const K cte1 = s->p.noshift ? ZERO : UNO;  /* prof_j.F90:40-44 */
     for (int j = 1; j <= s->m; ++j) {
         int i = icoord;
-        K d = ((((((((RA(0, i, j) + RA(1, i, j)) + RA(2, i, j)) + RA(3, i, j)) + RA(4, i, j)) + RA(5, i, j)) + RA(6, i, j)) + RA(7, i, j)) + RA(8, i, j)) + cte1;
-        K uu = (((RA(0, i, j) - RA(4, i, j)) + (RA(1, i, j) - RA(5, i, j))) + (RA(2, i, j) - RA(6, i, j))) / d;
-        K vv = (((RA(1, i, j) - RA(0, i, j)) + (RA(3, i, j) - RA(7, i, j))) + (RA(5, i, j) - RA(4, i, j))) / d;
+        S t = ((((((((A_(0, i, j) + A_(1, i, j)) + A_(2, i, j)) + A_(3, i, j)) + A_(4, i, j)) + A_(5, i, j)) + A_(6, i, j)) + A_(7, i, j)) + A_(8, i, j));
+        K d = (K)t + cte1;
+        S nu = ((A_(0, i, j) - A_(4, i, j)) + (A_(1, i, j) - A_(5, i, j))) + (A_(2, i, j) - A_(6, i, j));
+        S nv = ((A_(1, i, j) - A_(0, i, j)) + (A_(3, i, j) - A_(7, i, j))) + (A_(5, i, j) - A_(4, i, j));
+        K uu = (K)nu / d;
+        K vv = (K)nv / d;
         den[j - 1] = (double)d; u[j - 1] = (double)uu; v[j - 1] = (double)vv;
     }
 }
@@ -674,7 +680,7 @@ static inline float FN(vtk_den)(const orc_state *s, int i, int j)
 {
     S t = ((((((((A_(0, i, j) + A_(1, i, j)) + A_(2, i, j)) + A_(3, i, j)) + A_(4, i, j)) + A_(5, i, j)) + A_(6, i, j)) +
             A_(7, i, j)) + A_(8, i, j));
-    return (float)(t + (S)1.0f);
+    return (float)(t + (S)(s->p.noshift ? 0.0f : 1.0f));  /* cte1: vtk_xy.binary.F90:46-50 */
 }
 static inline S FN(vtk_u)(const orc_state *s, int i, int j)
 {

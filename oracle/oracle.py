@@ -36,6 +36,7 @@ class _Params(ctypes.Structure):
         ("obs_icoord", ctypes.c_int), ("obs_jcoord", ctypes.c_int),
         ("init_v", ctypes.c_int), ("svisc", ctypes.c_double), ("u0", ctypes.c_double),
         ("les", ctypes.c_int), ("cte_s", ctypes.c_double), ("trick1", ctypes.c_int),
+        ("noshift", ctypes.c_int),
     ]
 
 
@@ -96,7 +97,8 @@ class Oracle:
 
     def __init__(self, l, m, prec=SINGLE, tcase=LDC, svisc=0.1, u0=0.1, fused=True,
                  obstacle=OBS_NONE, obs_order=OBS_SNAPSHOT, radius=16,
-                 obs_icoord=-1, obs_jcoord=-1, init_v=0, les=False, cte_s=0.1, trick1=False):
+                 obs_icoord=-1, obs_jcoord=-1, init_v=0, les=False, cte_s=0.1, trick1=False,
+                 noshift=False):
         self.l, self.m, self.prec, self.tcase = l, m, prec, tcase
         # namelist values are read as mykind
         if prec == SINGLE:
@@ -104,7 +106,8 @@ class Oracle:
             u0 = float(np.float32(u0))
             cte_s = float(np.float32(cte_s))
         p = _Params(l, m, prec, tcase, int(fused), obstacle, obs_order, radius,
-                    obs_icoord, obs_jcoord, init_v, svisc, u0, int(les), cte_s, int(trick1))
+                    obs_icoord, obs_jcoord, init_v, svisc, u0, int(les), cte_s, int(trick1),
+                    int(noshift))
         self._h = lib().orc_create(ctypes.byref(p))
         if not self._h:
             raise ValueError("oracle: invalid parameters")

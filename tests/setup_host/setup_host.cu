@@ -64,17 +64,18 @@ extern "C" int host_trick1(int lx, int ly, int tcase)
 }
 
 // the nine (0:l+1, 0:m+1) population planes of the reference initial state, in the storage kind
-extern "C" void host_init(int l, int m, int vortex, int prec, void *out)
+// (deviations, or whole populations when noshift is set)
+extern "C" void host_init(int l, int m, int vortex, int prec, int noshift, void *out)
 {
     const size_t n = 9 * (size_t)(l + 2) * (size_t)(m + 2);
     if (prec == 1) {
         std::vector<double> a;
-        init_reference<double, double>(l, m, vortex != 0, a);
+        init_reference<double, double>(l, m, vortex != 0, a, noshift != 0);
         std::memcpy(out, a.data(), n * sizeof(double));
     } else {
         std::vector<float> a;
-        if (prec == 2) init_reference<double, float>(l, m, vortex != 0, a);
-        else init_reference<float, float>(l, m, vortex != 0, a);
+        if (prec == 2) init_reference<double, float>(l, m, vortex != 0, a, noshift != 0);
+        else init_reference<float, float>(l, m, vortex != 0, a, noshift != 0);
         std::memcpy(out, a.data(), n * sizeof(float));
     }
 }

@@ -241,25 +241,32 @@ def test_varm_host_reader_matches_reference_loop(dtype):
         assert u[j - 1] == su * rvol and w[j - 1] == sw * rvol and den[j - 1] == sd * rvol
 
 
-@pytest.mark.parametrize("dtype", [np.float32, np.float64])
-def test_prof_i_host_reader_matches_reference_loop(dtype):
-    """Solver.prof_i (prof_i.dat) against a cell-by-cell restatement of SRC/prof_i.F90:47-62."""
+@pytest.mark.parametrize("noshift", [False, True])
+@pytest.mark.parametrize("dtype,compute", [(np.float32, "f32"), (np.float64, "f64"), (np.float32, "f64")])
+def test_prof_i_host_reader_matches_reference_loop(dtype, compute, noshift):
+    """Solver.prof_i (prof_i.dat) against a cell-by-cell restatement of SRC/prof_i.F90:47-62: the
+    stored values summed in the storage kind, cte1 (1, or 0 for populations stored whole,
+    SRC/prof_i.F90:40-44) added and the velocities divided in the compute kind (FP64 under MIXED2)."""
     from types import SimpleNamespace
     from bgk2d_gpu_gb300.solver import Solver
     lx, ly, jc = 9, 6, 3
     rng = np.random.default_rng(4)
     a = (rng.standard_normal((9, ly + 2, lx + 2)) * 0.01).astype(dtype)
-    u, v, den = Solver.prof_i(SimpleNamespace(lx=lx, ly=ly), jc, a)
-    k = dtype
+    if noshift:
+        a = a + np.array([1 / 36, 1 / 36, 1 / 9, 1 / 9, 1 / 36, 1 / 36, 1 / 9, 1 / 9, 4 / 9], dtype)[:, None, None]
+    me = SimpleNamespace(lx=lx, ly=ly, compute=compute, _cte1=0 if noshift else 1)
+    me._kind = lambda arr: Solver._kind(me, arr)
+    u, v, den = Solver.prof_i(me, jc, a)
+    k = np.float64 if compute == "f64" else dtype
     for i in range(1, lx + 1):
         x = [a[q, jc, i] for q in range(9)]
         d = x[0]
         for q in range(1, 9):
             d = d + x[q]
-        d = d + k(1)
-        assert den[i - 1] == d
-        assert u[i - 1] == (x[0] + x[1] + x[2] - x[4] - x[5] - x[6]) / d
-        assert v[i - 1] == (x[1] + x[3] + x[5] - x[0] - x[4] - x[7]) / d
+        d = k(d) + k(0 if noshift else 1)
+        assert den[i - 1] == d and den.dtype == k
+        assert u[i - 1] == k(x[0] + x[1] + x[2] - x[4] - x[5] - x[6]) / d
+        assert v[i - 1] == k(x[1] + x[3] + x[5] - x[0] - x[4] - x[7]) / d
 
 
 def test_periodic_vortex_conserves_mass(oracle_mod):

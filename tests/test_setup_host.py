@@ -33,7 +33,7 @@ def hostlib(tmp_path_factory):
     dp = ctypes.POINTER(ctypes.c_double)
     L.host_setup.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 2 + [ctypes.c_int] * 5 + [dp, ip, ip]
     L.host_setup.restype = ctypes.c_int
-    L.host_init.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p]
+    L.host_init.argtypes = [ctypes.c_int] * 5 + [ctypes.c_void_p]
     L.host_init.restype = None
     L.host_trick1.argtypes = [ctypes.c_int] * 3
     L.host_trick1.restype = ctypes.c_int
@@ -83,19 +83,20 @@ def test_scalars_masks_and_boxes(hostlib, oracle_mod, prec, case):
         assert mask.sum() > 0 and bb.tolist() == want_bb.tolist()
 
 
+@pytest.mark.parametrize("noshift", [0, 1])
 @pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("tcase,vortex", [(LDC, 0), (TGV, 1)])
-def test_initial_state(hostlib, oracle_mod, prec, tcase, vortex):
+def test_initial_state(hostlib, oracle_mod, prec, tcase, vortex, noshift):
     O = oracle_mod
     l, m = 37, 29
-    o = O.Oracle(l, m, prec=prec, tcase=tcase, svisc=0.05, u0=0.0 if tcase == TGV else 0.1)
+    o = O.Oracle(l, m, prec=prec, tcase=tcase, svisc=0.05, u0=0.0 if tcase == TGV else 0.1, noshift=bool(noshift))
     want = o.raw()
     o.close()
     got = np.empty(want.shape, dtype=want.dtype)
-    hostlib.host_init(l, m, vortex, prec, got.ctypes.data_as(ctypes.c_void_p))
+    hostlib.host_init(l, m, vortex, prec, noshift, got.ctypes.data_as(ctypes.c_void_p))
     itype = np.uint64 if want.dtype == np.float64 else np.uint32
     assert np.array_equal(got.view(itype), want.view(itype))  # bit for bit, signs of zero included
-    if vortex:
+    if vortex or noshift:
         assert np.abs(want).max() > 0
 
 
