@@ -25,7 +25,7 @@ STATUS_NAMES = {0: "OK", 1: "BGK_E_INVALID", 2: "BGK_E_NOMEM", 3: "BGK_E_CUDA", 
 STORE = {"f32": 0, "f64": 1, "f16": 2, "bf16": 3}
 COMPUTE = {"f32": 0, "f64": 1}
 SCHEME = {"pingpong": 0, "aa": 1, "original": 2}
-CASE = {"LDC": 0, "TGV": 1, "POF": 2, "VKS": 3, "COU": 4, "BFS": 5, "CUSTOM": 9}
+CASE = {"LDC": 0, "TGV": 1, "POF": 2, "VKS": 3, "COU": 4, "BFS": 5, "MYV": 6, "CUSTOM": 9}
 FACE = {"wall": 0, "periodic": 1, "inflow": 2, "outflow_eq": 3, "outflow_zg": 4}
 OBS = {None: 0, "none": 0, "circle": 1, "square": 2, "half_circle": 3, "mask": 4}
 INIT = {"rest": 0, "tgv_ref": 1, "tgv": 2}
@@ -41,7 +41,8 @@ class CaseDesc(ctypes.Structure):
         ("obs_icoord", I32), ("obs_jcoord", I32),
         ("obs_mask", ctypes.POINTER(I32)),
         ("init_v", I32), ("tgv_u0", F64), ("device", I32), ("les", I32), ("cte_s", F64), ("trick1", I32),
-        ("noshift", I32), ("reserved", I32 * 2),
+        ("noshift", I32), ("force_y", I32),
+        ("reserved", I32 * 1),
     ]
 
 

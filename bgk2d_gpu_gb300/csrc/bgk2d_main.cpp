@@ -9,12 +9,13 @@
 // SRC/save_raw.F90), tec_xy/tec_om VTK files (SRC/vtk_xy.binary.F90, SRC/vtk_om.binary.F90, from
 // fields computed on the device) and bgk.perf.
 //
-//   bgk2d_gb300 [--input bgk.input] [--case LDC|TGV|POF|VKS|COU|BFS] [--prec single|double|mixed2|f16|bf16]
-//               [--scheme pingpong|aa|original] [--les 0|1] [--trick1 0|1] [--noshift 0|1] [--dir OUTDIR]
-//               [--check-input 0|1]
+//   bgk2d_gb300 [--input bgk.input] [--case LDC|TGV|POF|VKS|COU|BFS|MYV] [--prec single|double|mixed2|f16|bf16]
+//               [--scheme pingpong|aa|original] [--les 0|1] [--trick1 0|1] [--noshift 0|1]
+//               [--forcing-y 0|1] [--dir OUTDIR] [--check-input 0|1]
 // `--les 1` stands for the reference's -DLES build (Smagorinsky constant from the namelist key cteS),
 // `--trick1 1` for its -DTRICK1 build (lid-cavity boundaries in one merged loop; square LDC only),
-// `--noshift 1` for its -DNOSHIFT build (whole populations, not deviations; FP32/FP64 only).
+// `--noshift 1` for its -DNOSHIFT build (whole populations, not deviations; FP32/FP64 only),
+// `--forcing-y 1` for -DFORCING_Y (the POF/MYV body force along y); `--case MYV` is -DMYVERSION.
 // `--check-input 1` parses the input, prints the case it describes and exits, without a GPU.
 #include <cctype>
 #include <chrono>
@@ -333,7 +334,7 @@ int die(const char *what, int rc)
 int main(int argc, char **argv)
 {
     std::string input = "bgk.input", tcase = "LDC", prec = "single", scheme = "pingpong", dir = ".", les = "0";
-    std::string check = "0", trick1 = "0", noshift = "0";
+    std::string check = "0", trick1 = "0", noshift = "0", forcing_y = "0";
     const auto bad = [](const char *what, const std::string &v) {
         std::fprintf(stderr, "bgk2d_gb300: bad %s '%s'\n", what, v.c_str());
         return 2;
@@ -349,6 +350,7 @@ int main(int argc, char **argv)
         else if (k == "--les") les = v;
         else if (k == "--trick1") trick1 = v;
         else if (k == "--noshift") noshift = v;
+        else if (k == "--forcing-y") forcing_y = v;
         else if (k == "--check-input") check = v;
         else return bad("option", k);
     }
@@ -358,6 +360,7 @@ int main(int argc, char **argv)
     if (les != "0" && les != "1") return bad("--les", les);
     if (trick1 != "0" && trick1 != "1") return bad("--trick1", trick1);
     if (noshift != "0" && noshift != "1") return bad("--noshift", noshift);
+    if (forcing_y != "0" && forcing_y != "1") return bad("--forcing-y", forcing_y);
     if (check != "0" && check != "1") return bad("--check-input", check);
     auto kv = read_namelist(input);
     if (kv.empty()) { std::fprintf(stderr, "bgk2d_gb300: no &parameters namelist in %s\n", input.c_str()); return 1; }
@@ -379,6 +382,7 @@ int main(int argc, char **argv)
     d.les = les == "1";
     d.trick1 = trick1 == "1";
     d.noshift = noshift == "1";
+    d.force_y = forcing_y == "1";
     d.cte_s = getd("ctes", 0.1);
     d.scheme = scheme == "aa" ? BGK_SCHEME_AA : scheme == "original" ? BGK_SCHEME_ORIGINAL : BGK_SCHEME_PINGPONG;
     if (prec == "double") { d.storage = BGK_STORE_F64; d.compute = BGK_COMPUTE_F64; }
@@ -386,7 +390,8 @@ int main(int argc, char **argv)
     else if (prec == "f16") d.storage = BGK_STORE_F16;
     else if (prec == "bf16") d.storage = BGK_STORE_BF16;
     const std::map<std::string, int> cases = {{"LDC", BGK_CASE_LDC}, {"TGV", BGK_CASE_TGV}, {"POF", BGK_CASE_POF},
-                                              {"VKS", BGK_CASE_VKS}, {"COU", BGK_CASE_COU}, {"BFS", BGK_CASE_BFS}};
+                                              {"VKS", BGK_CASE_VKS}, {"COU", BGK_CASE_COU}, {"BFS", BGK_CASE_BFS},
+                                              {"MYV", BGK_CASE_MYV}};
     if (!cases.count(tcase)) { std::fprintf(stderr, "bgk2d_gb300: unknown case %s\n", tcase.c_str()); return 1; }
     d.tcase = cases.at(tcase);
     // init_v is read but, as in SRC/init.F90 (whose argument is unused), the initial state depends
@@ -394,9 +399,9 @@ int main(int argc, char **argv)
     if (d.tcase == BGK_CASE_TGV) d.init_v = BGK_INIT_TGV_REF;
     (void)init_v;
     if (check == "1") {
-        std::printf("case=%s prec=%s scheme=%s les=%d trick1=%d noshift=%d lx=%d ly=%d ipad=%d jpad=%d svisc=%.17g u0=%.17g "
+        std::printf("case=%s prec=%s scheme=%s les=%d trick1=%d noshift=%d forcing_y=%d lx=%d ly=%d ipad=%d jpad=%d svisc=%.17g u0=%.17g "
                     "ctes=%.17g radius=%d itfin=%d ivtim=%d isignal=%d itsave=%d icheck=%d irestart=%d\n",
-                    tcase.c_str(), prec.c_str(), scheme.c_str(), d.les, d.trick1, d.noshift, d.lx, d.ly, d.ipad, d.jpad, d.svisc, d.u0,
+                    tcase.c_str(), prec.c_str(), scheme.c_str(), d.les, d.trick1, d.noshift, d.force_y, d.lx, d.ly, d.ipad, d.jpad, d.svisc, d.u0,
                     d.cte_s, d.radius, itfin, ivtim, isignal, itsave, icheck, irestart);
         return 0;
     }

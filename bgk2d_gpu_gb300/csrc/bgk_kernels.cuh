@@ -82,7 +82,7 @@ __device__ __forceinline__ K add_zero_times(K x, K d)
 }
 
 template <typename K, int CV = 0>
-__device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced, K cte_s = (K)0)
+__device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, int forced, K cte_s = (K)0)
 {
     constexpr bool NS = (CV & CV_NOSHIFT) != 0;
     const K uno = (K)1, cte1 = (K)1;  // cte0 = uno - cte1 = +0: cte0 + z is add_zero(z)
@@ -128,7 +128,9 @@ __device__ __forceinline__ void collide(K (&x)[9], K omega, K fgrad, bool forced
     if constexpr ((CV & CV_LES) != 0) omega = les_omega<K>(x01 - e01, x03 - e03, x05 - e05, x08 - e08, x10 - e10, x12 - e12, x14 - e14,
                                   x17 - e17, omega, cte_s);
     if (forced || sizeof(K) == 4) {
-        const K fx = forced ? fgrad * rho : (K)0, fy = (K)0;
+        // forced: 1 along x (forcex = fgrad*rho), 2 along y (forcey, -DFORCING_Y); the other is +0
+        const K f = forced ? fgrad * rho : (K)0;
+        const K fx = forced == 2 ? (K)0 : f, fy = forced == 2 ? f : (K)0;
         x[0] = (x01 - omega * (x01 - e01)) + (fx - fy);
         x[1] = (x03 - omega * (x03 - e03)) + (fx + fy);
         x[2] = (x05 - omega * (x05 - e05)) + (fx);
@@ -215,8 +217,25 @@ template <> __device__ __forceinline__ F2 splat<F2>(float a) { return f2_pack(a,
 // (les_scaled below).
 template <typename T> __device__ __forceinline__ T les_rate(T p2, float omega, float cte_s);
 
+// Body force on scaled deviations (SRC/col_MC.F90:285-291): along x (forced = 1) +F on 01, 03, 05
+// and -F on 10, 12, 14; along y (forced = 2, -DFORCING_Y) -F on 01, 10, 17 and +F on 03, 08, 12.
+// In scaled units F is 32 F on the diagonals and 8 F on the axes, both exact.
+template <typename T>
+__device__ __forceinline__ void force_scaled(T (&D)[9], T rho, float fgrad, int forced)
+{
+    const T F = op_mul(splat<T>(fgrad), rho);
+    const T F32 = op_mul(splat<T>(32.0f), F), F8 = op_mul(splat<T>(8.0f), F);
+    if (forced == 2) {
+        D[D01] = op_sub(D[D01], F32); D[D03] = op_add(D[D03], F32); D[D08] = op_add(D[D08], F8);
+        D[D10] = op_sub(D[D10], F32); D[D12] = op_add(D[D12], F32); D[D17] = op_sub(D[D17], F8);
+    } else {
+        D[D01] = op_add(D[D01], F32); D[D03] = op_add(D[D03], F32); D[D05] = op_add(D[D05], F8);
+        D[D10] = op_sub(D[D10], F32); D[D12] = op_sub(D[D12], F32); D[D14] = op_sub(D[D14], F8);
+    }
+}
+
 template <typename T, bool LES = false>
-__device__ __forceinline__ void collide_scaled(T (&D)[9], float omega, float fgrad, bool forced, float cte_s = 0.0f)
+__device__ __forceinline__ void collide_scaled(T (&D)[9], float omega, float fgrad, int forced, float cte_s = 0.0f)
 {
     const T i32 = splat<T>(1.0f / 32.0f), i8 = splat<T>(1.0f / 8.0f);
     const T sd = op_add(op_add(D[D01], D[D03]), op_add(D[D10], D[D12]));
@@ -259,12 +278,7 @@ __device__ __forceinline__ void collide_scaled(T (&D)[9], float omega, float fgr
         const T w = les_rate<T>(p2, omega, cte_s);
 #pragma unroll
         for (int q = 0; q < 9; ++q) D[q] = op_sub(D[q], op_mul(w, N[q]));
-        if (forced) {
-            const T F = op_mul(splat<T>(fgrad), rho);
-            const T F32 = op_mul(splat<T>(32.0f), F), F8 = op_mul(splat<T>(8.0f), F);
-            D[D01] = op_add(D[D01], F32); D[D03] = op_add(D[D03], F32); D[D05] = op_add(D[D05], F8);
-            D[D10] = op_sub(D[D10], F32); D[D12] = op_sub(D[D12], F32); D[D14] = op_sub(D[D14], F8);
-        }
+        if (forced) force_scaled(D, rho, fgrad, forced);
         return;
     }
     const T omc = splat<T>(__fsub_rn(1.0f, omega)), k = splat<T>(__fmul_rn(omega, 8.0f / 9.0f));
@@ -282,13 +296,7 @@ __device__ __forceinline__ void collide_scaled(T (&D)[9], float omega, float fgr
     pair(D03, D10, op_add(kjx, kjy), op_add(ux45, uy45));
     pair(D01, D12, op_sub(kjx, kjy), op_sub(ux45, uy45));
     D[D19] = op_fma(omc, D[D19], kA);
-    if (forced) {
-        // +F on 01,03,05 and -F on 10,12,14 (SRC/col_MC.F90:285-291); 32 F and 8 F are exact
-        const T F = op_mul(splat<T>(fgrad), rho);
-        const T F32 = op_mul(splat<T>(32.0f), F), F8 = op_mul(splat<T>(8.0f), F);
-        D[D01] = op_add(D[D01], F32); D[D03] = op_add(D[D03], F32); D[D05] = op_add(D[D05], F8);
-        D[D10] = op_sub(D[D10], F32); D[D12] = op_sub(D[D12], F32); D[D14] = op_sub(D[D14], F8);
-    }
+    if (forced) force_scaled(D, rho, fgrad, forced);
 }
 
 // Smagorinsky rate of one cell from p2 = |P|^2 (SRC/col_MC.F90:178-248, as les_omega):
@@ -316,7 +324,7 @@ template <> __device__ __forceinline__ F2 les_rate<F2>(F2 p2, float omega, float
 
 // collision on unscaled deviations in compute kind K, for any storage kind
 template <typename S, typename K, int CV = 0>
-__device__ __forceinline__ void collide_stored(K (&v)[9], K omega, K fgrad, bool forced, K cte_s)
+__device__ __forceinline__ void collide_stored(K (&v)[9], K omega, K fgrad, int forced, K cte_s)
 {
     if constexpr (Is16<S>::value) {
         static_assert((CV & CV_NOSHIFT) == 0, "the 16-bit kinds store scaled deviations only");
@@ -510,7 +518,7 @@ __device__ __forceinline__ K pull_rule(const Lattice &L, int q, int x, int y, Pl
 
 // relax N cells in place: x[q][c] holds direction q of cell c (scaled 16-bit units when RAW)
 template <typename S, typename K, bool RAW, int N = vec_of<S>(), int CV = 0>
-__device__ __forceinline__ void relax_vec(K (&x)[9][N], K omega, K fgrad, bool forced, K cte_s)
+__device__ __forceinline__ void relax_vec(K (&x)[9][N], K omega, K fgrad, int forced, K cte_s)
 {
     if constexpr (RAW) {
         // two cells per packed FP32 instruction
@@ -606,7 +614,7 @@ __device__ void pp_cell_slow(const Lattice &L, const S *src, S *dst, int x, int 
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) v[q] = pull_rule<S, K, HAS_OBS>(L, q, x, y, plane_at, own, ghost_xhi);
     v[8] = ldq<S, K>(src + D19 * pe, me, D19);
-    if constexpr (COLLIDE) collide_stored<S, K, CV>(v, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
+    if constexpr (COLLIDE) collide_stored<S, K, CV>(v, lat_omega<K>(L), lat_fgrad<K>(L), L.forced, lat_cte_s<K>(L));
 #pragma unroll
     for (int q = 0; q < 9; ++q) dst[q * pe + me] = Store<S>::template putq<K>(v[q], q);
 }
@@ -710,7 +718,7 @@ __device__ __forceinline__ void pp_tile(const Lattice &L, const int bx, const in
     if (right_cell)
         pp_edge_pull<S, K, HAS_OBS, RAW, false, N>(L, src, RAW ? L.lx : xv + N - 1, y, RAW ? L.lx - xv : N - 1, x);
 
-    if constexpr (COLLIDE) relax_vec<S, K, RAW, N, CV>(x, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
+    if constexpr (COLLIDE) relax_vec<S, K, RAW, N, CV>(x, lat_omega<K>(L), lat_fgrad<K>(L), L.forced, lat_cte_s<K>(L));
     const int64_t me = cell_index<S>(L, xv, y);
     uint32_t rh[npair<N>()] = {};
 #pragma unroll
@@ -948,7 +956,7 @@ __device__ void aa_p_cell_slow(const Lattice &L, S *base, int x, int y)
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) v[q] = pull_rule<S, K, HAS_OBS>(L, q, x, y, plane_at, own, ghost_xhi);
     v[8] = ldq<S, K>(base + D19 * pe, me, D19);
-    collide_stored<S, K, CV>(v, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
+    collide_stored<S, K, CV>(v, lat_omega<K>(L), lat_fgrad<K>(L), L.forced, lat_cte_s<K>(L));
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) aa_push_rule<S, K, HAS_OBS>(L, base, q, x, y, v[q]);
     base[D19 * pe + me] = Store<S>::template putq<K>(v[8], D19);
@@ -1147,7 +1155,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
     const bool left_edge = (tx % W) == 0 || left_slow;
     const bool right_edge = (tx % W) == W - 1 || right_slow;
 
-    relax_vec<S, K, RAW, VEC, CV>(x, lat_omega<K>(L), lat_fgrad<K>(L), L.forced != 0, lat_cte_s<K>(L));
+    relax_vec<S, K, RAW, VEC, CV>(x, lat_omega<K>(L), lat_fgrad<K>(L), L.forced, lat_cte_s<K>(L));
     K (&g)[9][VEC] = x;
     const bool store = !slow;
     uint32_t rh[npair<VEC>()] = {};
@@ -1190,7 +1198,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
     bool slow = (k == nv - 1) && ((L.lx % VEC) != 0 || outflow);
     if (HAS_OBS) slow = slow || (y >= L.ob_y0 && y <= L.ob_y1 && xv + VEC - 1 >= L.ob_x0 && xv <= L.ob_x1);
     const K omega = lat_omega<K>(L), fgrad = lat_fgrad<K>(L);
-    const bool forced = L.forced != 0;
+    const int forced = L.forced;
     if (slow) {
         const int xe = min(xv + VEC - 1, L.lx);
 #pragma unroll 1
@@ -1288,7 +1296,7 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
     S *base = reinterpret_cast<S *>(L.planes) + (parity ? 9 : 0) * pe;
     const int64_t me = cell_index<S>(L, xv, y);
     const K omega = lat_omega<K>(L), fgrad = lat_fgrad<K>(L);
-    const bool forced = L.forced != 0;
+    const int forced = L.forced;
     if (k == nv - 1 && (L.lx % N) != 0) {  // ragged row end: the cells up to lx one by one
         const int xe = L.lx;
 #pragma unroll 1

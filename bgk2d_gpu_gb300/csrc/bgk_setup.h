@@ -135,7 +135,7 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
 {
     const int l = d.lx, m = d.ly;
     K u0 = (K)d.u0, svisc = (K)d.svisc, u00;
-    const bool force_case = d.tcase == BGK_CASE_POF || d.tcase == BGK_CASE_CUSTOM;
+    const bool force_case = d.tcase == BGK_CASE_POF || d.tcase == BGK_CASE_MYV || d.tcase == BGK_CASE_CUSTOM;
     if (force_case) { u00 = (K)0; }
     else { u00 = u0; u0 = (K)0; }
     K omega = ((K)1 + (K)1) / (((K)6 * svisc) + (K)1);
@@ -147,7 +147,9 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
     cs.fgrad = (double)fgrad;
     cs.u00 = (double)u00;
     cs.u0 = (double)u0;
-    cs.forced = (force_case && fgrad != (K)0) ? 1 : 0;
+    // 1: the body force along x (SRC/col_MC.F90:268-274), 2: along y (-DFORCING_Y)
+    cs.forced = (force_case && fgrad != (K)0) ? (d.force_y ? 2 : 1) : 0;
+    if (d.force_y && !force_case) return "force_y: a body-forced case only (POF, MYV or CUSTOM)";
     for (int f = 0; f < 4; ++f)
         for (int q = 0; q < 9; ++q) cs.wt[f][q] = 0.0;
     const K force = u00 / (K)6.0;  // SRC/bcond.driven.F90:41
@@ -163,6 +165,9 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
     case BGK_CASE_POF:
         cs.faces[XLO] = cs.faces[XHI] = FK_PERIODIC;
         cs.faces[YLO] = cs.faces[YHI] = FK_WALL;
+        break;
+    case BGK_CASE_MYV:  // SRC/boundaries.F90:46-48: bcond_periodic, with the volume force
+        cs.faces[XLO] = cs.faces[XHI] = cs.faces[YLO] = cs.faces[YHI] = FK_PERIODIC;
         break;
     case BGK_CASE_VKS:
         cs.faces[XLO] = FK_INFLOW;

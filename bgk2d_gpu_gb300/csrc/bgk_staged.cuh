@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(T, MINB > 0 ? MINB : ((N * sizeof(S) <= 8) ? 1
     const int xv = 1 + k * N;
     const int i0 = VEC + t * N;  // staged index of the thread's first cell
     const K omega = lat_omega<K>(L), fgrad = lat_fgrad<K>(L), cte_s = lat_cte_s<K>(L);
-    const bool forced = L.forced != 0;
+    const int forced = L.forced;
     constexpr int NW = T / 32;
 
     // No block-wide barrier per row: each warp moves on as soon as its next row has landed, and

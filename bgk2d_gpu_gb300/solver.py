@@ -49,7 +49,7 @@ class Solver:
                  scheme="pingpong", radius=16, obstacle=None, obs_center=(-1, -1), obs_mask=None,
                  init="rest", omega=None, u_inflow=None, inflow_profile=0, faces=None,
                  wall_u=None, tgv_u0=0.02, ipad=0, jpad=0, device=0, les=False, cte_s=0.1,
-                 trick1=False, noshift=False):
+                 trick1=False, noshift=False, force_y=False):
         L = _lib.load()
         d = CaseDesc()
         L.bgk_default_desc(ctypes.byref(d))
@@ -84,6 +84,7 @@ class Solver:
         d.cte_s = float(cte_s)
         d.trick1 = int(bool(trick1))
         d.noshift = int(bool(noshift))
+        d.force_y = int(bool(force_y))
         if faces is not None:
             for i, f in enumerate(faces):
                 d.faces[i] = _lib.FACE[f]

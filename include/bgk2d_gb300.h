@@ -71,6 +71,8 @@ extern "C" {
 #define BGK_CASE_COU 4     /* bcond_couette */
 #define BGK_CASE_BFS 5     /* bcond_step: backward-facing step, stepx = lx/20, stepy = ly/2
                               (SRC/input.F90:74-75); ping-pong only, lx >= 40 */
+#define BGK_CASE_MYV 6     /* -DMYVERSION: bcond_periodic with the CHANNEL body force fgrad
+                              (SRC/boundaries.F90:46-48, SRC/build.bcond.F90:39-41) */
 #define BGK_CASE_CUSTOM 9  /* faces[] and wall_u[] given explicitly */
 
 /* face kinds for BGK_CASE_CUSTOM; faces are x_lo (i=0), x_hi (i=lx+1), y_lo, y_hi */
@@ -127,7 +129,11 @@ typedef struct bgk_case_desc {
                                  f themselves instead of the deviations f - w (SRC/col_MC.F90:70-75,
                                  SRC/init.F90:73-77, SRC/diagno.F90:42-46, ...).  FP32 and FP64
                                  storage only; ping-pong, AA and two-pass; not in batches */
-    int32_t reserved[2];
+    int32_t force_y;          /* 1: the reference's -DFORCING_Y build: the body force of
+                                 BGK_CASE_POF / BGK_CASE_MYV / a forced BGK_CASE_CUSTOM acts along
+                                 y (forcey = fgrad*rho, SRC/col_MC.F90:268-282); refused for the
+                                 other cases */
+    int32_t reserved[1];
 } bgk_case_desc;
 
 typedef struct bgk_handle bgk_handle;

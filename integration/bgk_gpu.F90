@@ -22,7 +22,8 @@ module bgk_gpu
   integer(c_int), parameter :: BGK_SCHEME_PINGPONG = 0, BGK_SCHEME_AA = 1, BGK_SCHEME_ORIGINAL = 2
   ! the compile-time case flags of SRC/Makefile
   integer(c_int), parameter :: BGK_CASE_LDC = 0, BGK_CASE_TGV = 1, BGK_CASE_POF = 2, &
-                               BGK_CASE_VKS = 3, BGK_CASE_COU = 4, BGK_CASE_BFS = 5
+                               BGK_CASE_VKS = 3, BGK_CASE_COU = 4, BGK_CASE_BFS = 5, &
+                               BGK_CASE_MYV = 6
   integer(c_int), parameter :: BGK_OBS_NONE = 0, BGK_OBS_CIRCLE = 1, BGK_OBS_SQUARE = 2, &
                                BGK_OBS_HALF_CIRCLE = 3
   integer(c_int), parameter :: BGK_INIT_REST = 0, BGK_INIT_TGV_REF = 1
@@ -44,7 +45,8 @@ module bgk_gpu
      real(c_double)  :: cte_s
      integer(c_int)  :: trick1
      integer(c_int)  :: noshift
-     integer(c_int)  :: reserved(2)
+     integer(c_int)  :: force_y
+     integer(c_int)  :: reserved(1)
   end type bgk_case_desc
 
   interface

@@ -31,7 +31,9 @@ extern "C" {
 /* precision: SRC/precision.F90:13-47 */
 enum { ORC_SINGLE = 0, ORC_DOUBLE = 1, ORC_MIXED2 = 2 };
 /* test case (compile-time -D flag in the reference, SRC/Makefile:155-187) */
-enum { ORC_LDC = 0, ORC_TGV = 1, ORC_POF = 2, ORC_VKS = 3, ORC_COU = 4, ORC_BFS = 5 };
+enum { ORC_LDC = 0, ORC_TGV = 1, ORC_POF = 2, ORC_VKS = 3, ORC_COU = 4, ORC_BFS = 5,
+       ORC_MYV = 6 /* -DMYVERSION: periodic boundaries with the CHANNEL volume force
+                    * (SRC/boundaries.F90:46-48, SRC/build.bcond.F90:39-41) */ };
 /* obstacle shapes: SRC/build.obs.F90 (default circle, SQUARE, HALF_CIRCLE) */
 enum { ORC_OBS_NONE = 0, ORC_OBS_CIRCLE = 1, ORC_OBS_SQUARE = 2, ORC_OBS_HALF_CIRCLE = 3 };
 /* order of the racy in-place obstacle loop (SRC/bcond.obs.F90:59-71):
@@ -59,6 +61,8 @@ typedef struct {
                         * LDC on a square box only (SRC/check_case.F90:173-178) */
     int noshift;       /* 1: -DNOSHIFT, the populations f themselves are stored instead of f - w
                         * (cte1/cte0 of SRC/col_MC.F90:70-75, SRC/init.F90:73-77, ...) */
+    int force_y;       /* 1: -DFORCING_Y, the volume force of CHANNEL / MYVERSION acts along y
+                        * (forcey = fgrad*rho, SRC/col_MC.F90:268-282, SRC/col.F90:212-226) */
 } orc_params;
 
 orc_state *orc_create(const orc_params *p);

@@ -74,7 +74,7 @@ static void FN(setup_scalars)(orc_state *s)
     K u0 = (K)s->p.u0;
     K svisc = (K)s->p.svisc;
     K u00;
-    if (s->p.tcase == ORC_POF) { u00 = (K)0; }       /* CHANNEL: u0 is a volume force */
+    if (s->p.tcase == ORC_POF || s->p.tcase == ORC_MYV) { u00 = (K)0; }  /* CHANNEL, MYVERSION: volume force */
     else { u00 = u0; u0 = (K)0; }                     /* wall-driven */
     K omega = (UNO + UNO) / (((K)6 * svisc) + (K)1);
     K fgrad = (((K)4 * u0) * svisc) / (((K)3 * (K)s->m) * (K)s->m);
@@ -369,7 +369,7 @@ static void FN(bcond_obs)(orc_state *s)
 static void FN(boundaries)(orc_state *s)
 {
     switch (s->p.tcase) {
-    case ORC_TGV: FN(bcond_periodic)(s); break;
+    case ORC_TGV: case ORC_MYV: FN(bcond_periodic)(s); break;
     case ORC_POF: FN(bcond_channel)(s); break;
     case ORC_VKS: FN(bcond_inflow)(s); break;
     case ORC_COU: FN(bcond_couette)(s); break;
@@ -434,7 +434,8 @@ static inline void FN(collide)(const K *x, K omega, K fgrad, int forced, int les
         omega = UNO / ts;
     }
     K forcex = ZERO, forcey = ZERO;
-    if (forced) forcex = fgrad * rho;
+    if (forced == 2) forcey = fgrad * rho;  /* FORCING_Y */
+    else if (forced) forcex = fgrad * rho;
     out[0] = (x01 - omega * (x01 - e01)) + (forcex - forcey);
     out[1] = (x03 - omega * (x03 - e03)) + (forcex + forcey);
     out[2] = (x05 - omega * (x05 - e05)) + (forcex);
@@ -487,13 +488,13 @@ static void FN(col_MC_rows_plain)(orc_state *s, int j0, int j1)
 /* col_MC.F90:97-293 for rows j0..j1, then (by the caller) the pointer swap :311-341 */
 static void FN(col_MC_rows)(orc_state *s, int j0, int j1)
 {
-    if (s->p.tcase != ORC_POF && !s->p.les) {
+    if (s->p.tcase != ORC_POF && s->p.tcase != ORC_MYV && !s->p.les) {
         FN(col_MC_rows_plain)(s, j0, j1);
         return;
     }
     const int l = s->l;
     const K omega = (K)s->omega, fgrad = (K)s->fgrad, cte_s = (K)s->p.cte_s;
-    const int forced = (s->p.tcase == ORC_POF), les = s->p.les;
+    const int forced = (s->p.tcase == ORC_POF || s->p.tcase == ORC_MYV) ? (s->p.force_y ? 2 : 1) : 0, les = s->p.les;
     K x[9], o[9];
     for (int j = j0; j <= j1; ++j) {
         for (int i = 1; i <= l; ++i) {
@@ -523,7 +524,7 @@ static void FN(movef_col)(orc_state *s)
 {
     const int l = s->l, m = s->m;
     const K omega = (K)s->omega, fgrad = (K)s->fgrad, cte_s = (K)s->p.cte_s;
-    const int forced = (s->p.tcase == ORC_POF), les = s->p.les;
+    const int forced = (s->p.tcase == ORC_POF || s->p.tcase == ORC_MYV) ? (s->p.force_y ? 2 : 1) : 0, les = s->p.les;
     for (int j = 1; j <= m; ++j) {
         for (int i = 1; i <= l; ++i) {
             B_(0, i, j) = A_(0, i - 1, j + 1);

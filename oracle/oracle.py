@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libbgk_oracle.so")
 
 SINGLE, DOUBLE, MIXED2 = 0, 1, 2
-LDC, TGV, POF, VKS, COU, BFS = 0, 1, 2, 3, 4, 5
+LDC, TGV, POF, VKS, COU, BFS, MYV = 0, 1, 2, 3, 4, 5, 6
 OBS_NONE, OBS_CIRCLE, OBS_SQUARE, OBS_HALF_CIRCLE = 0, 1, 2, 3
 OBS_SERIAL, OBS_SNAPSHOT = 0, 1
 
@@ -37,6 +37,7 @@ class _Params(ctypes.Structure):
         ("init_v", ctypes.c_int), ("svisc", ctypes.c_double), ("u0", ctypes.c_double),
         ("les", ctypes.c_int), ("cte_s", ctypes.c_double), ("trick1", ctypes.c_int),
         ("noshift", ctypes.c_int),
+        ("force_y", ctypes.c_int),
     ]
 
 
@@ -98,7 +99,7 @@ class Oracle:
     def __init__(self, l, m, prec=SINGLE, tcase=LDC, svisc=0.1, u0=0.1, fused=True,
                  obstacle=OBS_NONE, obs_order=OBS_SNAPSHOT, radius=16,
                  obs_icoord=-1, obs_jcoord=-1, init_v=0, les=False, cte_s=0.1, trick1=False,
-                 noshift=False):
+                 noshift=False, force_y=False):
         self.l, self.m, self.prec, self.tcase = l, m, prec, tcase
         # namelist values are read as mykind
         if prec == SINGLE:
@@ -107,7 +108,7 @@ class Oracle:
             cte_s = float(np.float32(cte_s))
         p = _Params(l, m, prec, tcase, int(fused), obstacle, obs_order, radius,
                     obs_icoord, obs_jcoord, init_v, svisc, u0, int(les), cte_s, int(trick1),
-                    int(noshift))
+                    int(noshift), int(force_y))
         self._h = lib().orc_create(ctypes.byref(p))
         if not self._h:
             raise ValueError("oracle: invalid parameters")

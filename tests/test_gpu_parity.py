@@ -541,3 +541,32 @@ def test_noshift_bfs_les_and_limits(oracle_mod, bgk, prec):
     for st16 in ("f16", "bf16"):
         with pytest.raises(bgk.BgkError):
             bgk.Solver(64, 64, storage=st16, noshift=True)
+
+
+@pytest.mark.parametrize("scheme", ["pingpong", "aa", "original"])
+@pytest.mark.parametrize("prec", ["single", "double", "mixed2"])
+@pytest.mark.parametrize("case,force_y", [("MYV", False), ("MYV", True), ("POF", True)])
+def test_body_force_variants_bit_exact(oracle_mod, bgk, case, force_y, prec, scheme):
+    """-DMYVERSION (periodic boundaries with the CHANNEL volume force, SRC/boundaries.F90:46-48,
+    SRC/build.bcond.F90:39-41) and -DFORCING_Y (the force along y, SRC/col_MC.F90:268-282)."""
+    lx, ly = 64, 40
+    oprec, st, cp = PRECS[prec]
+    otc = oracle_mod.MYV if case == "MYV" else oracle_mod.POF
+    o = oracle_mod.Oracle(lx, ly, prec=oprec, tcase=otc, svisc=0.1, u0=0.1, fused=scheme != "original",
+                          force_y=force_y)
+    with bgk.Solver(lx, ly, tcase=case, svisc=0.1, u0=0.1, storage=st, compute=cp, scheme=scheme,
+                    force_y=force_y) as s:
+        for n in (1, 2, 40, 75):
+            s.step(n)
+            o.step(n)
+            assert_same(o, s, scheme)
+        assert list(s.diagno(2)) == list(o.diagno(0))
+        d = s.diagno()
+    # the mean flow follows the force: along x, or along y with FORCING_Y
+    assert (abs(d[1]) > 100 * abs(d[0])) if force_y else (abs(d[0]) > 100 * abs(d[1]))
+
+
+def test_force_y_needs_a_forced_case(bgk):
+    for tc in ("LDC", "TGV", "COU"):
+        with pytest.raises(bgk.BgkError):
+            bgk.Solver(64, 48, tcase=tc, force_y=True)
