@@ -115,6 +115,10 @@ def load(build_if_missing: bool = True):
         "bgk_residual": (I32, [H, P(F64)]),
         "bgk_fields": (I32, [H, P(F64), P(F64), P(F64)]),
         "bgk_vtk_fields": (I32, [H, P(F32), P(F32), P(F32), P(F32), P(F32)]),
+        "bgk_prof_i": (I32, [H, I32, P(F64), P(F64), P(F64)]),
+        "bgk_prof_j": (I32, [H, I32, P(F64), P(F64), P(F64)]),
+        "bgk_varm": (I32, [H, P(F64), P(F64), P(F64)]),
+        "bgk_probe": (I32, [H, I32, I32, P(F64)]),
         "bgk_get_obs": (I32, [H, P(I32), P(I32)]),
         "bgk_get_scalars": (I32, [H, P(F64), P(I64)]),
         "bgk_footprint": (I32, [H, P(I64), P(I32)]),

@@ -111,77 +111,57 @@ struct Pops {
     }
 };
 
-// host readers with the reference's per-cell arithmetic.  prof_i, prof_j and varm add the stored
-// values as they lie in the arrays, in the storage kind S (real(sp) under MIXED2), then add cte1
-// and divide in the compute kind K; probe copies the values into K temporaries first
-// (SRC/probe.F90:46-54).  cte1 = 1, or 0 for populations stored whole (SRC/prof_j.F90:40-44,
-// prof_i.F90:40-44, probe.F90:40-44, varm.F90:42-46).
-template <typename S, typename K>
-void prof_j(const Pops &a, int icoord, FILE *f, int itime, K cte1)
+// The profile files of SRC/prof_j.F90:84-85, SRC/prof_i.F90, SRC/probe.F90 and SRC/varm.F90 (u_med.dat),
+// from the readers computed on the device (bgk_prof_j, bgk_prof_i, bgk_probe, bgk_varm: the
+// reference's arithmetic, in its storage and compute kinds), so that a diagnostic stop moves
+// profiles over the host link instead of the nine population planes.
+int write_prof_j(bgk_handle *h, int icoord, int ly, FILE *f, int itime)
 {
+    std::vector<double> u(ly), v(ly), den(ly);
+    const int rc = bgk_prof_j(h, icoord, u.data(), v.data(), den.data());
+    if (rc) return rc;
     std::fprintf(f, "# t=%7d\n", itime);
-    for (int j = 1; j <= a.ly; ++j) {
-        S x[9];
-        for (int q = 0; q < 9; ++q) x[q] = (S)a.at(q, icoord, j);
-        K den = (K)((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8]) + cte1;
-        K u = (K)(((x[0] - x[4]) + (x[1] - x[5])) + (x[2] - x[6])) / den;
-        K v = (K)(((x[1] - x[0]) + (x[3] - x[7])) + (x[5] - x[4])) / den;
-        std::fprintf(f, "%s %s %s %s \n", fortran_e(j - 0.5).c_str(), fortran_e(u).c_str(), fortran_e(v).c_str(),
-                     fortran_e(den).c_str());
-    }
+    for (int j = 1; j <= ly; ++j)
+        std::fprintf(f, "%s %s %s %s \n", fortran_e(j - 0.5).c_str(), fortran_e(u[j - 1]).c_str(),
+                     fortran_e(v[j - 1]).c_str(), fortran_e(den[j - 1]).c_str());
     std::fprintf(f, "\n\n");
+    return BGK_OK;
 }
 
-template <typename S, typename K>
-void prof_i(const Pops &a, int jcoord, FILE *f, int itime, K cte1)
+int write_prof_i(bgk_handle *h, int jcoord, int lx, FILE *f, int itime)
 {
+    std::vector<double> u(lx), v(lx), den(lx);
+    const int rc = bgk_prof_i(h, jcoord, u.data(), v.data(), den.data());
+    if (rc) return rc;
     std::fprintf(f, "# t=%7d\n", itime);
-    for (int i = 1; i <= a.lx; ++i) {
-        S x[9];
-        for (int q = 0; q < 9; ++q) x[q] = (S)a.at(q, i, jcoord);
-        K den = (K)((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8]) + cte1;
-        K u = (K)(((((x[0] + x[1]) + x[2]) - x[4]) - x[5]) - x[6]) / den;
-        K v = (K)(((((x[1] + x[3]) + x[5]) - x[0]) - x[4]) - x[7]) / den;
-        std::fprintf(f, "%s %s %s %s \n", fortran_e(i - 0.5).c_str(), fortran_e(u).c_str(), fortran_e(v).c_str(),
-                     fortran_e(den).c_str());
-    }
+    for (int i = 1; i <= lx; ++i)
+        std::fprintf(f, "%s %s %s %s \n", fortran_e(i - 0.5).c_str(), fortran_e(u[i - 1]).c_str(),
+                     fortran_e(v[i - 1]).c_str(), fortran_e(den[i - 1]).c_str());
     std::fprintf(f, "\n\n");
+    return BGK_OK;
 }
 
-template <typename S, typename T>
-void probe(const Pops &a, int i0, int j0, FILE *f, int itime, T cte1)
+int write_probe(bgk_handle *h, int i0, int j0, FILE *f, int itime)
 {
-    T x[9];
-    for (int q = 0; q < 9; ++q) x[q] = (T)(S)a.at(q, i0, j0);
-    T rho = (((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8])) + cte1;
-    T xj = ((((x[0] + x[1]) + x[2]) - x[4]) - x[5]) - x[6];
-    T yj = ((((x[1] + x[3]) + x[5]) - x[0]) - x[4]) - x[7];
-    std::fprintf(f, "%8d%s %s %s \n", itime, fortran_e(xj / rho).c_str(), fortran_e(yj / rho).c_str(),
-                 fortran_e(rho).c_str());
+    double o[3];
+    const int rc = bgk_probe(h, i0, j0, o);
+    if (rc) return rc;
+    std::fprintf(f, "%8d%s %s %s \n", itime, fortran_e(o[0]).c_str(), fortran_e(o[1]).c_str(), fortran_e(o[2]).c_str());
+    return BGK_OK;
 }
 
-// row means of u, w and rho over i = 1..lx (SRC/varm.F90:49-88, u_med.dat): sums over i in order
-// in the storage kind, times rvol = 1.0/float(l) (a default-real quotient)
-template <typename S, typename T>
-void varm(const Pops &a, FILE *f, int itime, T cte1)
+// row means of u, w and rho over i = 1..lx (SRC/varm.F90:49-88, u_med.dat)
+int write_varm(bgk_handle *h, int ly, FILE *f, int itime)
 {
-    const T rvol = (T)(1.0f / (float)a.lx);
+    std::vector<double> u(ly), w(ly), den(ly);
+    const int rc = bgk_varm(h, u.data(), w.data(), den.data());
+    if (rc) return rc;
     std::fprintf(f, "# t=%7d\n", itime);
-    for (int j = 1; j <= a.ly; ++j) {
-        T u = 0, w = 0, den = 0;
-        for (int i = 1; i <= a.lx; ++i) {
-            S x[9];
-            for (int q = 0; q < 9; ++q) x[q] = (S)a.at(q, i, j);
-            const T rho = (T)((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8]) + cte1;
-            const T rhoinv = (T)1 / rho;
-            den = den + rho;
-            u = u + (T)(((((x[0] + x[1]) + x[2]) - x[4]) - x[5]) - x[6]) * rhoinv;
-            w = w + (T)(((((x[1] + x[3]) + x[5]) - x[0]) - x[4]) - x[7]) * rhoinv;
-        }
-        std::fprintf(f, "%5d%s %s %s \n", j, fortran_e(u * rvol).c_str(), fortran_e(w * rvol).c_str(),
-                     fortran_e(den * rvol).c_str());
-    }
+    for (int j = 1; j <= ly; ++j)
+        std::fprintf(f, "%5d%s %s %s \n", j, fortran_e(u[j - 1]).c_str(), fortran_e(w[j - 1]).c_str(),
+                     fortran_e(den[j - 1]).c_str());
     std::fprintf(f, "\n\n");
+    return BGK_OK;
 }
 
 // peak resident set size in MB, as SRC/get_mem.c reports it
@@ -440,22 +420,13 @@ int main(int argc, char **argv)
         std::fprintf(stderr, "bgk2d_gb300: cannot write the output files in %s\n", dir.c_str());
         return 1;
     }
-    const bool dbl = d.storage == BGK_STORE_F64;
-    const double c1 = d.noshift ? 0.0 : 1.0;  // cte1 of the host readers
-    // the readers in (storage, compute) kinds: FP64/FP64, FP32/FP64 (MIXED2), FP32/FP32 otherwise
-    // (the 16-bit kinds download FP32 values)
-    auto readers_in = [&](auto s_tag, auto k_tag, int itime, bool with_probe) {
-        using S = decltype(s_tag);
-        using K = decltype(k_tag);
-        if (with_probe) probe<S, K>(pops, lx / 2, ly / 2, fprobe, itime, (K)c1);
-        varm<S, K>(pops, fumed, itime, (K)c1);
-        prof_i<S, K>(pops, ly / 2, fpi, itime, (K)c1);
-        prof_j<S, K>(pops, lx / 2, fpj, itime, (K)c1);
-    };
-    auto readers = [&](int itime, bool with_probe) {
-        if (dbl) readers_in(0.0, 0.0, itime, with_probe);
-        else if (d.compute == BGK_COMPUTE_F64) readers_in(0.0f, 0.0, itime, with_probe);
-        else readers_in(0.0f, 0.0f, itime, with_probe);
+    // probe, varm, prof_i and prof_j in the order of SRC/diagnostic.F90:70-82, computed on the device
+    auto readers = [&](int itime, bool with_probe) -> int {
+        int r = with_probe ? write_probe(h, lx / 2, ly / 2, fprobe, itime) : BGK_OK;
+        if (!r) r = write_varm(h, ly, fumed, itime);
+        if (!r) r = write_prof_i(h, ly / 2, lx, fpi, itime);
+        if (!r) r = write_prof_j(h, lx / 2, ly, fpj, itime);
+        return r;
     };
     // SRC/diagnostic.F90:70-82 at every icheck (diagno, probe, varm, prof_i, prof_j, draglift);
     // SRC/bgk2d.F90:122-125 once after the loop (diagno, varm, prof_i, prof_j)
@@ -466,8 +437,7 @@ int main(int argc, char **argv)
         std::fprintf(fdiag, "%8d%s %s %s %s \n", itime, fortran_e(dg[0]).c_str(), fortran_e(dg[1]).c_str(),
                      fortran_e(dg[2]).c_str(), fortran_e(dg[3]).c_str());
         std::fflush(fdiag);
-        if ((r = bgk_download(h, pops.p, lx + 2))) return r;
-        readers(itime, !final_call);
+        if ((r = readers(itime, !final_call))) return r;
         if (fdrag && !final_call) {
             double fl[2];
             if ((r = bgk_draglift_reference(h, fl))) return r;  // the reference's own sums
@@ -476,8 +446,7 @@ int main(int argc, char **argv)
         return BGK_OK;
     };
     if (irestart != 1) {  // SRC/initialize.F90:116-123 writes the initial profiles and velocity field
-        if ((rc = bgk_download(h, pops.p, lx + 2))) return die("bgk_download", rc);
-        readers(0, false);
+        if ((rc = readers(0, false))) return die("profiles", rc);
         if (lx > 2 && ly > 2 && (rc = write_vtk(h, dir, 0, lx, ly, false))) return die("vtk", rc);
     }
     const auto t1 = std::chrono::steady_clock::now();

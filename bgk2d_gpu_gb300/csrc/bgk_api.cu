@@ -855,6 +855,54 @@ int bgk_fields(bgk_handle *h, double *rho, double *u, double *v)
     return BGK_OK;
 }
 
+// one of the reference's profile readers on the device (kind as KernelTable::readers); n values
+// per output array
+static int readers_impl(bgk_handle *h, int kind, int a, int b, double *o0, double *o1, double *o2, size_t n)
+{
+    double *d = nullptr;
+    if (dalloc(h, &d, 3 * n * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(h, BGK_E_NOMEM, "readers buffer");
+    }
+    cudaError_t e = h->T.readers(h->L, h->cur, h->phase, h->cs.has_obs, kind, a, b, d, h->st);
+    h->launches++;
+    double *outs[3] = {o0, o1, o2};
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+        e = cudaMemcpyAsync(outs[k], d + k * n, n * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+    dfree(h, d);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (e != cudaSuccess) return fail(h, BGK_E_CUDA, "readers: %s", cudaGetErrorString(e));
+    return BGK_OK;
+}
+
+int bgk_prof_i(bgk_handle *h, int32_t jcoord, double *u, double *v, double *den)
+{
+    CHECK_HANDLE(h);
+    if (!u || !v || !den || jcoord < 1 || jcoord > h->desc.ly) return fail(h, BGK_E_INVALID, "prof_i arguments");
+    return readers_impl(h, 0, jcoord, 0, u, v, den, (size_t)h->desc.lx);
+}
+
+int bgk_prof_j(bgk_handle *h, int32_t icoord, double *u, double *v, double *den)
+{
+    CHECK_HANDLE(h);
+    if (!u || !v || !den || icoord < 1 || icoord > h->desc.lx) return fail(h, BGK_E_INVALID, "prof_j arguments");
+    return readers_impl(h, 1, icoord, 0, u, v, den, (size_t)h->desc.ly);
+}
+
+int bgk_varm(bgk_handle *h, double *u, double *w, double *den)
+{
+    CHECK_HANDLE(h);
+    if (!u || !w || !den) return fail(h, BGK_E_INVALID, "varm arguments");
+    return readers_impl(h, 2, 0, 0, u, w, den, (size_t)h->desc.ly);
+}
+
+int bgk_probe(bgk_handle *h, int32_t i0, int32_t j0, double out[3])
+{
+    CHECK_HANDLE(h);
+    if (!out || i0 < 1 || i0 > h->desc.lx || j0 < 1 || j0 > h->desc.ly) return fail(h, BGK_E_INVALID, "probe arguments");
+    return readers_impl(h, 3, i0, j0, out, out + 1, out + 2, 1);
+}
+
 int bgk_vtk_fields(bgk_handle *h, float *u, float *w, float *rho, float *vort, float *stream)
 {
     CHECK_HANDLE(h);

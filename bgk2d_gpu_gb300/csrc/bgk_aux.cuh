@@ -1,6 +1,8 @@
 // bgk_aux.cuh -- state access, host-layout conversion and FP64 reductions (templated bodies).
 #pragma once
 
+#include <type_traits>
+
 #include "bgk_kernels.cuh"
 #include "bgk_table.h"
 
@@ -510,6 +512,112 @@ __global__ void fields_kernel(Lattice L, int cur, int phase, double *rho, double
         u[c] = (double)xj;
         v[c] = (double)yj;
     }
+}
+
+// ---------------------------------------------------------------------------------------------
+// The reference's profile readers on the device (SRC/prof_i.F90:47-62, SRC/prof_j.F90:47-67,
+// SRC/varm.F90:49-88, SRC/probe.F90:46-62), so that a diagnostic stop downloads profiles instead
+// of the nine planes.  Their arithmetic is that of the host readers on downloaded arrays: the
+// values as they download (H: FP64 for FP64 storage, FP32 otherwise) summed in H as they lie in
+// the arrays, cte1 (1, or 0 for populations stored whole) added and the quotients taken in the
+// compute kind K; probe copies the values into K temporaries first.  Results are K values held
+// exactly in doubles.
+template <typename S> using ReaderKind = typename std::conditional<std::is_same<S, double>::value, double, float>::type;
+
+template <typename S, typename K, bool HAS_OBS>
+__device__ __forceinline__ void reader_cell(const Lattice &L, int cur, int phase, int x, int y,
+                                            ReaderKind<S> (&c)[9])
+{
+#pragma unroll
+    for (int q = 0; q < 9; ++q) c[q] = (ReaderKind<S>)post_value<S, K, HAS_OBS>(L, cur, phase, q, x, y);
+}
+
+// kind 0: prof_i along row a (lx values), kind 1: prof_j along column a (ly values);
+// out = u[n], v[n], den[n]
+template <typename S, typename K, bool HAS_OBS>
+__global__ void prof_kernel(Lattice L, int cur, int phase, int kind, int a, double *out)
+{
+    using H = ReaderKind<S>;
+    const int n = kind == 0 ? L.lx : L.ly;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int x = kind == 0 ? t + 1 : a, y = kind == 0 ? a : t + 1;
+    H c[9];
+    reader_cell<S, K, HAS_OBS>(L, cur, phase, x, y, c);
+    const K cte1 = L.noshift ? (K)0 : (K)1;
+    const H s = ((((((((c[0] + c[1]) + c[2]) + c[3]) + c[4]) + c[5]) + c[6]) + c[7]) + c[8]);
+    const K den = (K)s + cte1;
+    H nu, nv;
+    if (kind == 0) {  // prof_i.F90:55-62
+        nu = ((((c[0] + c[1]) + c[2]) - c[4]) - c[5]) - c[6];
+        nv = ((((c[1] + c[3]) + c[5]) - c[0]) - c[4]) - c[7];
+    } else {          // prof_j.F90:56-67
+        nu = ((c[0] - c[4]) + (c[1] - c[5])) + (c[2] - c[6]);
+        nv = ((c[1] - c[0]) + (c[3] - c[7])) + (c[5] - c[4]);
+    }
+    out[t] = (double)((K)nu / den);
+    out[n + t] = (double)((K)nv / den);
+    out[2 * n + t] = (double)den;
+}
+
+// varm: one block per row j; the per-cell terms in parallel, their sums over i = 1..lx in order
+// by one thread (varm.F90:53-69); out = u[ly], w[ly], den[ly], each times rvol = 1.0/float(lx)
+constexpr int VARM_NT = 256;
+template <typename S, typename K, bool HAS_OBS>
+__global__ void __launch_bounds__(VARM_NT) varm_kernel(Lattice L, int cur, int phase, double *out)
+{
+    using H = ReaderKind<S>;
+    __shared__ K sh[3][VARM_NT];
+    const int j = blockIdx.x + 1, t = threadIdx.x;
+    const K cte1 = L.noshift ? (K)0 : (K)1;
+    K su = (K)0, sw = (K)0, sd = (K)0;
+    for (int i0 = 1; i0 <= L.lx; i0 += VARM_NT) {
+        const int i = i0 + t;
+        if (i <= L.lx) {
+            H c[9];
+            reader_cell<S, K, HAS_OBS>(L, cur, phase, i, j, c);
+            const K rho = (K)((((((((c[0] + c[1]) + c[2]) + c[3]) + c[4]) + c[5]) + c[6]) + c[7]) + c[8]) + cte1;
+            const K rhoinv = (K)1 / rho;
+            sh[0][t] = rho;
+            sh[1][t] = (K)(((((c[0] + c[1]) + c[2]) - c[4]) - c[5]) - c[6]) * rhoinv;
+            sh[2][t] = (K)(((((c[1] + c[3]) + c[5]) - c[0]) - c[4]) - c[7]) * rhoinv;
+        }
+        __syncthreads();
+        if (t == 0) {
+            const int cnt = min(VARM_NT, L.lx - i0 + 1);
+            for (int k = 0; k < cnt; ++k) {
+                sd = sd + sh[0][k];
+                su = su + sh[1][k];
+                sw = sw + sh[2][k];
+            }
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        const K rvol = (K)(1.0f / (float)L.lx);  // a default-real quotient (varm.F90:71)
+        out[j - 1] = (double)(su * rvol);
+        out[L.ly + j - 1] = (double)(sw * rvol);
+        out[2 * L.ly + j - 1] = (double)(sd * rvol);
+    }
+}
+
+// probe at (i0, j0): u, v, rho (probe.F90:46-62), in K temporaries
+template <typename S, typename K, bool HAS_OBS>
+__global__ void probe_kernel(Lattice L, int cur, int phase, int i0, int j0, double *out)
+{
+    using H = ReaderKind<S>;
+    H c[9];
+    reader_cell<S, K, HAS_OBS>(L, cur, phase, i0, j0, c);
+    K x[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) x[q] = (K)c[q];
+    const K cte1 = L.noshift ? (K)0 : (K)1;
+    const K rho = ((((((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5]) + x[6]) + x[7]) + x[8]) + cte1;
+    const K xj = ((((x[0] + x[1]) + x[2]) - x[4]) - x[5]) - x[6];
+    const K yj = ((((x[1] + x[3]) + x[5]) - x[0]) - x[4]) - x[7];
+    out[0] = (double)(xj / rho);
+    out[1] = (double)(yj / rho);
+    out[2] = (double)rho;
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -276,6 +276,29 @@ cudaError_t fields(const Lattice &L, int cur, int phase, bool obs, double *rho, 
     return cudaGetLastError();
 }
 
+// the reference's profile readers: kind 0 prof_i (row a), 1 prof_j (column a), 2 varm, 3 probe
+// at (a, b); out holds 3 x (lx, ly, ly, 1) doubles
+template <typename S, typename K, bool OBS>
+void readers_launch(const Lattice &L, int cur, int phase, int kind, int a, int b, double *out, cudaStream_t st)
+{
+    if (kind <= 1) {
+        const int n = kind == 0 ? L.lx : L.ly;
+        prof_kernel<S, K, OBS><<<(n + 255) / 256, 256, 0, st>>>(L, cur, phase, kind, a, out);
+    } else if (kind == 2) {
+        varm_kernel<S, K, OBS><<<L.ly, VARM_NT, 0, st>>>(L, cur, phase, out);
+    } else {
+        probe_kernel<S, K, OBS><<<1, 1, 0, st>>>(L, cur, phase, a, b, out);
+    }
+}
+
+template <typename S, typename K>
+cudaError_t readers(const Lattice &L, int cur, int phase, bool obs, int kind, int a, int b, double *out, cudaStream_t st)
+{
+    if (obs) readers_launch<S, K, true>(L, cur, phase, kind, a, b, out, st);
+    else readers_launch<S, K, false>(L, cur, phase, kind, a, b, out, st);
+    return cudaGetLastError();
+}
+
 template <typename S, typename K, bool OBS>
 void vtk_launch(const Lattice &L, int cur, int phase, float *u, float *w, float *rho, float *vort, float *stream,
                 float *phi, cudaStream_t st)
@@ -340,6 +363,7 @@ KernelTable make_table()
     t.draglift = &draglift<S, K>;
     t.draglift_seq = &draglift_seq<S, K>;
     t.fields = &fields<S, K>;
+    t.readers = &readers<S, K>;
     t.vtk = &vtk<S, K>;
     t.batch_step = &batch_step<S, K>;
     t.xfer = &xfer<S, K>;

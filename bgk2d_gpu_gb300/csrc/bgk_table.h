@@ -72,6 +72,9 @@ struct KernelTable {
                               int grid, int pf, cudaStream_t st);
     cudaError_t (*fields)(const Lattice &L, int cur, int phase, bool obs, double *rho, double *u, double *v,
                           cudaStream_t st);
+    // the reference's profile readers (0 prof_i row a, 1 prof_j column a, 2 varm, 3 probe at (a, b))
+    cudaError_t (*readers)(const Lattice &L, int cur, int phase, bool obs, int kind, int a, int b, double *out,
+                           cudaStream_t st);
     cudaError_t (*vtk)(const Lattice &L, int cur, int phase, bool obs, float *u, float *w, float *rho, float *vort,
                        float *stream, float *phi, cudaStream_t st);
     // all nine mapped host planes <-> state buffer cur, one launch per chunk of rows

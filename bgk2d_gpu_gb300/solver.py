@@ -301,9 +301,25 @@ class Solver:
         """The compute kind of the reference readers for arrays `a`."""
         return np.float64 if getattr(self, "compute", None) == "f64" else a.dtype.type
 
+    def _device_reader(self, name, n, *args):
+        """One of the profile readers on the device (bgk_prof_i / _prof_j / _varm / _probe): three
+        arrays of n compute-kind values."""
+        out = np.zeros((3, n))
+        dp = ctypes.POINTER(ctypes.c_double)
+        ptrs = [out[k].ctypes.data_as(dp) for k in range(3)]
+        if name == "bgk_probe":  # out[3] contiguous: the (3, 1) array
+            self._check(self._L.bgk_probe(self._h, *args, ptrs[0]), "probe")
+        else:
+            self._check(getattr(self._L, name)(self._h, *args, *ptrs), name[4:])
+        k = np.float64 if self.storage == "f64" or self.compute == "f64" else np.float32
+        return tuple(out[q].astype(k) for q in range(3))  # exact: the values are of kind k
+
     def prof_j(self, icoord, pops=None):
-        """u, v, rho along column icoord, j = 1..ly (SRC/prof_j.F90:47-67)."""
-        a = self.download() if pops is None else pops
+        """u, v, rho along column icoord, j = 1..ly (SRC/prof_j.F90:47-67); computed on the device
+        (bgk_prof_j) unless downloaded populations `pops` are given."""
+        if pops is None:
+            return self._device_reader("bgk_prof_j", self.ly, int(icoord))
+        a = pops
         k = self._kind(a)
         c = a[:, 1:self.ly + 1, icoord]
         den = c[0] + c[1]
@@ -315,8 +331,11 @@ class Solver:
         return u, v, den
 
     def prof_i(self, jcoord, pops=None):
-        """u, v, rho along row jcoord, i = 1..lx (SRC/prof_i.F90:47-62)."""
-        a = self.download() if pops is None else pops
+        """u, v, rho along row jcoord, i = 1..lx (SRC/prof_i.F90:47-62); on the device (bgk_prof_i)
+        unless `pops` are given."""
+        if pops is None:
+            return self._device_reader("bgk_prof_i", self.lx, int(jcoord))
+        a = pops
         k = self._kind(a)
         c = a[:, jcoord, 1:self.lx + 1]
         den = c[0] + c[1]
@@ -328,13 +347,19 @@ class Solver:
         return u, v, den
 
     def varm(self, pops=None):
-        """Row means of u, w and rho (u_med.dat; SRC/varm.F90:49-88), see `varm`."""
-        a = self.download() if pops is None else pops
-        return varm(a, self.lx, self.ly, noshift=self.noshift, kind=self._kind(a))
+        """Row means of u, w and rho (u_med.dat; SRC/varm.F90:49-88), see `varm`; on the device
+        (bgk_varm) unless `pops` are given."""
+        if pops is None:
+            return self._device_reader("bgk_varm", self.ly)
+        return varm(pops, self.lx, self.ly, noshift=self.noshift, kind=self._kind(pops))
 
     def probe(self, i0, j0, pops=None):
-        """u, v, rho at one node (SRC/probe.F90:46-62)."""
-        a = self.download() if pops is None else pops
+        """u, v, rho at one node (SRC/probe.F90:46-62); on the device (bgk_probe) unless `pops`
+        are given."""
+        if pops is None:
+            u, v, r = self._device_reader("bgk_probe", 1, int(i0), int(j0))
+            return u[0], v[0], r[0]
+        a = pops
         k = self._kind(a)
         x = a[:, j0, i0].astype(k)
         rho = x[0] + x[1] + x[2] + x[3] + x[4] + x[5] + x[6] + x[7] + x[8] + k(self._cte1)

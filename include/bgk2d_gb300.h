@@ -211,6 +211,20 @@ int bgk_get_obs(bgk_handle *h, int32_t *mask, int32_t bbox[5]);
  * FUSED build that term reads the ghost row of the buffer written two steps earlier).  Any
  * output pointer may be NULL. */
 int bgk_vtk_fields(bgk_handle *h, float *u, float *w, float *rho, float *vort, float *stream);
+/* The profile readers the reference runs on the host after a device-to-host update at each
+ * diagnostic stop (SRC/diagnostic.F90:70-82), computed on the device with their arithmetic, so that
+ * profiles cross the bus instead of 9 populations: the stored values summed in the storage kind as
+ * they lie in the arrays, cte1 added and the quotients taken in the compute kind (FP64 under
+ * MIXED2); probe in compute-kind temporaries.  The doubles hold compute-kind values exactly.
+ *   bgk_prof_i: u, v, den along row jcoord, i = 1..lx (SRC/prof_i.F90:47-62; lx values each)
+ *   bgk_prof_j: u, v, den along column icoord, j = 1..ly (SRC/prof_j.F90:47-67; ly values each)
+ *   bgk_varm:   row means of u, w, den over i = 1..lx for j = 1..ly (SRC/varm.F90:49-88, u_med.dat)
+ *   bgk_probe:  u, v, rho at (i0, j0) (SRC/probe.F90:46-62)
+ * Coordinates outside 1..lx / 1..ly return BGK_E_INVALID. */
+int bgk_prof_i(bgk_handle *h, int32_t jcoord, double *u, double *v, double *den);
+int bgk_prof_j(bgk_handle *h, int32_t icoord, double *u, double *v, double *den);
+int bgk_varm(bgk_handle *h, double *u, double *w, double *den);
+int bgk_probe(bgk_handle *h, int32_t i0, int32_t j0, double out[3]);
 /* omega, fgrad, u00, u0 after build_bcond + hencol, and the step counter */
 int bgk_get_scalars(bgk_handle *h, double out[4], int64_t *itime);
 

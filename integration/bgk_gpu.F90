@@ -140,6 +140,35 @@ module bgk_gpu
        real(c_double), intent(out) :: out
      end function bgk_residual
 
+     ! the profile readers of prof_i / prof_j / varm / probe computed on the device, for a loop
+     ! that writes those files without downloading the populations
+     integer(c_int) function bgk_prof_i(h, jcoord, u, v, den) bind(c, name="bgk_prof_i")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       integer(c_int), value :: jcoord
+       real(c_double), intent(out) :: u(*), v(*), den(*)
+     end function bgk_prof_i
+
+     integer(c_int) function bgk_prof_j(h, icoord, u, v, den) bind(c, name="bgk_prof_j")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       integer(c_int), value :: icoord
+       real(c_double), intent(out) :: u(*), v(*), den(*)
+     end function bgk_prof_j
+
+     integer(c_int) function bgk_varm(h, u, w, den) bind(c, name="bgk_varm")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       real(c_double), intent(out) :: u(*), w(*), den(*)
+     end function bgk_varm
+
+     integer(c_int) function bgk_probe(h, i0, j0, out) bind(c, name="bgk_probe")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       integer(c_int), value :: i0, j0
+       real(c_double), intent(out) :: out(3)
+     end function bgk_probe
+
      integer(c_int) function bgk_vtk_fields(h, u, w, rho, vort, stream) bind(c, name="bgk_vtk_fields")
        import :: c_int, c_ptr, c_float
        type(c_ptr), value :: h

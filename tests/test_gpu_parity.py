@@ -570,3 +570,35 @@ def test_force_y_needs_a_forced_case(bgk):
     for tc in ("LDC", "TGV", "COU"):
         with pytest.raises(bgk.BgkError):
             bgk.Solver(64, 48, tcase=tc, force_y=True)
+
+
+@pytest.mark.parametrize("scheme", ["pingpong", "aa"])
+@pytest.mark.parametrize("storage,compute", [("f32", "f32"), ("f64", "f64"), ("f32", "f64"), ("f16", "f32"),
+                                             ("bf16", "f32")])
+def test_device_profile_readers_equal_host_readers(bgk, storage, compute, scheme):
+    """bgk_prof_i / bgk_prof_j / bgk_varm / bgk_probe (the readers of SRC/prof_i.F90, prof_j.F90,
+    varm.F90 and probe.F90 on the device) give, bit for bit, what the host readers give on the
+    downloaded populations: cavities (with NOSHIFT for the exact kinds) and a channel with a
+    cylinder, after an odd and an even number of steps."""
+    cases = [dict(lx=90, ly=52, tcase="LDC", svisc=0.02, u0=0.1),
+             dict(lx=160, ly=62, tcase="VKS", svisc=0.05, u0=0.1, radius=6)]
+    if storage in ("f32", "f64"):
+        cases.append(dict(lx=70, ly=37, tcase="LDC", svisc=0.02, u0=0.1, noshift=True))
+    for kw in cases:
+        with bgk.Solver(storage=storage, compute=compute, scheme=scheme, **kw) as s:
+            for n in (37, 2):
+                s.step(n)
+                a = s.download()
+                for dev, host in ((s.prof_i(kw["ly"] // 3), s.prof_i(kw["ly"] // 3, pops=a)),
+                                  (s.prof_j(kw["lx"] // 2), s.prof_j(kw["lx"] // 2, pops=a)),
+                                  (s.varm(), s.varm(pops=a)),
+                                  (s.probe(5, kw["ly"] - 2), s.probe(5, kw["ly"] - 2, pops=a))):
+                    for d, h in zip(dev, host):
+                        d, h = np.asarray(d), np.asarray(h)
+                        assert d.dtype == h.dtype and np.array_equal(d, h), (kw, n, d, h)
+        with pytest.raises(bgk.BgkError):
+            s2 = bgk.Solver(storage=storage, compute=compute, scheme=scheme, **kw)
+            try:
+                s2.prof_i(0)
+            finally:
+                s2.close()
