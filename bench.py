@@ -312,10 +312,10 @@ def run_profile_advance(args, storage, compute):
     return 0
 
 
-def measure_variant(bgk, storage, scheme, steps, warmup, dev, tune=True, les=False, compute=None):
+def measure_variant(bgk, storage, scheme, steps, warmup, dev, tune=True, les=False, compute=None, **kw):
     compute = compute or ("f64" if storage == "f64" else "f32")
     with bgk.Solver(LX, LY, tcase="LDC", svisc=SVISC, u0=U0, storage=storage, compute=compute, scheme=scheme,
-                    device=dev, les=les) as s:
+                    device=dev, les=les, **kw) as s:
         cfg = s.tune(4 if compute == "f64" else 10)[0] if tune else None
         pf = s.prefetch()
         s.step(warmup)
@@ -682,18 +682,21 @@ def main():
         import ctypes
         pk = (ctypes.c_double * 3)()
         fp64_peak = float(sum(pk)) / 3 / 1e9 if L.bgk_peak_fp64(local, pk) == 0 else None
-        # les_*: the Smagorinsky collision (SRC/col_MC.F90:178-248), cteS = 0.1
+        # les_*: the Smagorinsky collision (SRC/col_MC.F90:178-248), cteS = 0.1; noshift_f32: whole
+        # populations in the planes (the NOSHIFT build, SRC/col_MC.F90:70-75)
         for name, st, sch, les in (("pingpong_f32", "f32", "pingpong", False), ("aa_f32", "f32", "aa", False),
                                    ("pingpong_f16", "f16", "pingpong", False), ("aa_f16", "f16", "aa", False),
                                    ("pingpong_bf16", "bf16", "pingpong", False),
                                    ("pingpong_f64", "f64", "pingpong", False), ("aa_f64", "f64", "aa", False),
                                    ("original_f32", "f32", "original", False),
                                    ("les_f32", "f32", "pingpong", True), ("les_f16", "f16", "pingpong", True),
+                                   ("noshift_f32", "f32", "pingpong", False),
                                    ("mixed2_f32", "f32", "pingpong", False)):
             # mixed2: FP32 storage with the FP64 collision of the reference's MIXED2 build
             cp = "f64" if name.startswith("mixed2") else None
             n = vsteps if st != "f64" and cp is None else max(10, vsteps // 4)
-            g, msv, cfg, pf = measure_variant(bgk, st, sch, n, 5, local, les=les, compute=cp)
+            g, msv, cfg, pf = measure_variant(bgk, st, sch, n, 5, local, les=les, compute=cp,
+                                              noshift=name.startswith("noshift"))
             # the two-pass form moves every population twice per step (stream, then collide)
             bw = BYTES_PER_CELL[st] * (2 if sch == "original" else 1) * LX * LY / (msv * 1e-3) / 1e9
             variants[name] = {"GLUPS": round(g, 3), "ms_per_step": round(msv, 4), "algorithmic_GBps": round(bw, 1),
