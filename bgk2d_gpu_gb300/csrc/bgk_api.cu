@@ -441,6 +441,26 @@ void release(bgk_handle *h)
 template <typename K>
 std::string setup_for(const bgk_case_desc &d, CaseSetup &cs) { return setup_case<K>(d, cs); }
 
+// one of the reference's profile readers on the device (kind as KernelTable::readers); n values
+// per output array
+int readers_impl(bgk_handle *h, int kind, int a, int b, double *o0, double *o1, double *o2, size_t n)
+{
+    double *d = nullptr;
+    if (dalloc(h, &d, 3 * n * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(h, BGK_E_NOMEM, "readers buffer");
+    }
+    cudaError_t e = h->T.readers(h->L, h->cur, h->phase, h->cs.has_obs, kind, a, b, d, h->st);
+    h->launches++;
+    double *outs[3] = {o0, o1, o2};
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+        e = cudaMemcpyAsync(outs[k], d + k * n, n * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+    dfree(h, d);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (e != cudaSuccess) return fail(h, BGK_E_CUDA, "readers: %s", cudaGetErrorString(e));
+    return BGK_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -852,26 +872,6 @@ int bgk_fields(bgk_handle *h, double *rho, double *u, double *v)
     dfree(h, d);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
     if (e != cudaSuccess) return fail(h, BGK_E_CUDA, "fields: %s", cudaGetErrorString(e));
-    return BGK_OK;
-}
-
-// one of the reference's profile readers on the device (kind as KernelTable::readers); n values
-// per output array
-static int readers_impl(bgk_handle *h, int kind, int a, int b, double *o0, double *o1, double *o2, size_t n)
-{
-    double *d = nullptr;
-    if (dalloc(h, &d, 3 * n * sizeof(double)) != cudaSuccess) {
-        cudaGetLastError();
-        return fail(h, BGK_E_NOMEM, "readers buffer");
-    }
-    cudaError_t e = h->T.readers(h->L, h->cur, h->phase, h->cs.has_obs, kind, a, b, d, h->st);
-    h->launches++;
-    double *outs[3] = {o0, o1, o2};
-    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
-        e = cudaMemcpyAsync(outs[k], d + k * n, n * sizeof(double), cudaMemcpyDeviceToHost, h->st);
-    dfree(h, d);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
-    if (e != cudaSuccess) return fail(h, BGK_E_CUDA, "readers: %s", cudaGetErrorString(e));
     return BGK_OK;
 }
 
