@@ -233,10 +233,6 @@ int download_impl(bgk_handle *h, void *const pops[9], int64_t ld)
 int launch_step(bgk_handle *h)
 {
     if (h->L.scheme == BGK_SCHEME_PINGPONG) {
-        if (h->cs.bfs) {  // the step's boundary routine writes the source buffer's ghosts first
-            CK(h, h->T.bcond_step(h->L, h->cur, h->cs.stepx, h->cs.stepy, h->st));
-            h->launches++;
-        }
         if (h->two_pass) {
             CK(h, h->T.step(STEP_STREAM, h->L, h->cur, h->cs.has_obs, h->cfg, h->st));
             CK(h, h->T.step(STEP_COLLIDE, h->L, h->cur ^ 1, h->cs.has_obs, h->cfg, h->st));
@@ -295,7 +291,7 @@ int steps_impl(bgk_handle *h, int32_t n)
         const int slot = h->L.scheme == BGK_SCHEME_PINGPONG ? h->cur : 0;
         if (!h->graph[slot] && (rc = build_graph(h, slot))) return rc;
         CK(h, cudaGraphLaunch(h->graph[slot], h->st));
-        h->launches += (int64_t)h->graph_steps * (1 + (h->cs.bfs ? 1 : 0) + (h->two_pass ? 1 : 0));
+        h->launches += (int64_t)h->graph_steps * (1 + (h->two_pass ? 1 : 0));
         h->itime += h->graph_steps;
         n -= h->graph_steps;
     }
@@ -339,9 +335,9 @@ constexpr int PIPE_STEPS = 16;
 bool pipeline_ok(const bgk_handle *h)
 {
     // pulls reach one row up and one row down, nothing else: no periodic y faces (row 1 pulls
-    // from row ly), no whole-lattice boundary kernel (BFS), no two-pass form, no collision
-    // variant (LES, NOSHIFT: the waves run the plain collision)
-    return h->L.scheme == BGK_SCHEME_PINGPONG && !h->two_pass && !h->cs.bfs && !h->L.les && !h->L.noshift &&
+    // from row ly), no two-pass form, no collision variant (LES, NOSHIFT: the waves run the plain
+    // collision)
+    return h->L.scheme == BGK_SCHEME_PINGPONG && !h->two_pass && !h->L.les && !h->L.noshift &&
            h->cs.faces[YLO] != FK_PERIODIC && h->cs.faces[YHI] != FK_PERIODIC && h->desc.ly >= 8;
 }
 
@@ -428,7 +424,7 @@ void release(bgk_handle *h)
     for (int i = 0; i < 2; ++i)
         if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
     if (h->st) {
-        for (void *p : {(void *)h->d_planes, (void *)h->d_mask, (void *)h->d_inflow, (void *)h->d_partial,
+        for (void *p : {(void *)h->d_planes, (void *)h->d_mask, h->d_step_aux, (void *)h->d_inflow, (void *)h->d_partial,
                         (void *)h->d_out, (void *)h->d_status, (void *)h->d_uprev, (void *)h->d_vprev, h->d_stage})
             dfree(h, p);
         cudaStreamSynchronize(h->st);
@@ -559,6 +555,9 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
     }
     L.corner_x = h->cs.corner_x;
     L.noshift = h->cs.noshift;
+    L.inflow_y0 = h->cs.inflow_y0;
+    L.step_x = h->cs.bfs ? h->cs.stepx : 0;
+    L.step_y = h->cs.bfs ? h->cs.stepy : 0;
     L.omega = h->cs.omega;
     L.fgrad = h->cs.fgrad;
     L.forced = h->cs.forced;
@@ -589,9 +588,21 @@ int bgk_create(const bgk_case_desc *desc, bgk_handle **out)
     cudaMemcpyAsync(h->d_mask, bits.data(), bits.size() * 4, cudaMemcpyHostToDevice, h->st);
     cudaStreamSynchronize(h->st);  // `bits` and the inflow table are host temporaries
     L.mask = h->d_mask;
+    L.step_aux = nullptr;
+    if (h->cs.bfs && L.scheme == BGK_SCHEME_AA) {
+        if (dalloc(h, &h->d_step_aux, 128) != cudaSuccess) {  // 10 storage elements
+            cudaGetLastError(); release(h); delete h; return BGK_E_NOMEM;
+        }
+        cudaMemsetAsync(h->d_step_aux, 0, 128, h->st);
+        L.step_aux = h->d_step_aux;
+    }
     if (h->cs.has_obs) {
         L.ob_x0 = h->cs.bbox[0] - 1; L.ob_x1 = h->cs.bbox[1] + 1;
         L.ob_y0 = h->cs.bbox[2] - 1; L.ob_y1 = h->cs.bbox[3] + 1;
+        if (h->cs.bfs) {  // and the step corner's neighbours (step_bounce)
+            L.ob_x1 = std::max(L.ob_x1, h->cs.stepx + 1);
+            L.ob_y1 = std::max(L.ob_y1, h->cs.stepy + 1);
+        }
     } else {
         L.ob_x0 = L.ob_y0 = 1 << 30; L.ob_x1 = L.ob_y1 = -1;
     }
@@ -682,12 +693,8 @@ int bgk_propagation(bgk_handle *h)
     CHECK_HANDLE(h);
     NOT_IN_BATCH(h);
     if (!h->two_pass || h->streamed) return BGK_OK;  // fused: the pull streaming is part of the step
-    // two-pass: the streaming pass (and the step's boundary kernel) now, the collision in
+    // two-pass: the streaming pass (with the boundary rules) now, the collision in
     // bgk_collision, as SRC/propagation.F90 and SRC/collision.F90 split them
-    if (h->cs.bfs) {
-        CK(h, h->T.bcond_step(h->L, h->cur, h->cs.stepx, h->cs.stepy, h->st));
-        h->launches++;
-    }
     CK(h, h->T.step(STEP_STREAM, h->L, h->cur, h->cs.has_obs, h->cfg, h->st));
     h->launches++;
     h->streamed = true;

@@ -28,6 +28,9 @@ __device__ __forceinline__ K post_value(const Lattice &L, int cur, int phase, in
         tx = tx < 1 ? L.lx : 1;
     }
     if (HAS_OBS) {
+        // a push a backward-facing step's corner holds back (aa_push_rule)
+        if (L.step_aux && step_bounce(L, tx, ty, q))
+            return Store<S>::template getq<K>(reinterpret_cast<const S *>(L.step_aux)[5 + step_slot(L, tx, q)], q);
         if (obs_bit(L, tx, ty)) return ldq<S, K>(base + opp_of(q) * pe, cell_index<S>(L, x, y), q);
     }
     return ldq<S, K>(base + q * pe, cell_index<S>(L, tx, ty), q);
@@ -231,71 +234,6 @@ __global__ void aa_fill_outflow_kernel(Lattice L)
 #pragma unroll
     for (int q = 0; q < 9; ++q) g[q] = ldq<S, K>(base + opp_of(q) * pe, i, q);
     aa_outflow_ghost<S, K>(L, base, y, g);
-}
-
-// Backward-facing step (SRC/bcond.step.F90:66-264) on the source buffer of a ping-pong step, in
-// the reference's order: the equilibrium outflow column x = lx+1 (all rows) and the parabolic
-// inflow column x = 0 (rows stepy..ly+1); the no-slip ghost rows y = 0 and ly+1 (x = 1..lx); the
-// top of the step (row stepy-1, from x = 1..stepx); its vertical face (column stepx-1, from rows
-// 1..stepy).  Later loops overwrite values of earlier ones where they meet, as the reference's
-// sequential loops do, so one block runs the four loops in order.  The step kernel then pulls
-// these stored values (faces of kind FK_STORED).  Inflow values come from L.inflow.
-template <typename S, typename K>
-__device__ __forceinline__ void bfs_bcond_block(const Lattice &L, const int cur, const int stepx, const int stepy)
-{
-    const int64_t pe = L.plane_elems;
-    S *a = reinterpret_cast<S *>(L.planes) + (cur ? 9 : 0) * pe;
-    const int l = L.lx, m = L.ly;
-    auto at = [&](int q, int x, int y) -> S & { return a[q * pe + cell_index<S>(L, x, y)]; };
-    for (int j = threadIdx.x; j <= m + 1; j += blockDim.x) {
-        K v[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = Store<S>::template getq<K>(at(q, l, j), q);
-#pragma unroll
-        for (int q = D10; q <= D14; ++q)
-            at(q, l + 1, j) = Store<S>::template putq<K>(outflow_eq<K>(q, v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], L.noshift != 0), q);
-        if (j >= stepy) {
-#pragma unroll
-            for (int t = 0; t < 3; ++t) at(t, 0, j) = Store<S>::template putq<K>((K)L.inflow[(int64_t)t * (m + 2) + j], t);
-        }
-    }
-    __syncthreads();
-    for (int i = 1 + threadIdx.x; i <= l; i += blockDim.x) {
-        at(D08, i, 0) = at(D17, i, 1);
-        at(D12, i + 1, 0) = at(D01, i, 1);
-        at(D03, i - 1, 0) = at(D10, i, 1);
-        at(D10, i + 1, m + 1) = at(D03, i, m);
-        at(D17, i, m + 1) = at(D08, i, m);
-        at(D01, i - 1, m + 1) = at(D12, i, m);
-    }
-    __syncthreads();
-    for (int i = 1 + threadIdx.x; i <= stepx; i += blockDim.x) {
-        at(D08, i, stepy - 1) = at(D17, i, stepy);
-        at(D12, i + 1, stepy - 1) = at(D01, i, stepy);
-        at(D03, i - 1, stepy - 1) = at(D10, i, stepy);
-    }
-    __syncthreads();
-    for (int j = 1 + threadIdx.x; j <= stepy; j += blockDim.x) {
-        at(D03, stepx - 1, j - 1) = at(D10, stepx, j);
-        at(D01, stepx - 1, j + 1) = at(D12, stepx, j);
-        at(D05, stepx - 1, j) = at(D14, stepx, j);
-    }
-}
-
-template <typename S, typename K>
-__global__ void bfs_bcond_kernel(const Lattice L, const int cur, const int stepx, const int stepy)
-{
-    bfs_bcond_block<S, K>(L, cur, stepx, stepy);
-}
-
-// the same boundary routine for the backward-facing-step members of a batch, one block each:
-// entry = (member, stepx, stepy, -), source buffer cur[member] ^ parity
-template <typename S, typename K>
-__global__ void batch_bfs_kernel(const Lattice *__restrict__ lats, const int *__restrict__ cur,
-                                 const int4 *__restrict__ members, const int parity)
-{
-    const int4 e = members[blockIdx.x];
-    bfs_bcond_block<S, K>(lats[e.x], cur[e.x] ^ parity, e.y, e.z);
 }
 
 // moments with the reference's per-cell arithmetic (SRC/diagno.F90:82-93); cte1 = 1, or 0 for

@@ -27,9 +27,6 @@ struct bgk_batch {
     int ntiles = 0;
     size_t cap_lats = 0, cap_tiles = 0;
     int nles = 0;                   // LES members' tiles, stored after the ntiles others
-    int4 *d_bfs = nullptr;          // backward-facing-step members: (member, stepx, stepy, -)
-    int nbfs = 0;
-    size_t cap_bfs = 0;
     bool dirty = true;              // work list / device arrays need a rebuild
     cudaStream_t st = nullptr;
     cudaEvent_t done = nullptr, ev0 = nullptr, ev1 = nullptr;
@@ -53,12 +50,11 @@ int rebuild(bgk_batch *b)
     const TileCfg tc = TILE_CFGS[b->cfg];
     std::vector<Lattice> lats;
     std::vector<int> cur;
-    std::vector<int4> tiles, les_tiles, bfs;
+    std::vector<int4> tiles, les_tiles;
     for (size_t i = 0; i < b->members.size(); ++i) {
         bgk_handle *h = b->members[i];
         lats.push_back(h->L);
         cur.push_back(h->cur);
-        if (h->cs.bfs) bfs.push_back(make_int4((int)i, h->cs.stepx, h->cs.stepy, 0));
         // LES members: the Smagorinsky kernel's own shape (128 x 1 threads, the cells per
         // thread of the single-domain LES step), in a list of their own
         const bool les = h->L.les != 0;
@@ -106,20 +102,6 @@ int rebuild(bgk_batch *b)
             return BGK_E_NOMEM;
         }
     }
-    if (bfs.size() > b->cap_bfs) {
-        if (b->d_bfs) cudaFreeAsync(b->d_bfs, b->st);
-        b->d_bfs = nullptr;
-        b->cap_bfs = std::max<size_t>(bfs.size(), 2 * b->cap_bfs);
-        if (cudaMallocAsync((void **)&b->d_bfs, b->cap_bfs * sizeof(int4), b->st) != cudaSuccess) {
-            cudaGetLastError();
-            b->d_bfs = nullptr;
-            b->cap_bfs = 0;
-            return BGK_E_NOMEM;
-        }
-    }
-    if (!bfs.empty() &&
-        cudaMemcpyAsync(b->d_bfs, bfs.data(), bfs.size() * sizeof(int4), cudaMemcpyHostToDevice, b->st) != cudaSuccess)
-        return BGK_E_CUDA;
     if (!lats.empty()) {
         if (cudaMemcpyAsync(b->d_lats, lats.data(), lats.size() * sizeof(Lattice), cudaMemcpyHostToDevice, b->st) ||
             cudaMemcpyAsync(b->d_cur, cur.data(), cur.size() * sizeof(int), cudaMemcpyHostToDevice, b->st) ||
@@ -129,7 +111,6 @@ int rebuild(bgk_batch *b)
     if (cudaStreamSynchronize(b->st) != cudaSuccess) return BGK_E_CUDA;
     b->ntiles = (int)nplain;
     b->nles = (int)les_tiles.size();
-    b->nbfs = (int)bfs.size();
     b->dirty = false;
     b->generation++;
     return BGK_OK;
@@ -155,12 +136,6 @@ int grid_of(const bgk_batch *b)
 int launch_one(bgk_batch *b, int parity)
 {
     if (b->ntiles == 0 && b->nles == 0) return BGK_OK;
-    // backward-facing-step members: their boundary routine writes the source buffers' ghost and
-    // step-face values first (the step kernel pulls them as stored faces)
-    if (b->nbfs > 0) {
-        if (b->T.batch_bfs(b->d_lats, b->d_cur, b->d_bfs, b->nbfs, parity, b->st) != cudaSuccess) return BGK_E_CUDA;
-        b->launches++;
-    }
     if (b->ntiles > 0) {
         if (b->T.batch_step(b->d_lats, b->d_cur, b->d_tiles, b->ntiles, parity, b->cfg, grid_of(b), b->pf, b->st) !=
             cudaSuccess)
@@ -216,7 +191,7 @@ int step_impl(bgk_batch *b, int n, bool use_graph)
         while (n >= b->graph_steps) {
             if (b->graph_built_for != b->generation && (rc = capture(b))) return rc;
             if (cudaGraphLaunch(b->graph, b->st) != cudaSuccess) return BGK_E_CUDA;
-            b->launches += (int64_t)b->graph_steps * ((b->nbfs > 0) + (b->ntiles > 0) + (b->nles > 0));
+            b->launches += (int64_t)b->graph_steps * ((b->ntiles > 0) + (b->nles > 0));
             advance_members(b, b->graph_steps);  // graph_steps is even: buffers unchanged
             n -= b->graph_steps;
         }
@@ -279,7 +254,6 @@ int bgk_batch_destroy(bgk_batch *b)
     if (b->d_lats) cudaFreeAsync(b->d_lats, b->st);
     if (b->d_cur) cudaFreeAsync(b->d_cur, b->st);
     if (b->d_tiles) cudaFreeAsync(b->d_tiles, b->st);
-    if (b->d_bfs) cudaFreeAsync(b->d_bfs, b->st);
     cudaStreamSynchronize(b->st);
     if (b->done) cudaEventDestroy(b->done);
     if (b->ev0) cudaEventDestroy(b->ev0);

@@ -36,8 +36,7 @@ __host__ __device__ constexpr int opp_of(int q) {
 }
 
 enum Face { XLO = 0, XHI = 1, YLO = 2, YHI = 3 };
-enum FaceKind { FK_WALL = 0, FK_PERIODIC = 1, FK_INFLOW = 2, FK_OUTFLOW_EQ = 3, FK_OUTFLOW_ZG = 4,
-                FK_STORED = 5 };  // STORED: ghost values written into the source buffer before the step
+enum FaceKind { FK_WALL = 0, FK_PERIODIC = 1, FK_INFLOW = 2, FK_OUTFLOW_EQ = 3, FK_OUTFLOW_ZG = 4 };
 
 // 16-bit storage keeps (f_q - w_q) * s_q with a power-of-two s_q close to 1/w_q, so the
 // scaling is exact and only the 16-bit rounding loses information.
@@ -199,6 +198,10 @@ struct Lattice {
     int32_t faces[4];        // FaceKind per face
     int32_t corner_x;        // 1: at a corner the x-face rule wins over the y-face rule (-DTRICK1)
     int32_t noshift;         // 1: planes hold the populations f, not the deviations f - w (-DNOSHIFT)
+    int32_t inflow_y0;       // an x_lo inflow face supplies rows >= inflow_y0; below it bounces back
+    int32_t step_x, step_y;  // backward-facing step corner (stepx, stepy), 0 without a step
+    void *step_aux;          // AA with a step: 10 storage elements, the five bounced-back inputs of
+                             // step_bounce (0-4) and the five pushes their neighbours hold back (5-9)
     double wt[4][9];         // wall term added to the bounced population, per face and direction
     double omega, fgrad;     // relaxation rate and body-force gradient (compute kind)
     int32_t forced;          // 1 when the x body force fgrad*rho is applied (CHANNEL)
@@ -244,6 +247,27 @@ __device__ __forceinline__ int64_t cell_index(const Lattice &L, int x, int y) {
 __device__ __forceinline__ bool obs_bit(const Lattice &L, int x, int y) {
     uint32_t w = __ldg(L.mask + (int64_t)y * L.mask_pitch + (x >> 5));
     return (w >> (x & 31)) & 1u;
+}
+
+// Backward-facing step (SRC/bcond.step.F90:207-255).  Its two face loops run one cell past the
+// solid block (i = 1..stepx at row stepy-1, j = 1..stepy at column stepx-1, the block being
+// x < stepx, y < stepy), so they also overwrite populations at fluid positions; after both loops,
+// in their order, four inputs of the corner cell (stepx, stepy) and one of (stepx-1, stepy) are
+// bounce-backs of the cell's own opposite population: 01, 05, 08 and 12 of the corner, 12 of its
+// left neighbour.  (The D01 input of (stepx, stepy-1) is overwritten twice and ends with its
+// normal value.)  Returns whether input q of cell (x, y) is such a bounce-back.
+__device__ __forceinline__ bool step_bounce(const Lattice &L, int x, int y, int q)
+{
+    if (L.step_x <= 0 || y != L.step_y) return false;
+    if (x == L.step_x) return q == D01 || q == D05 || q == D08 || q == D12;
+    return x == L.step_x - 1 && q == D12;
+}
+
+// index 0..4 of a step_bounce input (x, y, q) among the five (L.step_aux)
+__device__ __forceinline__ int step_slot(const Lattice &L, int x, int q)
+{
+    if (x != L.step_x) return 4;
+    return q == D01 ? 0 : q == D05 ? 1 : q == D08 ? 2 : 3;
 }
 
 }  // namespace bgk

@@ -34,6 +34,7 @@ struct bgk_handle {
     void *d_planes = nullptr;
     size_t planes_bytes = 0;
     uint32_t *d_mask = nullptr;
+    void *d_step_aux = nullptr;    // Lattice::step_aux (AA with a backward-facing step)
     double *d_inflow = nullptr;
     double *d_partial = nullptr;
     double *d_out = nullptr;

@@ -196,12 +196,6 @@ cudaError_t fill_outflow(const Lattice &L, cudaStream_t st)
     return cudaGetLastError();
 }
 
-template <typename S, typename K>
-cudaError_t bcond_step(const Lattice &L, int cur, int stepx, int stepy, cudaStream_t st)
-{
-    bfs_bcond_kernel<S, K><<<1, 1024, 0, st>>>(L, cur, stepx, stepy);
-    return cudaGetLastError();
-}
 
 template <typename S, typename K>
 cudaError_t batch_les(const Lattice *lats, const int *cur, const int4 *tiles, int n, int parity, cudaStream_t st)
@@ -211,12 +205,6 @@ cudaError_t batch_les(const Lattice *lats, const int *cur, const int4 *tiles, in
     return cudaGetLastError();
 }
 
-template <typename S, typename K>
-cudaError_t batch_bfs(const Lattice *lats, const int *cur, const int4 *members, int n, int parity, cudaStream_t st)
-{
-    batch_bfs_kernel<S, K><<<n, 1024, 0, st>>>(lats, cur, members, parity);
-    return cudaGetLastError();
-}
 
 template <typename S>
 cudaError_t init_tgv(const Lattice &L, double u0, cudaStream_t st)
@@ -353,8 +341,6 @@ KernelTable make_table()
     t.scatter = &scatter<S>;
     t.gather = &gather<S, K>;
     t.fill_outflow = &fill_outflow<S, K>;
-    t.bcond_step = &bcond_step<S, K>;
-    t.batch_bfs = &batch_bfs<S, K>;
     t.batch_les = &batch_les<S, K>;
     t.init_tgv = &init_tgv<S>;
     t.diagno = &diagno<S, K>;

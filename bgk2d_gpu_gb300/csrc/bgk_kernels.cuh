@@ -479,11 +479,10 @@ __device__ __forceinline__ K pull_rule(const Lattice &L, int q, int x, int y, Pl
     int sx = x - cx_of(q), sy = y - cy_of(q);
     const int l = L.lx, m = L.ly;
     const int oq = opp_of(q);
+    if (HAS_OBS && step_bounce(L, x, y, q)) return own(oq);
     if ((sy < 1 || sy > m) && !(L.corner_x && (sx < 1 || sx > l))) {
         const int f = sy < 1 ? YLO : YHI;
-        if (L.faces[f] == FK_STORED) {
-            return plane_at(q, sx, sy);
-        } else if (L.faces[f] == FK_PERIODIC) {
+        if (L.faces[f] == FK_PERIODIC) {
             sy = (sy < 1) ? m : 1;
         } else {
             K v = own(oq);
@@ -494,11 +493,10 @@ __device__ __forceinline__ K pull_rule(const Lattice &L, int q, int x, int y, Pl
     if (sx < 1 || sx > l) {
         const int f = sx < 1 ? XLO : XHI;
         const int kind = L.faces[f];
-        if (kind == FK_STORED) {
-            return plane_at(q, sx, sy);
-        } else if (kind == FK_PERIODIC) {
+        if (kind == FK_PERIODIC) {
             sx = (sx < 1) ? l : 1;
-        } else if (kind == FK_WALL) {
+        } else if (kind == FK_WALL || (kind == FK_INFLOW && sy < L.inflow_y0)) {
+            // below the inflow rows of a backward-facing step the x_lo face is the step's wall
             K v = own(oq);
             const K wt = (K)L.wt[f][q];
             return wt != (K)0 ? rnd<S, K>(q, v + wt) : v;
@@ -584,6 +582,8 @@ __device__ __forceinline__ bool needs_rule(const Lattice &L, int x, int y)
 {
     if (x == 1 || x == L.lx || y == 1 || y == L.ly) return true;
     if (HAS_OBS) {
+        // the corner of a backward-facing step and its neighbours: step_bounce pulls and pushes
+        if (L.step_x > 0 && abs(x - L.step_x) <= 1 && abs(y - L.step_y) <= 1) return true;
         if (y >= L.ob_y0 && y <= L.ob_y1 && x >= L.ob_x0 && x <= L.ob_x1) {
             for (int dy = -1; dy <= 1; ++dy)
                 for (int dx = -1; dx <= 1; ++dx)
@@ -865,7 +865,8 @@ __device__ __forceinline__ void aa_push_rule(const Lattice &L, S *base, int q, i
             tx = (tx < 1) ? l : 1;
         } else {
             base[q * pe + cell_index<S>(L, tx, ty)] = gs;
-            if (kind == FK_WALL) {
+            // below the inflow rows of a backward-facing step the x_lo face is the step's wall
+            if (kind == FK_WALL || (kind == FK_INFLOW && ty < L.inflow_y0)) {
                 const K wt = (K)L.wt[f][oq];
                 const S b = wt != (K)0 ? Store<S>::template putq<K>(gr + wt, oq) : Store<S>::template putq<K>(gr, oq);
                 base[oq * pe + cell_index<S>(L, x, y)] = b;
@@ -874,6 +875,19 @@ __device__ __forceinline__ void aa_push_rule(const Lattice &L, S *base, int q, i
         }
     }
     if (HAS_OBS) {
+        // backward-facing step (step_bounce).  A target whose input q is the bounce-back of its
+        // own opposite population takes nothing from this push: the slot keeps the target's own
+        // phase-0 value, which the target pulls in this step (pull_rule), and no other cell
+        // touches it; the pushed value goes to L.step_aux[5..9] instead, where the readers of the
+        // phase-1 state find it (post_value).  The cell whose input oq is such a bounce-back
+        // keeps the value of this push in L.step_aux[0..4], where its next (local) step reads it
+        // (aa_l_kernel): its own slot oq belongs to the neighbour x - c_oq during this step.
+        S *aux = reinterpret_cast<S *>(L.step_aux);
+        if (step_bounce(L, x, y, oq)) aux[step_slot(L, x, oq)] = gs;
+        if (step_bounce(L, tx, ty, q)) {
+            aux[5 + step_slot(L, tx, q)] = gs;
+            return;
+        }
         if (obs_bit(L, tx, ty)) {
             base[oq * pe + cell_index<S>(L, x, y)] = Store<S>::template putq<K>(gr, oq);
             return;
@@ -899,6 +913,7 @@ __device__ __forceinline__ void aa_incoming(const Lattice &L, S *base, int x, in
                 if (L.faces[sy < 1 ? YLO : YHI] != FK_PERIODIC) continue;  // bounced instead
                 sy = sy < 1 ? m : 1;
             }
+            if (sy < L.inflow_y0) continue;  // the step's wall below the inflow rows: bounced instead
             base[q * pe + cell_index<S>(L, x, y)] =
                 Store<S>::template putq<K>((K)L.inflow[(int64_t)t * (m + 2) + sy], q);
         }
@@ -1210,6 +1225,15 @@ __global__ void __launch_bounds__(TXV *TY, TXV * TY != 128 ? 1 : (N * sizeof(S) 
             K v[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) v[q] = ldq<S, K>(base + q * pe, i, q);
+            if (HAS_OBS && L.step_x > 0) {
+                // backward-facing step: an input that is the bounce-back of the cell's own opposite
+                // population comes from L.step_aux, where the previous step's push kept it
+                // (aa_push_rule); the cell's own slot for it was left unwritten
+#pragma unroll 1
+                for (int q = 0; q < 8; ++q)
+                    if (step_bounce(L, xc, y, q))
+                        v[q] = Store<S>::template getq<K>(reinterpret_cast<const S *>(L.step_aux)[step_slot(L, xc, q)], q);
+            }
             collide_stored<S, K, CV>(v, omega, fgrad, forced, lat_cte_s<K>(L));
             K g[9];
 #pragma unroll

@@ -19,8 +19,9 @@ struct CaseSetup {
     double wt[4][9];
     double omega, fgrad, u00, u0;   // values of the compute kind
     int forced;
-    int bfs = 0;                    // backward-facing step: boundary kernel before each step
+    int bfs = 0;                    // backward-facing step (solid block, inflow above it, outflow)
     int stepx = 0, stepy = 0;       // step corner (SRC/input.F90:74-75)
+    int inflow_y0 = 0;              // first row of the x_lo inflow (the step's wall below it)
     int corner_x = 0;               // the x-wall rule sets the corner ghosts (-DTRICK1)
     int noshift = 0;                // populations stored whole, not as deviations (-DNOSHIFT)
     int les;                        // Smagorinsky eddy viscosity on
@@ -181,13 +182,19 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
         cs.wt[YHI][D10] = (double)(-force);
         break;
     case BGK_CASE_BFS:
-        // every ghost value is written by the step's boundary kernel (SRC/bcond.step.F90)
-        cs.faces[XLO] = cs.faces[XHI] = cs.faces[YLO] = cs.faces[YHI] = FK_STORED;
+        // SRC/bcond.step.F90 as face and obstacle rules: the equilibrium outflow at x_hi
+        // (:66-101), the parabolic inflow at x_lo from row stepy up (:118-151) with the step's
+        // wall below it, no-slip walls at y (:168-190), and the block x < stepx, y < stepy as
+        // obstacle cells, whose faces (:207-255) are the obstacle bounce-back except at the
+        // step's corner (step_bounce)
+        cs.faces[XLO] = FK_INFLOW;
+        cs.faces[XHI] = FK_OUTFLOW_EQ;
+        cs.faces[YLO] = cs.faces[YHI] = FK_WALL;
         cs.bfs = 1;
         cs.stepx = l / 20;
         cs.stepy = m / 2;
+        cs.inflow_y0 = cs.stepy;
         if (cs.stepx < 2 || m < 4) return "backward-facing step needs lx >= 40 and ly >= 4";
-        if (d.scheme == BGK_SCHEME_AA) return "backward-facing step: ping-pong or two-pass scheme only";
         break;
     case BGK_CASE_CUSTOM:
         for (int f = 0; f < 4; ++f) cs.faces[f] = d.faces[f];
@@ -214,13 +221,13 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
         cs.corner_x = 1;
     }
     for (int f = 0; f < 4; ++f)
-        if ((cs.faces[f] < FK_WALL || cs.faces[f] > FK_OUTFLOW_ZG) && !cs.bfs) return "unknown face kind";
+        if (cs.faces[f] < FK_WALL || cs.faces[f] > FK_OUTFLOW_ZG) return "unknown face kind";
     if ((cs.faces[XLO] == FK_PERIODIC) != (cs.faces[XHI] == FK_PERIODIC)) return "x faces: periodic must pair";
     if ((cs.faces[YLO] == FK_PERIODIC) != (cs.faces[YHI] == FK_PERIODIC)) return "y faces: periodic must pair";
     if (cs.faces[XHI] == FK_INFLOW) return "inflow is supported on the x_lo face only";
     if (cs.faces[XLO] == FK_OUTFLOW_EQ || cs.faces[XLO] == FK_OUTFLOW_ZG) return "outflow is supported on the x_hi face only";
     for (int f = YLO; f <= YHI; ++f)
-        if (cs.faces[f] != FK_WALL && cs.faces[f] != FK_PERIODIC && !cs.bfs) return "y faces must be walls or periodic";
+        if (cs.faces[f] != FK_WALL && cs.faces[f] != FK_PERIODIC) return "y faces must be walls or periodic";
 
     // inflow table (u_inflow=0.1 is a default-real literal in SRC/bcond.inflow.F90:59)
     const K uin = d.u_inflow > 0 ? (K)d.u_inflow : (K)0.1f;
@@ -236,8 +243,7 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
             inflow_eq<K>(xj, e, d.noshift != 0);
             for (int t = 0; t < 3; ++t) cs.inflow[(size_t)t * (m + 2) + j] = (double)e[t];
         }
-    }
-    if (cs.faces[XLO] == FK_INFLOW) {
+    } else if (cs.faces[XLO] == FK_INFLOW) {
         for (int j = 0; j <= m + 1; ++j) {
             K u = uin;
             if (d.inflow_profile == 1) {
@@ -253,6 +259,7 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
     // obstacle (SRC/build.obs.F90; VKS always has one, SRC/Makefile:176)
     int shape = d.obstacle;
     if (d.tcase == BGK_CASE_VKS && shape == BGK_OBS_NONE) shape = BGK_OBS_CIRCLE;
+    if (cs.bfs && shape != BGK_OBS_NONE) return "backward-facing step: no obstacle besides the step";
     cs.radius = d.radius;
     cs.icoord = d.obs_icoord >= 0 ? d.obs_icoord : 2 * l / 5;
     cs.jcoord = d.obs_jcoord >= 0 ? d.obs_jcoord : m / 2;
@@ -274,12 +281,20 @@ inline std::string setup_case(const bgk_case_desc &d, CaseSetup &cs)
         if (shape < BGK_OBS_CIRCLE || shape > BGK_OBS_HALF_CIRCLE) return "unknown obstacle shape";
         if (d.radius > m - 2) return "radius too big";  // SRC/input.F90:83-86
         build_obs<K>(l, m, shape, d.radius, cs.icoord, cs.jcoord, cs.obs, cs.bbox);
+    } else if (cs.bfs) {
+        // the solid block x = 1..stepx-1, y = 1..stepy-1 of the step; it touches the x_lo and
+        // y_lo faces, whose rules never reach into it from a fluid cell
+        cs.obs.assign((size_t)l * (size_t)m, 0);
+        for (int j = 1; j < cs.stepy; ++j)
+            for (int i = 1; i < cs.stepx; ++i) cs.obs[(size_t)(i - 1) + (size_t)(j - 1) * l] = 1;
+        cs.bbox[0] = 1; cs.bbox[1] = cs.stepx - 1; cs.bbox[2] = 1; cs.bbox[3] = cs.stepy - 1;
+        cs.bbox[4] = (cs.stepx - 1) * (cs.stepy - 1);
     } else {
         cs.obs.assign((size_t)l * (size_t)m, 0);
     }
     if (cs.bbox[4] > 0) {
         cs.has_obs = true;
-        if (cs.bbox[0] < 2 || cs.bbox[1] > l - 1 || cs.bbox[2] < 2 || cs.bbox[3] > m - 1)
+        if (!cs.bfs && (cs.bbox[0] < 2 || cs.bbox[1] > l - 1 || cs.bbox[2] < 2 || cs.bbox[3] > m - 1))
             return "obstacle must not touch the domain boundary";
     }
     return "";

@@ -52,10 +52,6 @@ struct KernelTable {
     cudaError_t (*scatter)(const Lattice &L, int cur, int q, const void *src, int64_t ld, cudaStream_t st);
     cudaError_t (*gather)(const Lattice &L, int cur, int phase, int q, void *dst, int64_t ld, bool obs, cudaStream_t st);
     cudaError_t (*fill_outflow)(const Lattice &L, cudaStream_t st);
-    cudaError_t (*bcond_step)(const Lattice &L, int cur, int stepx, int stepy, cudaStream_t st);
-    // the backward-facing-step boundary routine of n batch members (entries member, stepx, stepy)
-    cudaError_t (*batch_bfs)(const Lattice *lats, const int *cur, const int4 *members, int n, int parity,
-                             cudaStream_t st);
     // the Smagorinsky step of a batch's LES members over their n work-list entries
     cudaError_t (*batch_les)(const Lattice *lats, const int *cur, const int4 *tiles, int n, int parity, cudaStream_t st);
     cudaError_t (*init_tgv)(const Lattice &L, double u0, cudaStream_t st);

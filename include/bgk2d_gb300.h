@@ -70,7 +70,8 @@ extern "C" {
 #define BGK_CASE_VKS 3     /* bcond_inflow (+ obstacle, drag/lift) */
 #define BGK_CASE_COU 4     /* bcond_couette */
 #define BGK_CASE_BFS 5     /* bcond_step: backward-facing step, stepx = lx/20, stepy = ly/2
-                              (SRC/input.F90:74-75); ping-pong only, lx >= 40 */
+                              (SRC/input.F90:74-75); lx >= 40, ly >= 4.  The block x < stepx,
+                              y < stepy is an obstacle: bgk_get_obs returns it */
 #define BGK_CASE_MYV 6     /* -DMYVERSION: bcond_periodic with the CHANNEL body force fgrad
                               (SRC/boundaries.F90:46-48, SRC/build.bcond.F90:39-41) */
 #define BGK_CASE_CUSTOM 9  /* faces[] and wall_u[] given explicitly */

@@ -20,7 +20,7 @@ ORACLE_CASE = {"LDC": 0, "TGV": 1, "POF": 2, "VKS": 3, "COU": 4, "BFS": 5, "MYV"
 def draw(rng):
     tc = str(rng.choice(["LDC", "LDC", "TGV", "POF", "COU", "VKS", "MYV", "BFS"]))
     prec = str(rng.choice(list(PRECS)))
-    scheme = str(rng.choice(["pingpong", "aa", "original"] if tc != "BFS" else ["pingpong", "original"]))
+    scheme = str(rng.choice(["pingpong", "aa", "original"]))
     if tc == "VKS":
         lx, ly = int(rng.integers(40, 131)), int(rng.integers(18, 71))
     elif tc == "BFS":

@@ -252,17 +252,18 @@ def _bfs_fluid(a, lx, ly):
     return g[:, keep]
 
 
-@pytest.mark.parametrize("tile", [2, 6])
+@pytest.mark.parametrize("scheme,tile", [("pingpong", 2), ("pingpong", 6), ("aa", 2), ("aa", 5)])
 @pytest.mark.parametrize("prec", ["single", "double", "mixed2"])
-def test_bfs_bit_exact(oracle_mod, bgk, prec, tile):
-    """Backward-facing step (SRC/bcond.step.F90): outflow, parabolic inflow above the step, no-slip
-    walls and the step faces written by a boundary kernel before each fused step.  The solid block
-    holds values nobody reads back (the reference poisons its second buffer with huge(), this
-    code with zeros), so the fluid cells are compared."""
+def test_bfs_bit_exact(oracle_mod, bgk, prec, scheme, tile):
+    """Backward-facing step (SRC/bcond.step.F90) folded into the step's rules: equilibrium outflow,
+    parabolic inflow above the step and the step's wall below it, no-slip walls, the solid block
+    as obstacle cells and the five bounce-backs at its corner (step_bounce).  The solid block
+    holds values nobody reads back (the reference poisons its second buffer with huge()), so the
+    fluid cells are compared, in ping-pong (register and staged kernels) and AA."""
     oprec, st, cp = PRECS[prec]
     lx, ly = 200, 64
     o = oracle_mod.Oracle(lx, ly, prec=oprec, tcase=oracle_mod.BFS, svisc=0.02, u0=0.1)
-    with bgk.Solver(lx, ly, tcase="BFS", svisc=0.02, u0=0.1, storage=st, compute=cp) as s:
+    with bgk.Solver(lx, ly, tcase="BFS", svisc=0.02, u0=0.1, storage=st, compute=cp, scheme=scheme) as s:
         s.set_tile(tile)
         for n in (1, 2, 40, 75):
             s.step(n)
@@ -296,11 +297,19 @@ def test_bfs_fluid_cells_never_read_the_solid_block(oracle_mod, bgk, prec, tile)
             assert not np.isfinite(got[:, 1:sy - 1, 1:sx - 1]).any()  # the block itself stays poisoned
 
 
-def test_bfs_rejects_aa(bgk):
-    """The backward-facing step has no AA form (AA keeps no ghost frame for its boundary routine
-    to write before the step); batches take BFS members (tests/test_gpu_batch.py)."""
-    with pytest.raises(bgk.BgkError):
-        bgk.Solver(200, 64, tcase="BFS", scheme="aa")
+@pytest.mark.parametrize("scheme", ["pingpong", "aa"])
+def test_bfs_small_steps_and_tiles(oracle_mod, bgk, scheme):
+    """Backward-facing steps down to the smallest (lx = 40: stepx = 2, a one-column block; ly = 4
+    and 5: stepy = 2, a one-row block), odd sizes, every tile shape of the scheme; fluid cells
+    bit-exact against the oracle."""
+    for lx, ly in ((40, 4), (41, 5), (60, 9), (83, 31), (140, 6)):
+        for tile in range(9 if scheme == "pingpong" else 6):
+            o = oracle_mod.Oracle(lx, ly, prec=0, tcase=oracle_mod.BFS, svisc=0.02, u0=0.1)
+            with bgk.Solver(lx, ly, tcase="BFS", svisc=0.02, u0=0.1, scheme=scheme) as s:
+                s.set_tile(tile)
+                s.step(23)
+                o.step(23)
+                assert np.array_equal(_bfs_fluid(s.download(), lx, ly), _bfs_fluid(o.raw(), lx, ly)), (lx, ly, tile)
 
 
 @pytest.mark.parametrize("scheme", ["pingpong", "aa"])
