@@ -19,7 +19,7 @@ def make_cases(bgk, storage):
         dict(lx=512, ly=128, tcase="CUSTOM", svisc=0.02, u0=0.0, faces=("inflow", "outflow_zg", "wall", "wall"),
              u_inflow=0.05, inflow_profile=1, obstacle="circle", radius=16, obs_center=(128, 65)),
         dict(lx=160, ly=62, tcase="VKS", svisc=0.05, u0=0.1, radius=6),
-        # backward-facing steps: their boundary routine runs as one batched launch before each step
+        # backward-facing steps: their boundary rules are the fused step's own
         dict(lx=200, ly=64, tcase="BFS", svisc=0.02, u0=0.1),
         dict(lx=120, ly=50, tcase="BFS", svisc=0.03, u0=0.1),
         # Smagorinsky members: their step runs as a batched launch of its own
