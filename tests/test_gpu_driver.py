@@ -24,15 +24,15 @@ ipad=0        /
 """
 
 
-def run_driver(bgk, tmp, case="LDC", prec="single", **kw):
+def run_driver(bgk, tmp, case="LDC", prec="single", extra=(), **kw):
     from bgk2d_gpu_gb300 import build
     exe = build.EXE_PATH
     assert os.path.exists(exe)
     p = dict(lx=64, ly=48, svisc=0.0384, itfin=300, isignal=100, itsave=150, icheck=100, irestart=0, ivtim=1000000)
     p.update(kw)
     (tmp / "bgk.input").write_text(NAMELIST.format(**p))
-    r = subprocess.run([exe, "--input", str(tmp / "bgk.input"), "--case", case, "--prec", prec, "--dir", str(tmp)],
-                       capture_output=True, text=True, timeout=300)
+    r = subprocess.run([exe, "--input", str(tmp / "bgk.input"), "--case", case, "--prec", prec, "--dir", str(tmp),
+                        *extra], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     return p
 
@@ -157,3 +157,32 @@ def test_driver_vtk_files(bgk, tmp_path):
     assert np.array_equal(xy["u"], u.ravel()) and np.array_equal(xy["rho"], r.ravel())
     assert np.array_equal(xy["velocity"][1::3], w.ravel())
     assert np.array_equal(om["vorticity"], vort.ravel()) and np.array_equal(om["stream"], st.ravel())
+
+
+@pytest.mark.parametrize("case,prec,extra,skw", [
+    ("BFS", "single", ["--scheme", "aa"], dict(scheme="aa")),
+    ("MYV", "single", ["--forcing-y", "1"], dict(force_y=True)),
+    ("LDC", "double", ["--noshift", "1"], dict(noshift=True, storage="f64")),
+    ("LDC", "mixed2", ["--trick1", "1"], dict(trick1=True, storage="f32", compute="f64")),
+])
+def test_driver_build_variants_match_solver(bgk, tmp_path, case, prec, extra, skw):
+    """The driver's switches for the reference's build variants (AA scheme with the backward-facing
+    step, FORCING_Y with MYVERSION, NOSHIFT, TRICK1): the files it writes hold what the library
+    gives for the same case: diagno.dat, the profiles computed on the device, and a checkpoint
+    that restarts exactly."""
+    p = run_driver(bgk, tmp_path, case=case, prec=prec, extra=extra, lx=48, ly=48, svisc=0.02)
+    with bgk.Solver(p["lx"], p["ly"], tcase=case, svisc=p["svisc"], u0=0.1, **skw) as s:
+        s.step(300)
+        d = s.diagno(2)
+        u, v, den = s.prof_j(p["lx"] // 2)
+    rows = [ln.split() for ln in (tmp_path / "diagno.dat").read_text().splitlines()]
+    np.testing.assert_allclose([float(x) for x in rows[-1][1:]], d, rtol=1e-5, atol=1e-12)
+    last = (tmp_path / "prof_j.dat").read_text().split("# t=")[-1].strip().splitlines()[1:]
+    vals = np.array([[float(x) for x in ln.split()] for ln in last])
+    np.testing.assert_allclose(vals[:, 1], u, rtol=1e-5, atol=1e-11)
+    np.testing.assert_allclose(vals[:, 3], den, rtol=1e-5)
+    b = tmp_path / "b"
+    b.mkdir()
+    shutil.copy(tmp_path / "save.00000150.bin", b / "restore.bin")
+    run_driver(bgk, b, case=case, prec=prec, extra=extra, lx=48, ly=48, svisc=0.02, irestart=1)
+    assert (tmp_path / "diagno.dat").read_text().splitlines()[-1] == (b / "diagno.dat").read_text().splitlines()[-1]
