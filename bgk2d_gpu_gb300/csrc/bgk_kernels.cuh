@@ -495,8 +495,9 @@ __device__ __forceinline__ K pull_rule(const Lattice &L, int q, int x, int y, Pl
         const int kind = L.faces[f];
         if (kind == FK_PERIODIC) {
             sx = (sx < 1) ? l : 1;
-        } else if (kind == FK_WALL || (kind == FK_INFLOW && sy < L.inflow_y0)) {
-            // below the inflow rows of a backward-facing step the x_lo face is the step's wall
+        } else if (kind == FK_WALL || (HAS_OBS && kind == FK_INFLOW && sy < L.inflow_y0)) {
+            // below the inflow rows of a backward-facing step (a case with obstacle cells, the
+            // step's block) the x_lo face is the step's wall
             K v = own(oq);
             const K wt = (K)L.wt[f][q];
             return wt != (K)0 ? rnd<S, K>(q, v + wt) : v;
@@ -866,7 +867,7 @@ __device__ __forceinline__ void aa_push_rule(const Lattice &L, S *base, int q, i
         } else {
             base[q * pe + cell_index<S>(L, tx, ty)] = gs;
             // below the inflow rows of a backward-facing step the x_lo face is the step's wall
-            if (kind == FK_WALL || (kind == FK_INFLOW && ty < L.inflow_y0)) {
+            if (kind == FK_WALL || (HAS_OBS && kind == FK_INFLOW && ty < L.inflow_y0)) {
                 const K wt = (K)L.wt[f][oq];
                 const S b = wt != (K)0 ? Store<S>::template putq<K>(gr + wt, oq) : Store<S>::template putq<K>(gr, oq);
                 base[oq * pe + cell_index<S>(L, x, y)] = b;
