@@ -93,6 +93,7 @@ std::map<std::string, std::string> read_namelist(const std::string &path)
     return kv;
 }
 
+// the nine (0:l+1, 0:m+1) host planes of a checkpoint (save.XXXXXXXX.bin / restore.bin)
 struct Pops {
     int lx, ly, hb;
     std::vector<char> mem;
@@ -103,11 +104,6 @@ struct Pops {
         n = (size_t)(l + 2) * (m + 2);
         mem.resize(9 * n * hb);
         for (int q = 0; q < 9; ++q) p[q] = mem.data() + q * n * hb;
-    }
-    double at(int q, int i, int j) const
-    {
-        const size_t k = (size_t)i + (size_t)j * (lx + 2);
-        return hb == 8 ? ((const double *)p[q])[k] : (double)((const float *)p[q])[k];
     }
 };
 
