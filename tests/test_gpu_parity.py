@@ -298,6 +298,22 @@ def test_bfs_fluid_cells_never_read_the_solid_block(oracle_mod, bgk, prec, tile)
 
 
 @pytest.mark.parametrize("scheme", ["pingpong", "aa"])
+@pytest.mark.parametrize("prec", ["single", "double"])
+def test_bfs_long_run(oracle_mod, bgk, prec, scheme):
+    """1500 steps of a backward-facing step (the flow separates behind the step and reattaches):
+    the fluid cells stay bit-identical to the oracle's."""
+    oprec, st, cp = PRECS[prec]
+    lx, ly = 160, 40
+    o = oracle_mod.Oracle(lx, ly, prec=oprec, tcase=oracle_mod.BFS, svisc=0.01, u0=0.1)
+    with bgk.Solver(lx, ly, tcase="BFS", svisc=0.01, u0=0.1, storage=st, compute=cp, scheme=scheme) as s:
+        s.step(1500)
+        o.step(1500)
+        assert np.array_equal(_bfs_fluid(s.download(), lx, ly), _bfs_fluid(o.raw(), lx, ly))
+        u, _, _ = s.prof_j(lx // 2)
+        assert np.abs(u).max() > 0.01  # the inflow has reached mid-channel
+
+
+@pytest.mark.parametrize("scheme", ["pingpong", "aa"])
 def test_bfs_small_steps_and_tiles(oracle_mod, bgk, scheme):
     """Backward-facing steps down to the smallest (lx = 40: stepx = 2, a one-column block; ly = 4
     and 5: stepy = 2, a one-row block), odd sizes, every tile shape of the scheme; fluid cells
