@@ -335,9 +335,8 @@ constexpr int PIPE_STEPS = 16;
 bool pipeline_ok(const bgk_handle *h)
 {
     // pulls reach one row up and one row down, nothing else: no periodic y faces (row 1 pulls
-    // from row ly), no two-pass form, no collision variant (LES, NOSHIFT: the waves run the plain
-    // collision)
-    return h->L.scheme == BGK_SCHEME_PINGPONG && !h->two_pass && !h->L.les && !h->L.noshift &&
+    // from row ly), no two-pass form
+    return h->L.scheme == BGK_SCHEME_PINGPONG && !h->two_pass &&
            h->cs.faces[YLO] != FK_PERIODIC && h->cs.faces[YHI] != FK_PERIODIC && h->desc.ly >= 8;
 }
 
@@ -358,7 +357,10 @@ int run_waves(bgk_handle *h, const HostPlanes *in, const HostPlanes *out, int K)
     // bands of about ly/128 rows (32 at 4096^2); BGK_PIPE_ROWS / BGK_PIPE_XFER override the band
     // height and the blocks of each transfer
     const int R = std::max(1, std::min(ly, env_int("BGK_PIPE_ROWS", std::max(4, (ly + 127) / 128))));
-    const int cdiv = (h->cfg < NUM_CFG && TILE_CFGS[h->cfg].cdiv == 2) || h->T.elem_bytes == 2 ? 2 : 1;
+    // the shape of the handle's step: a collision variant (LES, NOSHIFT) has one, 16 bytes per
+    // thread for the exact kinds and 8 for the 16-bit ones
+    const bool cv = h->L.les || h->L.noshift;
+    const int cdiv = h->T.elem_bytes == 2 ? 2 : cv ? 1 : (h->cfg < NUM_CFG && TILE_CFGS[h->cfg].cdiv == 2) ? 2 : 1;
     const int nvec = (lx + h->T.vec / cdiv - 1) / (h->T.vec / cdiv);
     const int gx = (nvec + 127) / 128;
     // 256 blocks of 128 threads each way keep the host link busy

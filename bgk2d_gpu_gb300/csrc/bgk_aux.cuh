@@ -188,8 +188,9 @@ __device__ __forceinline__ void band_rows(const Lattice &L, const WaveArgs &a, i
 // One wave of bgk_advance_host (WaveArgs): grid rows 0.. carry the upload of band up_band, then
 // the download of band down_band (xfer_rows grid rows each, scheduled first so that the host
 // link is busy from the start of the wave), then band_rows grid rows per step item.  The step
-// items are pp_kernel's tiles (128 x 1 threads, N cells per thread) of one row each.
-template <typename S, typename K, typename H, bool HAS_OBS, int N>
+// items are pp_kernel's tiles (128 x 1 threads, N cells per thread) of one row each, with the
+// handle's collision variant CV.
+template <typename S, typename K, typename H, bool HAS_OBS, int N, int CV = 0>
 __global__ void __launch_bounds__(128, (N * sizeof(S) <= 8 || (sizeof(S) == 4 && N == 4)) ? 8 : (sizeof(S) == 2 ? 4 : 1))
     wave_kernel(const Lattice L, const WaveArgs a)
 {
@@ -218,7 +219,7 @@ __global__ void __launch_bounds__(128, (N * sizeof(S) <= 8 || (sizeof(S) == 4 &&
     const int k = a.k_lo + by / a.band_rows;
     const int y = (a.wave - 2 * k) * a.band_rows + by % a.band_rows + 1;
     if (y > L.ly) return;
-    pp_tile<S, K, 128, 1, HAS_OBS, N>(L, (int)blockIdx.x, y - 1, (a.cur0 + k - 1) & 1);
+    pp_tile<S, K, 128, 1, HAS_OBS, N, CV>(L, (int)blockIdx.x, y - 1, (a.cur0 + k - 1) & 1);
 }
 
 // AA phase-0 outflow ghosts at x = lx+1, from cell (lx, y)'s stored post-collision values

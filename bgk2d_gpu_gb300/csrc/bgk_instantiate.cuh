@@ -177,7 +177,25 @@ template <typename S, typename K, bool OBS, int N>
 cudaError_t wave_launch(const Lattice &L, const WaveArgs &a, int grid_y, cudaStream_t st)
 {
     const int nv = (L.lx + N - 1) / N;
-    wave_kernel<S, K, Host<S>, OBS, N><<<dim3((unsigned)((nv + 127) / 128), (unsigned)grid_y), 128, 0, st>>>(L, a);
+    const dim3 grid((unsigned)((nv + 127) / 128), (unsigned)grid_y);
+    // a collision variant steps with its own kernel shape: 16 bytes per thread for the exact
+    // kinds, 8 for the 16-bit ones (step_cv); the caller passes that N
+    if (L.les || L.noshift) {
+        if constexpr (Is16<S>::value) {
+            if constexpr (N == vec_of<S>() / 2) {
+                wave_kernel<S, K, Host<S>, OBS, N, CV_LES><<<grid, 128, 0, st>>>(L, a);
+                return cudaGetLastError();
+            }
+        } else if constexpr (N == vec_of<S>()) {
+            const int cv = (L.les ? CV_LES : 0) | (L.noshift ? CV_NOSHIFT : 0);
+            if (cv == CV_LES) wave_kernel<S, K, Host<S>, OBS, N, CV_LES><<<grid, 128, 0, st>>>(L, a);
+            else if (cv == CV_NOSHIFT) wave_kernel<S, K, Host<S>, OBS, N, CV_NOSHIFT><<<grid, 128, 0, st>>>(L, a);
+            else wave_kernel<S, K, Host<S>, OBS, N, CV_LES | CV_NOSHIFT><<<grid, 128, 0, st>>>(L, a);
+            return cudaGetLastError();
+        }
+        return cudaErrorInvalidValue;
+    }
+    wave_kernel<S, K, Host<S>, OBS, N><<<grid, 128, 0, st>>>(L, a);
     return cudaGetLastError();
 }
 

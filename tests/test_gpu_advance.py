@@ -70,6 +70,33 @@ def test_advance_other_boundaries(bgk, case):
     _run(bgk, torch, case, "f32", 120 if case == "bfs" else 64, 50, 20)
 
 
+@pytest.mark.parametrize("storage,extra", [("f32", dict(les=True, cte_s=0.2)), ("f16", dict(les=True, cte_s=0.2)),
+                                           ("f32", dict(noshift=True)), ("f64", dict(noshift=True)),
+                                           ("f64", dict(noshift=True, les=True, cte_s=0.2))])
+def test_advance_collision_variants_pipelined(bgk, storage, extra):
+    """Handles with the Smagorinsky collision or whole-population storage go through the same
+    pipelined waves (their own kernel variant inside) and match the three calls bit for bit."""
+    torch = pytest.importorskip("torch")
+    lx, ly, K = 96, 70, 20
+    kw = dict(tcase="LDC", svisc=0.01, u0=0.1, storage=storage, **extra)
+    with bgk.Solver(lx, ly, **kw) as a, bgk.Solver(lx, ly, **kw) as b:
+        a.step(7)
+        start = a.download()
+        b.upload(start)
+        b.step(K)
+        want = b.download()
+        src = _pinned(torch, start, lx + 2)
+        dst = _pinned(torch, np.zeros_like(start), lx + 2)
+        n0 = a.launches()
+        a.advance_host(src, dst, K)
+        # one launch per wave: more than the K + 2 of the sequential calls
+        assert a.launches() - n0 > K + 2
+        assert np.array_equal(dst.numpy(), want)
+        a.step(3)
+        b.step(3)
+        assert np.array_equal(a.download(), b.download())
+
+
 def test_advance_aa_takes_the_sequential_path(bgk):
     torch = pytest.importorskip("torch")
     _run(bgk, torch, "ldc", "f32", 64, 40, 9, scheme="aa")
