@@ -29,6 +29,7 @@ CASES16 = {
     "cou": ("COU", 83, 40, 0.1, 0.1, {}),
     "vks": ("VKS", 160, 62, 0.05, 0.1, {"radius": 6}),
     "myv_fy": ("MYV", 96, 40, 0.1, 0.1, {"force_y": True}),  # -DMYVERSION -DFORCING_Y
+    "bfs": ("BFS", 120, 40, 0.05, 0.1, {}),
 }
 TOL = {"f16": 2e-3, "bf16": 2e-2}
 STEPS = 300
