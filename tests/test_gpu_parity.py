@@ -124,6 +124,32 @@ def test_obstacle_mask_bit_exact(oracle_mod, bgk):
             assert np.array_equal(bb, rbb)
 
 
+@pytest.mark.parametrize("scheme", ["pingpong", "original"])
+@pytest.mark.parametrize("prec", list(PRECS))
+def test_large_obstacles_every_tile_shape(oracle_mod, bgk, prec, scheme):
+    """Obstacles wide enough that whole vectors and their neighbourhoods lie inside them (circle,
+    square and half circle of radius 3 to 20, centred and off-centre, in the periodic cylinder
+    channel), stepped with every tile shape: the populations, obstacle cells included, equal the
+    oracle's (SRC/build.obs.F90, SRC/bcond.obs.F90)."""
+    oprec, st, cp = PRECS[prec]
+    tiles = range(9) if scheme == "pingpong" else range(6)
+    for shape, name, lx, ly, r, c in ((1, "circle", 200, 90, 20, (-1, -1)), (2, "square", 181, 70, 17, (60, 33)),
+                                      (3, "half_circle", 150, 64, 12, (-1, -1)), (1, "circle", 97, 40, 3, (40, 20))):
+        o = oracle_mod.Oracle(lx, ly, prec=oprec, tcase=ORACLE_CASE["VKS"], svisc=0.05, u0=0.1,
+                              fused=scheme != "original", obs_order=oracle_mod.OBS_SNAPSHOT, obstacle=shape, radius=r,
+                              obs_icoord=c[0], obs_jcoord=c[1])
+        o.step(25)
+        for tile in tiles:
+            with bgk.Solver(lx, ly, tcase="VKS", svisc=0.05, u0=0.1, storage=st, compute=cp, scheme=scheme,
+                            obstacle=name, radius=r, obs_center=c) as s:
+                s.set_tile(tile)
+                s.step(25)
+                try:
+                    assert_same(o, s, scheme)
+                except AssertionError as e:
+                    raise AssertionError(f"{name} r={r} tile {tile}: {e}") from None
+
+
 def test_scalars_match_hencol(oracle_mod, bgk):
     for prec in ("single", "double"):
         for case in ("ldc", "pof", "cou"):
