@@ -350,10 +350,10 @@ int env_int(const char *name, int dflt)
 // and with the download into `out` (or leaving the state on the device).  The waves' own blocks
 // move each band between the mapped host planes and the state.  (Copy-engine forms, 3D copies per
 // band or per-plane copies of chunks of bands through a device staging copy, measured slower:
-// 6.98-7.27 ms against 6.6 ms for 20 steps of the 4096^2 cavity.  So did uploads by the waves
-// with downloads by the copy engines from a device copy of the host planes, in chunks of 256 to
-// 2048 rows: 6.6-7.8 ms, although one 604 MB read by the SMs and one 604 MB copy-engine write
-// to the host took 4.35 ms together against 6.1 ms one after the other.)
+// 6.98-7.27 ms against 6.6 ms for 20 steps of the 4096^2 cavity.  So did either direction by the
+// copy engines through a device copy of the host planes and the other by the waves, in chunks of
+// 128 to 2048 rows: 6.6-7.8 ms, although one 604 MB transfer each way, one by the SMs and one by
+// the copy engines, took 4.15-4.35 ms together against 6.1 ms one after the other.)
 int run_waves(bgk_handle *h, const HostPlanes *in, const HostPlanes *out, int K)
 {
     const int lx = h->desc.lx, ly = h->desc.ly;
