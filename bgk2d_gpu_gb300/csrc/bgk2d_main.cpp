@@ -11,11 +11,14 @@
 //
 //   bgk2d_gb300 [--input bgk.input] [--case LDC|TGV|POF|VKS|COU|BFS|MYV] [--prec single|double|mixed2|f16|bf16]
 //               [--scheme pingpong|aa|original] [--les 0|1] [--trick1 0|1] [--noshift 0|1]
-//               [--forcing-y 0|1] [--dir OUTDIR] [--check-input 0|1]
+//               [--forcing-y 0|1] [--obstacle circle|square|half_circle|read[:FILE]] [--dir OUTDIR]
+//               [--check-input 0|1]
 // `--les 1` stands for the reference's -DLES build (Smagorinsky constant from the namelist key cteS),
 // `--trick1 1` for its -DTRICK1 build (lid-cavity boundaries in one merged loop; square LDC only),
 // `--noshift 1` for its -DNOSHIFT build (whole populations, not deviations; FP32/FP64 only),
 // `--forcing-y 1` for -DFORCING_Y (the POF/MYV body force along y); `--case MYV` is -DMYVERSION.
+// `--obstacle` picks the obstacle of an -DOBSTACLE build: the circle (default of VKS), -DSQUARE,
+// -DHALF_CIRCLE, or -DREAD, which takes the mask from fort.96 (or FILE).
 // `--check-input 1` parses the input, prints the case it describes and exits, without a GPU.
 #include <cctype>
 #include <chrono>
@@ -299,6 +302,42 @@ int write_obstacle_files(bgk_handle *h, const std::string &dir, int lx, int ly)
     return BGK_OK;
 }
 
+// The obstacle file of the reference's READ build (SRC/build.obs.F90:148-168, unit 96): one
+// list-directed record `x y obs` per cell, i fastest within each row j; x and y are read and
+// dropped, and a cell is an obstacle where obs is 1.  The reference reads a hardwired 414 x 414
+// block ("WARNING: hardwired parameters"); this reads the domain's lx x ly cells, and rejects a
+// file with fewer records or a non-integer obs.
+bool read_obstacle_file(const std::string &path, int lx, int ly, std::vector<int32_t> &mask, int &nobs)
+{
+    std::ifstream f(path);
+    if (!f) return false;
+    auto next = [&f](std::string &t) -> bool {  // values separated by blanks, newlines or commas
+        t.clear();
+        char c;
+        while (f.get(c)) {
+            if (std::isspace((unsigned char)c) || c == ',') {
+                if (!t.empty()) return true;
+            } else {
+                t.push_back(c);
+            }
+        }
+        return !t.empty();
+    };
+    mask.assign((size_t)lx * (size_t)ly, 0);
+    nobs = 0;
+    std::string x, y, o;
+    for (int j = 0; j < ly; ++j)
+        for (int i = 0; i < lx; ++i) {
+            if (!next(x) || !next(y) || !next(o)) return false;
+            char *end = nullptr;
+            const long v = std::strtol(o.c_str(), &end, 10);
+            if (end == o.c_str() || *end != '\0') return false;
+            mask[(size_t)i + (size_t)j * lx] = (int32_t)v;
+            nobs += v == 1;
+        }
+    return true;
+}
+
 int die(const char *what, int rc)
 {
     std::fprintf(stderr, "bgk2d_gb300: %s failed (status %d)\n", what, rc);
@@ -310,7 +349,7 @@ int die(const char *what, int rc)
 int main(int argc, char **argv)
 {
     std::string input = "bgk.input", tcase = "LDC", prec = "single", scheme = "pingpong", dir = ".", les = "0";
-    std::string check = "0", trick1 = "0", noshift = "0", forcing_y = "0";
+    std::string check = "0", trick1 = "0", noshift = "0", forcing_y = "0", obstacle;
     const auto bad = [](const char *what, const std::string &v) {
         std::fprintf(stderr, "bgk2d_gb300: bad %s '%s'\n", what, v.c_str());
         return 2;
@@ -327,6 +366,7 @@ int main(int argc, char **argv)
         else if (k == "--trick1") trick1 = v;
         else if (k == "--noshift") noshift = v;
         else if (k == "--forcing-y") forcing_y = v;
+        else if (k == "--obstacle") obstacle = v;
         else if (k == "--check-input") check = v;
         else return bad("option", k);
     }
@@ -338,6 +378,9 @@ int main(int argc, char **argv)
     if (noshift != "0" && noshift != "1") return bad("--noshift", noshift);
     if (forcing_y != "0" && forcing_y != "1") return bad("--forcing-y", forcing_y);
     if (check != "0" && check != "1") return bad("--check-input", check);
+    const bool obs_read = obstacle == "read" || obstacle.rfind("read:", 0) == 0;
+    if (!obstacle.empty() && !obs_read && obstacle != "circle" && obstacle != "square" && obstacle != "half_circle")
+        return bad("--obstacle", obstacle);
     auto kv = read_namelist(input);
     if (kv.empty()) { std::fprintf(stderr, "bgk2d_gb300: no &parameters namelist in %s\n", input.c_str()); return 1; }
     auto geti = [&](const char *k, int d) { return kv.count(k) ? std::atoi(kv[k].c_str()) : d; };
@@ -370,15 +413,30 @@ int main(int argc, char **argv)
                                               {"MYV", BGK_CASE_MYV}};
     if (!cases.count(tcase)) { std::fprintf(stderr, "bgk2d_gb300: unknown case %s\n", tcase.c_str()); return 1; }
     d.tcase = cases.at(tcase);
+    std::vector<int32_t> obs_mask;
+    int obs_cells = -1;  // obstacle cells of a mask read from a file
+    if (obstacle == "circle") d.obstacle = BGK_OBS_CIRCLE;
+    else if (obstacle == "square") d.obstacle = BGK_OBS_SQUARE;
+    else if (obstacle == "half_circle") d.obstacle = BGK_OBS_HALF_CIRCLE;
+    else if (obs_read) {
+        const std::string path = obstacle.size() > 5 ? obstacle.substr(5) : "fort.96";
+        if (lx < 1 || ly < 1 || !read_obstacle_file(path, lx, ly, obs_mask, obs_cells)) {
+            std::fprintf(stderr, "bgk2d_gb300: cannot read %d x %d obstacle records from %s\n", lx, ly, path.c_str());
+            return 1;
+        }
+        d.obstacle = BGK_OBS_MASK;
+        d.obs_mask = obs_mask.data();
+    }
     // init_v is read but, as in SRC/init.F90 (whose argument is unused), the initial state depends
     // on the case alone: the periodic vortex for TGV, rest flow otherwise
     if (d.tcase == BGK_CASE_TGV) d.init_v = BGK_INIT_TGV_REF;
     (void)init_v;
     if (check == "1") {
         std::printf("case=%s prec=%s scheme=%s les=%d trick1=%d noshift=%d forcing_y=%d lx=%d ly=%d ipad=%d jpad=%d svisc=%.17g u0=%.17g "
-                    "ctes=%.17g radius=%d itfin=%d ivtim=%d isignal=%d itsave=%d icheck=%d irestart=%d\n",
+                    "ctes=%.17g radius=%d itfin=%d ivtim=%d isignal=%d itsave=%d icheck=%d irestart=%d obstacle=%s obs_cells=%d\n",
                     tcase.c_str(), prec.c_str(), scheme.c_str(), d.les, d.trick1, d.noshift, d.force_y, d.lx, d.ly, d.ipad, d.jpad, d.svisc, d.u0,
-                    d.cte_s, d.radius, itfin, ivtim, isignal, itsave, icheck, irestart);
+                    d.cte_s, d.radius, itfin, ivtim, isignal, itsave, icheck, irestart,
+                    obstacle.empty() ? "default" : obs_read ? "read" : obstacle.c_str(), obs_cells);
         return 0;
     }
 

@@ -129,3 +129,43 @@ def test_driver_reads_fortran_namelist_and_rejects_bad_options(bgk, tmp_path):
     for args in (["--prec", "dobule"], ["--scheme", "ab"], ["--bogus", "1"], ["--input"]):
         r = subprocess.run([build.EXE_PATH, *args], capture_output=True, text=True, timeout=60)
         assert r.returncode == 2, (args, r.stderr)
+
+def _write_fort96(path, mask, sep="  "):
+    ly, lx = mask.shape
+    with open(path, "w") as f:
+        for j in range(ly):
+            for i in range(lx):
+                f.write(f"{sep}{float(i + 1):.6E}{sep}{float(j + 1):.6E}{sep}{int(mask[j, i])}\n")
+
+
+def test_driver_reads_the_read_build_obstacle_file(bgk, tmp_path):
+    """--obstacle read:FILE takes the mask of the reference's READ build from its fort.96 records
+    (`x y obs`, i fastest, list-directed: blanks or commas), counting the cells where obs is 1;
+    a short file or a non-integer obs stops the driver (status 1), an unknown shape is a bad
+    option (status 2)."""
+    import numpy as np
+    from bgk2d_gpu_gb300 import build
+    lx, ly = 12, 10
+    mask = np.zeros((ly, lx), dtype=int)
+    mask[3:6, 4:7] = 1
+    mask[7, 2] = 2  # not 1: not an obstacle cell, as the reference's obs(i,j) == 1 tests
+    (tmp_path / "bgk.input").write_text("&parameters\nlx=12\nly=10\nitfin=5 /\n")
+
+    def check(*args):
+        return subprocess.run([build.EXE_PATH, "--input", str(tmp_path / "bgk.input"), "--check-input", "1",
+                               "--case", "VKS", *args], capture_output=True, text=True, timeout=60)
+
+    for sep in ("  ", ", "):
+        _write_fort96(tmp_path / "fort.96", mask, sep)
+        r = check("--obstacle", f"read:{tmp_path / 'fort.96'}")
+        assert r.returncode == 0, r.stderr
+        v = dict(kv.split("=") for kv in r.stdout.split())
+        assert (v["obstacle"], v["obs_cells"]) == ("read", "9")
+    lines = (tmp_path / "fort.96").read_text().splitlines()
+    (tmp_path / "short.96").write_text("\n".join(lines[:-1]) + "\n")
+    assert check("--obstacle", f"read:{tmp_path / 'short.96'}").returncode == 1
+    (tmp_path / "real.96").write_text("\n".join(lines[:-1] + ["  1.2E+01  1.0E+01  1.0"]) + "\n")
+    assert check("--obstacle", f"read:{tmp_path / 'real.96'}").returncode == 1
+    assert check("--obstacle", "hexagon").returncode == 2
+    r = check("--obstacle", "half_circle")
+    assert r.returncode == 0 and "obstacle=half_circle" in r.stdout

@@ -112,6 +112,36 @@ def test_driver_vks_writes_drag_lift(bgk, tmp_path):
     assert np.array_equal(vals.reshape(62, 160), mask.astype(float)) and vals.sum() == bbox[4]
 
 
+def test_driver_obstacle_shapes_and_read_file(bgk, tmp_path):
+    """--obstacle square / half_circle (the -DSQUARE and -DHALF_CIRCLE builds) give the solver's
+    masks and diagnostics; --obstacle read:FILE (the -DREAD build's fort.96) with the square's
+    mask as records gives the square run's outputs byte for byte."""
+    kw = dict(lx=160, ly=62, svisc=0.05, itfin=200, itsave=1000000)
+    runs = {}
+    for shape in ("square", "half_circle"):
+        d = tmp_path / shape
+        d.mkdir()
+        run_driver(bgk, d, case="VKS", extra=("--obstacle", shape), **kw)
+        with bgk.Solver(160, 62, tcase="VKS", svisc=0.05, u0=0.1, obstacle=shape) as s:
+            mask, _ = s.obs()
+            s.step(200)
+            want = s.diagno(2)  # diagno.dat holds the reference's own compute-kind sums
+        rows = np.loadtxt(d / "obstacle.dat", dtype=np.int64)
+        assert np.array_equal(rows[:, 2].reshape(62, 160), mask), shape
+        last = (d / "diagno.dat").read_text().splitlines()[-1].split()
+        np.testing.assert_allclose([float(x) for x in last[1:]], want, rtol=1e-5, atol=1e-12)
+        runs[shape] = mask
+    d = tmp_path / "read"
+    d.mkdir()
+    with open(d / "fort.96", "w") as f:
+        for j in range(62):
+            for i in range(160):
+                f.write(f"  {float(i + 1):.6E}  {float(j + 1):.6E}  {int(runs['square'][j, i])}\n")
+    run_driver(bgk, d, case="VKS", extra=("--obstacle", f"read:{d / 'fort.96'}"), **kw)
+    for name in ("diagno.dat", "drag.lift.dat", "obstacle.dat", "prof_j.dat", "probe.dat"):
+        assert (d / name).read_bytes() == (tmp_path / "square" / name).read_bytes(), name
+
+
 def _vtk_sections(path):
     """(header lines, {section name: float32 array}) of a legacy binary VTK file as written by
     SRC/vtk_xy.binary.F90 / vtk_om.binary.F90."""
