@@ -172,16 +172,20 @@ def test_upload_download_roundtrip(oracle_mod, bgk):
             assert_same(o, s, scheme)
 
 
-def test_ldc_256_re100_20000_steps(oracle_mod, bgk):
-    """The small plain case: LDC 256^2, Re=100, FP32, 20000 steps, bit-identical to the oracle."""
-    o = oracle_mod.Oracle(256, 256, prec=0, tcase=0, svisc=0.256, u0=0.1)
-    with bgk.Solver(256, 256, tcase="LDC", svisc=0.256, u0=0.1) as s:
+@pytest.mark.parametrize("scheme", ["pingpong", "aa"])
+@pytest.mark.parametrize("prec", ["single", "double", "mixed2"])
+def test_ldc_256_re100_20000_steps(oracle_mod, bgk, prec, scheme):
+    """The small plain case: LDC 256^2, Re=100, 20000 steps, bit-identical to the oracle in every
+    precision and in both single-buffer and two-buffer schemes, profiles included."""
+    oprec, st, cp = PRECS[prec]
+    o = oracle_mod.Oracle(256, 256, prec=oprec, tcase=0, svisc=0.256, u0=0.1)
+    with bgk.Solver(256, 256, tcase="LDC", svisc=0.256, u0=0.1, storage=st, compute=cp, scheme=scheme) as s:
         s.step(20000)
         o.step(20000, threads=16)
-        assert_same(o, s, "pingpong")
+        assert_same(o, s, scheme)
         u, v, d = s.prof_j(128)
         ou, ov, od = o.prof_j(128)
-        assert np.array_equal(u, ou.astype(np.float32)) and np.array_equal(d, od.astype(np.float32))
+        assert np.array_equal(u, ou) and np.array_equal(v, ov) and np.array_equal(d, od)
 
 
 @pytest.mark.parametrize("prec", ["single", "double"])
