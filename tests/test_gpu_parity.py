@@ -350,6 +350,33 @@ def test_long_runs_stay_bit_exact(oracle_mod, bgk, case, prec, scheme):
             np.testing.assert_array_equal(s.diagno(2), o.diagno(0))
 
 
+VARIANT_RUNS = {  # name: (case, lx, ly, svisc, u0, oracle and solver keywords)
+    "les_cavity": ("LDC", 72, 56, 0.01, 0.1, dict(les=True, cte_s=0.2)),
+    "les_cylinder": ("VKS", 160, 62, 0.02, 0.1, dict(les=True, cte_s=0.2)),
+    "noshift_cavity": ("LDC", 72, 56, 0.02, 0.1, dict(noshift=True)),
+    "trick1_cavity": ("LDC", 64, 64, 0.02, 0.1, dict(trick1=True)),
+    "myversion_force_y": ("MYV", 64, 48, 0.05, 0.1, dict(force_y=True)),
+}
+
+
+@pytest.mark.parametrize("scheme", ["pingpong", "aa"])
+@pytest.mark.parametrize("prec", list(PRECS))
+@pytest.mark.parametrize("name", list(VARIANT_RUNS))
+def test_build_variants_long_runs_stay_bit_exact(oracle_mod, bgk, name, prec, scheme):
+    """3000 steps of the reference's build variants (LES on a cavity and on the cylinder's wake,
+    NOSHIFT, TRICK1, MYVERSION with FORCING_Y): the populations stay identical to the oracle's."""
+    tc, lx, ly, svisc, u0, kw = VARIANT_RUNS[name]
+    oprec, st, cp = PRECS[prec]
+    okw = dict(kw, obstacle=1, radius=6) if tc == "VKS" else dict(kw)
+    skw = dict(kw, radius=6) if tc == "VKS" else dict(kw)
+    o = oracle_mod.Oracle(lx, ly, prec=oprec, tcase={"LDC": 0, "VKS": 3, "MYV": 6}[tc], svisc=svisc, u0=u0,
+                          obs_order=oracle_mod.OBS_SNAPSHOT, **okw)
+    with bgk.Solver(lx, ly, tcase=tc, svisc=svisc, u0=u0, storage=st, compute=cp, scheme=scheme, **skw) as s:
+        s.step(3000)
+        o.step(3000)
+        assert_same(o, s, scheme)
+
+
 @pytest.mark.parametrize("scheme", ["pingpong", "aa"])
 @pytest.mark.parametrize("prec", ["single", "double"])
 def test_bfs_long_run(oracle_mod, bgk, prec, scheme):
