@@ -55,6 +55,36 @@ def test_batch_equals_alone(bgk, storage):
         s.close()
 
 
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_batch_long_run_with_members_joining_and_leaving(bgk, storage):
+    """2000 steps of the mixed batch in chunks of graph and direct launches, with a member leaving
+    halfway and another joining late (the work list rebuilt each time): every member equals the
+    same case stepped alone for the same number of steps."""
+    members, cases = make_cases(bgk, storage)
+    alone = [bgk.Solver(storage=storage, **c) for c in cases]
+    late = len(cases) - 1
+    with bgk.Batch(storage) as b:
+        for i, s in enumerate(members):
+            if i != late:
+                b.add(s)
+        done = [0] * len(cases)
+        for k, chunk in enumerate((500, 1, 257, 33, 200, 9, 1000)):
+            if k == 3:
+                b.remove(members[0])
+            if k == 4:
+                b.add(members[late])
+            b.step(chunk)
+            for i, s in enumerate(alone):
+                if (i != late or k >= 4) and (i != 0 or k < 3):
+                    s.step(chunk)
+                    done[i] += chunk
+        for i, (s, a) in enumerate(zip(members, alone)):
+            assert s.scalars()["itime"] == a.scalars()["itime"] == done[i], i
+            assert np.array_equal(s.download(), a.download()), cases[i]
+    for s in members + alone:
+        s.close()
+
+
 def test_batch_member_cannot_step_alone(bgk):
     s = bgk.Solver(64, 64)
     with bgk.Batch("f32") as b:
